@@ -1,0 +1,354 @@
+"""Benchmark of the SBP-SAT RK4 hot path on GB300.
+
+Workload (one bench "step"): 1000 classical RK4 steps of the 2D first-order
+acoustic wave system (u, v, p), rho = K = 1 on [-1,1]^2, N x N = 4096^2 grid
+points, SBP order 4, characteristic SAT boundaries, FP64, Gaussian pressure
+pulse of width 0.05 at the origin, dt = 0.2 h. Synthetic data.
+
+  value     grid-point stage updates per second (N^2 * 4 stages * 1000 steps
+            per bench step), state resident in HBM, whole job over all ranks.
+  e2e       the same metric through the C ABI call a user makes (sbp_rk4 with
+            a pinned host array: H2D copy, layout packing, 1000 steps,
+            unpacking, D2H copy inside the timed region).
+  roofline  algorithmic HBM bytes of the fused stage kernel (16*c*s = 384 B per
+            point per RK4 step for c = 3 components of s = 8 bytes) divided
+            by its measured time, against the measured copy bandwidth.
+
+`--impl reference` times the reference's CPU implementation of the same path
+(the reference's own headers when built here as oracle/_ref, else the oracle
+restatement) on all host cores, on a bounded sample of the same workload.
+
+Multi-GPU: the path is one grid per device; `--gpus N` runs N independent
+replicas (one per rank, launched by torch.distributed.run) and reports the
+sum of their throughputs over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "hpc-reading-course_gb300")
+sys.path.insert(0, os.path.join(PKG, "python"))
+sys.path.insert(0, PKG)
+
+METRIC = "RK4 point-updates/s"
+UNIT = "grid-point stage updates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=4096)
+    ap.add_argument("--order", type=int, default=4, choices=[2, 4, 6])
+    ap.add_argument("--rk-steps", type=int, default=1000)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--bc", default="characteristic", choices=["characteristic", "free_surface"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def initial_state(n: int):
+    """Gaussian pressure pulse exp(-(x^2+y^2)/0.05^2), u = v = 0, AoS (j, i, comp)."""
+    import numpy as np
+
+    x = np.linspace(-1.0, 1.0, n)
+    p = np.exp(-(x[None, :] ** 2 + x[:, None] ** 2) / 0.05**2)
+    v = np.zeros((n, n, 3))
+    v[:, :, 2] = p
+    return v.ravel()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self._t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [s.strip() for s in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(order: int, precision: str):
+    """DRAM bytes per launch of the stage kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"wave_stage_{precision}_o{order}_traffic.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_point_stage:"):
+                    return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(n: int, order: int, precision: str, bc: str, budget_s: float, repeats: int = 1):
+    """The reference path on the host cores: oracle/_ref when built here and
+    loadable, else the oracle restatement (OpenMP over all cores). Returns
+    (point-stage updates/s, description)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+
+    import oracle as O
+
+    O.build()
+    port = O.Port()
+    threads = os.cpu_count() or 1
+    port.set_threads(threads)
+    v = initial_state(n)
+    h = 2.0 / (n - 1)
+    ones = np.ones(n * n)
+    if bc == "characteristic":
+        pb = O.Problem(O.WAVE_VAR_2D, order, n, n, rho=ones, K=ones, bc=O.BC_CHARACTERISTIC)
+    else:
+        pb = O.Problem(O.WAVE_HOM_2D, order, n, n)
+    t0 = time.perf_counter()
+    v = port.rk4(pb, v, 0.0, 0.2 * h, 1)
+    t1 = time.perf_counter() - t0
+    steps = max(1, min(1000, int(budget_s / max(t1, 1e-6))))
+    rates = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        v = port.rk4(pb, v, 0.0, 0.2 * h, steps)
+        el = time.perf_counter() - t0
+        rates.append(n * n * 4 * steps / el)
+    kind = "port"
+    sample = (f"{steps} RK4 steps of the {n}x{n} order-{order} FP64 wave workload "
+              f"({'characteristic' if bc == 'characteristic' else 'free-surface'} SAT), oracle restatement "
+              f"(oracle/sbp_oracle.c, -O2, OpenMP) on {threads} threads")
+    return rates, kind, threads, sample
+
+
+def run_reference(args, rank: int):
+    if rank != 0:
+        return
+    budget = 3.0
+    rates, kind, threads, sample = cpu_baseline(args.n, args.order, args.precision, args.bc, budget,
+                                                repeats=args.warmup + args.steps)
+    timed = rates[args.warmup:]
+    value = statistics.median(timed)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_of(args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_of(args):
+    return {"workload": f"2D acoustic wave (u,v,p), rho=K=1, {args.n}x{args.n}, SBP order {args.order}, "
+                        f"{args.bc} SAT, {args.precision.upper()}, Gaussian pulse w=0.05, dt=0.2h, "
+                        f"{args.rk_steps} RK4 steps per bench step",
+            "grid": [args.n, args.n], "order": args.order, "rk4_steps_per_step": args.rk_steps,
+            "precision": args.precision, "bc": args.bc,
+            "l2_flush": f"inputs larger than L2: {args.n * args.n * 3 * (8 if args.precision == 'fp64' else 4) / 1e6:.0f}"
+                        " MB per state vector, 4 state vectors",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist = dist_mod
+        import torch
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    if args.impl == "reference":
+        run_reference(args, rank)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    import numpy as np
+    import torch
+
+    import build as gpu_build
+    import sbpgpu
+
+    if rank == 0:
+        gpu_build.build()
+    if dist:
+        dist.barrier()
+    gpu_build.build()
+    torch.cuda.set_device(local)
+    n, order = args.n, args.order
+    prec = sbpgpu.FP64 if args.precision == "fp64" else sbpgpu.FP32
+    bc = sbpgpu.BC_CHARACTERISTIC if args.bc == "characteristic" else sbpgpu.BC_REFERENCE
+    h = 2.0 / (n - 1)
+    dt = 0.2 * h
+    ctx = sbpgpu.Context(sbpgpu.WAVE_HOM_2D, order, n, n, bc=bc, precision=prec, device=local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=local)
+    v0 = initial_state(n)
+    ctx.set_state(v0)
+    ctx.synchronize()
+
+    def sync_all():
+        ctx.synchronize()
+        if dist:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        ctx.step_resident(0.0, dt, args.rk_steps)
+    sync_all()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.launches
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    sync_all()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        ctx.step_resident(0.0, dt, args.rk_steps)
+    ev1.record(stream)
+    ctx.synchronize()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    launches = ctx.launches - launches0
+    if dist:
+        t = torch.tensor([elapsed_ms], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    sync_all()
+    clock_info = clocks.stop()
+
+    ms_per_step = elapsed_ms / args.steps
+    units_per_step = n * n * 4 * args.rk_steps
+    value = world * units_per_step / (ms_per_step * 1e-3)
+    es = 8 if args.precision == "fp64" else 4
+    scalars_per_pt_step = 16 * 3 if args.precision == "fp64" else 19 * 3
+    bytes_per_launch = scalars_per_pt_step * es * n * n / 4.0
+    kernel_ms = elapsed_ms / max(launches, 1)
+    achieved = bytes_per_launch / (kernel_ms * 1e-3) / 1e9
+    peak, peak_src = measured_peaks()
+    traffic_pp = profiled_traffic(order, args.precision)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": (traffic_pp * n * n if traffic_pp else None), "peak_source": peak_src,
+                "algorithmic_bytes_per_launch": bytes_per_launch,
+                "kernel": "wave_stage_kernel (fused RHS + SAT + RK4 stage)", "avg_launch_ms": kernel_ms}
+    if args.precision == "fp64":
+        try:
+            rate = sbpgpu.probe_dfma_rate(local)
+            dp_ops = {2: 13.25, 4: 21.25, 6: 29.25}[order]
+            roofline["fp64_alu"] = {"dfma_per_s": rate, "dp_instr_per_point_stage": dp_ops,
+                                    "bound_point_stage_per_s": rate / dp_ops,
+                                    "frac_of_dp_bound": (units_per_step / (ms_per_step * 1e-3)) / (rate / dp_ops)}
+        except sbpgpu.SbpError:
+            pass
+
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty(n * n * 3, dtype=torch.float64, pin_memory=True).numpy()
+        times = []
+        for k in range(args.warmup + args.steps):
+            host[:] = v0
+            sync_all()
+            t0 = time.perf_counter()
+            ctx.rk4_ptr(host.ctypes.data, 0.0, dt, args.rk_steps, sbpgpu.HOST)
+            el = time.perf_counter() - t0
+            if k >= args.warmup:
+                times.append(el)
+        el = statistics.median(times)
+        if dist:
+            t = torch.tensor([el], dtype=torch.float64, device=f"cuda:{local}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            el = float(t.item())
+        e2e = {"value": world * units_per_step / el, "unit": UNIT, "h2d_bytes_per_step": host.nbytes,
+               "d2h_bytes_per_step": host.nbytes, "ms_per_step": el * 1e3,
+               "call": "sbp_rk4(ctx, 0, dt, steps, host_aos, SBP_HOST)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rates, kind, threads, sample = cpu_baseline(n, order, args.precision, args.bc, 10.0)
+        cpu = {"value": rates[0], "unit": UNIT, "cores": threads, "kind": kind, "sample": sample}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
+                "data": "synthetic (Gaussian pressure pulse)", "config": config_of(args),
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clock_info,
+                "gpu_launches": launches}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,96 @@
+"""Build libsbpgpu.so (CUDA kernels + C ABI) for sm_103a, in tree.
+
+    python hpc-reading-course_gb300/build.py [--force] [--verbose]
+
+Translation units compile in parallel: one per SBP order for the fused wave
+stage kernels, one for the remaining kernels, one for the host runtime.
+Outputs: hpc-reading-course_gb300/_build/*.o and hpc-reading-course_gb300/lib/libsbpgpu.so.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIB_DIR = os.path.join(PKG, "lib")
+LIB = os.path.join(LIB_DIR, "libsbpgpu.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I", os.path.join(ROOT, "include"),
+              "--expt-relaxed-constexpr"] + ARCH
+
+
+def nvcc() -> str:
+    path = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(path):
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libsbpgpu.so")
+    return path
+
+
+def units():
+    """(object file, source, extra flags) for every translation unit."""
+    out = []
+    for order in (2, 4, 6):
+        out.append((f"wave2d_o{order}.o", "wave2d_inst.cu", [f"-DSBP_ORDER={order}"]))
+    out.append(("kernels.o", "kernels.cu", []))
+    out.append(("sbp_runtime.o", "sbp_runtime.cpp", ["-x", "cu"]))
+    return out
+
+
+def _sources_mtime() -> float:
+    m = 0.0
+    for d in (CSRC, os.path.join(ROOT, "include")):
+        for f in os.listdir(d):
+            m = max(m, os.path.getmtime(os.path.join(d, f)))
+    return max(m, os.path.getmtime(__file__))
+
+
+def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> str:
+    """Compile and link; returns the path of the shared library."""
+    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(LIB_DIR, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime():
+        return LIB
+    cc = nvcc()
+    flags = NVCC_FLAGS + (extra_flags or [])
+
+    def compile_one(u):
+        obj, src, extra = u
+        cmd = [cc] + flags + extra + ["-c", os.path.join(CSRC, src), "-o", os.path.join(BUILD, obj)]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        return obj, r
+
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        results = list(ex.map(compile_one, units()))
+    failed = [(o, r) for o, r in results if r.returncode != 0]
+    for o, r in results:
+        if verbose or r.returncode != 0:
+            sys.stderr.write(r.stdout + r.stderr)
+    if failed:
+        raise RuntimeError("nvcc failed for: " + ", ".join(o for o, _ in failed))
+    objs = [os.path.join(BUILD, o) for o, _, _ in units()]
+    tmp = LIB + ".tmp"
+    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stdout + r.stderr)
+        raise RuntimeError("link of libsbpgpu.so failed")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("--verbose", action="store_true")
+    a = ap.parse_args()
+    print(build(force=a.force, verbose=a.verbose))

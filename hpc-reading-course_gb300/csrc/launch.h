@@ -1,0 +1,77 @@
+// launch.h -- host-side launchers for the SBP kernels (implemented in the .cu
+// files of this directory, one translation unit per operator order for the
+// 2D wave kernels so they compile in parallel).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "line_kernels.cuh"
+#include "wave2d.cuh"
+
+namespace sbp {
+
+struct WaveMaps {
+  CUtensorMap p, u, v;  // the same state buffer seen with the p, u and v tile boxes
+};
+
+template <typename T>
+cudaError_t launch_wave_o2(int kind, int stage, const WaveMaps& m, const WaveParams<T>& prm, dim3 grid, cudaStream_t s);
+template <typename T>
+cudaError_t launch_wave_o4(int kind, int stage, const WaveMaps& m, const WaveParams<T>& prm, dim3 grid, cudaStream_t s);
+template <typename T>
+cudaError_t launch_wave_o6(int kind, int stage, const WaveMaps& m, const WaveParams<T>& prm, dim3 grid, cudaStream_t s);
+
+// Sets the dynamic shared-memory opt-in of every stage kernel of (order, kind).
+template <typename T> cudaError_t configure_wave_o2(int kind);
+template <typename T> cudaError_t configure_wave_o4(int kind);
+template <typename T> cudaError_t configure_wave_o6(int kind);
+template <typename T> inline cudaError_t configure_wave(int order, int kind) {
+  return order == 2 ? configure_wave_o2<T>(kind) : (order == 4 ? configure_wave_o4<T>(kind) : configure_wave_o6<T>(kind));
+}
+
+template <typename T>
+inline cudaError_t launch_wave(int order, int kind, int stage, const WaveMaps& m, const WaveParams<T>& prm,
+                               cudaStream_t s) {
+  const dim3 grid((prm.nx + kWaveTX - 1) / kWaveTX, (prm.ny + kWaveTY - 1) / kWaveTY);
+  switch (order) {
+    case 2: return launch_wave_o2<T>(kind, stage, m, prm, grid, s);
+    case 4: return launch_wave_o4<T>(kind, stage, m, prm, grid, s);
+    case 6: return launch_wave_o6<T>(kind, stage, m, prm, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// Shared memory bytes of one wave tile (for occupancy reports).
+int wave_smem_bytes(int order, bool fp32);
+
+template <typename T>
+cudaError_t launch_line(int order, int kind, int stage, const LineParams<T>& prm, cudaStream_t s);
+
+// AoS FP64 (reference layout) <-> SoA planes of T with a row pitch.
+template <typename T>
+cudaError_t launch_pack(const double* aos, T* soa, int nx, int ny, int dofs, long long pitch, long long plane,
+                        cudaStream_t s);
+template <typename T>
+cudaError_t launch_unpack(const T* soa, double* aos, int nx, int ny, int dofs, long long pitch, long long plane,
+                          cudaStream_t s);
+
+// Number of partial sums the reductions write (scratch of 2*kReduceBlocks doubles).
+constexpr int kReduceBlocks = 592;  // 4 blocks per SM on 148-152 SMs
+
+// Sum of squared differences and max |difference| between the SoA state and
+// an AoS FP64 array: out[0] = sum e^2, out[1] = max |e|.
+template <typename T>
+cudaError_t launch_error_norms(const T* soa, const double* aos, int nx, int ny, int dofs, long long pitch,
+                               long long plane, double* partial, double* out, cudaStream_t s);
+// Energy norm squared sum_c sum_j sum_i hy*wy_j * hx*wx_i * v^2 with the
+// closure quadrature at both ends of each direction: out[0].
+template <typename T>
+cudaError_t launch_hnorm(const T* soa, int nx, int ny, int dofs, long long pitch, long long plane, int order,
+                         double hx, double hy, double* partial, double* out, cudaStream_t s);
+
+// FP64 fused-multiply-add throughput probe: each thread runs `iters`
+// iterations of 8 independent DFMA chains; result written to out[0].
+cudaError_t launch_dfma_probe(double* out, int blocks, int threads, int iters, cudaStream_t s);
+
+}  // namespace sbp

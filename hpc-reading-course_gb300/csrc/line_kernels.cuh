@@ -1,0 +1,115 @@
+// line_kernels.cuh -- fused RHS + SAT + RK4-stage kernels for the scalar
+// advection problems (1D and 2D) and the 1D reflection system:
+//   advection  u_t = -(a u_x + b u_y)          (code/demo/advection/advection_rhs.h)
+//   reflection [u; v]_t = [v_x; u_x]           (code/demo/reflection/reflection_rhs.h)
+// One thread per grid point; stencil taps are read through the read-only
+// cache (neighbouring threads share them in L1). These problems have 1-2
+// components and are a small fraction of the work of the 2D wave system.
+#pragma once
+
+#include "sbp_device.cuh"
+#include "wave2d.cuh"
+
+namespace sbp {
+
+enum LineKind : int { LK_ADV1D = 0, LK_REFL1D = 1, LK_ADV2D = 2 };
+
+template <typename T> struct LineParams {
+  int nx, ny;
+  long long pitch, plane;
+  const T* in;
+  T* un;
+  T* acc;
+  T* wout;
+  T* kout;
+  T* comp;
+  DirTaps<T> dx, dy;  // advection: -a*hix, -b*hiy scaled; reflection: +hix scaled
+  double sat[4];      // advection SAT factors 0.5*tau*hi*HI[0] for W, S, E, N
+  int bc;             // 0: none, 1: the reference's boundary treatment
+  int compensated;
+  T c_acc, c_w;
+  int* err;
+};
+
+// D1 along a line at index i with scaled taps; region choice as rhs_serial.
+template <typename T, int ORD>
+__device__ __forceinline__ T d1_line(const T* __restrict__ line, long long st, int n, int i, const DirTaps<T>& d) {
+  constexpr int W = OpShape<ORD>::W, CS = OpShape<ORD>::CS, R = (W - 1) / 2;
+  if (i >= CS && i < n - CS) {
+    const T* c = line + (long long)(i - R) * st;
+    T s = d.taps[0] * __ldg(c);
+#pragma unroll
+    for (int k = 1; k < W; k++)
+      if (k != R) s = fma(d.taps[k], __ldg(c + k * st), s);
+    return s;
+  }
+  return closure_line<T, ORD>(line, st, n, i, d.cls);
+}
+
+template <typename T, int ORD, int KIND, int STAGE>
+__global__ void __launch_bounds__(256) line_stage_kernel(const __grid_constant__ LineParams<T> prm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = prm.nx, ny = prm.ny;
+  if (i >= nx || j >= ny) return;
+  const long long pitch = prm.pitch, plane = prm.plane;
+  const long long q = (long long)j * pitch + i;
+  constexpr int NC = (KIND == LK_REFL1D) ? 2 : 1;
+  T k[NC];
+  T cen[NC];
+  if constexpr (KIND == LK_ADV1D) {
+    k[0] = d1_line<T, ORD>(prm.in, 1, nx, i, prm.dx);
+    cen[0] = prm.in[q];
+    if (prm.bc) {  // SAT_bc_l / SAT_bc_r (advection_rhs.h:94-119)
+      if (i == 0) k[0] = (T)((double)k[0] + prm.sat[0] * (double)cen[0]);
+      if (i == nx - 1) k[0] = (T)((double)k[0] + prm.sat[2] * (double)cen[0]);
+    }
+  } else if constexpr (KIND == LK_ADV2D) {
+    const T* row = prm.in + (long long)j * pitch;
+    const T* col = prm.in + i;
+    k[0] = d1_line<T, ORD>(row, 1, nx, i, prm.dx) + d1_line<T, ORD>(col, pitch, ny, j, prm.dy);
+    cen[0] = prm.in[q];
+    if (prm.bc) {  // SAT_bc_{west,south,east,north} (advection_rhs.h:460-528)
+      double kk = (double)k[0];
+      const double u = (double)cen[0];
+      if (i == 0) kk += prm.sat[0] * u;
+      if (j == 0) kk += prm.sat[1] * u;
+      if (i == nx - 1) kk += prm.sat[2] * u;
+      if (j == ny - 1) kk += prm.sat[3] * u;
+      k[0] = (T)kk;
+    }
+  } else {  // LK_REFL1D: dst(i,1) = D1 u, dst(i,0) = D1 v
+    k[1] = d1_line<T, ORD>(prm.in, 1, nx, i, prm.dx);
+    k[0] = d1_line<T, ORD>(prm.in + plane, 1, nx, i, prm.dx);
+    cen[0] = prm.in[q];
+    cen[1] = prm.in[plane + q];
+    if (prm.bc && (i == 0 || i == nx - 1)) k[0] = T(0);  // proj_dirichlet_bc_{l,r}
+  }
+#pragma unroll
+  for (int c = 0; c < NC; c++) {
+    const long long o = c * plane + q;
+    if constexpr (STAGE == ST_RHS) {
+      prm.kout[o] = k[c];
+    } else if constexpr (STAGE == ST_FIRST) {
+      prm.acc[o] = prm.compensated ? prm.c_acc * k[c] : fma(prm.c_acc, k[c], cen[c]);
+      prm.wout[o] = fma(prm.c_w, k[c], cen[c]);
+    } else if constexpr (STAGE == ST_MID) {
+      const T u0 = prm.un[o];
+      prm.acc[o] = fma(prm.c_acc, k[c], prm.acc[o]);
+      prm.wout[o] = fma(prm.c_w, k[c], u0);
+    } else {
+      const T d = fma(prm.c_acc, k[c], prm.acc[o]);
+      if (prm.compensated) {
+        const T u0 = prm.un[o], e = prm.comp[o];
+        const T yv = d - e;
+        const T tv = u0 + yv;
+        prm.comp[o] = (tv - u0) - yv;
+        prm.un[o] = tv;
+      } else {
+        prm.un[o] = d;
+      }
+    }
+  }
+}
+
+}  // namespace sbp

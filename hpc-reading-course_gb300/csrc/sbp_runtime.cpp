@@ -1,0 +1,661 @@
+// sbp_runtime.cpp -- host runtime behind the C ABI (include/sbpgpu.h):
+// device-resident SoA state, TMA descriptors, the RK4 stage sequence and its
+// CUDA-graph step loop, the layout conversion at the reference boundary, and
+// the FP64 norms.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+
+#include "../../include/sbpgpu.h"
+#include "launch.h"
+#include "sbp_ops.h"
+
+using namespace sbp;
+
+namespace {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+bool is_wave(int problem) {
+  return problem == SBP_WAVE_HOM_2D || problem == SBP_WAVE_MMS_2D || problem == SBP_WAVE_VAR_2D;
+}
+bool is_2d(int problem) { return is_wave(problem) || problem == SBP_ADVECTION_2D; }
+int dofs_of(int problem) {
+  if (is_wave(problem)) return 3;
+  return problem == SBP_REFLECTION_1D ? 2 : 1;
+}
+
+}  // namespace
+
+struct sbp_ctx {
+  sbp_desc d{};
+  int dofs = 0;
+  bool fp32 = false, two_d = false, wave = false, time_dependent = false;
+  long long nx = 0, ny = 1, pitch = 0, plane = 0, npts = 0, nscalar = 0;
+  size_t es = 8;
+  double hix = 1, hiy = 1, hx = 1, hy = 1;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  // device buffers: SoA planes (dofs * plane elements of T each)
+  void *un = nullptr, *acc = nullptr, *wa = nullptr, *wb = nullptr, *comp = nullptr;
+  double* io = nullptr;       // AoS FP64 staging, nscalar
+  double* partial = nullptr;  // reduction scratch, 2 * kReduceBlocks
+  double* red = nullptr;      // reduction result, 4
+  void *rinv = nullptr, *kmod = nullptr;     // WAVE_VAR: T planes
+  double *rho64 = nullptr, *k64 = nullptr;   // WAVE_VAR: nx*ny FP64
+  int* err = nullptr;
+  WaveMaps maps_un{}, maps_wa{}, maps_wb{};
+  std::map<long long, cudaGraphExec_t> graphs;
+  double graph_dt = 0.0;
+  long long launches = 0;
+  std::string msg;
+};
+
+namespace {
+
+// Message of the last sbp_create failure on this thread (no context exists then).
+thread_local std::string g_create_error;
+
+int fail(sbp_ctx* c, int code, const std::string& m) {
+  if (c) c->msg = m;
+  return code;
+}
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(ctx, SBP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+void fill_taps(DirTaps<T>& t, int order, double scale) {
+  const ops::Operator& op = ops::get(order);
+  std::memset(&t, 0, sizeof(t));
+  for (int s = 0; s < op.width; s++) t.taps[s] = (T)(scale * op.interior[s]);
+  for (int r = 0; r < op.cls_sz; r++)
+    for (int s = 0; s < op.cls_width; s++) t.cls[r][s] = (T)(scale * op.closure[r][s]);
+}
+
+int make_maps(sbp_ctx* ctx, void* base, WaveMaps& m) {
+  EncodeTiledFn enc = encode_tiled();
+  if (!enc) return fail(ctx, SBP_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const int R = ctx->d.order / 2;
+  const int hxa = 16 / (int)ctx->es;
+  const int HX = (R + hxa - 1) / hxa * hxa, HY = R;
+  const cuuint64_t dims[3] = {(cuuint64_t)ctx->nx, (cuuint64_t)ctx->ny, 3};
+  const cuuint64_t strides[2] = {(cuuint64_t)(ctx->pitch * ctx->es), (cuuint64_t)(ctx->plane * ctx->es)};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUtensorMapDataType dt = ctx->fp32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  const cuuint32_t boxP[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)(kWaveTY + 2 * HY), 1};
+  const cuuint32_t boxU[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)kWaveTY, 1};
+  const cuuint32_t boxV[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)(kWaveTY + 2 * HY), 1};
+  CUtensorMap* outs[3] = {&m.p, &m.u, &m.v};
+  const cuuint32_t* boxes[3] = {boxP, boxU, boxV};
+  for (int k = 0; k < 3; k++) {
+    CUresult r = enc(outs[k], dt, 3, base, dims, strides, boxes[k], estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(ctx, SBP_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(r));
+  }
+  return SBP_OK;
+}
+
+// Stage-independent kernel parameters.
+template <typename T>
+WaveParams<T> wave_params(sbp_ctx* ctx) {
+  WaveParams<T> p;
+  std::memset(&p, 0, sizeof(p));
+  p.nx = (int)ctx->nx;
+  p.ny = (int)ctx->ny;
+  p.pitch = ctx->pitch;
+  p.plane = ctx->plane;
+  p.rinv = (const T*)ctx->rinv;
+  p.kmod = (const T*)ctx->kmod;
+  p.rho64 = ctx->rho64;
+  p.k64 = ctx->k64;
+  fill_taps<T>(p.dx, ctx->d.order, -ctx->hix);
+  fill_taps<T>(p.dy, ctx->d.order, -ctx->hiy);
+  const double hi0 = ops::get(ctx->d.order).hinv0;
+  p.bwx = ctx->hix * hi0;
+  p.bwy = ctx->hiy * hi0;
+  p.bc = ctx->d.bc == SBP_BC_CHARACTERISTIC ? BC_CHARACTERISTIC : BC_FREE_SURFACE;
+  p.compensated = ctx->fp32 ? 1 : 0;
+  p.xl0 = ctx->d.xl[0];
+  p.xl1 = ctx->d.xl[1];
+  p.hix = ctx->hix;
+  p.hiy = ctx->hiy;
+  p.err = ctx->err;
+  return p;
+}
+
+int wave_kind(const sbp_ctx* ctx) {
+  return ctx->d.problem == SBP_WAVE_HOM_2D ? WK_HOM : (ctx->d.problem == SBP_WAVE_VAR_2D ? WK_VAR : WK_MMS);
+}
+
+template <typename T>
+LineParams<T> line_params(sbp_ctx* ctx) {
+  LineParams<T> p;
+  std::memset(&p, 0, sizeof(p));
+  p.nx = (int)ctx->nx;
+  p.ny = (int)ctx->ny;
+  p.pitch = ctx->pitch;
+  p.plane = ctx->plane;
+  const double hi0 = ops::get(ctx->d.order).hinv0;
+  const double a = ctx->d.a, b = ctx->d.b;
+  if (ctx->d.problem == SBP_REFLECTION_1D) {
+    fill_taps<T>(p.dx, ctx->d.order, ctx->hix);
+  } else {
+    fill_taps<T>(p.dx, ctx->d.order, -a * ctx->hix);
+    fill_taps<T>(p.dy, ctx->d.order, -b * ctx->hiy);
+    // SAT_bc_* (advection_rhs.h:94-119, 460-528): 0.5 * tau * hi * HI[0]
+    p.sat[0] = 0.5 * (-0.5 * (a + std::fabs(a))) * (ctx->hix * hi0);
+    p.sat[1] = 0.5 * (-0.5 * (b + std::fabs(b))) * (ctx->hiy * hi0);
+    p.sat[2] = 0.5 * (0.5 * (a - std::fabs(a))) * (ctx->hix * hi0);
+    p.sat[3] = 0.5 * (0.5 * (b - std::fabs(b))) * (ctx->hiy * hi0);
+  }
+  p.bc = 1;
+  p.compensated = ctx->fp32 ? 1 : 0;
+  p.err = ctx->err;
+  return p;
+}
+
+int line_kind(const sbp_ctx* ctx) {
+  return ctx->d.problem == SBP_ADVECTION_1D ? LK_ADV1D : (ctx->d.problem == SBP_REFLECTION_1D ? LK_REFL1D : LK_ADV2D);
+}
+
+// Launches one kernel of the stage sequence. `in` is the state the RHS is
+// evaluated on; `in_maps` its TMA descriptors (2D wave only).
+template <typename T>
+int launch_stage(sbp_ctx* ctx, int stage, int rk, double t, double dt, void* in, const WaveMaps* in_maps,
+                 void* kout, int bc_on) {
+  T c_acc = 0, c_w = 0;
+  if (stage == ST_FIRST) {
+    c_acc = (T)(dt / 6);
+    c_w = (T)(0.5 * dt);
+  } else if (stage == ST_MID) {
+    c_acc = (T)(dt / 3);
+    c_w = (T)(rk == 2 ? 0.5 * dt : dt);
+  } else if (stage == ST_LAST) {
+    c_acc = (T)(dt / 6);
+  }
+  void* wout = (rk == 1 || rk == 3) ? ctx->wa : ctx->wb;
+  if (ctx->wave) {
+    WaveParams<T> p = wave_params<T>(ctx);
+    p.in = (const T*)in;
+    p.un = (T*)ctx->un;
+    p.acc = (T*)ctx->acc;
+    p.wout = (T*)wout;
+    p.kout = (T*)kout;
+    p.comp = (T*)ctx->comp;
+    p.c_acc = c_acc;
+    p.c_w = c_w;
+    p.t = t;
+    if (!bc_on) p.bc = BC_NONE;
+    CK(launch_wave<T>(ctx->d.order, wave_kind(ctx), stage, *in_maps, p, ctx->stream));
+  } else {
+    LineParams<T> p = line_params<T>(ctx);
+    p.in = (const T*)in;
+    p.un = (T*)ctx->un;
+    p.acc = (T*)ctx->acc;
+    p.wout = (T*)wout;
+    p.kout = (T*)kout;
+    p.comp = (T*)ctx->comp;
+    p.c_acc = c_acc;
+    p.c_w = c_w;
+    p.bc = bc_on;
+    CK(launch_line<T>(ctx->d.order, line_kind(ctx), stage, p, ctx->stream));
+  }
+  ctx->launches++;
+  return SBP_OK;
+}
+
+// One classical RK4 step on the resident state (time_stepping.h:127-142):
+// stage 1 reads u^n and writes acc, wa; stage 2 reads wa, writes acc, wb;
+// stage 3 reads wb, writes acc, wa; stage 4 reads wa, acc and writes u^{n+1}.
+template <typename T>
+int enqueue_step(sbp_ctx* ctx, double t, double dt) {
+  int rc;
+  if ((rc = launch_stage<T>(ctx, ST_FIRST, 1, t, dt, ctx->un, &ctx->maps_un, nullptr, 1))) return rc;
+  if ((rc = launch_stage<T>(ctx, ST_MID, 2, t + 0.5 * dt, dt, ctx->wa, &ctx->maps_wa, nullptr, 1))) return rc;
+  if ((rc = launch_stage<T>(ctx, ST_MID, 3, t + 0.5 * dt, dt, ctx->wb, &ctx->maps_wb, nullptr, 1))) return rc;
+  return launch_stage<T>(ctx, ST_LAST, 4, t + dt, dt, ctx->wa, &ctx->maps_wa, nullptr, 1);
+}
+
+void drop_graphs(sbp_ctx* ctx) {
+  for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+  ctx->graphs.clear();
+}
+
+template <typename T>
+int run_chunk_graph(sbp_ctx* ctx, long long steps, double dt) {
+  if (ctx->graph_dt != dt) {
+    drop_graphs(ctx);
+    ctx->graph_dt = dt;
+  }
+  auto it = ctx->graphs.find(steps);
+  if (it == ctx->graphs.end()) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = ctx->launches;
+    int rc = SBP_OK;
+    for (long long s = 0; s < steps && rc == SBP_OK; s++) rc = enqueue_step<T>(ctx, 0.0, dt);
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->launches = before;  // captured, not yet run
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    CK(ce);
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    CK(ie);
+    it = ctx->graphs.emplace(steps, ex).first;
+  }
+  CK(cudaGraphLaunch(it->second, ctx->stream));
+  ctx->launches += 4 * steps;
+  return SBP_OK;
+}
+
+template <typename T>
+int rk4_resident_t(sbp_ctx* ctx, double t0, double dt, long long nsteps) {
+  if (ctx->time_dependent) {  // stage times change every step: direct launches
+    double t = t0;
+    for (long long s = 0; s < nsteps; s++) {
+      int rc = enqueue_step<T>(ctx, t, dt);
+      if (rc) return rc;
+      t = t + dt;
+    }
+    return SBP_OK;
+  }
+  const long long chunk = 50;
+  long long left = nsteps;
+  while (left >= chunk) {
+    int rc = run_chunk_graph<T>(ctx, chunk, dt);
+    if (rc) return rc;
+    left -= chunk;
+  }
+  if (left > 0) return run_chunk_graph<T>(ctx, left, dt);
+  return SBP_OK;
+}
+
+int check_device_errors(sbp_ctx* ctx) {
+  int h = 0;
+  CK(cudaMemcpyAsync(&h, ctx->err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (h) {
+    cudaMemsetAsync(ctx->err, 0, sizeof(int), ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    return fail(ctx, SBP_ERR_DEVICE, (h & ERR_TMA_TIMEOUT) ? "a TMA tile wait timed out in a stage kernel"
+                                                           : "a kernel reported an error");
+  }
+  return SBP_OK;
+}
+
+// AoS FP64 input (host or device) -> a device AoS pointer.
+int stage_in(sbp_ctx* ctx, const double* src, int where, const double** dev) {
+  if (!src) return fail(ctx, SBP_ERR_INVALID, "null array");
+  if (where == SBP_DEVICE) {
+    *dev = src;
+    return SBP_OK;
+  }
+  if (where != SBP_HOST) return fail(ctx, SBP_ERR_INVALID, "where must be SBP_HOST or SBP_DEVICE");
+  CK(cudaMemcpyAsync(ctx->io, src, ctx->nscalar * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  *dev = ctx->io;
+  return SBP_OK;
+}
+
+int pack_into(sbp_ctx* ctx, const double* aos, void* soa) {
+  if (ctx->fp32)
+    CK(launch_pack<float>(aos, (float*)soa, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane, ctx->stream));
+  else
+    CK(launch_pack<double>(aos, (double*)soa, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane,
+                           ctx->stream));
+  ctx->launches++;
+  return SBP_OK;
+}
+
+int unpack_to(sbp_ctx* ctx, const void* soa, double* dst, int where) {
+  if (!dst) return fail(ctx, SBP_ERR_INVALID, "null array");
+  double* out = (where == SBP_DEVICE) ? dst : ctx->io;
+  if (ctx->fp32)
+    CK(launch_unpack<float>((const float*)soa, out, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane,
+                            ctx->stream));
+  else
+    CK(launch_unpack<double>((const double*)soa, out, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane,
+                             ctx->stream));
+  ctx->launches++;
+  if (where != SBP_DEVICE)
+    CK(cudaMemcpyAsync(dst, ctx->io, ctx->nscalar * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  return SBP_OK;
+}
+
+int rhs_impl(sbp_ctx* ctx, double t, const double* src, double* dst, int where, int bc_on) {
+  if (!ctx) return SBP_ERR_INVALID;
+  CK(cudaSetDevice(ctx->d.device));
+  const double* dev = nullptr;
+  int rc;
+  if ((rc = stage_in(ctx, src, where, &dev))) return rc;
+  if ((rc = pack_into(ctx, dev, ctx->wa))) return rc;
+  if (ctx->fp32)
+    rc = launch_stage<float>(ctx, ST_RHS, 0, t, 0.0, ctx->wa, &ctx->maps_wa, ctx->wb, bc_on);
+  else
+    rc = launch_stage<double>(ctx, ST_RHS, 0, t, 0.0, ctx->wa, &ctx->maps_wa, ctx->wb, bc_on);
+  if (rc) return rc;
+  if ((rc = unpack_to(ctx, ctx->wb, dst, where))) return rc;
+  return check_device_errors(ctx);
+}
+
+void release(sbp_ctx* ctx) {
+  if (!ctx) return;
+  drop_graphs(ctx);
+  void* bufs[] = {ctx->un, ctx->acc, ctx->wa, ctx->wb, ctx->comp, ctx->io, ctx->partial, ctx->red,
+                  ctx->rinv, ctx->kmod, ctx->rho64, ctx->k64, ctx->err};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int sbp_create(const sbp_desc* desc, sbp_ctx** out) {
+  if (!desc || !out) return SBP_ERR_INVALID;
+  *out = nullptr;
+  sbp_ctx* ctx = new (std::nothrow) sbp_ctx();
+  if (!ctx) return SBP_ERR_INVALID;
+  ctx->d = *desc;
+  const sbp_desc& d = ctx->d;
+  auto bad = [&](const std::string& m) {
+    g_create_error = m;
+    delete ctx;
+    return SBP_ERR_INVALID;
+  };
+  if (d.problem < SBP_WAVE_HOM_2D || d.problem > SBP_WAVE_VAR_2D) return bad("unknown problem");
+  if (d.order != 2 && d.order != 4 && d.order != 6) return bad("order must be 2, 4 or 6");
+  if (d.precision != SBP_FP64 && d.precision != SBP_FP32) return bad("unknown precision");
+  if (d.bc != SBP_BC_REFERENCE && d.bc != SBP_BC_CHARACTERISTIC) return bad("unknown boundary treatment");
+  ctx->two_d = is_2d(d.problem);
+  ctx->wave = is_wave(d.problem);
+  ctx->dofs = dofs_of(d.problem);
+  ctx->fp32 = d.precision == SBP_FP32;
+  ctx->es = ctx->fp32 ? 4 : 8;
+  ctx->nx = d.nx;
+  ctx->ny = ctx->two_d ? d.ny : 1;
+  const long long m = ops::min_points(d.order);
+  if (ctx->nx < m || (ctx->two_d && ctx->ny < m)) return bad("grid smaller than the operator's minimum size");
+  if (ctx->nx > (1LL << 30) || ctx->ny > (1LL << 30)) return bad("grid too large");
+  if (d.bc == SBP_BC_CHARACTERISTIC && !(d.problem == SBP_WAVE_HOM_2D || d.problem == SBP_WAVE_VAR_2D))
+    return bad("characteristic boundary terms exist for the wave problems with rho, K fields only");
+  if (d.problem == SBP_WAVE_MMS_2D && ctx->fp32) return bad("the manufactured-solution problem is FP64 only");
+  if (d.problem == SBP_WAVE_VAR_2D && (!d.rho || !d.K)) return bad("rho and K are required");
+  if (!(d.xr[0] > d.xl[0]) || (ctx->two_d && !(d.xr[1] > d.xl[1]))) return bad("empty domain");
+  ctx->time_dependent = d.problem == SBP_WAVE_MMS_2D;
+  ctx->hix = (ctx->nx - 1) / (d.xr[0] - d.xl[0]);
+  ctx->hx = 1.0 / ctx->hix;
+  if (ctx->two_d) {
+    ctx->hiy = (ctx->ny - 1) / (d.xr[1] - d.xl[1]);
+    ctx->hy = 1.0 / ctx->hiy;
+  }
+  ctx->pitch = (ctx->nx + 63) / 64 * 64;
+  ctx->plane = ctx->pitch * ctx->ny;
+  ctx->npts = ctx->nx * ctx->ny;
+  ctx->nscalar = ctx->npts * ctx->dofs;
+
+  if (cudaSetDevice(d.device) != cudaSuccess) return bad("cudaSetDevice failed");
+  auto cuda_fail = [&](const char* what, cudaError_t e) {
+    g_create_error = std::string(what) + ": " + cudaGetErrorString(e);
+    release(ctx);
+    delete ctx;
+    return SBP_ERR_CUDA;
+  };
+  cudaError_t e;
+  if (d.stream) {
+    ctx->stream = (cudaStream_t)d.stream;
+  } else {
+    if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess)
+      return cuda_fail("cudaStreamCreate", e);
+    ctx->own_stream = true;
+  }
+  const size_t state_bytes = (size_t)ctx->dofs * ctx->plane * ctx->es;
+  void** bufs[] = {&ctx->un, &ctx->acc, &ctx->wa, &ctx->wb};
+  for (void** b : bufs) {
+    if ((e = cudaMalloc(b, state_bytes)) != cudaSuccess) return cuda_fail("cudaMalloc(state)", e);
+    cudaMemset(*b, 0, state_bytes);
+  }
+  if (ctx->fp32) {
+    if ((e = cudaMalloc(&ctx->comp, state_bytes)) != cudaSuccess) return cuda_fail("cudaMalloc(comp)", e);
+    cudaMemset(ctx->comp, 0, state_bytes);
+  }
+  if ((e = cudaMalloc((void**)&ctx->io, ctx->nscalar * sizeof(double))) != cudaSuccess)
+    return cuda_fail("cudaMalloc(io)", e);
+  if ((e = cudaMalloc((void**)&ctx->partial, 2 * kReduceBlocks * sizeof(double))) != cudaSuccess)
+    return cuda_fail("cudaMalloc(partial)", e);
+  if ((e = cudaMalloc((void**)&ctx->red, 4 * sizeof(double))) != cudaSuccess) return cuda_fail("cudaMalloc(red)", e);
+  if ((e = cudaMalloc((void**)&ctx->err, sizeof(int))) != cudaSuccess) return cuda_fail("cudaMalloc(err)", e);
+  cudaMemset(ctx->err, 0, sizeof(int));
+
+  if (d.problem == SBP_WAVE_VAR_2D) {
+    const size_t np = (size_t)ctx->npts;
+    double* rinv_h = new (std::nothrow) double[np];
+    if (!rinv_h) return cuda_fail("host allocation", cudaErrorMemoryAllocation);
+    for (size_t q = 0; q < np; q++) rinv_h[q] = 1.0 / d.rho[q];
+    if ((e = cudaMalloc((void**)&ctx->rho64, np * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&ctx->k64, np * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&ctx->rinv, ctx->plane * ctx->es)) != cudaSuccess ||
+        (e = cudaMalloc(&ctx->kmod, ctx->plane * ctx->es)) != cudaSuccess) {
+      delete[] rinv_h;
+      return cuda_fail("cudaMalloc(coefficients)", e);
+    }
+    cudaMemcpy(ctx->rho64, d.rho, np * sizeof(double), cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->k64, d.K, np * sizeof(double), cudaMemcpyHostToDevice);
+    // pack 1/rho and K into padded planes of T via the AoS->SoA kernel (dofs = 1)
+    double* tmp = nullptr;
+    if ((e = cudaMalloc((void**)&tmp, np * sizeof(double))) != cudaSuccess) {
+      delete[] rinv_h;
+      return cuda_fail("cudaMalloc(tmp)", e);
+    }
+    cudaMemcpy(tmp, rinv_h, np * sizeof(double), cudaMemcpyHostToDevice);
+    delete[] rinv_h;
+    if (ctx->fp32) {
+      launch_pack<float>(tmp, (float*)ctx->rinv, (int)ctx->nx, (int)ctx->ny, 1, ctx->pitch, ctx->plane, 0);
+      launch_pack<float>(ctx->k64, (float*)ctx->kmod, (int)ctx->nx, (int)ctx->ny, 1, ctx->pitch, ctx->plane, 0);
+    } else {
+      launch_pack<double>(tmp, (double*)ctx->rinv, (int)ctx->nx, (int)ctx->ny, 1, ctx->pitch, ctx->plane, 0);
+      launch_pack<double>(ctx->k64, (double*)ctx->kmod, (int)ctx->nx, (int)ctx->ny, 1, ctx->pitch, ctx->plane, 0);
+    }
+    e = cudaDeviceSynchronize();
+    cudaFree(tmp);
+    if (e != cudaSuccess) return cuda_fail("coefficient upload", e);
+  }
+  if (ctx->wave) {
+    if (make_maps(ctx, ctx->un, ctx->maps_un) || make_maps(ctx, ctx->wa, ctx->maps_wa) ||
+        make_maps(ctx, ctx->wb, ctx->maps_wb)) {
+      g_create_error = ctx->msg;
+      release(ctx);
+      delete ctx;
+      return SBP_ERR_CUDA;
+    }
+    // shared-memory opt-in of the stage kernels, done here (not under stream capture)
+    e = ctx->fp32 ? configure_wave<float>(d.order, wave_kind(ctx)) : configure_wave<double>(d.order, wave_kind(ctx));
+    if (e != cudaSuccess) return cuda_fail("configure stage kernels", e);
+  }
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess) return cuda_fail("create", e);
+  *out = ctx;
+  return SBP_OK;
+}
+
+int sbp_destroy(sbp_ctx* ctx) {
+  if (!ctx) return SBP_ERR_INVALID;
+  cudaSetDevice(ctx->d.device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  release(ctx);
+  delete ctx;
+  return SBP_OK;
+}
+
+const char* sbp_last_error(const sbp_ctx* ctx) { return ctx ? ctx->msg.c_str() : g_create_error.c_str(); }
+
+int sbp_dofs(const sbp_ctx* ctx) { return ctx ? ctx->dofs : SBP_ERR_INVALID; }
+
+int sbp_rhs(sbp_ctx* ctx, double t, const double* src, double* dst, int where) {
+  return rhs_impl(ctx, t, src, dst, where, 1);
+}
+
+int sbp_apply(sbp_ctx* ctx, double t, const double* src, double* dst, int where) {
+  return rhs_impl(ctx, t, src, dst, where, 0);
+}
+
+long long sbp_rk4_nsteps(double t_end, double* dt) {
+  if (!dt || !(*dt > 0) || !(t_end > 0)) return SBP_ERR_INVALID;
+  const long long n = std::llround(t_end / *dt);
+  if (n > 0 && std::fabs((double)n * *dt - t_end) > 1e-14) *dt = t_end / (double)n;
+  return n;
+}
+
+int sbp_set_state(sbp_ctx* ctx, const double* v, int where) {
+  if (!ctx) return SBP_ERR_INVALID;
+  CK(cudaSetDevice(ctx->d.device));
+  const double* dev = nullptr;
+  int rc;
+  if ((rc = stage_in(ctx, v, where, &dev))) return rc;
+  if ((rc = pack_into(ctx, dev, ctx->un))) return rc;
+  if (ctx->comp) CK(cudaMemsetAsync(ctx->comp, 0, (size_t)ctx->dofs * ctx->plane * ctx->es, ctx->stream));
+  return SBP_OK;
+}
+
+int sbp_get_state(sbp_ctx* ctx, double* v, int where) {
+  if (!ctx) return SBP_ERR_INVALID;
+  CK(cudaSetDevice(ctx->d.device));
+  int rc = unpack_to(ctx, ctx->un, v, where);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SBP_OK;
+}
+
+int sbp_rk4_resident(sbp_ctx* ctx, double t0, double dt, long long nsteps) {
+  if (!ctx) return SBP_ERR_INVALID;
+  if (nsteps < 0 || !(dt > 0)) return fail(ctx, SBP_ERR_INVALID, "need dt > 0 and nsteps >= 0");
+  CK(cudaSetDevice(ctx->d.device));
+  return ctx->fp32 ? rk4_resident_t<float>(ctx, t0, dt, nsteps) : rk4_resident_t<double>(ctx, t0, dt, nsteps);
+}
+
+int sbp_synchronize(sbp_ctx* ctx) {
+  if (!ctx) return SBP_ERR_INVALID;
+  CK(cudaSetDevice(ctx->d.device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return check_device_errors(ctx);
+}
+
+int sbp_rk4(sbp_ctx* ctx, double t0, double dt, long long nsteps, double* v, int where) {
+  int rc;
+  if ((rc = sbp_set_state(ctx, v, where))) return rc;
+  if ((rc = sbp_rk4_resident(ctx, t0, dt, nsteps))) return rc;
+  if ((rc = sbp_get_state(ctx, v, where))) return rc;
+  return check_device_errors(ctx);
+}
+
+int sbp_ts_rk4(sbp_ctx* ctx, double t_end, double dt, double* v, int where) {
+  if (!ctx) return SBP_ERR_INVALID;
+  double d = dt;
+  const long long n = sbp_rk4_nsteps(t_end, &d);
+  if (n < 0) return fail(ctx, SBP_ERR_INVALID, "need t_end > 0 and dt > 0");
+  return sbp_rk4(ctx, 0.0, d, n, v, where);
+}
+
+int sbp_error_norms(sbp_ctx* ctx, const double* exact, int where, double* l2, double* linf) {
+  if (!ctx || !l2 || !linf) return SBP_ERR_INVALID;
+  CK(cudaSetDevice(ctx->d.device));
+  const double* dev = nullptr;
+  int rc;
+  if ((rc = stage_in(ctx, exact, where, &dev))) return rc;
+  if (ctx->fp32)
+    CK(launch_error_norms<float>((const float*)ctx->un, dev, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch,
+                                 ctx->plane, ctx->partial, ctx->red, ctx->stream));
+  else
+    CK(launch_error_norms<double>((const double*)ctx->un, dev, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch,
+                                  ctx->plane, ctx->partial, ctx->red, ctx->stream));
+  ctx->launches += 2;
+  double h[2];
+  CK(cudaMemcpyAsync(h, ctx->red, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const double hprod = ctx->two_d ? ctx->hx * ctx->hy : ctx->hx;
+  *l2 = std::sqrt(hprod) * std::sqrt(h[0]);
+  *linf = h[1];
+  return SBP_OK;
+}
+
+int sbp_hnorm(sbp_ctx* ctx, double* hn) {
+  if (!ctx || !hn) return SBP_ERR_INVALID;
+  CK(cudaSetDevice(ctx->d.device));
+  if (ctx->fp32)
+    CK(launch_hnorm<float>((const float*)ctx->un, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane,
+                           ctx->d.order, ctx->hx, ctx->hy, ctx->partial, ctx->red, ctx->stream));
+  else
+    CK(launch_hnorm<double>((const double*)ctx->un, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane,
+                            ctx->d.order, ctx->hx, ctx->hy, ctx->partial, ctx->red, ctx->stream));
+  ctx->launches += 2;
+  double h = 0;
+  CK(cudaMemcpyAsync(&h, ctx->red, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *hn = std::sqrt(h);
+  return SBP_OK;
+}
+
+int sbp_get_stream(const sbp_ctx* ctx, void** stream) {
+  if (!ctx || !stream) return SBP_ERR_INVALID;
+  *stream = (void*)ctx->stream;
+  return SBP_OK;
+}
+
+long long sbp_launch_count(const sbp_ctx* ctx) { return ctx ? ctx->launches : SBP_ERR_INVALID; }
+
+int sbp_probe_dfma_rate(int device, double* rate) {
+  if (!rate) return SBP_ERR_INVALID;
+  if (cudaSetDevice(device) != cudaSuccess) return SBP_ERR_CUDA;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  double* out = nullptr;
+  if (cudaMalloc((void**)&out, 2 * sizeof(double)) != cudaSuccess) return SBP_ERR_CUDA;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  launch_dfma_probe(out, blocks, threads, 256, 0);  // warm-up
+  cudaEventRecord(e0, 0);
+  launch_dfma_probe(out, blocks, threads, iters, 0);
+  cudaEventRecord(e1, 0);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess || ms <= 0) return SBP_ERR_CUDA;
+  *rate = (double)blocks * threads * iters * 8.0 / (ms * 1e-3);
+  return SBP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,281 @@
+// wave2d.cuh -- fused RHS + SAT + RK4-stage kernel for the 2D first-order
+// acoustic wave system (u, v, p):
+//   F_u = -(1/rho) D1x p,  F_v = -(1/rho) D1y p,  F_p = -K (D1x u + D1y v)
+// with the reference's operators (code/include/sbpops/D1_central.h) and its
+// region split (code/include/partitioned_rhs/rhs.h:373-398): closure rows for
+// the first/last cls_sz lines of each direction, the central stencil between.
+//
+// One CTA owns a TX x TY tile of grid points. Thread 0 issues three TMA tile
+// loads of the stage input into shared memory: p with an x and y halo, u with
+// an x halo, v with a y halo (the star stencil needs no corners of u, v). The
+// interior stencils read shared memory; closure rows (boundary strips only)
+// read their taps straight from global memory. The SAT terms and the RK4
+// stage update are applied to the point's RHS in registers, so each stage
+// reads its state once and writes its outputs once.
+//
+// State layout in HBM: structure of arrays, component planes [u | v | p],
+// each ny rows of `pitch` elements (pitch a multiple of 64, so every row
+// starts 512-byte aligned for FP64 and 256-byte aligned for FP32).
+#pragma once
+
+#include "sbp_device.cuh"
+
+namespace sbp {
+
+enum WaveKind : int { WK_HOM = 0, WK_VAR = 1, WK_MMS = 2 };
+enum BcKind : int { BC_NONE = 0, BC_FREE_SURFACE = 1, BC_CHARACTERISTIC = 2 };
+enum Stage : int { ST_RHS = 0, ST_FIRST = 1, ST_MID = 2, ST_LAST = 4 };
+
+template <typename T> struct WaveParams {
+  int nx, ny;
+  long long pitch;    // elements per row
+  long long plane;    // elements per component plane (ny * pitch)
+  const T* in;        // stage input state (3 planes); closure taps are read here
+  T* un;              // u^n (3 planes); written in place by ST_LAST
+  T* acc;             // RK4 accumulator (3 planes)
+  T* wout;            // next stage input (3 planes)
+  T* kout;            // ST_RHS output (3 planes)
+  T* comp;            // FP32: compensation term of the summed update (3 planes)
+  const T* rinv;      // WK_VAR: 1/rho (1 plane)
+  const T* kmod;      // WK_VAR: K (1 plane)
+  const double* rho64;  // WK_VAR: rho in FP64, read at boundary points
+  const double* k64;    // WK_VAR: K in FP64, read at boundary points
+  DirTaps<T> dx, dy;  // -hix * stencils, -hiy * stencils
+  double bwx, bwy;    // hix * HI[0], hiy * HI[0]: SAT weights (FP64)
+  T c_acc, c_w;       // acc (+)= c_acc * k ; w = u^n + c_w * k
+  int bc;             // BcKind
+  int compensated;    // FP32: Kahan-compensated final update
+  double t, xl0, xl1, hix, hiy;  // WK_MMS: stage time and grid geometry
+  int* err;
+};
+
+constexpr int kWaveTX = 64;   // tile width (x, contiguous)
+constexpr int kWaveTY = 32;   // tile height (y)
+constexpr int kWaveThreads = 256;
+
+// x halo rounded up so that (tile origin - halo) * sizeof(T) is a multiple of
+// 16 bytes (TMA rule for the innermost coordinate); the tile origin is a
+// multiple of 64.
+template <typename T, int ORD> struct WaveTile {
+  static constexpr int R = (OpShape<ORD>::W - 1) / 2;
+  static constexpr int HXA = 16 / sizeof(T);                  // alignment unit in elements
+  static constexpr int HX = ((R + HXA - 1) / HXA) * HXA;      // x halo loaded
+  static constexpr int HY = R;                                // y halo loaded
+  static constexpr int PW = kWaveTX + 2 * HX;                 // p/u tile row length
+  static constexpr int PH = kWaveTY + 2 * HY;                 // p/v tile rows
+  static constexpr int align128(int b) { return (b + 127) / 128 * 128; }
+  static constexpr int BYTES_P = PH * PW * (int)sizeof(T);
+  static constexpr int BYTES_U = kWaveTY * PW * (int)sizeof(T);
+  static constexpr int BYTES_V = PH * kWaveTX * (int)sizeof(T);
+  static constexpr int OFF_U = align128(BYTES_P);
+  static constexpr int OFF_V = OFF_U + align128(BYTES_U);
+  static constexpr int OFF_BAR = OFF_V + align128(BYTES_V);
+  static constexpr int SMEM = OFF_BAR + 128;
+  static constexpr uint32_t TX_BYTES = BYTES_P + BYTES_U + BYTES_V;
+};
+
+// Closure row of D1 along one line: left block for i < CS, mirrored negated
+// block for i >= n - CS (D1_central.h:57-65, :95-104), scaled taps.
+template <typename T, int ORD>
+__device__ __forceinline__ T closure_line(const T* __restrict__ line, long long st, int n, int i,
+                                          const T (&cls)[6][9]) {
+  constexpr int CW = OpShape<ORD>::CW;
+  T s;
+  if (i < OpShape<ORD>::CS) {
+    s = cls[i][0] * __ldg(line);
+#pragma unroll
+    for (int k = 1; k < CW; k++) s = fma(cls[i][k], __ldg(line + k * st), s);
+  } else {
+    const int r = n - 1 - i;
+    const T* base = line + (long long)(n - CW) * st;
+    s = -cls[r][CW - 1] * __ldg(base);
+#pragma unroll
+    for (int k = 1; k < CW; k++) s = fma(-cls[r][CW - 1 - k], __ldg(base + k * st), s);
+  }
+  return s;
+}
+
+// The manufactured density and forcing of the reference's forced wave demo
+// (code/demo/wave/wave_eq_rhs.h:42-64), evaluated in FP64.
+__device__ __forceinline__ double mms_x(double xl, int i, double hi) { return xl + (double)i / hi; }
+
+template <typename T, int ORD, int KIND, int STAGE>
+__global__ void __launch_bounds__(kWaveThreads)
+    wave_stage_kernel(const __grid_constant__ CUtensorMap mapP, const __grid_constant__ CUtensorMap mapU,
+                      const __grid_constant__ CUtensorMap mapV, const __grid_constant__ WaveParams<T> prm) {
+  using Tile = WaveTile<T, ORD>;
+  constexpr int W = OpShape<ORD>::W, CS = OpShape<ORD>::CS, R = Tile::R;
+  constexpr int HX = Tile::HX, HY = Tile::HY, PW = Tile::PW;
+  extern __shared__ __align__(128) unsigned char smem[];
+  T* sP = reinterpret_cast<T*>(smem);
+  T* sU = reinterpret_cast<T*>(smem + Tile::OFF_U);
+  T* sV = reinterpret_cast<T*>(smem + Tile::OFF_V);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
+
+  const int i0 = blockIdx.x * kWaveTX, j0 = blockIdx.y * kWaveTY;
+  if (threadIdx.x == 0) {
+    prefetch_tensormap(&mapP);
+    mbar_init(bar, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(bar, Tile::TX_BYTES);
+    tma_load_3d(sP, &mapP, i0 - HX, j0 - HY, 2, bar);
+    tma_load_3d(sU, &mapU, i0 - HX, j0, 0, bar);
+    tma_load_3d(sV, &mapV, i0, j0 - HY, 1, bar);
+  }
+  if (!mbar_wait_bounded(bar, 0)) {
+    if (threadIdx.x == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
+    mbar_wait_bounded(bar, 0);  // let copies in flight land before the CTA exits
+    return;
+  }
+
+  const int nx = prm.nx, ny = prm.ny;
+  const long long pitch = prm.pitch, plane = prm.plane;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int ROWS = kWaveTY / (kWaveThreads / 32);
+
+#pragma unroll 1
+  for (int rr = 0; rr < ROWS; rr++) {
+    const int y = warp * ROWS + rr;
+    const int j = j0 + y;
+    if (j >= ny) break;
+    const bool yint = (j >= CS) && (j < ny - CS);
+#pragma unroll
+    for (int cc = 0; cc < kWaveTX / 32; cc++) {
+      const int x = lane + 32 * cc;
+      const int i = i0 + x;
+      if (i >= nx) continue;
+      const bool xint = (i >= CS) && (i < nx - CS);
+      const T* rowP = sP + (y + HY) * PW + (x + HX - R);
+      const T* rowU = sU + y * PW + (x + HX - R);
+      const T* colP = sP + (y) * PW + (x + HX);          // row y+HY-R
+      const T* colV = sV + (y) * kWaveTX + x;            // row y+HY-R
+      const T pc = rowP[R], uc = rowU[R], vc = colV[R * kWaveTX];
+
+      // D1x p, D1y p (scaled by -hi)
+      T dxp, dyp, kp;
+      if (xint) {
+        dxp = prm.dx.taps[0] * rowP[0];
+#pragma unroll
+        for (int s = 1; s < W; s++)
+          if (s != R) dxp = fma(prm.dx.taps[s], rowP[s], dxp);
+      } else {
+        dxp = closure_line<T, ORD>(prm.in + 2 * plane + (long long)j * pitch, 1, nx, i, prm.dx.cls);
+      }
+      if (yint) {
+        dyp = prm.dy.taps[0] * colP[0];
+#pragma unroll
+        for (int s = 1; s < W; s++)
+          if (s != R) dyp = fma(prm.dy.taps[s], colP[s * PW], dyp);
+      } else {
+        dyp = closure_line<T, ORD>(prm.in + 2 * plane + i, pitch, ny, j, prm.dy.cls);
+      }
+      // D1x u + D1y v as one chain where both are interior
+      if (xint) {
+        kp = prm.dx.taps[0] * rowU[0];
+#pragma unroll
+        for (int s = 1; s < W; s++)
+          if (s != R) kp = fma(prm.dx.taps[s], rowU[s], kp);
+      } else {
+        kp = closure_line<T, ORD>(prm.in + (long long)j * pitch, 1, nx, i, prm.dx.cls);
+      }
+      if (yint) {
+#pragma unroll
+        for (int s = 0; s < W; s++)
+          if (s != R) kp = fma(prm.dy.taps[s], colV[s * kWaveTX], kp);
+      } else {
+        kp += closure_line<T, ORD>(prm.in + plane + i, pitch, ny, j, prm.dy.cls);
+      }
+
+      const long long q = (long long)j * pitch + i;
+      T ku, kv;
+      if constexpr (KIND == WK_HOM) {
+        ku = dxp;
+        kv = dyp;
+      } else if constexpr (KIND == WK_VAR) {
+        const T ri = prm.rinv[q];
+        ku = ri * dxp;
+        kv = ri * dyp;
+        kp = prm.kmod[q] * kp;
+      } else {  // WK_MMS (FP64)
+        const double PI = 3.14159265358979323846264;
+        const double xx = mms_x(prm.xl0, i, prm.hix), yy = mms_x(prm.xl1, j, prm.hiy);
+        const double ri = 1. / (2 + xx * yy);
+        const double ct = cos(5 * PI * prm.t);
+        const double fu = -(3 * PI * ct * cos(3 * PI * xx) * sin(4 * PI * yy) * (xx * yy + 1)) / (xx * yy + 2);
+        const double fv = -(4 * PI * ct * cos(4 * PI * yy) * sin(3 * PI * xx) * (xx * yy + 1)) / (xx * yy + 2);
+        ku = (T)(ri * (double)dxp + fu);
+        kv = (T)(ri * (double)dyp + fv);
+      }
+
+      // SAT boundary terms (FP64 weights), reference order west, south, east, north
+      const bool edge = (i == 0) || (j == 0) || (i == nx - 1) || (j == ny - 1);
+      if (prm.bc != BC_NONE && edge) {
+        double rho = 1.0, kk = 1.0;
+        if constexpr (KIND == WK_VAR) {
+          rho = prm.rho64[(long long)j * nx + i];
+          kk = prm.k64[(long long)j * nx + i];
+        }
+        const double p64 = (double)pc;
+        double ku64 = (double)ku, kv64 = (double)kv, kp64 = (double)kp;
+        if (prm.bc == BC_FREE_SURFACE) {
+          // free_surface_bc_* (code/demo/wave_hom/wave_eq_hom_rhs.h:389-441); rho^-1 for WK_VAR
+          const double ri = (KIND == WK_VAR) ? 1.0 / rho : 1.0;
+          if (i == 0) ku64 = (KIND == WK_VAR) ? ku64 - ri * (prm.bwx * p64) : ku64 - prm.bwx * p64;
+          if (j == 0) kv64 = (KIND == WK_VAR) ? kv64 - ri * (prm.bwy * p64) : kv64 - prm.bwy * p64;
+          if (i == nx - 1) ku64 = (KIND == WK_VAR) ? ku64 + ri * (prm.bwx * p64) : ku64 + prm.bwx * p64;
+          if (j == ny - 1) kv64 = (KIND == WK_VAR) ? kv64 + ri * (prm.bwy * p64) : kv64 + prm.bwy * p64;
+        } else {
+          // characteristic SAT on the incoming characteristic p + Z u_n
+          const double z = sqrt(rho * kk), c = sqrt(kk / rho), hr = 0.5 / rho, hc = 0.5 * c;
+          const double u64 = (double)uc, v64 = (double)vc;
+          if (i == 0) { const double g = prm.bwx * (p64 + z * u64); ku64 -= hr * g; kp64 -= hc * g; }
+          if (j == 0) { const double g = prm.bwy * (p64 + z * v64); kv64 -= hr * g; kp64 -= hc * g; }
+          if (i == nx - 1) { const double g = prm.bwx * (p64 - z * u64); ku64 += hr * g; kp64 -= hc * g; }
+          if (j == ny - 1) { const double g = prm.bwy * (p64 - z * v64); kv64 += hr * g; kp64 -= hc * g; }
+        }
+        ku = (T)ku64;
+        kv = (T)kv64;
+        kp = (T)kp64;
+      }
+
+      // RK4 stage update (classical RK4, code/include/time_stepping/time_stepping.h:127-142)
+      const T kc[3] = {ku, kv, kp};
+      const T cen[3] = {uc, vc, pc};
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const long long o = c * plane + q;
+        if constexpr (STAGE == ST_RHS) {
+          prm.kout[o] = kc[c];
+        } else if constexpr (STAGE == ST_FIRST) {
+          // acc = u + dt/6 k1 (FP32 compensated: acc = dt/6 k1), w = u + dt/2 k1
+          const T a = prm.compensated ? prm.c_acc * kc[c] : fma(prm.c_acc, kc[c], cen[c]);
+          st_stream(prm.acc + o, a);
+          st_stream(prm.wout + o, fma(prm.c_w, kc[c], cen[c]));
+        } else if constexpr (STAGE == ST_MID) {
+          const T u0 = ld_stream(prm.un + o);
+          const T a = ld_stream(prm.acc + o);
+          st_stream(prm.acc + o, fma(prm.c_acc, kc[c], a));
+          st_stream(prm.wout + o, fma(prm.c_w, kc[c], u0));
+        } else {  // ST_LAST
+          const T a = ld_stream(prm.acc + o);
+          const T d = fma(prm.c_acc, kc[c], a);
+          if (prm.compensated) {
+            // Kahan summation of the step increment into the FP32 state
+            const T u0 = prm.un[o], e = prm.comp[o];
+            const T yv = d - e;
+            const T tv = u0 + yv;
+            st_stream(prm.comp + o, (tv - u0) - yv);
+            st_stream(prm.un + o, tv);
+          } else {
+            st_stream(prm.un + o, d);
+          }
+        }
+      }
+    }
+  }
+}
+
+}  // namespace sbp

@@ -1,0 +1,239 @@
+"""ctypes binding of libsbpgpu.so (include/sbpgpu.h).
+
+This is the binding a Python caller of the reference's RHS-callback /
+ts_rk4 surface uses; it holds no numerics. Every compute call goes to the
+CUDA library, and loading fails loudly when the library is missing -- there
+is no CPU fallback.
+
+Arrays are numpy float64 in the reference's AoS layout (element (j, i, comp)
+at dofs*(i + nx*j) + comp); host arrays are passed with where=HOST. Device
+arrays (e.g. torch CUDA tensors) are passed by address with where=DEVICE.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "lib", "libsbpgpu.so")
+
+OK, ERR_INVALID, ERR_CUDA, ERR_DEVICE, ERR_UNSUPPORTED = 0, -1, -2, -3, -4
+WAVE_HOM_2D, WAVE_MMS_2D, ADVECTION_1D, ADVECTION_2D, REFLECTION_1D, WAVE_VAR_2D = 1, 2, 3, 4, 5, 6
+BC_REFERENCE, BC_CHARACTERISTIC = 0, 1
+FP64, FP32 = 0, 1
+HOST, DEVICE = 0, 1
+TWO_D = {WAVE_HOM_2D, WAVE_MMS_2D, WAVE_VAR_2D, ADVECTION_2D}
+DOFS = {WAVE_HOM_2D: 3, WAVE_MMS_2D: 3, WAVE_VAR_2D: 3, ADVECTION_1D: 1, ADVECTION_2D: 1, REFLECTION_1D: 2}
+
+# Every exported entry point of include/sbpgpu.h.
+EXPORTS = ("sbp_create", "sbp_destroy", "sbp_last_error", "sbp_dofs", "sbp_rhs", "sbp_apply", "sbp_rk4_nsteps",
+           "sbp_ts_rk4", "sbp_rk4", "sbp_set_state", "sbp_get_state", "sbp_rk4_resident", "sbp_synchronize",
+           "sbp_error_norms", "sbp_hnorm", "sbp_get_stream", "sbp_launch_count", "sbp_probe_dfma_rate")
+
+_dp = C.POINTER(C.c_double)
+
+
+class Desc(C.Structure):
+    _fields_ = [("problem", C.c_int), ("order", C.c_int), ("bc", C.c_int), ("precision", C.c_int),
+                ("nx", C.c_longlong), ("ny", C.c_longlong),
+                ("xl", C.c_double * 2), ("xr", C.c_double * 2),
+                ("a", C.c_double), ("b", C.c_double),
+                ("rho", _dp), ("K", _dp),
+                ("stream", C.c_void_p), ("device", C.c_int)]
+
+
+class SbpError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"libsbpgpu error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Load the CUDA library (once). Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError(f"{path} is missing: build it with `python hpc-reading-course_gb300/build.py` "
+                      "(the SBP hot path has no CPU implementation in the product)")
+    L = C.CDLL(path)
+    P = C.c_void_p
+    L.sbp_create.argtypes = [C.POINTER(Desc), C.POINTER(P)]
+    L.sbp_destroy.argtypes = [P]
+    L.sbp_last_error.argtypes = [P]
+    L.sbp_last_error.restype = C.c_char_p
+    L.sbp_dofs.argtypes = [P]
+    for n in ("sbp_rhs", "sbp_apply"):
+        getattr(L, n).argtypes = [P, C.c_double, C.c_void_p, C.c_void_p, C.c_int]
+    L.sbp_rk4_nsteps.argtypes = [C.c_double, _dp]
+    L.sbp_rk4_nsteps.restype = C.c_longlong
+    L.sbp_ts_rk4.argtypes = [P, C.c_double, C.c_double, C.c_void_p, C.c_int]
+    L.sbp_rk4.argtypes = [P, C.c_double, C.c_double, C.c_longlong, C.c_void_p, C.c_int]
+    L.sbp_set_state.argtypes = [P, C.c_void_p, C.c_int]
+    L.sbp_get_state.argtypes = [P, C.c_void_p, C.c_int]
+    L.sbp_rk4_resident.argtypes = [P, C.c_double, C.c_double, C.c_longlong]
+    L.sbp_synchronize.argtypes = [P]
+    L.sbp_error_norms.argtypes = [P, C.c_void_p, C.c_int, _dp, _dp]
+    L.sbp_hnorm.argtypes = [P, _dp]
+    L.sbp_get_stream.argtypes = [P, C.POINTER(C.c_void_p)]
+    L.sbp_launch_count.argtypes = [P]
+    L.sbp_launch_count.restype = C.c_longlong
+    L.sbp_probe_dfma_rate.argtypes = [C.c_int, _dp]
+    _lib = L
+    return L
+
+
+def rk4_nsteps(t_end: float, dt: float):
+    """The reference's step rule: (steps, adjusted dt)."""
+    d = C.c_double(dt)
+    n = load().sbp_rk4_nsteps(t_end, C.byref(d))
+    return n, d.value
+
+
+def probe_dfma_rate(device: int = 0) -> float:
+    r = C.c_double(0.0)
+    rc = load().sbp_probe_dfma_rate(device, C.byref(r))
+    if rc:
+        raise SbpError(rc, "DFMA probe failed")
+    return r.value
+
+
+def _host(a: np.ndarray) -> np.ndarray:
+    if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+        raise TypeError("host arrays must be C-contiguous float64")
+    return a
+
+
+class Context:
+    """One problem instance on one device (sbp_create / sbp_destroy)."""
+
+    def __init__(self, problem: int, order: int, nx: int, ny: int = 1, *, bc: int = BC_REFERENCE,
+                 precision: int = FP64, xl=(-1.0, -1.0), xr=(1.0, 1.0), a: float = 1.0, b: float = 0.0,
+                 rho=None, K=None, stream: int | None = None, device: int = 0):
+        L = load()
+        self._L = L
+        self.problem, self.order, self.nx = problem, order, nx
+        self.ny = ny if problem in TWO_D else 1
+        self.dofs = DOFS.get(problem, 0)
+        self.precision = precision
+        self.xl, self.xr = tuple(xl), tuple(xr)
+        self._rho = None if rho is None else np.ascontiguousarray(rho, dtype=np.float64).ravel()
+        self._K = None if K is None else np.ascontiguousarray(K, dtype=np.float64).ravel()
+        d = Desc(problem, order, bc, precision, nx, self.ny, (C.c_double * 2)(*xl), (C.c_double * 2)(*xr), a, b,
+                 None, None, stream, device)
+        if self._rho is not None:
+            d.rho = self._rho.ctypes.data_as(_dp)
+            d.K = self._K.ctypes.data_as(_dp)
+        h = C.c_void_p()
+        rc = L.sbp_create(C.byref(d), C.byref(h))
+        if rc:
+            raise SbpError(rc, L.sbp_last_error(None).decode())
+        self._h = h
+
+    # -- helpers
+    @property
+    def size(self) -> int:
+        return self.nx * self.ny * self.dofs
+
+    @property
+    def hx(self) -> float:
+        return (self.xr[0] - self.xl[0]) / (self.nx - 1)
+
+    @property
+    def hy(self) -> float:
+        return (self.xr[1] - self.xl[1]) / (self.ny - 1) if self.problem in TWO_D else 1.0
+
+    def _check(self, rc: int):
+        if rc:
+            raise SbpError(rc, self._L.sbp_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.sbp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- the reference surface
+    def rhs(self, src: np.ndarray, t: float = 0.0) -> np.ndarray:
+        """dst = F(t, src): the RHS callback body (host arrays)."""
+        src = _host(src)
+        dst = np.empty_like(src)
+        self._check(self._L.sbp_rhs(self._h, t, src.ctypes.data, dst.ctypes.data, HOST))
+        return dst
+
+    def apply(self, src: np.ndarray, t: float = 0.0) -> np.ndarray:
+        """The matrix-free apply without boundary terms (host arrays)."""
+        src = _host(src)
+        dst = np.empty_like(src)
+        self._check(self._L.sbp_apply(self._h, t, src.ctypes.data, dst.ctypes.data, HOST))
+        return dst
+
+    def rhs_ptr(self, t: float, src_ptr: int, dst_ptr: int, where: int):
+        self._check(self._L.sbp_rhs(self._h, t, src_ptr, dst_ptr, where))
+
+    def ts_rk4(self, v: np.ndarray, t_end: float, dt: float) -> np.ndarray:
+        out = np.array(_host(v), copy=True)
+        self._check(self._L.sbp_ts_rk4(self._h, t_end, dt, out.ctypes.data, HOST))
+        return out
+
+    def rk4(self, v: np.ndarray, t0: float, dt: float, nsteps: int) -> np.ndarray:
+        out = np.array(_host(v), copy=True)
+        self._check(self._L.sbp_rk4(self._h, t0, dt, nsteps, out.ctypes.data, HOST))
+        return out
+
+    def rk4_ptr(self, ptr: int, t0: float, dt: float, nsteps: int, where: int):
+        self._check(self._L.sbp_rk4(self._h, t0, dt, nsteps, ptr, where))
+
+    # -- resident state
+    def set_state(self, v: np.ndarray):
+        self._check(self._L.sbp_set_state(self._h, _host(v).ctypes.data, HOST))
+
+    def set_state_ptr(self, ptr: int, where: int):
+        self._check(self._L.sbp_set_state(self._h, ptr, where))
+
+    def get_state(self) -> np.ndarray:
+        out = np.empty(self.size)
+        self._check(self._L.sbp_get_state(self._h, out.ctypes.data, HOST))
+        return out
+
+    def step_resident(self, t0: float, dt: float, nsteps: int):
+        self._check(self._L.sbp_rk4_resident(self._h, t0, dt, nsteps))
+
+    def synchronize(self):
+        self._check(self._L.sbp_synchronize(self._h))
+
+    def error_norms(self, exact: np.ndarray):
+        l2, mx = C.c_double(), C.c_double()
+        self._check(self._L.sbp_error_norms(self._h, _host(exact).ctypes.data, HOST, C.byref(l2), C.byref(mx)))
+        return l2.value, mx.value
+
+    def hnorm(self) -> float:
+        h = C.c_double()
+        self._check(self._L.sbp_hnorm(self._h, C.byref(h)))
+        return h.value
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(self._L.sbp_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    @property
+    def launches(self) -> int:
+        return self._L.sbp_launch_count(self._h)

@@ -1,0 +1,145 @@
+/*
+ * sbpgpu.h -- C ABI of the GB300 (sm_103a) implementation of the matrix-free
+ * SBP-SAT hot path of VidarStiernstrom/HPC-reading-course: the right-hand
+ * side of first-order hyperbolic systems with summation-by-parts first
+ * derivatives of order 2, 4 or 6, SAT boundary terms, and the classical RK4
+ * time stepper that calls it.
+ *
+ * Library: hpc-reading-course_gb300/lib/libsbpgpu.so. Plain C types only.
+ * Every function returns an int status (SBP_OK = 0, negative on error) and
+ * never throws; sbp_last_error() gives the message of the last failure on a
+ * context. A context is bound to one CUDA stream and one device; calls on one
+ * context must not run concurrently (as the reference's callbacks, which run
+ * one per MPI rank).
+ *
+ * Array format at the boundary is the reference's: FP64, array-of-structs,
+ * element (j, i, comp) at dofs*(i + nx*j) + comp (code/include/grids/layout.h:124-127;
+ * 1D: layout.h:65-68), the layout a single-rank PETSc DMDA vector has.
+ * `where` says whether such an array is in host memory (SBP_HOST) or device
+ * memory (SBP_DEVICE). Inside the library the state is device-resident
+ * structure-of-arrays with padded rows.
+ */
+#ifndef SBPGPU_H
+#define SBPGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SBP_OK 0
+#define SBP_ERR_INVALID (-1)     /* bad argument (size, order, pointer, problem) */
+#define SBP_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define SBP_ERR_DEVICE (-3)      /* a kernel reported an error (e.g. a bounded wait gave up) */
+#define SBP_ERR_UNSUPPORTED (-4) /* combination not provided (e.g. FP32 manufactured-solution problem) */
+
+/* Problems: the reference demos plus the variable-coefficient wave system. */
+typedef enum {
+  SBP_WAVE_HOM_2D = 1,   /* code/demo/wave_hom: (u,v,p), rho = K = 1 */
+  SBP_WAVE_MMS_2D = 2,   /* code/demo/wave: rho^-1 = 1/(2+xy), manufactured forcing */
+  SBP_ADVECTION_1D = 3,  /* code/demo/advection, u_t + a u_x = 0 */
+  SBP_ADVECTION_2D = 4,  /* code/demo/advection, u_t + a u_x + b u_y = 0 */
+  SBP_REFLECTION_1D = 5, /* code/demo/reflection, [u;v]_t = [v_x;u_x] */
+  SBP_WAVE_VAR_2D = 6    /* (u,v,p) with rho(x,y), K(x,y) fields; no reference counterpart */
+} sbp_problem;
+
+typedef enum {
+  SBP_BC_REFERENCE = 0,      /* the demo's own boundary treatment: free-surface SAT
+                                (wave), inflow SAT (advection), projection (reflection) */
+  SBP_BC_CHARACTERISTIC = 1  /* wave problems: non-reflecting SAT on p + Z u_n */
+} sbp_bc;
+
+typedef enum { SBP_FP64 = 0, SBP_FP32 = 1 } sbp_precision;
+typedef enum { SBP_HOST = 0, SBP_DEVICE = 1 } sbp_where;
+
+typedef struct sbp_ctx sbp_ctx;
+
+/* Problem description; the fields play the role of the reference's AppCtx
+ * (code/demo/wave_hom/wave_eq_hom_sim.cpp:36-45) plus the compile-time order
+ * of op_defs.h (code/include/sbpops/op_defs.h:7-30). */
+typedef struct {
+  int problem;        /* sbp_problem */
+  int order;          /* 2, 4 or 6 */
+  int bc;             /* sbp_bc */
+  int precision;      /* sbp_precision: SBP_FP32 keeps an FP32 state with a
+                         compensated (Kahan) RK4 update; SAT weights and all
+                         norms stay FP64 */
+  long long nx, ny;   /* grid points per direction (ny ignored in 1D) */
+  double xl[2], xr[2];/* domain [xl, xr]; h = (xr - xl)/(N - 1) as the demos */
+  double a, b;        /* advection velocities (x, y) */
+  const double* rho;  /* SBP_WAVE_VAR_2D: host array of nx*ny densities, (j,i) row-major */
+  const double* K;    /* SBP_WAVE_VAR_2D: host array of nx*ny bulk moduli */
+  void* stream;       /* cudaStream_t to run on, or NULL for a private stream */
+  int device;         /* CUDA device ordinal */
+} sbp_desc;
+
+/* Creates a context: validates the description (N >= max(closure width,
+ * 2*closure size) per direction), allocates the device state and scratch,
+ * builds the TMA descriptors. Replaces the DMDA/AppCtx set-up of the demos'
+ * main() (e.g. wave_eq_hom_sim.cpp:99-134). */
+int sbp_create(const sbp_desc* desc, sbp_ctx** ctx);
+int sbp_destroy(sbp_ctx* ctx);
+const char* sbp_last_error(const sbp_ctx* ctx);
+/* Scalars per grid point of the context's problem (3, 2 or 1). */
+int sbp_dofs(const sbp_ctx* ctx);
+
+/* RHS callback body: dst = F(t, src) = matrix-free apply + boundary terms.
+ * Replaces PetscErrorCode rhs_serial(TS, PetscReal t, Vec src, Vec dst, void*)
+ * (code/demo/wave_hom/wave_eq_hom_sim.cpp:291-308; wave_eq_sim.cpp:291-308;
+ * advection_1D_sim.cpp:212-228; advection_2D_sim.cpp:232-249;
+ * reflection_sim.cpp:249-265). Synchronous. */
+int sbp_rhs(sbp_ctx* ctx, double t, const double* src, double* dst, int where);
+
+/* Matrix-free apply without boundary terms: wave_eq_hom_serial
+ * (wave_eq_hom_rhs.h:365), wave_eq_serial (wave_eq_rhs.h:389),
+ * advection_serial (advection_rhs.h:83,440), reflection_serial
+ * (reflection_rhs.h:98). Synchronous. */
+int sbp_apply(sbp_ctx* ctx, double t, const double* src, double* dst, int where);
+
+/* Step count rule of the reference's RK4: round(t_end/dt) steps; dt is
+ * replaced by t_end/steps when the two disagree by more than 1e-14
+ * (code/include/time_stepping/time_stepping.h:104-109). */
+long long sbp_rk4_nsteps(double t_end, double* dt);
+
+/* Classical RK4 from t = 0 to t_end in place on v: the time-stepper entry
+ * PetscErrorCode ts_rk4(DM, t_end, dt, Vec v, rhs, ctx)
+ * (code/src/time_stepping/ts_rk.cpp:54-65), with the step rule above.
+ * Copies v in, runs the CUDA-graph step loop, copies v out. Synchronous. */
+int sbp_ts_rk4(sbp_ctx* ctx, double t_end, double dt, double* v, int where);
+
+/* nsteps classical RK4 steps of size dt from t0, in place on v. Synchronous. */
+int sbp_rk4(sbp_ctx* ctx, double t0, double dt, long long nsteps, double* v, int where);
+
+/* Device-resident state: load / read back the context's state, and step it
+ * without host transfers. sbp_rk4_resident only enqueues work on the
+ * context's stream; sbp_synchronize waits and reports kernel errors. */
+int sbp_set_state(sbp_ctx* ctx, const double* v, int where);
+int sbp_get_state(sbp_ctx* ctx, double* v, int where);
+int sbp_rk4_resident(sbp_ctx* ctx, double t0, double dt, long long nsteps);
+int sbp_synchronize(sbp_ctx* ctx);
+
+/* Norms of the resident state, reduced on the device in FP64.
+ * error_l2 = sqrt(prod h) * ||state - exact||_2 and error_max = ||state - exact||_inf
+ * over every component (error_l2 / error_max, code/include/util/vec_util.h:47-61);
+ * exact is an AoS FP64 array (host or device). */
+int sbp_error_norms(sbp_ctx* ctx, const double* exact, int where, double* error_l2, double* error_max);
+/* Energy norm sqrt(sum_comp v^T H v) with the closure quadrature at both ends
+ * of each direction (tensor product in 2D). The 1D form extends
+ * H_central::get_norm_1D (code/include/sbpops/H_central.h:70-103), which on a
+ * single rank applies the left closure weights only; the 2D form is
+ * get_norm_2D, a TODO returning -1 in the reference (H_central.h:177-183). */
+int sbp_hnorm(sbp_ctx* ctx, double* hnorm);
+
+/* The context's CUDA stream (cudaStream_t) and the number of kernels the
+ * context has launched so far (graph replays count each kernel node). */
+int sbp_get_stream(const sbp_ctx* ctx, void** stream);
+long long sbp_launch_count(const sbp_ctx* ctx);
+
+/* Measured FP64 FMA throughput of the current device in DFMA/s (a
+ * 1-second-scale probe). No counterpart in the reference; used to state the
+ * FP64 ALU roof beside the HBM roof. */
+int sbp_probe_dfma_rate(int device, double* dfma_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SBPGPU_H */

@@ -1,0 +1,85 @@
+"""Generate tests/golden/ref_rhs.npz from the reference's own headers.
+
+Runs where the reference checkout exists (it builds oracle/_ref from the
+headers where they lie, against the shims in oracle/shim/) and records, for
+seeded inputs, the output of the reference's RHS callback body
+(``*_serial`` followed by ``*_bc_serial``) and of ``H_central::get_norm_1D``.
+The fixtures travel with the repository; the reference checkout does not.
+
+    python tests/golden/make_golden.py [--ref-dir PATH]
+
+Reference defects visible in the fixtures (kept as they are, documented in
+the tests): the 1D advection right SAT and the 2D advection south SAT read
+``closure_invquad`` out of bounds (code/demo/advection/advection_rhs.h:118,490),
+so those boundary entries may be non-finite.
+"""
+import argparse
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle as O  # noqa: E402
+
+MIN_N = {2: 3, 4: 8, 6: 12}
+
+
+def cases():
+    """(name, problem, order, n, a, b, t, input kind) for every fixture."""
+    out = []
+    for order in (2, 4, 6):
+        for n in sorted({MIN_N[order], 13, 33}):
+            for prob in (O.WAVE_HOM_2D, O.WAVE_MMS_2D):
+                out.append((prob, order, n, 0.0, 0.0, 0.37, "random"))
+            out.append((O.WAVE_HOM_2D, order, n, 0.0, 0.0, 0.0, "mms"))
+            out.append((O.ADVECTION_2D, order, n, 1.5, -1.0, 0.0, "random"))
+        for n in sorted({MIN_N[order], 33, 201}):
+            out.append((O.ADVECTION_1D, order, n, 1.0, 0.0, 0.0, "random"))
+            out.append((O.ADVECTION_1D, order, n, 1.5, 0.0, 0.0, "gauss"))
+            out.append((O.REFLECTION_1D, order, n, 0.0, 0.0, 0.0, "random"))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref-dir", default="/root/reference")
+    ap.add_argument("--out", default=os.path.join(HERE, "ref_rhs.npz"))
+    args = ap.parse_args()
+    O.build(ref_dir=args.ref_dir)
+    if not O.Reference.available():
+        sys.exit("oracle/_ref was not built: the reference checkout is needed")
+    ref, port = O.Reference(), O.Port()
+    rng = np.random.default_rng(20261203)
+    blobs = {}
+    meta = []
+    for k, (prob, order, n, a, b, t, kind) in enumerate(cases()):
+        pb = O.Problem(prob, order, n, n, a=a, b=b)
+        if kind == "random":
+            src = rng.standard_normal(pb.size)
+        elif kind == "mms":
+            src = port.init_wave_mms(n, n, 0.21)
+        else:
+            src = port.init_adv1d(n, a, 0.0)
+        dst = ref.rhs(pb, src, t=t)
+        blobs[f"src{k}"] = src
+        blobs[f"dst{k}"] = dst
+        meta.append([prob, order, n, a, b, t])
+    # get_norm_1D on one rank: left-closure weights only (H_central.h:70-103)
+    hn = []
+    for order in (2, 4, 6):
+        for n, dofs in ((MIN_N[order], 1), (50, 2), (201, 1)):
+            v = rng.standard_normal(n * dofs)
+            h = 2.0 / (n - 1)
+            blobs[f"hn_v{len(hn)}"] = v
+            hn.append([order, n, dofs, h, ref.hnorm1d(v, n, dofs, h, order)])
+    blobs["meta"] = np.array(meta, dtype=np.float64)
+    blobs["hnorm"] = np.array(hn, dtype=np.float64)
+    np.savez_compressed(args.out, **blobs)
+    print(f"wrote {len(meta)} RHS cases and {len(hn)} H-norm cases to {args.out}")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,252 @@
+"""Parity of the CUDA path (called through the C ABI) with the oracle.
+
+Tolerance (FP64): norm-wise relative max error ||gpu - oracle||_inf / ||oracle||_inf
+<= 1e-12. The GPU folds 1/h into the stencil weights and contracts products
+into FMAs, so results differ from the reference's rounding in the last bits;
+the stencil sums cancel, so the bound is norm-wise, not pointwise.
+FP32 state: <= 1e-5 relative for one RHS (stencil arithmetic in FP32).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 1e-5
+
+
+def relerr(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def _fields(n_x, n_y, seed):
+    rng = np.random.default_rng(seed)
+    x = np.linspace(-1, 1, n_x)
+    y = np.linspace(-1, 1, n_y)
+    X, Y = np.meshgrid(x, y)
+    rho = 1.0 + 0.4 * np.tanh(np.sin(3 * X + rng.uniform()) * np.cos(2 * Y))
+    K = 1.2 + 0.5 * np.tanh(np.cos(2 * X - Y + rng.uniform()))
+    return rho.ravel(), K.ravel()
+
+
+def _ctx(sbp, prob, order, nx, ny, **kw):
+    return sbp.Context(prob, order, nx, ny, **kw)
+
+
+SIZES_2D = [(None, None), (33, 33), (64, 64), (97, 45), (130, 71)]
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+@pytest.mark.parametrize("size", SIZES_2D)
+def test_wave_hom_rhs(sbp, port, order, size):
+    nx, ny = size
+    if nx is None:
+        nx = ny = {2: 3, 4: 8, 6: 12}[order]
+    rng = np.random.default_rng(order * 1000 + nx)
+    src = rng.standard_normal(3 * nx * ny)
+    pb = O.Problem(O.WAVE_HOM_2D, order, nx, ny)
+    with _ctx(sbp, sbp.WAVE_HOM_2D, order, nx, ny) as c:
+        assert relerr(c.rhs(src), port.rhs(pb, src)) <= TOL64
+        assert relerr(c.apply(src), port.apply(pb, src)) <= TOL64
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+@pytest.mark.parametrize("size", [(33, 33), (70, 41)])
+def test_wave_mms_rhs(sbp, port, order, size):
+    nx, ny = size
+    rng = np.random.default_rng(5 + order)
+    src = rng.standard_normal(3 * nx * ny)
+    pb = O.Problem(O.WAVE_MMS_2D, order, nx, ny)
+    with _ctx(sbp, sbp.WAVE_MMS_2D, order, nx, ny) as c:
+        for t in (0.0, 0.37):
+            assert relerr(c.rhs(src, t), port.rhs(pb, src, t)) <= TOL64
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+@pytest.mark.parametrize("bc", [0, 1])
+@pytest.mark.parametrize("size", [(37, 37), (129, 66)])
+def test_wave_var_rhs(sbp, port, order, bc, size):
+    nx, ny = size
+    rho, K = _fields(nx, ny, order + 10 * bc)
+    rng = np.random.default_rng(11)
+    src = rng.standard_normal(3 * nx * ny)
+    pb = O.Problem(O.WAVE_VAR_2D, order, nx, ny, rho=rho, K=K, bc=bc)
+    with _ctx(sbp, sbp.WAVE_VAR_2D, order, nx, ny, rho=rho, K=K, bc=bc) as c:
+        assert relerr(c.rhs(src), port.rhs(pb, src)) <= TOL64
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+def test_wave_hom_characteristic_matches_unit_coefficients(sbp, port, order):
+    nx, ny = 75, 40
+    ones = np.ones(nx * ny)
+    src = np.random.default_rng(2).standard_normal(3 * nx * ny)
+    pb = O.Problem(O.WAVE_VAR_2D, order, nx, ny, rho=ones, K=ones, bc=O.BC_CHARACTERISTIC)
+    with _ctx(sbp, sbp.WAVE_HOM_2D, order, nx, ny, bc=sbp.BC_CHARACTERISTIC) as c:
+        assert relerr(c.rhs(src), port.rhs(pb, src)) <= TOL64
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+@pytest.mark.parametrize("n", [None, 33, 201])
+def test_advection_1d_rhs(sbp, port, order, n):
+    n = n or {2: 3, 4: 8, 6: 12}[order]
+    for a in (1.0, 1.5, -0.8):
+        src = np.random.default_rng(n).standard_normal(n)
+        pb = O.Problem(O.ADVECTION_1D, order, n, a=a)
+        with _ctx(sbp, sbp.ADVECTION_1D, order, n, a=a) as c:
+            assert relerr(c.rhs(src), port.rhs(pb, src)) <= TOL64
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+@pytest.mark.parametrize("size", [(12, 12), (33, 33), (80, 47)])
+def test_advection_2d_rhs(sbp, port, order, size):
+    nx, ny = size
+    if nx < {2: 3, 4: 8, 6: 12}[order]:
+        pytest.skip("below minimum size")
+    src = np.random.default_rng(nx * ny).standard_normal(nx * ny)
+    for a, b in ((1.5, -1.0), (-0.5, 0.7)):
+        pb = O.Problem(O.ADVECTION_2D, order, nx, ny, a=a, b=b)
+        with _ctx(sbp, sbp.ADVECTION_2D, order, nx, ny, a=a, b=b) as c:
+            assert relerr(c.rhs(src), port.rhs(pb, src)) <= TOL64
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+@pytest.mark.parametrize("n", [None, 40, 201])
+def test_reflection_rhs(sbp, port, order, n):
+    n = n or {2: 3, 4: 8, 6: 12}[order]
+    src = np.random.default_rng(n + 1).standard_normal(2 * n)
+    pb = O.Problem(O.REFLECTION_1D, order, n)
+    with _ctx(sbp, sbp.REFLECTION_1D, order, n) as c:
+        assert relerr(c.rhs(src), port.rhs(pb, src)) <= TOL64
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+@pytest.mark.parametrize("prob", ["hom", "var_char", "mms"])
+def test_rk4_steps_match_oracle(sbp, port, order, prob):
+    nx, ny = 90, 77
+    h = 2.0 / (nx - 1)
+    kw, okw = {}, {}
+    if prob == "var_char":
+        rho, K = _fields(nx, ny, 3)
+        kw = dict(rho=rho, K=K, bc=1)
+        okw = dict(rho=rho, K=K, bc=1)
+        P, OP = sbp.WAVE_VAR_2D, O.WAVE_VAR_2D
+    elif prob == "mms":
+        P, OP = sbp.WAVE_MMS_2D, O.WAVE_MMS_2D
+    else:
+        P, OP = sbp.WAVE_HOM_2D, O.WAVE_HOM_2D
+    v0 = port.init_wave_pulse(nx, ny, 0.1, -0.2, 0.3, 1.0) + 0.1 * port.init_wave_mms(nx, ny, 0.05)
+    dt = 0.2 * h
+    pb = O.Problem(OP, order, nx, ny, **okw)
+    with _ctx(sbp, P, order, nx, ny, **kw) as c:
+        # 57 steps: one 50-step graph chunk plus a 7-step chunk
+        got = c.rk4(v0, 0.0, dt, 57)
+    ref = port.rk4(pb, v0, 0.0, dt, 57)
+    assert relerr(got, ref) <= TOL64
+
+
+@pytest.mark.parametrize("prob", ["adv1d", "adv2d", "refl"])
+def test_rk4_line_problems_match_oracle(sbp, port, prob):
+    order = 4
+    if prob == "adv1d":
+        n = 201
+        c = sbp.Context(sbp.ADVECTION_1D, order, n, a=1.0)
+        pb = O.Problem(O.ADVECTION_1D, order, n, a=1.0)
+        v0 = port.init_adv1d(n, 1.0, 0.0)
+    elif prob == "adv2d":
+        n = 65
+        c = sbp.Context(sbp.ADVECTION_2D, order, n, n, a=1.5, b=-1.0)
+        pb = O.Problem(O.ADVECTION_2D, order, n, n, a=1.5, b=-1.0)
+        v0 = port.init_adv2d(n, n, 1.5, -1.0, 0.0)
+    else:
+        n = 101
+        c = sbp.Context(sbp.REFLECTION_1D, order, n)
+        pb = O.Problem(O.REFLECTION_1D, order, n)
+        v0 = port.init_reflection(n, 0.0)
+    dt = 0.1 * 2.0 / (n - 1)
+    with c:
+        got = c.rk4(v0, 0.0, dt, 120)
+    assert relerr(got, port.rk4(pb, v0, 0.0, dt, 120)) <= TOL64
+
+
+def test_kat_advection_config_on_gpu(sbp, port):
+    """BASELINE config 1 through ts_rk4's replacement: L2 = 3.930261e-04."""
+    n, a = 201, 1.0
+    with sbp.Context(sbp.ADVECTION_1D, 4, n, a=a) as c:
+        v = c.ts_rk4(port.init_adv1d(n, a, 0.0), 1.8, 0.1 * 2.0 / (n - 1))
+        c.set_state(v)
+        l2, mx = c.error_norms(port.init_adv1d(n, a, 1.8))
+    assert l2 == pytest.approx(3.930261e-04, rel=1e-6)
+    assert mx == pytest.approx(9.271863e-04, rel=1e-6)
+
+
+@pytest.mark.parametrize("order,expected", [(2, 1.113e-1), (4, 4.090e-3), (6, 5.975e-3)])
+def test_kat_wave_mms_on_gpu(sbp, port, order, expected):
+    n, T = 81, 0.5
+    h = 2.0 / (n - 1)
+    with sbp.Context(sbp.WAVE_HOM_2D, order, n, n) as c:
+        v = c.ts_rk4(port.init_wave_mms(n, n, 0.0), T, 0.2 * h)
+        c.set_state(v)
+        l2, _ = c.error_norms(port.init_wave_mms(n, n, T))
+    assert l2 == pytest.approx(expected, rel=2e-3)
+
+
+def test_device_norms_match_oracle(sbp, port):
+    nx, ny, order = 150, 97, 6
+    rng = np.random.default_rng(9)
+    v, ex = rng.standard_normal(3 * nx * ny), rng.standard_normal(3 * nx * ny)
+    hx, hy = 2.0 / (nx - 1), 2.0 / (ny - 1)
+    with sbp.Context(sbp.WAVE_HOM_2D, order, nx, ny) as c:
+        c.set_state(v)
+        l2, mx = c.error_norms(ex)
+        hn = c.hnorm()
+    assert l2 == pytest.approx(port.error_l2(v, ex, hx * hy), rel=1e-13)
+    assert mx == port.error_max(v, ex)
+    assert hn == pytest.approx(port.hnorm(v, nx, ny, 3, hx, hy, order), rel=1e-13)
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+def test_fp32_rhs(sbp, port, order):
+    nx, ny = 101, 88
+    x = np.linspace(-1, 1, nx)
+    y = np.linspace(-1, 1, ny)
+    X, Y = np.meshgrid(x, y)
+    src = np.stack([np.sin(2 * X) * np.cos(Y), np.cos(X + Y), np.exp(-4 * (X**2 + Y**2))], axis=-1).ravel()
+    pb = O.Problem(O.WAVE_HOM_2D, order, nx, ny)
+    with _ctx(sbp, sbp.WAVE_HOM_2D, order, nx, ny, precision=sbp.FP32) as c:
+        assert relerr(c.rhs(src), port.rhs(pb, src)) <= TOL32
+
+
+def test_fp32_compensated_rk4_close_to_fp64(sbp, port):
+    n, order = 257, 4
+    h = 2.0 / (n - 1)
+    v0 = port.init_wave_pulse(n, n, 0.0, 0.0, 0.1, 1.0)
+    with sbp.Context(sbp.WAVE_HOM_2D, order, n, n, bc=1) as c64, \
+            sbp.Context(sbp.WAVE_HOM_2D, order, n, n, bc=1, precision=sbp.FP32) as c32:
+        a = c64.rk4(v0, 0.0, 0.2 * h, 400)
+        b = c32.rk4(v0, 0.0, 0.2 * h, 400)
+    assert relerr(b, a) < 2e-5
+
+
+def test_large_grid_energy_and_symmetry(sbp, port):
+    """At a production size (1024^2, order 4) with the characteristic SAT:
+    the discrete energy never grows, and a centred pulse stays symmetric in p
+    under x -> -x (exact for the symmetric operator pair)."""
+    n, order = 1024, 4
+    h = 2.0 / (n - 1)
+    v = port.init_wave_pulse(n, n, 0.0, 0.0, 0.05, 1.0)
+    ones = np.ones(n * n)
+    with sbp.Context(sbp.WAVE_HOM_2D, order, n, n, bc=1) as c:
+        c.set_state(v)
+        e_prev = c.hnorm()
+        for _ in range(5):
+            c.step_resident(0.0, 0.2 * h, 40)
+            c.synchronize()
+            e = c.hnorm()
+            assert np.isfinite(e) and e <= e_prev * (1 + 1e-12)
+            e_prev = e
+        out = c.get_state().reshape(n, n, 3)
+    p = out[:, :, 2]
+    assert np.max(np.abs(p - p[:, ::-1])) <= 1e-10 * np.max(np.abs(p))
+    assert np.max(np.abs(p - p.T)) <= 1e-10 * np.max(np.abs(p))
