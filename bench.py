@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=4096)
+    ap.add_argument("--grid", type=int, default=4096)
     ap.add_argument("--order", type=int, default=4, choices=[2, 4, 6])
     ap.add_argument("--rk-steps", type=int, default=1000)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
@@ -185,7 +185,7 @@ def run_reference(args, rank: int):
     if rank != 0:
         return
     budget = 3.0
-    rates, kind, threads, sample = cpu_baseline(args.n, args.order, args.precision, args.bc, budget,
+    rates, kind, threads, sample = cpu_baseline(args.grid, args.order, args.precision, args.bc, budget,
                                                 repeats=args.warmup + args.steps)
     timed = rates[args.warmup:]
     value = statistics.median(timed)
@@ -201,12 +201,12 @@ def run_reference(args, rank: int):
 
 
 def config_of(args):
-    return {"workload": f"2D acoustic wave (u,v,p), rho=K=1, {args.n}x{args.n}, SBP order {args.order}, "
+    return {"workload": f"2D acoustic wave (u,v,p), rho=K=1, {args.grid}x{args.grid}, SBP order {args.order}, "
                         f"{args.bc} SAT, {args.precision.upper()}, Gaussian pulse w=0.05, dt=0.2h, "
                         f"{args.rk_steps} RK4 steps per bench step",
-            "grid": [args.n, args.n], "order": args.order, "rk4_steps_per_step": args.rk_steps,
+            "grid": [args.grid, args.grid], "order": args.order, "rk4_steps_per_step": args.rk_steps,
             "precision": args.precision, "bc": args.bc,
-            "l2_flush": f"inputs larger than L2: {args.n * args.n * 3 * (8 if args.precision == 'fp64' else 4) / 1e6:.0f}"
+            "l2_flush": f"inputs larger than L2: {args.grid * args.grid * 3 * (8 if args.precision == 'fp64' else 4) / 1e6:.0f}"
                         " MB per state vector, 4 state vectors",
             "parallelism": f"replicas x{args.gpus}"}
 
@@ -246,7 +246,7 @@ def main():
         dist.barrier()
     gpu_build.build()
     torch.cuda.set_device(local)
-    n, order = args.n, args.order
+    n, order = args.grid, args.order
     prec = sbpgpu.FP64 if args.precision == "fp64" else sbpgpu.FP32
     bc = sbpgpu.BC_CHARACTERISTIC if args.bc == "characteristic" else sbpgpu.BC_REFERENCE
     h = 2.0 / (n - 1)

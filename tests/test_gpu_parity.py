@@ -31,7 +31,7 @@ def _fields(n_x, n_y, seed):
     return rho.ravel(), K.ravel()
 
 
-def _ctx(sbp, prob, order, nx, ny, **kw):
+def _ctx(sbp, prob, order, nx, ny=1, **kw):
     return sbp.Context(prob, order, nx, ny, **kw)
 
 
