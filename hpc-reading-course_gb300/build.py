@@ -41,6 +41,7 @@ def units():
         out.append((f"wave2d_o{order}.o", "wave2d_inst.cu", [f"-DSBP_ORDER={order}"]))
     out.append(("kernels.o", "kernels.cu", []))
     out.append(("sbp_runtime.o", "sbp_runtime.cpp", ["-x", "cu"]))
+    out.append(("noalloc.o", "noalloc.cu", []))
     return out
 
 

@@ -19,7 +19,8 @@ import numpy as np
 PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG, "lib", "libsbpgpu.so")
 
-OK, ERR_INVALID, ERR_CUDA, ERR_DEVICE, ERR_UNSUPPORTED = 0, -1, -2, -3, -4
+OK, ERR_INVALID, ERR_CUDA, ERR_DEVICE, ERR_UNSUPPORTED, ERR_TOO_LARGE = 0, -1, -2, -3, -4, -5
+NOALLOC_MAX_PLANE = 65536
 WAVE_HOM_2D, WAVE_MMS_2D, ADVECTION_1D, ADVECTION_2D, REFLECTION_1D, WAVE_VAR_2D = 1, 2, 3, 4, 5, 6
 BC_REFERENCE, BC_CHARACTERISTIC = 0, 1
 FP64, FP32 = 0, 1
@@ -30,7 +31,8 @@ DOFS = {WAVE_HOM_2D: 3, WAVE_MMS_2D: 3, WAVE_VAR_2D: 3, ADVECTION_1D: 1, ADVECTI
 # Every exported entry point of include/sbpgpu.h.
 EXPORTS = ("sbp_create", "sbp_destroy", "sbp_last_error", "sbp_dofs", "sbp_rhs", "sbp_apply", "sbp_rk4_nsteps",
            "sbp_ts_rk4", "sbp_rk4", "sbp_set_state", "sbp_get_state", "sbp_rk4_resident", "sbp_synchronize",
-           "sbp_error_norms", "sbp_hnorm", "sbp_get_stream", "sbp_launch_count", "sbp_probe_dfma_rate")
+           "sbp_error_norms", "sbp_hnorm", "sbp_get_stream", "sbp_launch_count", "sbp_probe_dfma_rate",
+           "sbp_wave_rhs_noalloc")
 
 _dp = C.POINTER(C.c_double)
 
@@ -84,6 +86,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.sbp_launch_count.argtypes = [P]
     L.sbp_launch_count.restype = C.c_longlong
     L.sbp_probe_dfma_rate.argtypes = [C.c_int, _dp]
+    L.sbp_wave_rhs_noalloc.argtypes = [C.POINTER(Desc), C.c_double, C.c_void_p, C.c_void_p]
     _lib = L
     return L
 
@@ -101,6 +104,15 @@ def probe_dfma_rate(device: int = 0) -> float:
     if rc:
         raise SbpError(rc, "DFMA probe failed")
     return r.value
+
+
+def wave_rhs_noalloc(order: int, nx: int, ny: int, t: float, src_ptr: int, dst_ptr: int, *,
+                     bc: int = BC_REFERENCE, xl=(-1.0, -1.0), xr=(1.0, 1.0), stream: int | None = None,
+                     device: int = 0) -> int:
+    """sbp_wave_rhs_noalloc on caller-owned device arrays; returns the status code."""
+    d = Desc(WAVE_HOM_2D, order, bc, FP64, nx, ny, (C.c_double * 2)(*xl), (C.c_double * 2)(*xr), 0.0, 0.0,
+             None, None, stream, device)
+    return load().sbp_wave_rhs_noalloc(C.byref(d), t, src_ptr, dst_ptr)
 
 
 def _host(a: np.ndarray) -> np.ndarray:

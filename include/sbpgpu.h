@@ -31,6 +31,7 @@ extern "C" {
 #define SBP_ERR_CUDA (-2)        /* a CUDA runtime call failed */
 #define SBP_ERR_DEVICE (-3)      /* a kernel reported an error (e.g. a bounded wait gave up) */
 #define SBP_ERR_UNSUPPORTED (-4) /* combination not provided (e.g. FP32 manufactured-solution problem) */
+#define SBP_ERR_TOO_LARGE (-5)   /* grid exceeds the static scratch of sbp_wave_rhs_noalloc */
 
 /* Problems: the reference demos plus the variable-coefficient wave system. */
 typedef enum {
@@ -138,6 +139,34 @@ long long sbp_launch_count(const sbp_ctx* ctx);
  * 1-second-scale probe). No counterpart in the reference; used to state the
  * FP64 ALU roof beside the HBM roof. */
 int sbp_probe_dfma_rate(int device, double* dfma_per_s);
+
+/* RHS of the 2D acoustic wave system (rho = K = 1, FP64) that allocates no
+ * device memory. It has no counterpart in the reference.
+ *
+ * sbp_rhs needs a context, and a context's staging buffers come from
+ * cudaMalloc. Some callers cannot allocate: a host framework that owns all
+ * device memory through its own pool and forbids plugins to call cudaMalloc,
+ * or a caller in a latency-bound loop that cannot take cudaMalloc's implicit
+ * device synchronisation. This entry point computes what sbp_rhs computes for
+ * that problem (free-surface or characteristic SAT, orders 2/4/6) with its
+ * scratch in one fixed-size static device array that every GPU loading the
+ * library holds until exit: 6 * SBP_NOALLOC_MAX_PLANE doubles (3 MiB) plus an
+ * error word.
+ *
+ * desc: problem SBP_WAVE_HOM_2D, precision SBP_FP64, order, bc, nx, ny, xl, xr,
+ *       device, stream (NULL = the legacy default stream); rho, K, a, b unused.
+ * src, dst: caller-owned DEVICE arrays of nx*ny*3 doubles in the reference's
+ *       AoS layout. Synchronous on desc->stream.
+ * Limit: roundup(nx, 64) * ny <= SBP_NOALLOC_MAX_PLANE (e.g. 256 x 256);
+ *       larger grids return SBP_ERR_TOO_LARGE before any GPU work.
+ * Sharing: all calls on a device use the same array; the error word is
+ *       cleared by each call, the rest is overwritten. Calls whose GPU work
+ *       overlaps (other streams or threads) race on the array: serialise them.
+ * First call on a device: does a one-time set-up on that device (the array's
+ *       device address, the kernels' shared-memory opt-in); make it before
+ *       any stream capture. */
+#define SBP_NOALLOC_MAX_PLANE 65536
+int sbp_wave_rhs_noalloc(const sbp_desc* desc, double t, const double* src, double* dst);
 
 #ifdef __cplusplus
 }
