@@ -37,6 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "hpc-reading-course_gb300")
 sys.path.insert(0, os.path.join(PKG, "python"))
 sys.path.insert(0, PKG)
+import fields  # noqa: E402  (seeded inputs: initial data and coefficient fields)
 
 METRIC = "RK4 point-updates/s"
 UNIT = "grid-point stage updates/s"
@@ -55,18 +56,16 @@ def parse():
     ap.add_argument("--bc", default="characteristic", choices=["characteristic", "free_surface"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--study", default=None, choices=["precision"],
+                    help="precision: variable rho, K (seeded Fourier fields) to --t-end in FP64 and in "
+                         "compensated FP32; prints errors of FP32 against FP64 and both wall times")
+    ap.add_argument("--t-end", type=float, default=1.0)
     return ap.parse_args()
 
 
 def initial_state(n: int):
     """Gaussian pressure pulse exp(-(x^2+y^2)/0.05^2), u = v = 0, AoS (j, i, comp)."""
-    import numpy as np
-
-    x = np.linspace(-1.0, 1.0, n)
-    p = np.exp(-(x[None, :] ** 2 + x[:, None] ** 2) / 0.05**2)
-    v = np.zeros((n, n, 3))
-    v[:, :, 2] = p
-    return v.ravel()
+    return fields.gaussian_pulse(n, n, 0.0, 0.0, 0.05, 1.0)
 
 
 class ClockSampler:
@@ -211,8 +210,57 @@ def config_of(args):
             "parallelism": f"replicas x{args.gpus}"}
 
 
+def run_precision_study(args):
+    """Variable rho, K = 1 + 0.5 tanh(8 seeded Fourier modes, |k| <= 6) (seeds 0, 1), pulse at the
+    origin, characteristic SAT, CFL 0.2 on the largest wave speed, to t_end: FP32 (compensated) vs FP64."""
+    import numpy as np
+    import torch
+
+    import build as gpu_build
+    import fields
+    import sbpgpu
+
+    gpu_build.build()
+    n, order = args.grid, args.order
+    rho, K = fields.fourier_field(n, 0), fields.fourier_field(n, 1)
+    h = 2.0 / (n - 1)
+    cmax = float(np.sqrt((K / rho).max()))
+    nsteps, dt = sbpgpu.rk4_nsteps(args.t_end, 0.2 * h / cmax)
+    v0 = fields.gaussian_pulse(n, n)
+    out, times = {}, {}
+    for name, prec in (("fp64", sbpgpu.FP64), ("fp32", sbpgpu.FP32)):
+        with sbpgpu.Context(sbpgpu.WAVE_VAR_2D, order, n, n, bc=sbpgpu.BC_CHARACTERISTIC, precision=prec,
+                            rho=rho, K=K) as ctx:
+            ctx.set_state(v0)
+            ctx.step_resident(0.0, dt, 3)  # warm-up (graph capture), then restart from v0
+            ctx.synchronize()
+            ctx.set_state(v0)
+            ctx.synchronize()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            stream = torch.cuda.ExternalStream(ctx.stream)
+            ev0.record(stream)
+            ctx.step_resident(0.0, dt, nsteps)
+            ev1.record(stream)
+            ctx.synchronize()
+            times[name] = ev0.elapsed_time(ev1) / 1e3
+            out[name] = ctx.get_state()
+    d = out["fp32"] - out["fp64"]
+    l2 = float(np.sqrt(h * h * np.sum(d * d)))
+    ref_l2 = float(np.sqrt(h * h * np.sum(out["fp64"] ** 2)))
+    line = {"study": "precision", "grid": [n, n], "order": order, "t_end": args.t_end, "steps": nsteps, "dt": dt,
+            "rho_range": [float(rho.min()), float(rho.max())], "K_range": [float(K.min()), float(K.max())],
+            "fp32_vs_fp64": {"l2": l2, "l2_rel": l2 / ref_l2, "max": float(np.abs(d).max()),
+                             "max_rel": float(np.abs(d).max() / np.abs(out["fp64"]).max())},
+            "seconds": times, "speedup_fp32": times["fp64"] / times["fp32"],
+            "fields": "1 + 0.5 tanh(sum of 8 Fourier modes, |k| <= 6, A ~ N(0,1)), seeds 0 (rho) and 1 (K)"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.study == "precision":
+        run_precision_study(args)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))

@@ -42,6 +42,7 @@ def units():
     out.append(("kernels.o", "kernels.cu", []))
     out.append(("sbp_runtime.o", "sbp_runtime.cpp", ["-x", "cu"]))
     out.append(("noalloc.o", "noalloc.cu", []))
+    out.append(("petsc_io.o", "petsc_io.cpp", []))
     return out
 
 

@@ -7,11 +7,22 @@ namespace sbp {
 
 int wave_smem_bytes(int order, bool fp32) {
   switch (order) {
-    case 2: return fp32 ? WaveTile<float, 2>::SMEM : WaveTile<double, 2>::SMEM;
-    case 4: return fp32 ? WaveTile<float, 4>::SMEM : WaveTile<double, 4>::SMEM;
-    case 6: return fp32 ? WaveTile<float, 6>::SMEM : WaveTile<double, 6>::SMEM;
+    case 2: return fp32 ? WaveTile<float, 2, ST_MID>::SMEM : WaveTile<double, 2, ST_MID>::SMEM;
+    case 4: return fp32 ? WaveTile<float, 4, ST_MID>::SMEM : WaveTile<double, 4, ST_MID>::SMEM;
+    case 6: return fp32 ? WaveTile<float, 6, ST_MID>::SMEM : WaveTile<double, 6, ST_MID>::SMEM;
     default: return -1;
   }
+}
+
+int device_sm_count() {
+  static int cache[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 148;
+  if (dev < 64 && cache[dev]) return cache[dev];
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
+  if (dev < 64) cache[dev] = n;
+  return n;
 }
 
 // ---------------------------------------------------------------- line kernels

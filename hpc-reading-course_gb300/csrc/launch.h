@@ -12,8 +12,15 @@
 namespace sbp {
 
 struct WaveMaps {
-  CUtensorMap p, u, v;  // the same state buffer seen with the p, u and v tile boxes
+  CUtensorMap p, u, v;  // the stage input seen with the p, u and v tile boxes (with halos)
+  CUtensorMap n, a, c;  // u^n, acc and the FP32 Kahan term as 3-component point boxes
 };
+
+// Tile height of the wave stage kernel for an element size (bytes).
+inline int wave_tile_height(int elem_bytes) { return elem_bytes == 8 ? 16 : 32; }
+
+// Streaming multiprocessors of the current device (cached per device).
+int device_sm_count();
 
 template <typename T>
 cudaError_t launch_wave_o2(int kind, int stage, const WaveMaps& m, const WaveParams<T>& prm, dim3 grid, cudaStream_t s);
@@ -33,7 +40,11 @@ template <typename T> inline cudaError_t configure_wave(int order, int kind) {
 template <typename T>
 inline cudaError_t launch_wave(int order, int kind, int stage, const WaveMaps& m, const WaveParams<T>& prm,
                                cudaStream_t s) {
-  const dim3 grid((prm.nx + kWaveTX - 1) / kWaveTX, (prm.ny + kWaveTY - 1) / kWaveTY);
+  // persistent grid: one CTA per SM, each walking the tiles with a fixed stride
+  const int ty = wave_tile_height((int)sizeof(T));
+  const long long ntiles = (long long)((prm.nx + kWaveTX - 1) / kWaveTX) * ((prm.ny + ty - 1) / ty);
+  const int nsm = device_sm_count();
+  const dim3 grid((unsigned)(ntiles < nsm ? ntiles : nsm));
   switch (order) {
     case 2: return launch_wave_o2<T>(kind, stage, m, prm, grid, s);
     case 4: return launch_wave_o4<T>(kind, stage, m, prm, grid, s);

@@ -126,9 +126,10 @@ extern "C" int sbp_wave_rhs_noalloc(const sbp_desc* d, double t, const double* s
   const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, 3};
   const cuuint64_t strides[2] = {(cuuint64_t)(pitch * 8), (cuuint64_t)(plane * 8)};
   const cuuint32_t estr[3] = {1, 1, 1};
-  const cuuint32_t boxP[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)(kWaveTY + 2 * HY), 1};
-  const cuuint32_t boxU[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)kWaveTY, 1};
-  const cuuint32_t boxV[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)(kWaveTY + 2 * HY), 1};
+  const int TY = wave_tile_height(8);
+  const cuuint32_t boxP[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)(TY + 2 * HY), 1};
+  const cuuint32_t boxU[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)TY, 1};
+  const cuuint32_t boxV[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)(TY + 2 * HY), 1};
   WaveMaps maps;
   CUtensorMap* mp[3] = {&maps.p, &maps.u, &maps.v};
   const cuuint32_t* boxes[3] = {boxP, boxU, boxV};
@@ -137,6 +138,7 @@ extern "C" int sbp_wave_rhs_noalloc(const sbp_desc* d, double t, const double* s
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return reject(SBP_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  maps.n = maps.a = maps.c = maps.p;  // the RHS-only stage loads no per-point operands
 
   WaveParams<double> p;
   std::memset(&p, 0, sizeof(p));

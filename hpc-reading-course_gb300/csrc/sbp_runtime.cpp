@@ -97,28 +97,37 @@ void fill_taps(DirTaps<T>& t, int order, double scale) {
     for (int s = 0; s < op.cls_width; s++) t.cls[r][s] = (T)(scale * op.closure[r][s]);
 }
 
-int make_maps(sbp_ctx* ctx, void* base, WaveMaps& m) {
+// Encodes one 3D tensor map (x, y, component) over a state buffer of the context.
+int encode_map(sbp_ctx* ctx, void* base, const cuuint32_t box[3], CUtensorMap* out) {
   EncodeTiledFn enc = encode_tiled();
   if (!enc) return fail(ctx, SBP_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-  const int R = ctx->d.order / 2;
-  const int hxa = 16 / (int)ctx->es;
-  const int HX = (R + hxa - 1) / hxa * hxa, HY = R;
   const cuuint64_t dims[3] = {(cuuint64_t)ctx->nx, (cuuint64_t)ctx->ny, 3};
   const cuuint64_t strides[2] = {(cuuint64_t)(ctx->pitch * ctx->es), (cuuint64_t)(ctx->plane * ctx->es)};
   const cuuint32_t estr[3] = {1, 1, 1};
   const CUtensorMapDataType dt = ctx->fp32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
-  const cuuint32_t boxP[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)(kWaveTY + 2 * HY), 1};
-  const cuuint32_t boxU[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)kWaveTY, 1};
-  const cuuint32_t boxV[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)(kWaveTY + 2 * HY), 1};
-  CUtensorMap* outs[3] = {&m.p, &m.u, &m.v};
-  const cuuint32_t* boxes[3] = {boxP, boxU, boxV};
-  for (int k = 0; k < 3; k++) {
-    CUresult r = enc(outs[k], dt, 3, base, dims, strides, boxes[k], estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(ctx, SBP_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(r));
-  }
+  CUresult r = enc(out, dt, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(ctx, SBP_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(r));
   return SBP_OK;
+}
+
+// Stencil-tile maps of a stage-input buffer plus the point maps of u^n, acc
+// and the Kahan term (the same for every input buffer).
+int make_maps(sbp_ctx* ctx, void* base, WaveMaps& m) {
+  const int R = ctx->d.order / 2;
+  const int hxa = 16 / (int)ctx->es;
+  const int HX = (R + hxa - 1) / hxa * hxa, HY = R;
+  const int TY = wave_tile_height((int)ctx->es);
+  const cuuint32_t boxP[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)(TY + 2 * HY), 1};
+  const cuuint32_t boxU[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)TY, 1};
+  const cuuint32_t boxV[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)(TY + 2 * HY), 1};
+  const cuuint32_t boxPt[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)TY, 3};
+  int rc;
+  if ((rc = encode_map(ctx, base, boxP, &m.p)) || (rc = encode_map(ctx, base, boxU, &m.u)) ||
+      (rc = encode_map(ctx, base, boxV, &m.v)) || (rc = encode_map(ctx, ctx->un, boxPt, &m.n)) ||
+      (rc = encode_map(ctx, ctx->acc, boxPt, &m.a)))
+    return rc;
+  return encode_map(ctx, ctx->comp ? ctx->comp : ctx->acc, boxPt, &m.c);
 }
 
 // Stage-independent kernel parameters.
@@ -140,7 +149,6 @@ WaveParams<T> wave_params(sbp_ctx* ctx) {
   p.bwx = ctx->hix * hi0;
   p.bwy = ctx->hiy * hi0;
   p.bc = ctx->d.bc == SBP_BC_CHARACTERISTIC ? BC_CHARACTERISTIC : BC_FREE_SURFACE;
-  p.compensated = ctx->fp32 ? 1 : 0;
   p.xl0 = ctx->d.xl[0];
   p.xl1 = ctx->d.xl[1];
   p.hix = ctx->hix;

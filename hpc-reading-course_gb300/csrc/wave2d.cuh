@@ -5,17 +5,22 @@
 // region split (code/include/partitioned_rhs/rhs.h:373-398): closure rows for
 // the first/last cls_sz lines of each direction, the central stencil between.
 //
-// One CTA owns a TX x TY tile of grid points. Thread 0 issues three TMA tile
-// loads of the stage input into shared memory: p with an x and y halo, u with
-// an x halo, v with a y halo (the star stencil needs no corners of u, v). The
-// interior stencils read shared memory; closure rows (boundary strips only)
-// read their taps straight from global memory. The SAT terms and the RK4
-// stage update are applied to the point's RHS in registers, so each stage
-// reads its state once and writes its outputs once.
+// Persistent, warp-specialised pipeline. One CTA per SM walks the tiles of
+// the grid (TX x TY points each) in a fixed stride. Warp 8 is the producer:
+// its lane 0 issues the TMA loads of tile k+1 into one of two shared-memory
+// stages while warps 0-7 compute tile k from the other:
+//   * the stage input with halos: p with an x and y halo, u with an x halo,
+//     v with a y halo (the star stencil needs no corners of u, v);
+//   * the per-point RK4 operands the stage needs, each as one 3-component
+//     box: u^n and acc for stages 2-3, acc for stage 4, plus u^n and the
+//     Kahan term for the FP32 stage 4.
+// Consumers touch global memory only for their outputs (coalesced streaming
+// stores), for closure-row taps (boundary strips) and for coefficient fields.
+// Every mbarrier wait is bounded by %globaltimer; a timeout sets an error bit
+// that the host reads and the CTA stops after letting its copies land.
 //
 // State layout in HBM: structure of arrays, component planes [u | v | p],
-// each ny rows of `pitch` elements (pitch a multiple of 64, so every row
-// starts 512-byte aligned for FP64 and 256-byte aligned for FP32).
+// each ny rows of `pitch` elements (pitch a multiple of 64).
 #pragma once
 
 #include "sbp_device.cuh"
@@ -44,34 +49,49 @@ template <typename T> struct WaveParams {
   double bwx, bwy;    // hix * HI[0], hiy * HI[0]: SAT weights (FP64)
   T c_acc, c_w;       // acc (+)= c_acc * k ; w = u^n + c_w * k
   int bc;             // BcKind
-  int compensated;    // FP32: Kahan-compensated final update
   double t, xl0, xl1, hix, hiy;  // WK_MMS: stage time and grid geometry
   int* err;
 };
 
-constexpr int kWaveTX = 64;   // tile width (x, contiguous)
-constexpr int kWaveTY = 32;   // tile height (y)
-constexpr int kWaveThreads = 256;
+constexpr int kWaveTX = 64;            // tile width (x, contiguous)
+constexpr int kWaveConsumerWarps = 8;  // compute warps
+constexpr int kWaveThreads = 32 * (kWaveConsumerWarps + 1);
 
-// x halo rounded up so that (tile origin - halo) * sizeof(T) is a multiple of
-// 16 bytes (TMA rule for the innermost coordinate); the tile origin is a
-// multiple of 64.
-template <typename T, int ORD> struct WaveTile {
+// FP32 keeps the state with a Kahan-compensated final update.
+template <typename T> struct IsCompensated { static constexpr bool value = false; };
+template <> struct IsCompensated<float> { static constexpr bool value = true; };
+
+// Tile geometry and shared-memory plan for (T, order, stage). The x halo is
+// rounded up so that (tile origin - halo) * sizeof(T) is a multiple of 16
+// bytes (TMA rule for the innermost coordinate); tile origins are multiples of 64.
+template <typename T, int ORD, int STAGE> struct WaveTile {
+  static constexpr bool COMP = IsCompensated<T>::value;
+  static constexpr int TY = sizeof(T) == 8 ? 16 : 32;        // tile height
   static constexpr int R = (OpShape<ORD>::W - 1) / 2;
-  static constexpr int HXA = 16 / sizeof(T);                  // alignment unit in elements
-  static constexpr int HX = ((R + HXA - 1) / HXA) * HXA;      // x halo loaded
+  static constexpr int HXA = 16 / sizeof(T);
+  static constexpr int HX = ((R + HXA - 1) / HXA) * HXA;     // x halo loaded
   static constexpr int HY = R;                                // y halo loaded
   static constexpr int PW = kWaveTX + 2 * HX;                 // p/u tile row length
-  static constexpr int PH = kWaveTY + 2 * HY;                 // p/v tile rows
+  static constexpr int PH = TY + 2 * HY;                      // p/v tile rows
+  static constexpr bool LOAD_UN = (STAGE == ST_MID) || (STAGE == ST_LAST && COMP);
+  static constexpr bool LOAD_ACC = (STAGE == ST_MID) || (STAGE == ST_LAST);
+  static constexpr bool LOAD_COMP = (STAGE == ST_LAST && COMP);
   static constexpr int align128(int b) { return (b + 127) / 128 * 128; }
   static constexpr int BYTES_P = PH * PW * (int)sizeof(T);
-  static constexpr int BYTES_U = kWaveTY * PW * (int)sizeof(T);
+  static constexpr int BYTES_U = TY * PW * (int)sizeof(T);
   static constexpr int BYTES_V = PH * kWaveTX * (int)sizeof(T);
+  static constexpr int BYTES_PT = 3 * TY * kWaveTX * (int)sizeof(T);  // one 3-component point box
   static constexpr int OFF_U = align128(BYTES_P);
   static constexpr int OFF_V = OFF_U + align128(BYTES_U);
-  static constexpr int OFF_BAR = OFF_V + align128(BYTES_V);
+  static constexpr int OFF_N = OFF_V + align128(BYTES_V);
+  static constexpr int OFF_A = OFF_N + (LOAD_UN ? BYTES_PT : 0);
+  static constexpr int OFF_C = OFF_A + (LOAD_ACC ? BYTES_PT : 0);
+  static constexpr int STAGE_BYTES = align128(OFF_C + (LOAD_COMP ? BYTES_PT : 0));
+  static constexpr int OFF_BAR = 2 * STAGE_BYTES;             // full[2], empty[2]
   static constexpr int SMEM = OFF_BAR + 128;
-  static constexpr uint32_t TX_BYTES = BYTES_P + BYTES_U + BYTES_V;
+  static constexpr uint32_t TX_BYTES = BYTES_P + BYTES_U + BYTES_V + (LOAD_UN ? BYTES_PT : 0) +
+                                       (LOAD_ACC ? BYTES_PT : 0) + (LOAD_COMP ? BYTES_PT : 0);
+  static_assert(SMEM <= 227 * 1024, "wave tile pipeline exceeds shared memory");
 };
 
 // Closure row of D1 along one line: left block for i < CS, mirrored negated
@@ -95,186 +115,224 @@ __device__ __forceinline__ T closure_line(const T* __restrict__ line, long long 
   return s;
 }
 
-// The manufactured density and forcing of the reference's forced wave demo
-// (code/demo/wave/wave_eq_rhs.h:42-64), evaluated in FP64.
 __device__ __forceinline__ double mms_x(double xl, int i, double hi) { return xl + (double)i / hi; }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 template <typename T, int ORD, int KIND, int STAGE>
-__global__ void __launch_bounds__(kWaveThreads)
+__global__ void __launch_bounds__(kWaveThreads, 1)
     wave_stage_kernel(const __grid_constant__ CUtensorMap mapP, const __grid_constant__ CUtensorMap mapU,
-                      const __grid_constant__ CUtensorMap mapV, const __grid_constant__ WaveParams<T> prm) {
-  using Tile = WaveTile<T, ORD>;
-  constexpr int W = OpShape<ORD>::W, CS = OpShape<ORD>::CS, R = Tile::R;
+                      const __grid_constant__ CUtensorMap mapV, const __grid_constant__ CUtensorMap mapN,
+                      const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapC,
+                      const __grid_constant__ WaveParams<T> prm) {
+  using Tile = WaveTile<T, ORD, STAGE>;
+  constexpr bool COMP = Tile::COMP;
+  constexpr int TY = Tile::TY, W = OpShape<ORD>::W, CS = OpShape<ORD>::CS, R = Tile::R;
   constexpr int HX = Tile::HX, HY = Tile::HY, PW = Tile::PW;
   extern __shared__ __align__(128) unsigned char smem[];
-  T* sP = reinterpret_cast<T*>(smem);
-  T* sU = reinterpret_cast<T*>(smem + Tile::OFF_U);
-  T* sV = reinterpret_cast<T*>(smem + Tile::OFF_V);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
+  uint64_t* empty = full + 2;
 
-  const int i0 = blockIdx.x * kWaveTX, j0 = blockIdx.y * kWaveTY;
+  const int nx = prm.nx, ny = prm.ny;
+  const int ntx = (nx + kWaveTX - 1) / kWaveTX;
+  const int ntiles = ntx * ((ny + TY - 1) / TY);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
   if (threadIdx.x == 0) {
-    prefetch_tensormap(&mapP);
-    mbar_init(bar, 1);
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    mbar_init(&empty[0], kWaveConsumerWarps);
+    mbar_init(&empty[1], kWaveConsumerWarps);
     fence_barrier_init();
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    mbar_arrive_expect_tx(bar, Tile::TX_BYTES);
-    tma_load_3d(sP, &mapP, i0 - HX, j0 - HY, 2, bar);
-    tma_load_3d(sU, &mapU, i0 - HX, j0, 0, bar);
-    tma_load_3d(sV, &mapV, i0, j0 - HY, 1, bar);
-  }
-  if (!mbar_wait_bounded(bar, 0)) {
-    if (threadIdx.x == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
-    mbar_wait_bounded(bar, 0);  // let copies in flight land before the CTA exits
+
+  if (warp == kWaveConsumerWarps) {
+    // ---------------- producer: TMA loads of tile k into stage k & 1
+    if (lane == 0) {
+      prefetch_tensormap(&mapP);
+      int k = 0;
+      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
+        const int b = k & 1;
+        if (k >= 2 && !mbar_wait_bounded(&empty[b], ((k >> 1) - 1) & 1)) {
+          atomicOr(prm.err, ERR_TMA_TIMEOUT);
+          break;
+        }
+        unsigned char* st = smem + b * Tile::STAGE_BYTES;
+        const int i0 = (tile % ntx) * kWaveTX, j0 = (tile / ntx) * TY;
+        mbar_arrive_expect_tx(&full[b], Tile::TX_BYTES);
+        tma_load_3d(st, &mapP, i0 - HX, j0 - HY, 2, &full[b]);
+        tma_load_3d(st + Tile::OFF_U, &mapU, i0 - HX, j0, 0, &full[b]);
+        tma_load_3d(st + Tile::OFF_V, &mapV, i0, j0 - HY, 1, &full[b]);
+        if (Tile::LOAD_UN) tma_load_3d(st + Tile::OFF_N, &mapN, i0, j0, 0, &full[b]);
+        if (Tile::LOAD_ACC) tma_load_3d(st + Tile::OFF_A, &mapA, i0, j0, 0, &full[b]);
+        if (Tile::LOAD_COMP) tma_load_3d(st + Tile::OFF_C, &mapC, i0, j0, 0, &full[b]);
+      }
+      // the CTA must not exit with copies in flight: wait for the last two stages
+      for (int kk = (k >= 2 ? k - 2 : 0); kk < k; kk++) mbar_wait_bounded(&full[kk & 1], (kk >> 1) & 1);
+    }
     return;
   }
 
-  const int nx = prm.nx, ny = prm.ny;
+  // ---------------- consumers: warps 0-7
   const long long pitch = prm.pitch, plane = prm.plane;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int ROWS = kWaveTY / (kWaveThreads / 32);
+  constexpr int ROWS = TY / kWaveConsumerWarps;
+  constexpr int TPT = TY * kWaveTX;  // points per tile (one component)
+  int k = 0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
+    const int b = k & 1;
+    if (!mbar_wait_bounded(&full[b], (k >> 1) & 1)) {
+      if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
+      break;
+    }
+    const unsigned char* st = smem + b * Tile::STAGE_BYTES;
+    const T* sP = reinterpret_cast<const T*>(st);
+    const T* sU = reinterpret_cast<const T*>(st + Tile::OFF_U);
+    const T* sV = reinterpret_cast<const T*>(st + Tile::OFF_V);
+    const T* sN = reinterpret_cast<const T*>(st + Tile::OFF_N);
+    const T* sA = reinterpret_cast<const T*>(st + Tile::OFF_A);
+    const T* sC = reinterpret_cast<const T*>(st + Tile::OFF_C);
+    const int i0 = (tile % ntx) * kWaveTX, j0 = (tile / ntx) * TY;
 
 #pragma unroll 1
-  for (int rr = 0; rr < ROWS; rr++) {
-    const int y = warp * ROWS + rr;
-    const int j = j0 + y;
-    if (j >= ny) break;
-    const bool yint = (j >= CS) && (j < ny - CS);
+    for (int rr = 0; rr < ROWS; rr++) {
+      const int y = warp * ROWS + rr;
+      const int j = j0 + y;
+      if (j >= ny) break;
+      const bool yint = (j >= CS) && (j < ny - CS);
 #pragma unroll
-    for (int cc = 0; cc < kWaveTX / 32; cc++) {
-      const int x = lane + 32 * cc;
-      const int i = i0 + x;
-      if (i >= nx) continue;
-      const bool xint = (i >= CS) && (i < nx - CS);
-      const T* rowP = sP + (y + HY) * PW + (x + HX - R);
-      const T* rowU = sU + y * PW + (x + HX - R);
-      const T* colP = sP + (y) * PW + (x + HX);          // row y+HY-R
-      const T* colV = sV + (y) * kWaveTX + x;            // row y+HY-R
-      const T pc = rowP[R], uc = rowU[R], vc = colV[R * kWaveTX];
+      for (int cc = 0; cc < kWaveTX / 32; cc++) {
+        const int x = lane + 32 * cc;
+        const int i = i0 + x;
+        if (i >= nx) continue;
+        const bool xint = (i >= CS) && (i < nx - CS);
+        const T* rowP = sP + (y + HY) * PW + (x + HX - R);
+        const T* rowU = sU + y * PW + (x + HX - R);
+        const T* colP = sP + y * PW + (x + HX);   // row y+HY-R
+        const T* colV = sV + y * kWaveTX + x;     // row y+HY-R
+        const T pc = rowP[R], uc = rowU[R], vc = colV[R * kWaveTX];
 
-      // D1x p, D1y p (scaled by -hi)
-      T dxp, dyp, kp;
-      if (xint) {
-        dxp = prm.dx.taps[0] * rowP[0];
+        T dxp, dyp, kp;
+        if (xint) {
+          dxp = prm.dx.taps[0] * rowP[0];
 #pragma unroll
-        for (int s = 1; s < W; s++)
-          if (s != R) dxp = fma(prm.dx.taps[s], rowP[s], dxp);
-      } else {
-        dxp = closure_line<T, ORD>(prm.in + 2 * plane + (long long)j * pitch, 1, nx, i, prm.dx.cls);
-      }
-      if (yint) {
-        dyp = prm.dy.taps[0] * colP[0];
-#pragma unroll
-        for (int s = 1; s < W; s++)
-          if (s != R) dyp = fma(prm.dy.taps[s], colP[s * PW], dyp);
-      } else {
-        dyp = closure_line<T, ORD>(prm.in + 2 * plane + i, pitch, ny, j, prm.dy.cls);
-      }
-      // D1x u + D1y v as one chain where both are interior
-      if (xint) {
-        kp = prm.dx.taps[0] * rowU[0];
-#pragma unroll
-        for (int s = 1; s < W; s++)
-          if (s != R) kp = fma(prm.dx.taps[s], rowU[s], kp);
-      } else {
-        kp = closure_line<T, ORD>(prm.in + (long long)j * pitch, 1, nx, i, prm.dx.cls);
-      }
-      if (yint) {
-#pragma unroll
-        for (int s = 0; s < W; s++)
-          if (s != R) kp = fma(prm.dy.taps[s], colV[s * kWaveTX], kp);
-      } else {
-        kp += closure_line<T, ORD>(prm.in + plane + i, pitch, ny, j, prm.dy.cls);
-      }
-
-      const long long q = (long long)j * pitch + i;
-      T ku, kv;
-      if constexpr (KIND == WK_HOM) {
-        ku = dxp;
-        kv = dyp;
-      } else if constexpr (KIND == WK_VAR) {
-        const T ri = prm.rinv[q];
-        ku = ri * dxp;
-        kv = ri * dyp;
-        kp = prm.kmod[q] * kp;
-      } else {  // WK_MMS (FP64)
-        const double PI = 3.14159265358979323846264;
-        const double xx = mms_x(prm.xl0, i, prm.hix), yy = mms_x(prm.xl1, j, prm.hiy);
-        const double ri = 1. / (2 + xx * yy);
-        const double ct = cos(5 * PI * prm.t);
-        const double fu = -(3 * PI * ct * cos(3 * PI * xx) * sin(4 * PI * yy) * (xx * yy + 1)) / (xx * yy + 2);
-        const double fv = -(4 * PI * ct * cos(4 * PI * yy) * sin(3 * PI * xx) * (xx * yy + 1)) / (xx * yy + 2);
-        ku = (T)(ri * (double)dxp + fu);
-        kv = (T)(ri * (double)dyp + fv);
-      }
-
-      // SAT boundary terms (FP64 weights), reference order west, south, east, north
-      const bool edge = (i == 0) || (j == 0) || (i == nx - 1) || (j == ny - 1);
-      if (prm.bc != BC_NONE && edge) {
-        double rho = 1.0, kk = 1.0;
-        if constexpr (KIND == WK_VAR) {
-          rho = prm.rho64[(long long)j * nx + i];
-          kk = prm.k64[(long long)j * nx + i];
-        }
-        const double p64 = (double)pc;
-        double ku64 = (double)ku, kv64 = (double)kv, kp64 = (double)kp;
-        if (prm.bc == BC_FREE_SURFACE) {
-          // free_surface_bc_* (code/demo/wave_hom/wave_eq_hom_rhs.h:389-441); rho^-1 for WK_VAR
-          const double ri = (KIND == WK_VAR) ? 1.0 / rho : 1.0;
-          if (i == 0) ku64 = (KIND == WK_VAR) ? ku64 - ri * (prm.bwx * p64) : ku64 - prm.bwx * p64;
-          if (j == 0) kv64 = (KIND == WK_VAR) ? kv64 - ri * (prm.bwy * p64) : kv64 - prm.bwy * p64;
-          if (i == nx - 1) ku64 = (KIND == WK_VAR) ? ku64 + ri * (prm.bwx * p64) : ku64 + prm.bwx * p64;
-          if (j == ny - 1) kv64 = (KIND == WK_VAR) ? kv64 + ri * (prm.bwy * p64) : kv64 + prm.bwy * p64;
+          for (int s = 1; s < W; s++)
+            if (s != R) dxp = fma(prm.dx.taps[s], rowP[s], dxp);
         } else {
-          // characteristic SAT on the incoming characteristic p + Z u_n
-          const double z = sqrt(rho * kk), c = sqrt(kk / rho), hr = 0.5 / rho, hc = 0.5 * c;
-          const double u64 = (double)uc, v64 = (double)vc;
-          if (i == 0) { const double g = prm.bwx * (p64 + z * u64); ku64 -= hr * g; kp64 -= hc * g; }
-          if (j == 0) { const double g = prm.bwy * (p64 + z * v64); kv64 -= hr * g; kp64 -= hc * g; }
-          if (i == nx - 1) { const double g = prm.bwx * (p64 - z * u64); ku64 += hr * g; kp64 -= hc * g; }
-          if (j == ny - 1) { const double g = prm.bwy * (p64 - z * v64); kv64 += hr * g; kp64 -= hc * g; }
+          dxp = closure_line<T, ORD>(prm.in + 2 * plane + (long long)j * pitch, 1, nx, i, prm.dx.cls);
         }
-        ku = (T)ku64;
-        kv = (T)kv64;
-        kp = (T)kp64;
-      }
-
-      // RK4 stage update (classical RK4, code/include/time_stepping/time_stepping.h:127-142)
-      const T kc[3] = {ku, kv, kp};
-      const T cen[3] = {uc, vc, pc};
+        if (yint) {
+          dyp = prm.dy.taps[0] * colP[0];
 #pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const long long o = c * plane + q;
-        if constexpr (STAGE == ST_RHS) {
-          prm.kout[o] = kc[c];
-        } else if constexpr (STAGE == ST_FIRST) {
-          // acc = u + dt/6 k1 (FP32 compensated: acc = dt/6 k1), w = u + dt/2 k1
-          const T a = prm.compensated ? prm.c_acc * kc[c] : fma(prm.c_acc, kc[c], cen[c]);
-          st_stream(prm.acc + o, a);
-          st_stream(prm.wout + o, fma(prm.c_w, kc[c], cen[c]));
-        } else if constexpr (STAGE == ST_MID) {
-          const T u0 = ld_stream(prm.un + o);
-          const T a = ld_stream(prm.acc + o);
-          st_stream(prm.acc + o, fma(prm.c_acc, kc[c], a));
-          st_stream(prm.wout + o, fma(prm.c_w, kc[c], u0));
-        } else {  // ST_LAST
-          const T a = ld_stream(prm.acc + o);
-          const T d = fma(prm.c_acc, kc[c], a);
-          if (prm.compensated) {
-            // Kahan summation of the step increment into the FP32 state
-            const T u0 = prm.un[o], e = prm.comp[o];
-            const T yv = d - e;
-            const T tv = u0 + yv;
-            st_stream(prm.comp + o, (tv - u0) - yv);
-            st_stream(prm.un + o, tv);
+          for (int s = 1; s < W; s++)
+            if (s != R) dyp = fma(prm.dy.taps[s], colP[s * PW], dyp);
+        } else {
+          dyp = closure_line<T, ORD>(prm.in + 2 * plane + i, pitch, ny, j, prm.dy.cls);
+        }
+        if (xint) {
+          kp = prm.dx.taps[0] * rowU[0];
+#pragma unroll
+          for (int s = 1; s < W; s++)
+            if (s != R) kp = fma(prm.dx.taps[s], rowU[s], kp);
+        } else {
+          kp = closure_line<T, ORD>(prm.in + (long long)j * pitch, 1, nx, i, prm.dx.cls);
+        }
+        if (yint) {
+#pragma unroll
+          for (int s = 0; s < W; s++)
+            if (s != R) kp = fma(prm.dy.taps[s], colV[s * kWaveTX], kp);
+        } else {
+          kp += closure_line<T, ORD>(prm.in + plane + i, pitch, ny, j, prm.dy.cls);
+        }
+
+        const long long q = (long long)j * pitch + i;
+        T ku, kv;
+        if constexpr (KIND == WK_HOM) {
+          ku = dxp;
+          kv = dyp;
+        } else if constexpr (KIND == WK_VAR) {
+          const T ri = __ldg(prm.rinv + q);
+          ku = ri * dxp;
+          kv = ri * dyp;
+          kp = __ldg(prm.kmod + q) * kp;
+        } else {  // WK_MMS (FP64): code/demo/wave/wave_eq_rhs.h:42-64
+          const double PI = 3.14159265358979323846264;
+          const double xx = mms_x(prm.xl0, i, prm.hix), yy = mms_x(prm.xl1, j, prm.hiy);
+          const double ri = 1. / (2 + xx * yy);
+          const double ct = cos(5 * PI * prm.t);
+          const double fu = -(3 * PI * ct * cos(3 * PI * xx) * sin(4 * PI * yy) * (xx * yy + 1)) / (xx * yy + 2);
+          const double fv = -(4 * PI * ct * cos(4 * PI * yy) * sin(3 * PI * xx) * (xx * yy + 1)) / (xx * yy + 2);
+          ku = (T)(ri * (double)dxp + fu);
+          kv = (T)(ri * (double)dyp + fv);
+        }
+
+        // SAT boundary terms (FP64 weights), reference order west, south, east, north
+        const bool edge = (i == 0) || (j == 0) || (i == nx - 1) || (j == ny - 1);
+        if (prm.bc != BC_NONE && edge) {
+          double rho = 1.0, kk = 1.0;
+          if constexpr (KIND == WK_VAR) {
+            rho = prm.rho64[(long long)j * nx + i];
+            kk = prm.k64[(long long)j * nx + i];
+          }
+          const double p64 = (double)pc;
+          double ku64 = (double)ku, kv64 = (double)kv, kp64 = (double)kp;
+          if (prm.bc == BC_FREE_SURFACE) {
+            // free_surface_bc_* (code/demo/wave_hom/wave_eq_hom_rhs.h:389-441); rho^-1 for WK_VAR
+            const double ri = (KIND == WK_VAR) ? 1.0 / rho : 1.0;
+            if (i == 0) ku64 = (KIND == WK_VAR) ? ku64 - ri * (prm.bwx * p64) : ku64 - prm.bwx * p64;
+            if (j == 0) kv64 = (KIND == WK_VAR) ? kv64 - ri * (prm.bwy * p64) : kv64 - prm.bwy * p64;
+            if (i == nx - 1) ku64 = (KIND == WK_VAR) ? ku64 + ri * (prm.bwx * p64) : ku64 + prm.bwx * p64;
+            if (j == ny - 1) kv64 = (KIND == WK_VAR) ? kv64 + ri * (prm.bwy * p64) : kv64 + prm.bwy * p64;
           } else {
-            st_stream(prm.un + o, d);
+            // characteristic SAT on the incoming characteristic p + Z u_n
+            const double z = sqrt(rho * kk), c = sqrt(kk / rho), hr = 0.5 / rho, hc = 0.5 * c;
+            const double u64 = (double)uc, v64 = (double)vc;
+            if (i == 0) { const double g = prm.bwx * (p64 + z * u64); ku64 -= hr * g; kp64 -= hc * g; }
+            if (j == 0) { const double g = prm.bwy * (p64 + z * v64); kv64 -= hr * g; kp64 -= hc * g; }
+            if (i == nx - 1) { const double g = prm.bwx * (p64 - z * u64); ku64 += hr * g; kp64 -= hc * g; }
+            if (j == ny - 1) { const double g = prm.bwy * (p64 - z * v64); kv64 += hr * g; kp64 -= hc * g; }
+          }
+          ku = (T)ku64;
+          kv = (T)kv64;
+          kp = (T)kp64;
+        }
+
+        // RK4 stage update (classical RK4, code/include/time_stepping/time_stepping.h:127-142)
+        const T kc[3] = {ku, kv, kp};
+        const T cen[3] = {uc, vc, pc};
+        const int sp = y * kWaveTX + x;  // point within a 3-component smem box
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const long long o = c * plane + q;
+          if constexpr (STAGE == ST_RHS) {
+            prm.kout[o] = kc[c];
+          } else if constexpr (STAGE == ST_FIRST) {
+            // acc = u + dt/6 k1 (FP32 compensated: acc = dt/6 k1), w = u + dt/2 k1
+            st_stream(prm.acc + o, COMP ? prm.c_acc * kc[c] : fma(prm.c_acc, kc[c], cen[c]));
+            st_stream(prm.wout + o, fma(prm.c_w, kc[c], cen[c]));
+          } else if constexpr (STAGE == ST_MID) {
+            st_stream(prm.acc + o, fma(prm.c_acc, kc[c], sA[c * TPT + sp]));
+            st_stream(prm.wout + o, fma(prm.c_w, kc[c], sN[c * TPT + sp]));
+          } else {  // ST_LAST
+            const T d = fma(prm.c_acc, kc[c], sA[c * TPT + sp]);
+            if constexpr (COMP) {
+              // Kahan summation of the step increment into the FP32 state
+              const T u0 = sN[c * TPT + sp], e = sC[c * TPT + sp];
+              const T yv = d - e;
+              const T tv = u0 + yv;
+              st_stream(prm.comp + o, (tv - u0) - yv);
+              st_stream(prm.un + o, tv);
+            } else {
+              st_stream(prm.un + o, d);
+            }
           }
         }
       }
     }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[b]);
   }
 }
 

@@ -1,0 +1,41 @@
+"""Seeded input fields for the wave workloads (host side, numpy).
+
+These produce problem *inputs* (initial data and coefficient fields); they
+do no part of the SBP computation, which runs in libsbpgpu.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def fourier_field(n: int, seed: int, modes: int = 8, kmax: float = 6.0, xl=(-1.0, -1.0), xr=(1.0, 1.0)):
+    """1 + 0.5 * tanh(sum_m A_m cos(k_m . x + phi_m)) on an n x n grid, (j, i) row-major.
+
+    k_m: integer wave vectors, uniform over the nonzero lattice points with
+    |k| <= kmax; A_m ~ N(0, 1); phi_m ~ U[0, 2 pi); all drawn from `seed`.
+    The range is inside (0.5, 1.5): 1 + 0.5 tanh(.) never reaches 2.
+    """
+    rng = np.random.default_rng(seed)
+    r = int(np.floor(kmax))
+    lattice = np.array([(a, b) for a in range(-r, r + 1) for b in range(-r, r + 1)
+                        if (a, b) != (0, 0) and a * a + b * b <= kmax * kmax], dtype=np.float64)
+    k = lattice[rng.integers(0, len(lattice), size=modes)]
+    amp = rng.standard_normal(modes)
+    phi = rng.uniform(0.0, 2 * np.pi, size=modes)
+    x = np.linspace(xl[0], xr[0], n)
+    y = np.linspace(xl[1], xr[1], n)
+    X, Y = np.meshgrid(x, y)
+    s = np.zeros_like(X)
+    for m in range(modes):
+        s += amp[m] * np.cos(k[m, 0] * X + k[m, 1] * Y + phi[m])
+    return (1.0 + 0.5 * np.tanh(s)).ravel()
+
+
+def gaussian_pulse(nx: int, ny: int, x0: float = 0.0, y0: float = 0.0, width: float = 0.05, amp: float = 1.0,
+                   xl=(-1.0, -1.0), xr=(1.0, 1.0)):
+    """Wave state (u, v, p) in the reference's AoS layout: p = amp exp(-|x - x0|^2 / width^2), u = v = 0."""
+    x = np.linspace(xl[0], xr[0], nx) - x0
+    y = np.linspace(xl[1], xr[1], ny) - y0
+    v = np.zeros((ny, nx, 3))
+    v[:, :, 2] = amp * np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / width**2)
+    return v.ravel()

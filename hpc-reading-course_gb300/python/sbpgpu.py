@@ -32,7 +32,7 @@ DOFS = {WAVE_HOM_2D: 3, WAVE_MMS_2D: 3, WAVE_VAR_2D: 3, ADVECTION_1D: 1, ADVECTI
 EXPORTS = ("sbp_create", "sbp_destroy", "sbp_last_error", "sbp_dofs", "sbp_rhs", "sbp_apply", "sbp_rk4_nsteps",
            "sbp_ts_rk4", "sbp_rk4", "sbp_set_state", "sbp_get_state", "sbp_rk4_resident", "sbp_synchronize",
            "sbp_error_norms", "sbp_hnorm", "sbp_get_stream", "sbp_launch_count", "sbp_probe_dfma_rate",
-           "sbp_wave_rhs_noalloc")
+           "sbp_wave_rhs_noalloc", "sbp_write_petsc_vec", "sbp_read_petsc_vec")
 
 _dp = C.POINTER(C.c_double)
 
@@ -87,6 +87,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.sbp_launch_count.restype = C.c_longlong
     L.sbp_probe_dfma_rate.argtypes = [C.c_int, _dp]
     L.sbp_wave_rhs_noalloc.argtypes = [C.POINTER(Desc), C.c_double, C.c_void_p, C.c_void_p]
+    L.sbp_write_petsc_vec.argtypes = [C.c_char_p, C.c_void_p, C.c_longlong]
+    L.sbp_read_petsc_vec.argtypes = [C.c_char_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -113,6 +115,28 @@ def wave_rhs_noalloc(order: int, nx: int, ny: int, t: float, src_ptr: int, dst_p
     d = Desc(WAVE_HOM_2D, order, bc, FP64, nx, ny, (C.c_double * 2)(*xl), (C.c_double * 2)(*xr), 0.0, 0.0,
              None, None, stream, device)
     return load().sbp_wave_rhs_noalloc(C.byref(d), t, src_ptr, dst_ptr)
+
+
+def write_petsc_vec(path: str, v: np.ndarray) -> None:
+    """Write a PETSc binary Vec file (what VecView on a binary viewer writes)."""
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    rc = load().sbp_write_petsc_vec(path.encode(), v.ctypes.data, v.size)
+    if rc:
+        raise SbpError(rc, f"cannot write {path}")
+
+
+def read_petsc_vec(path: str) -> np.ndarray:
+    """Read a PETSc binary Vec file."""
+    L = load()
+    n = C.c_longlong(0)
+    rc = L.sbp_read_petsc_vec(path.encode(), None, 0, C.byref(n))
+    if rc:
+        raise SbpError(rc, f"{path} is not a PETSc binary Vec file")
+    out = np.empty(n.value)
+    rc = L.sbp_read_petsc_vec(path.encode(), out.ctypes.data, out.size, C.byref(n))
+    if rc:
+        raise SbpError(rc, f"cannot read {path}")
+    return out
 
 
 def _host(a: np.ndarray) -> np.ndarray:

@@ -140,6 +140,15 @@ long long sbp_launch_count(const sbp_ctx* ctx);
  * FP64 ALU roof beside the HBM roof. */
 int sbp_probe_dfma_rate(int device, double* dfma_per_s);
 
+/* PETSc binary Vec files (host-side I/O): the format VecView writes on a
+ * binary viewer, as the reference's write_vector_to_binary does
+ * (code/src/util/io_util.cpp:4-14): big-endian int32 classid 1211214,
+ * big-endian int32 length, big-endian doubles. A single-rank DMDA vector is
+ * written in the AoS order of this library's boundary arrays.
+ * sbp_read_petsc_vec: with v == NULL only *n is set; fails if *n > capacity. */
+int sbp_write_petsc_vec(const char* path, const double* v, long long n);
+int sbp_read_petsc_vec(const char* path, double* v, long long capacity, long long* n);
+
 /* RHS of the 2D acoustic wave system (rho = K = 1, FP64) that allocates no
  * device memory. It has no counterpart in the reference.
  *
