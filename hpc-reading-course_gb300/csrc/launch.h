@@ -76,10 +76,11 @@ template <typename T>
 cudaError_t launch_error_norms(const T* soa, const double* aos, int nx, int ny, int dofs, long long pitch,
                                long long plane, double* partial, double* out, cudaStream_t s);
 // Energy norm squared sum_c sum_j sum_i hy*wy_j * hx*wx_i * v^2 with the
-// closure quadrature at both ends of each direction: out[0].
+// closure quadrature at both ends of each direction (of each block when
+// ysplit > 0): out[0].
 template <typename T>
 cudaError_t launch_hnorm(const T* soa, int nx, int ny, int dofs, long long pitch, long long plane, int order,
-                         double hx, double hy, double* partial, double* out, cudaStream_t s);
+                         double hx, double hy, int ysplit, double* partial, double* out, cudaStream_t s);
 
 // FP64 fused-multiply-add throughput probe: each thread runs `iters`
 // iterations of 8 independent DFMA chains; result written to out[0].

@@ -37,8 +37,10 @@ EncodeTiledFn encode_tiled() {
 }
 
 bool is_wave(int problem) {
-  return problem == SBP_WAVE_HOM_2D || problem == SBP_WAVE_MMS_2D || problem == SBP_WAVE_VAR_2D;
+  return problem == SBP_WAVE_HOM_2D || problem == SBP_WAVE_MMS_2D || problem == SBP_WAVE_VAR_2D ||
+         problem == SBP_WAVE_2BLOCK_2D;
 }
+bool has_fields(int problem) { return problem == SBP_WAVE_VAR_2D || problem == SBP_WAVE_2BLOCK_2D; }
 bool is_2d(int problem) { return is_wave(problem) || problem == SBP_ADVECTION_2D; }
 int dofs_of(int problem) {
   if (is_wave(problem)) return 3;
@@ -52,6 +54,7 @@ struct sbp_ctx {
   int dofs = 0;
   bool fp32 = false, two_d = false, wave = false, time_dependent = false;
   long long nx = 0, ny = 1, pitch = 0, plane = 0, npts = 0, nscalar = 0;
+  int ysplit = 0;  // two-block problems: first row of the upper block
   size_t es = 8;
   double hix = 1, hiy = 1, hx = 1, hy = 1;
   cudaStream_t stream = nullptr;
@@ -149,6 +152,7 @@ WaveParams<T> wave_params(sbp_ctx* ctx) {
   p.bwx = ctx->hix * hi0;
   p.bwy = ctx->hiy * hi0;
   p.bc = ctx->d.bc == SBP_BC_CHARACTERISTIC ? BC_CHARACTERISTIC : BC_FREE_SURFACE;
+  p.ysplit = ctx->ysplit;
   p.xl0 = ctx->d.xl[0];
   p.xl1 = ctx->d.xl[1];
   p.hix = ctx->hix;
@@ -158,7 +162,8 @@ WaveParams<T> wave_params(sbp_ctx* ctx) {
 }
 
 int wave_kind(const sbp_ctx* ctx) {
-  return ctx->d.problem == SBP_WAVE_HOM_2D ? WK_HOM : (ctx->d.problem == SBP_WAVE_VAR_2D ? WK_VAR : WK_MMS);
+  if (ctx->d.problem == SBP_WAVE_HOM_2D) return WK_HOM;
+  return has_fields(ctx->d.problem) ? WK_VAR : WK_MMS;
 }
 
 template <typename T>
@@ -401,7 +406,7 @@ int sbp_create(const sbp_desc* desc, sbp_ctx** out) {
     delete ctx;
     return SBP_ERR_INVALID;
   };
-  if (d.problem < SBP_WAVE_HOM_2D || d.problem > SBP_WAVE_VAR_2D) return bad("unknown problem");
+  if (d.problem < SBP_WAVE_HOM_2D || d.problem > SBP_WAVE_2BLOCK_2D) return bad("unknown problem");
   if (d.order != 2 && d.order != 4 && d.order != 6) return bad("order must be 2, 4 or 6");
   if (d.precision != SBP_FP64 && d.precision != SBP_FP32) return bad("unknown precision");
   if (d.bc != SBP_BC_REFERENCE && d.bc != SBP_BC_CHARACTERISTIC) return bad("unknown boundary treatment");
@@ -415,16 +420,22 @@ int sbp_create(const sbp_desc* desc, sbp_ctx** out) {
   const long long m = ops::min_points(d.order);
   if (ctx->nx < m || (ctx->two_d && ctx->ny < m)) return bad("grid smaller than the operator's minimum size");
   if (ctx->nx > (1LL << 30) || ctx->ny > (1LL << 30)) return bad("grid too large");
-  if (d.bc == SBP_BC_CHARACTERISTIC && !(d.problem == SBP_WAVE_HOM_2D || d.problem == SBP_WAVE_VAR_2D))
+  if (d.bc == SBP_BC_CHARACTERISTIC && !(d.problem == SBP_WAVE_HOM_2D || has_fields(d.problem)))
     return bad("characteristic boundary terms exist for the wave problems with rho, K fields only");
   if (d.problem == SBP_WAVE_MMS_2D && ctx->fp32) return bad("the manufactured-solution problem is FP64 only");
-  if (d.problem == SBP_WAVE_VAR_2D && (!d.rho || !d.K)) return bad("rho and K are required");
+  if (has_fields(d.problem) && (!d.rho || !d.K)) return bad("rho and K are required");
+  if (d.problem == SBP_WAVE_2BLOCK_2D && (ctx->ny % 2 || ctx->ny / 2 < m))
+    return bad("two-block grids need an even ny with ny/2 at least the operator's minimum size");
   if (!(d.xr[0] > d.xl[0]) || (ctx->two_d && !(d.xr[1] > d.xl[1]))) return bad("empty domain");
   ctx->time_dependent = d.problem == SBP_WAVE_MMS_2D;
   ctx->hix = (ctx->nx - 1) / (d.xr[0] - d.xl[0]);
   ctx->hx = 1.0 / ctx->hix;
   if (ctx->two_d) {
     ctx->hiy = (ctx->ny - 1) / (d.xr[1] - d.xl[1]);
+    if (d.problem == SBP_WAVE_2BLOCK_2D) {  // each block: ny/2 points over half the y extent
+      ctx->ysplit = (int)(ctx->ny / 2);
+      ctx->hiy = (ctx->ny / 2 - 1) / (0.5 * (d.xr[1] - d.xl[1]));
+    }
     ctx->hy = 1.0 / ctx->hiy;
   }
   ctx->pitch = (ctx->nx + 63) / 64 * 64;
@@ -465,7 +476,7 @@ int sbp_create(const sbp_desc* desc, sbp_ctx** out) {
   if ((e = cudaMalloc((void**)&ctx->err, sizeof(int))) != cudaSuccess) return cuda_fail("cudaMalloc(err)", e);
   cudaMemset(ctx->err, 0, sizeof(int));
 
-  if (d.problem == SBP_WAVE_VAR_2D) {
+  if (has_fields(d.problem)) {
     const size_t np = (size_t)ctx->npts;
     double* rinv_h = new (std::nothrow) double[np];
     if (!rinv_h) return cuda_fail("host allocation", cudaErrorMemoryAllocation);
@@ -620,10 +631,10 @@ int sbp_hnorm(sbp_ctx* ctx, double* hn) {
   CK(cudaSetDevice(ctx->d.device));
   if (ctx->fp32)
     CK(launch_hnorm<float>((const float*)ctx->un, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane,
-                           ctx->d.order, ctx->hx, ctx->hy, ctx->partial, ctx->red, ctx->stream));
+                           ctx->d.order, ctx->hx, ctx->hy, ctx->ysplit, ctx->partial, ctx->red, ctx->stream));
   else
     CK(launch_hnorm<double>((const double*)ctx->un, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane,
-                            ctx->d.order, ctx->hx, ctx->hy, ctx->partial, ctx->red, ctx->stream));
+                            ctx->d.order, ctx->hx, ctx->hy, ctx->ysplit, ctx->partial, ctx->red, ctx->stream));
   ctx->launches += 2;
   double h = 0;
   CK(cudaMemcpyAsync(&h, ctx->red, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

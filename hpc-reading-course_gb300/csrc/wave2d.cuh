@@ -49,6 +49,8 @@ template <typename T> struct WaveParams {
   double bwx, bwy;    // hix * HI[0], hiy * HI[0]: SAT weights (FP64)
   T c_acc, c_w;       // acc (+)= c_acc * k ; w = u^n + c_w * k
   int bc;             // BcKind
+  int ysplit;         // 0: one block; else rows [0,ysplit) and [ysplit,ny) are two blocks
+                      // sharing an interface line (WK_VAR only)
   double t, xl0, xl1, hix, hiy;  // WK_MMS: stage time and grid geometry
   int* err;
 };
@@ -117,6 +119,56 @@ __device__ __forceinline__ T closure_line(const T* __restrict__ line, long long 
 
 __device__ __forceinline__ double mms_x(double xl, int i, double hi) { return xl + (double)i / hi; }
 
+template <typename T> struct Rhs3 { T u, v, p; };
+
+// SAT boundary terms at a boundary point, FP64 weights, in the reference's
+// order west, south, east, north. Kept out of line so interior points branch
+// around it instead of issuing its FP64 instructions under a predicate.
+template <typename T, int KIND>
+__device__ __noinline__ Rhs3<T> apply_sat(const WaveParams<T>& prm, int i, int j, T pc, T uc, T vc, Rhs3<T> k) {
+  const int nx = prm.nx, ny = prm.ny;
+  double rho = 1.0, kk = 1.0;
+  if constexpr (KIND == WK_VAR) {
+    rho = prm.rho64[(long long)j * nx + i];
+    kk = prm.k64[(long long)j * nx + i];
+  }
+  const double p64 = (double)pc;
+  double ku64 = (double)k.u, kv64 = (double)k.v, kp64 = (double)k.p;
+  if (prm.bc == BC_NONE) {
+    // matrix-free apply only
+  } else if (prm.bc == BC_FREE_SURFACE) {
+    // free_surface_bc_* (code/demo/wave_hom/wave_eq_hom_rhs.h:389-441); rho^-1 for WK_VAR
+    const double ri = (KIND == WK_VAR) ? 1.0 / rho : 1.0;
+    if (i == 0) ku64 = (KIND == WK_VAR) ? ku64 - ri * (prm.bwx * p64) : ku64 - prm.bwx * p64;
+    if (j == 0) kv64 = (KIND == WK_VAR) ? kv64 - ri * (prm.bwy * p64) : kv64 - prm.bwy * p64;
+    if (i == nx - 1) ku64 = (KIND == WK_VAR) ? ku64 + ri * (prm.bwx * p64) : ku64 + prm.bwx * p64;
+    if (j == ny - 1) kv64 = (KIND == WK_VAR) ? kv64 + ri * (prm.bwy * p64) : kv64 + prm.bwy * p64;
+  } else {
+    // characteristic SAT on the incoming characteristic p + Z u_n
+    const double z = sqrt(rho * kk), c = sqrt(kk / rho), hr = 0.5 / rho, hc = 0.5 * c;
+    const double u64 = (double)uc, v64 = (double)vc;
+    if (i == 0) { const double g = prm.bwx * (p64 + z * u64); ku64 -= hr * g; kp64 -= hc * g; }
+    if (j == 0) { const double g = prm.bwy * (p64 + z * v64); kv64 -= hr * g; kp64 -= hc * g; }
+    if (i == nx - 1) { const double g = prm.bwx * (p64 - z * u64); ku64 += hr * g; kp64 -= hc * g; }
+    if (j == ny - 1) { const double g = prm.bwy * (p64 - z * v64); kv64 += hr * g; kp64 -= hc * g; }
+  }
+  if constexpr (KIND == WK_VAR) {
+    // Interface line between the two blocks: energy-conserving SAT on the jumps
+    // of p and v (Carpenter, Nordstrom & Gottlieb 1999): lower block
+    // F_v += w/(2 rho) [p], F_p += w K/2 [v]; upper block with the opposite sign.
+    const int ys = prm.ysplit;
+    if (ys > 0 && prm.bc != BC_NONE && (j == ys - 1 || j == ys)) {
+      const int jo = (j == ys - 1) ? ys : ys - 1;  // the other block's copy of the line
+      const long long qo = (long long)jo * prm.pitch + i;
+      const double po = (double)prm.in[2 * prm.plane + qo], vo = (double)prm.in[prm.plane + qo];
+      const double s = (j == ys - 1) ? 1.0 : -1.0;
+      kv64 += s * (0.5 / rho) * (prm.bwy * (p64 - po));
+      kp64 += s * (0.5 * kk) * (prm.bwy * ((double)vc - vo));
+    }
+  }
+  return Rhs3<T>{(T)ku64, (T)kv64, (T)kp64};
+}
+
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
@@ -179,6 +231,9 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
   // ---------------- consumers: warps 0-7
   const long long pitch = prm.pitch, plane = prm.plane;
   constexpr int ROWS = TY / kWaveConsumerWarps;
+  // FP64 is bound by the FP64 pipe: unrolling the warp's rows gives more
+  // independent FMA chains. FP32 is bound by HBM and runs faster rolled.
+  constexpr int ROW_UNROLL = sizeof(T) == 8 ? ROWS : 1;
   constexpr int TPT = TY * kWaveTX;  // points per tile (one component)
   int k = 0;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
@@ -196,12 +251,16 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
     const T* sC = reinterpret_cast<const T*>(st + Tile::OFF_C);
     const int i0 = (tile % ntx) * kWaveTX, j0 = (tile / ntx) * TY;
 
-#pragma unroll 1
+#pragma unroll ROW_UNROLL
     for (int rr = 0; rr < ROWS; rr++) {
       const int y = warp * ROWS + rr;
       const int j = j0 + y;
-      if (j >= ny) break;
-      const bool yint = (j >= CS) && (j < ny - CS);
+      if (j >= ny) continue;
+      // block-local row (two-block problems: the interface rows close each block)
+      const int jb0 = (prm.ysplit > 0 && j >= prm.ysplit) ? prm.ysplit : 0;
+      const int nyb = (prm.ysplit > 0) ? (j >= prm.ysplit ? ny - prm.ysplit : prm.ysplit) : ny;
+      const int jl = j - jb0;
+      const bool yint = (jl >= CS) && (jl < nyb - CS);
 #pragma unroll
       for (int cc = 0; cc < kWaveTX / 32; cc++) {
         const int x = lane + 32 * cc;
@@ -229,7 +288,7 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
           for (int s = 1; s < W; s++)
             if (s != R) dyp = fma(prm.dy.taps[s], colP[s * PW], dyp);
         } else {
-          dyp = closure_line<T, ORD>(prm.in + 2 * plane + i, pitch, ny, j, prm.dy.cls);
+          dyp = closure_line<T, ORD>(prm.in + 2 * plane + (long long)jb0 * pitch + i, pitch, nyb, jl, prm.dy.cls);
         }
         if (xint) {
           kp = prm.dx.taps[0] * rowU[0];
@@ -244,7 +303,7 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
           for (int s = 0; s < W; s++)
             if (s != R) kp = fma(prm.dy.taps[s], colV[s * kWaveTX], kp);
         } else {
-          kp += closure_line<T, ORD>(prm.in + plane + i, pitch, ny, j, prm.dy.cls);
+          kp += closure_line<T, ORD>(prm.in + plane + (long long)jb0 * pitch + i, pitch, nyb, jl, prm.dy.cls);
         }
 
         const long long q = (long long)j * pitch + i;
@@ -268,35 +327,14 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
           kv = (T)(ri * (double)dyp + fv);
         }
 
-        // SAT boundary terms (FP64 weights), reference order west, south, east, north
-        const bool edge = (i == 0) || (j == 0) || (i == nx - 1) || (j == ny - 1);
+        // SAT boundary terms (boundary points only)
+        const bool edge = (i == 0) || (j == 0) || (i == nx - 1) || (j == ny - 1) ||
+                          (prm.ysplit > 0 && (j == prm.ysplit - 1 || j == prm.ysplit));
         if (prm.bc != BC_NONE && edge) {
-          double rho = 1.0, kk = 1.0;
-          if constexpr (KIND == WK_VAR) {
-            rho = prm.rho64[(long long)j * nx + i];
-            kk = prm.k64[(long long)j * nx + i];
-          }
-          const double p64 = (double)pc;
-          double ku64 = (double)ku, kv64 = (double)kv, kp64 = (double)kp;
-          if (prm.bc == BC_FREE_SURFACE) {
-            // free_surface_bc_* (code/demo/wave_hom/wave_eq_hom_rhs.h:389-441); rho^-1 for WK_VAR
-            const double ri = (KIND == WK_VAR) ? 1.0 / rho : 1.0;
-            if (i == 0) ku64 = (KIND == WK_VAR) ? ku64 - ri * (prm.bwx * p64) : ku64 - prm.bwx * p64;
-            if (j == 0) kv64 = (KIND == WK_VAR) ? kv64 - ri * (prm.bwy * p64) : kv64 - prm.bwy * p64;
-            if (i == nx - 1) ku64 = (KIND == WK_VAR) ? ku64 + ri * (prm.bwx * p64) : ku64 + prm.bwx * p64;
-            if (j == ny - 1) kv64 = (KIND == WK_VAR) ? kv64 + ri * (prm.bwy * p64) : kv64 + prm.bwy * p64;
-          } else {
-            // characteristic SAT on the incoming characteristic p + Z u_n
-            const double z = sqrt(rho * kk), c = sqrt(kk / rho), hr = 0.5 / rho, hc = 0.5 * c;
-            const double u64 = (double)uc, v64 = (double)vc;
-            if (i == 0) { const double g = prm.bwx * (p64 + z * u64); ku64 -= hr * g; kp64 -= hc * g; }
-            if (j == 0) { const double g = prm.bwy * (p64 + z * v64); kv64 -= hr * g; kp64 -= hc * g; }
-            if (i == nx - 1) { const double g = prm.bwx * (p64 - z * u64); ku64 += hr * g; kp64 -= hc * g; }
-            if (j == ny - 1) { const double g = prm.bwy * (p64 - z * v64); kv64 += hr * g; kp64 -= hc * g; }
-          }
-          ku = (T)ku64;
-          kv = (T)kv64;
-          kp = (T)kp64;
+          const Rhs3<T> r = apply_sat<T, KIND>(prm, i, j, pc, uc, vc, Rhs3<T>{ku, kv, kp});
+          ku = r.u;
+          kv = r.v;
+          kp = r.p;
         }
 
         // RK4 stage update (classical RK4, code/include/time_stepping/time_stepping.h:127-142)

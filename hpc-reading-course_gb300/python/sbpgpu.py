@@ -22,11 +22,13 @@ LIB_PATH = os.path.join(PKG, "lib", "libsbpgpu.so")
 OK, ERR_INVALID, ERR_CUDA, ERR_DEVICE, ERR_UNSUPPORTED, ERR_TOO_LARGE = 0, -1, -2, -3, -4, -5
 NOALLOC_MAX_PLANE = 65536
 WAVE_HOM_2D, WAVE_MMS_2D, ADVECTION_1D, ADVECTION_2D, REFLECTION_1D, WAVE_VAR_2D = 1, 2, 3, 4, 5, 6
+WAVE_2BLOCK_2D = 7
 BC_REFERENCE, BC_CHARACTERISTIC = 0, 1
 FP64, FP32 = 0, 1
 HOST, DEVICE = 0, 1
-TWO_D = {WAVE_HOM_2D, WAVE_MMS_2D, WAVE_VAR_2D, ADVECTION_2D}
-DOFS = {WAVE_HOM_2D: 3, WAVE_MMS_2D: 3, WAVE_VAR_2D: 3, ADVECTION_1D: 1, ADVECTION_2D: 1, REFLECTION_1D: 2}
+TWO_D = {WAVE_HOM_2D, WAVE_MMS_2D, WAVE_VAR_2D, ADVECTION_2D, WAVE_2BLOCK_2D}
+DOFS = {WAVE_HOM_2D: 3, WAVE_MMS_2D: 3, WAVE_VAR_2D: 3, ADVECTION_1D: 1, ADVECTION_2D: 1, REFLECTION_1D: 2,
+        WAVE_2BLOCK_2D: 3}
 
 # Every exported entry point of include/sbpgpu.h.
 EXPORTS = ("sbp_create", "sbp_destroy", "sbp_last_error", "sbp_dofs", "sbp_rhs", "sbp_apply", "sbp_rk4_nsteps",
@@ -182,6 +184,8 @@ class Context:
 
     @property
     def hy(self) -> float:
+        if self.problem == WAVE_2BLOCK_2D:
+            return 0.5 * (self.xr[1] - self.xl[1]) / (self.ny // 2 - 1)
         return (self.xr[1] - self.xl[1]) / (self.ny - 1) if self.problem in TWO_D else 1.0
 
     def _check(self, rc: int):

@@ -40,7 +40,10 @@ typedef enum {
   SBP_ADVECTION_1D = 3,  /* code/demo/advection, u_t + a u_x = 0 */
   SBP_ADVECTION_2D = 4,  /* code/demo/advection, u_t + a u_x + b u_y = 0 */
   SBP_REFLECTION_1D = 5, /* code/demo/reflection, [u;v]_t = [v_x;u_x] */
-  SBP_WAVE_VAR_2D = 6    /* (u,v,p) with rho(x,y), K(x,y) fields; no reference counterpart */
+  SBP_WAVE_VAR_2D = 6,   /* (u,v,p) with rho(x,y), K(x,y) fields; no reference counterpart */
+  SBP_WAVE_2BLOCK_2D = 7 /* two SBP_WAVE_VAR_2D blocks, rows [0,ny/2) and [ny/2,ny), sharing the
+                            line y = (xl[1]+xr[1])/2 (stored in both blocks), coupled by an
+                            energy-conserving interface SAT; no reference counterpart */
 } sbp_problem;
 
 typedef enum {

@@ -24,9 +24,11 @@ PORT_SO = os.path.join(HERE, "_build", "libsbporacle.so")
 REF_SO = os.path.join(HERE, "_ref", "libsbpref.so")
 
 WAVE_HOM_2D, WAVE_MMS_2D, ADVECTION_1D, ADVECTION_2D, REFLECTION_1D, WAVE_VAR_2D = 1, 2, 3, 4, 5, 6
+WAVE_2BLOCK_2D = 7
 BC_REFERENCE, BC_CHARACTERISTIC = 0, 1
-DOFS = {WAVE_HOM_2D: 3, WAVE_MMS_2D: 3, WAVE_VAR_2D: 3, ADVECTION_1D: 1, ADVECTION_2D: 1, REFLECTION_1D: 2}
-TWO_D = {WAVE_HOM_2D, WAVE_MMS_2D, WAVE_VAR_2D, ADVECTION_2D}
+DOFS = {WAVE_HOM_2D: 3, WAVE_MMS_2D: 3, WAVE_VAR_2D: 3, ADVECTION_1D: 1, ADVECTION_2D: 1, REFLECTION_1D: 2,
+        WAVE_2BLOCK_2D: 3}
+TWO_D = {WAVE_HOM_2D, WAVE_MMS_2D, WAVE_VAR_2D, ADVECTION_2D, WAVE_2BLOCK_2D}
 
 _dp = C.POINTER(C.c_double)
 
@@ -63,6 +65,8 @@ class Problem:
         self.xl, self.xr = tuple(xl), tuple(xr)
         self.hix = (nx - 1) / (xr[0] - xl[0])
         self.hiy = (self.ny - 1) / (xr[1] - xl[1]) if problem in TWO_D else 1.0
+        if problem == WAVE_2BLOCK_2D:  # each block: ny/2 points over half of [xl1, xr1]
+            self.hiy = (self.ny // 2 - 1) / ((xr[1] - xl[1]) / 2)
         self.a, self.b = a, b
         self.rho = None if rho is None else np.ascontiguousarray(rho, dtype=np.float64).ravel()
         self.K = None if K is None else np.ascontiguousarray(K, dtype=np.float64).ravel()
@@ -100,6 +104,8 @@ class Port:
         L.orc_hnorm1d_reference.restype = C.c_double
         L.orc_hnorm.argtypes = [_dp, C.c_longlong, C.c_longlong, C.c_longlong, C.c_double, C.c_double, C.c_int]
         L.orc_hnorm.restype = C.c_double
+        L.orc_hnorm_2block.argtypes = L.orc_hnorm.argtypes
+        L.orc_hnorm_2block.restype = C.c_double
         L.orc_error_l2.argtypes = [_dp, _dp, C.c_longlong, C.c_double]
         L.orc_error_l2.restype = C.c_double
         L.orc_error_max.argtypes = [_dp, _dp, C.c_longlong]
@@ -156,6 +162,10 @@ class Port:
     def hnorm(self, v, nx, ny, dofs, hx, hy, order):
         v = np.ascontiguousarray(v, dtype=np.float64)
         return self.lib.orc_hnorm(_ptr(v), nx, ny, dofs, hx, hy, order)
+
+    def hnorm_2block(self, v, nx, ny, dofs, hx, hy, order):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        return self.lib.orc_hnorm_2block(_ptr(v), nx, ny, dofs, hx, hy, order)
 
     def error_l2(self, v1, v2, hprod):
         v1 = np.ascontiguousarray(v1, dtype=np.float64)

@@ -84,7 +84,8 @@ int orc_dofs(int problem) {
   switch (problem) {
     case ORC_WAVE_HOM_2D:
     case ORC_WAVE_MMS_2D:
-    case ORC_WAVE_VAR_2D: return 3;
+    case ORC_WAVE_VAR_2D:
+    case ORC_WAVE_2BLOCK_2D: return 3;
     case ORC_ADVECTION_1D:
     case ORC_ADVECTION_2D: return 1;
     case ORC_REFLECTION_1D: return 2;
@@ -103,7 +104,7 @@ long long orc_min_points(int order) {
 
 static int is_2d(int problem) {
   return problem == ORC_WAVE_HOM_2D || problem == ORC_WAVE_MMS_2D || problem == ORC_WAVE_VAR_2D ||
-         problem == ORC_ADVECTION_2D;
+         problem == ORC_ADVECTION_2D || problem == ORC_WAVE_2BLOCK_2D;
 }
 
 static int check(const orc_problem* p) {
@@ -112,7 +113,8 @@ static int check(const orc_problem* p) {
   if (m < 0) return -2;
   if (p->nx < m) return -3;
   if (is_2d(p->problem) && p->ny < m) return -3;
-  if (p->problem == ORC_WAVE_VAR_2D && (!p->rho || !p->K)) return -4;
+  if ((p->problem == ORC_WAVE_VAR_2D || p->problem == ORC_WAVE_2BLOCK_2D) && (!p->rho || !p->K)) return -4;
+  if (p->problem == ORC_WAVE_2BLOCK_2D && (p->ny % 2 || p->ny / 2 < m)) return -3;
   return 0;
 }
 
@@ -130,6 +132,7 @@ int orc_apply(const orc_problem* p, double t, const double* src, double* dst) {
     case ORC_WAVE_HOM_2D: DISPATCH(wave_hom_apply, p, src, dst); break;
     case ORC_WAVE_MMS_2D: DISPATCH(wave_mms_apply, p, t, src, dst); break;
     case ORC_WAVE_VAR_2D: DISPATCH(wave_var_apply, p, src, dst); break;
+    case ORC_WAVE_2BLOCK_2D: DISPATCH(wave_2block_apply, p, src, dst); break;
     case ORC_ADVECTION_1D: DISPATCH(adv1d_apply, p, src, dst); break;
     case ORC_ADVECTION_2D: DISPATCH(adv2d_apply, p, src, dst); break;
     case ORC_REFLECTION_1D: DISPATCH(refl_apply, p, src, dst); break;
@@ -144,6 +147,7 @@ int orc_bc(const orc_problem* p, const double* src, double* dst) {
     case ORC_WAVE_HOM_2D:
     case ORC_WAVE_MMS_2D: DISPATCH(wave_free_surface_bc, p, src, dst); break;
     case ORC_WAVE_VAR_2D: DISPATCH(wave_var_bc, p, src, dst); break;
+    case ORC_WAVE_2BLOCK_2D: DISPATCH(wave_2block_bc, p, src, dst); break;
     case ORC_ADVECTION_1D: DISPATCH(adv1d_bc, p, src, dst); break;
     case ORC_ADVECTION_2D: DISPATCH(adv2d_bc, p, src, dst); break;
     case ORC_REFLECTION_1D: /* proj_dirichlet_bc_{l,r} (reflection_rhs.h:108-120) */
@@ -209,6 +213,16 @@ double orc_hnorm1d_reference(const double* v, long long n, long long dofs, doubl
     case 2: return hnorm1d_reference_o2(v, n, dofs, h);
     case 4: return hnorm1d_reference_o4(v, n, dofs, h);
     case 6: return hnorm1d_reference_o6(v, n, dofs, h);
+    default: return -1;
+  }
+}
+
+double orc_hnorm_2block(const double* v, long long nx, long long ny, long long dofs, double hx, double hy,
+                        int order) {
+  switch (order) {
+    case 2: return hnorm_2block_o2(v, nx, ny, dofs, hx, hy);
+    case 4: return hnorm_2block_o4(v, nx, ny, dofs, hx, hy);
+    case 6: return hnorm_2block_o6(v, nx, ny, dofs, hx, hy);
     default: return -1;
   }
 }

@@ -26,7 +26,9 @@ enum orc_problem_kind {
   ORC_ADVECTION_1D = 3, /* code/demo/advection/advection_rhs.h:12-140 */
   ORC_ADVECTION_2D = 4, /* code/demo/advection/advection_rhs.h:155-558 */
   ORC_REFLECTION_1D = 5,/* code/demo/reflection/reflection_rhs.h */
-  ORC_WAVE_VAR_2D = 6   /* rho(x,y), K(x,y) fields; no reference counterpart */
+  ORC_WAVE_VAR_2D = 6,  /* rho(x,y), K(x,y) fields; no reference counterpart */
+  ORC_WAVE_2BLOCK_2D = 7 /* two ORC_WAVE_VAR_2D blocks (rows [0,ny/2) and [ny/2,ny)) sharing the
+                            interface line y = (xl1+xr1)/2, coupled by an interface SAT */
 };
 
 enum orc_bc_kind {
@@ -45,6 +47,11 @@ typedef struct {
   const double* rho;  /* ORC_WAVE_VAR_2D: nx*ny density, row-major (j,i) */
   const double* K;    /* ORC_WAVE_VAR_2D: nx*ny bulk modulus */
 } orc_problem;
+
+/* ORC_WAVE_2BLOCK_2D: each block has ny/2 points in y over half the domain,
+ * hiy = (ny/2 - 1) / ((xr1 - xl1)/2); the last row of the lower block and the
+ * first row of the upper block are the same physical line. rho and K cover
+ * all nx*ny points (each block's own values on the interface line). */
 
 /* Number of components per grid point of a problem kind. */
 int orc_dofs(int problem);
@@ -73,6 +80,10 @@ double orc_hnorm1d_reference(const double* v, long long n, long long dofs, doubl
 /* H-norm with both closures, 1D or 2D (tensor product); nx*ny points. */
 double orc_hnorm(const double* v, long long nx, long long ny, long long dofs,
                  double hx, double hy, int order);
+
+/* H-norm of a two-block state (ny/2 rows per block, each block's quadrature). */
+double orc_hnorm_2block(const double* v, long long nx, long long ny, long long dofs, double hx, double hy,
+                        int order);
 
 /* Discrete L2 error sqrt(prod h) * ||v1 - v2||_2 and max error
  * (code/include/util/vec_util.h:47-61). n = total scalars. */

@@ -250,3 +250,60 @@ def test_large_grid_energy_and_symmetry(sbp, port):
     p = out[:, :, 2]
     assert np.max(np.abs(p - p[:, ::-1])) <= 1e-10 * np.max(np.abs(p))
     assert np.max(np.abs(p - p.T)) <= 1e-10 * np.max(np.abs(p))
+
+
+def _two_layer_fields(nx, ny, seed):
+    rng = np.random.default_rng(seed)
+    rho = 1.0 + rng.uniform(0, 2, (ny, nx))
+    K = 1.0 + rng.uniform(0, 2, (ny, nx))
+    rho[ny // 2:] *= 4.0
+    K[ny // 2:] *= 4.0
+    return rho.ravel(), K.ravel()
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+@pytest.mark.parametrize("bc", [0, 1])
+@pytest.mark.parametrize("size", [(40, 2 * 29), (130, 2 * 70)])
+def test_two_block_interface_rhs(sbp, port, order, bc, size):
+    nx, ny = size
+    rho, K = _two_layer_fields(nx, ny, order + bc)
+    src = np.random.default_rng(13).standard_normal(3 * nx * ny)
+    pb = O.Problem(O.WAVE_2BLOCK_2D, order, nx, ny, rho=rho, K=K, bc=bc)
+    with _ctx(sbp, sbp.WAVE_2BLOCK_2D, order, nx, ny, rho=rho, K=K, bc=bc) as c:
+        assert relerr(c.rhs(src), port.rhs(pb, src)) <= TOL64
+        assert relerr(c.apply(src), port.apply(pb, src)) <= TOL64
+
+
+@pytest.mark.parametrize("order", [4, 6])
+def test_two_block_rk4_and_energy(sbp, port, order):
+    nx, ny = 96, 2 * 64
+    rho, K = _two_layer_fields(nx, ny, 5)
+    pb = O.Problem(O.WAVE_2BLOCK_2D, order, nx, ny, rho=rho, K=K, bc=1)
+    v0 = port.init_wave_pulse(nx, ny, 0.0, -0.2, 0.2, 1.0)
+    hy = 1.0 / (ny // 2 - 1)
+    dt = 0.2 * hy / np.sqrt((K / rho).max())
+    with _ctx(sbp, sbp.WAVE_2BLOCK_2D, order, nx, ny, rho=rho, K=K, bc=1) as c:
+        got = c.rk4(v0, 0.0, dt, 60)
+        c.set_state(got)
+        hn = c.hnorm()
+    assert relerr(got, port.rk4(pb, v0, 0.0, dt, 60)) <= TOL64
+    assert hn == pytest.approx(port.hnorm_2block(got, nx, ny, 3, 2.0 / (nx - 1), hy, order), rel=1e-13)
+
+
+def test_two_block_reflection_coefficient_on_gpu(sbp):
+    """Impedance ratio 4 across y = 0 (equal speeds): R = 0.6, T = 1.6."""
+    nx, nb, order = 81, 161, 4
+    ny = 2 * nb
+    rho = np.ones((ny, nx))
+    rho[nb:] = 4.0
+    rho = rho.ravel()
+    y = np.concatenate([np.linspace(-1, 0, nb), np.linspace(0, 1, nb)])
+    p = np.exp(-((y + 0.35) / 0.06) ** 2)
+    v = np.zeros((ny, nx, 3))
+    v[:, :, 2] = p[:, None]
+    v[:, :, 1] = p[:, None]
+    with sbp.Context(sbp.WAVE_2BLOCK_2D, order, nx, ny, rho=rho, K=rho.copy(), bc=1) as c:
+        out = c.ts_rk4(v.ravel(), 0.7, 0.2 / (nb - 1)).reshape(ny, nx, 3)
+    col = out[:, nx // 2, 2]
+    assert col[:nb].max() == pytest.approx(0.6, abs=0.01)
+    assert col[nb:].max() == pytest.approx(1.6, abs=0.01)

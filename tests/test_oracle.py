@@ -201,3 +201,70 @@ def test_error_norm_definitions(port):
     a, b = rng.standard_normal(1000), rng.standard_normal(1000)
     assert port.error_l2(a, b, 0.01) == pytest.approx(math.sqrt(0.01) * np.linalg.norm(a - b), rel=1e-14)
     assert port.error_max(a, b) == np.max(np.abs(a - b))
+
+
+def _two_layer(nx, ny, zr=4.0):
+    """rho = K = 1 below y = 0, rho = K = zr above (impedance ratio zr, equal speeds)."""
+    rho = np.ones((ny, nx))
+    rho[ny // 2:, :] = zr
+    return rho.ravel(), rho.ravel().copy()
+
+
+def _energy_rate(port, pb, v, rho, K, two_block=True):
+    """d/dt sum H (rho|u|^2 + p^2/K)/2 for the semi-discrete system: sum H (rho u.F_u + p F_p / K)."""
+    F = port.rhs(pb, v)
+    q, f = v.reshape(-1, 3), F.reshape(-1, 3)
+    w = np.empty_like(v).reshape(-1, 3)
+    w[:, 0] = rho * q[:, 0] * f[:, 0]
+    w[:, 1] = rho * q[:, 1] * f[:, 1]
+    w[:, 2] = q[:, 2] * f[:, 2] / K
+    # sum H w via the H-norm of sqrt-free weights: use hnorm on a field whose square is |w|
+    hx, hy = 1.0 / pb.hix, 1.0 / pb.hiy
+    pos, neg = np.sqrt(np.maximum(w, 0)).ravel(), np.sqrt(np.maximum(-w, 0)).ravel()
+    hn = port.hnorm_2block if two_block else port.hnorm
+    return hn(pos, pb.nx, pb.ny, 3, hx, hy, pb.order) ** 2 - hn(neg, pb.nx, pb.ny, 3, hx, hy, pb.order) ** 2
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+def test_interface_sat_conserves_energy(port, order):
+    """Free-surface outer boundaries + the interface SAT: the semi-discrete
+    energy rate is zero to rounding, for any state and any coefficients."""
+    nx, ny = 37, 2 * 29
+    rng = np.random.default_rng(order)
+    rho = 1.0 + rng.uniform(0, 3, nx * ny)
+    K = 1.0 + rng.uniform(0, 3, nx * ny)
+    pb = O.Problem(O.WAVE_2BLOCK_2D, order, nx, ny, rho=rho, K=K)
+    v = rng.standard_normal(3 * nx * ny)
+    rate = _energy_rate(port, pb, v, rho, K)
+    scale = np.abs(port.rhs(pb, v)).max() * np.abs(v).max()
+    assert abs(rate) < 1e-12 * scale
+    pbc = O.Problem(O.WAVE_2BLOCK_2D, order, nx, ny, rho=rho, K=K, bc=O.BC_CHARACTERISTIC)
+    assert _energy_rate(port, pbc, v, rho, K) < 1e-12 * scale  # characteristic outer boundary: dissipative
+
+
+@pytest.mark.parametrize("order", [4, 6])
+def test_interface_reflection_coefficient(port, order):
+    """A pressure pulse travelling in +y meets a layer with 4x the impedance:
+    reflected amplitude R = (Z2-Z1)/(Z2+Z1) = 0.6, transmitted T = 1 + R = 1.6."""
+    nx, nb = 81, 161
+    ny = 2 * nb
+    rho, K = _two_layer(nx, ny, 4.0)
+    pb = O.Problem(O.WAVE_2BLOCK_2D, order, nx, ny, rho=rho, K=K, bc=O.BC_CHARACTERISTIC)
+    x = np.linspace(-1, 1, nx)
+    yl = np.linspace(-1, 0, nb)
+    yu = np.linspace(0, 1, nb)
+    y = np.concatenate([yl, yu])
+    v = np.zeros((ny, nx, 3))
+    y0, w = -0.35, 0.06
+    p = np.exp(-((y - y0) / w) ** 2)
+    v[:, :, 2] = p[:, None]
+    v[:, :, 1] = p[:, None] / 1.0  # v = p / Z1 (right-moving in y)
+    h = 1.0 / (nb - 1)
+    T = 0.7
+    nt, dt = port.rk4_nsteps(T, 0.2 * h)
+    out = port.rk4(pb, v.ravel(), 0.0, dt, nt).reshape(ny, nx, 3)
+    col = out[:, nx // 2, 2]  # x = 0: untouched by the x-boundaries before t = 1
+    reflected = col[:nb].max()  # the reflected pulse, centred near y = -0.35 at t = 0.7
+    transmitted = col[nb:].max()
+    assert reflected == pytest.approx(0.6, abs=0.01)
+    assert transmitted == pytest.approx(1.6, abs=0.01)
