@@ -56,9 +56,11 @@ def parse():
     ap.add_argument("--bc", default="characteristic", choices=["characteristic", "free_surface"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--study", default=None, choices=["precision"],
+    ap.add_argument("--study", default=None, choices=["precision", "batched"],
                     help="precision: variable rho, K (seeded Fourier fields) to --t-end in FP64 and in "
-                         "compensated FP32; prints errors of FP32 against FP64 and both wall times")
+                         "compensated FP32; prints errors of FP32 against FP64 and both wall times. "
+                         "batched: 512 uneven wave/advection instances in one batch, FP64 and FP32")
+    ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--t-end", type=float, default=1.0)
     return ap.parse_args()
 
@@ -256,10 +258,81 @@ def run_precision_study(args):
     print(json.dumps(line), flush=True)
 
 
+def batched_instances(count: int, seed: int = 2):
+    """N = round(exp(U[ln 64, ln 512])) per side, order from {2, 4, 6}, speed c ~ U[0.5, 2];
+    even members are waves (rho = 1, K = c^2, characteristic SAT), odd members advection
+    with |(a, b)| = c in a random direction; dt = 0.2 h / c; pulses centred in [-0.5, 0.5]^2."""
+    import numpy as np
+
+    import sbpgpu
+
+    rng = np.random.default_rng(seed)
+    insts, states = [], []
+    for k in range(count):
+        nx = int(round(np.exp(rng.uniform(np.log(64), np.log(512)))))
+        ny = int(round(np.exp(rng.uniform(np.log(64), np.log(512)))))
+        order = int(rng.choice([2, 4, 6]))
+        c = float(rng.uniform(0.5, 2.0))
+        x0, y0 = rng.uniform(-0.5, 0.5, 2)
+        h = min(2.0 / (nx - 1), 2.0 / (ny - 1))
+        if k % 2 == 0:
+            insts.append(dict(problem=sbpgpu.WAVE_HOM_2D, order=order, nx=nx, ny=ny, c=c, dt=0.2 * h / c,
+                              bc=sbpgpu.BC_CHARACTERISTIC))
+            states.append(fields.gaussian_pulse(nx, ny, x0, y0, 0.1, 1.0))
+        else:
+            ang = rng.uniform(0.0, 2 * np.pi)
+            insts.append(dict(problem=sbpgpu.ADVECTION_2D, order=order, nx=nx, ny=ny, a=c * np.cos(ang),
+                              b=c * np.sin(ang), dt=0.2 * h / c))
+            x = np.linspace(-1, 1, nx) - x0
+            y = np.linspace(-1, 1, ny) - y0
+            states.append(np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / 0.1**2).ravel())
+    return insts, states
+
+
+def run_batched_study(args):
+    """One batch of --instances uneven instances; 100-step graph chunks; autotuned tile heights."""
+    import torch
+
+    import build as gpu_build
+    import sbpgpu
+
+    gpu_build.build()
+    insts, states = batched_instances(args.instances)
+    cache = os.environ.get("SBP_TUNE_CACHE", os.path.join(PKG, "_build", "batch_tiles.json"))
+    out = {"study": "batched", "instances": len(insts),
+           "waves": sum(1 for d in insts if d["problem"] == sbpgpu.WAVE_HOM_2D),
+           "orders": {o: sum(1 for d in insts if d["order"] == o) for o in (2, 4, 6)}}
+    for name, prec in (("fp64", sbpgpu.FP64), ("fp32", sbpgpu.FP32)):
+        with sbpgpu.Batch(insts, precision=prec) as b:
+            for k, v in enumerate(states):
+                b.set_state(k, v)
+            b.autotune(cache)
+            stream = torch.cuda.ExternalStream(b.stream)
+            b.step_resident(100)  # warm-up: graph capture
+            b.synchronize()
+            launches0 = b.launches
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            chunks = max(1, args.steps)
+            ev0.record(stream)
+            b.step_resident(100 * chunks)
+            ev1.record(stream)
+            b.synchronize()
+            sec = ev0.elapsed_time(ev1) / 1e3
+            units = b.points * 4 * 100 * chunks
+            out[name] = {"value": units / sec, "unit": UNIT, "seconds": sec, "rk4_steps": 100 * chunks,
+                         "points": b.points, "tile_heights": {o: b.tile_height(o) for o in (2, 4, 6)},
+                         "gpu_launches": b.launches - launches0}
+    out["tune_cache"] = cache
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.study == "precision":
         run_precision_study(args)
+        return
+    if args.study == "batched":
+        run_batched_study(args)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -39,10 +39,13 @@ def units():
     out = []
     for order in (2, 4, 6):
         out.append((f"wave2d_o{order}.o", "wave2d_inst.cu", [f"-DSBP_ORDER={order}"]))
+    for order in (2, 4, 6):
+        out.append((f"wave_batch_o{order}.o", "wave_batch_inst.cu", [f"-DSBP_ORDER={order}"]))
     out.append(("kernels.o", "kernels.cu", []))
     out.append(("sbp_runtime.o", "sbp_runtime.cpp", ["-x", "cu"]))
     out.append(("noalloc.o", "noalloc.cu", []))
     out.append(("petsc_io.o", "petsc_io.cpp", []))
+    out.append(("batch_runtime.o", "batch_runtime.cpp", ["-x", "cu"]))
     return out
 
 

@@ -1,0 +1,639 @@
+// batch_runtime.cpp -- the batched form behind include/sbpgpu.h (sbp_batch_*):
+// many independent 2D wave (rho = 1, K = c^2) and 2D advection instances of
+// uneven size and order, each with its own time step, advanced together.
+//
+// Device data: one pool per state buffer (u^n, acc, wa, wb, comp) holding
+// every instance's SoA planes; an array of per-instance parameter blocks and
+// (wave) tensor maps; per operator order, a tile list of (instance, tile)
+// pairs. Each RK4 stage launches, per order group, one persistent wave kernel
+// over its tile list and one advection kernel over its tiles. The step loop is
+// captured into CUDA graphs of 100 steps.
+//
+// Autotuner: the tile height of each order group's wave kernel (FP64 8 or
+// 16 rows, FP32 16 or 32) is chosen by timing the stage kernel on the batch
+// itself; choices are cached in a flat JSON file keyed by device, precision,
+// order and the group's size.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/sbpgpu.h"
+#include "launch.h"
+#include "sbp_ops.h"
+
+using namespace sbp;
+
+namespace {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+thread_local std::string g_batch_create_error;
+
+struct Geo {
+  bool wave;
+  int order, dofs;
+  long long nx, ny, pitch, plane;
+  size_t off;  // byte offset of the instance's planes in each pool
+};
+
+}  // namespace
+
+struct sbp_batch {
+  int precision = SBP_FP64, device = 0;
+  bool fp32 = false;
+  size_t es = 8;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::vector<sbp_instance> inst;
+  std::vector<Geo> geo;
+  size_t pool_bytes = 0, max_scalars = 0;
+  void *un = nullptr, *acc = nullptr, *wa = nullptr, *wb = nullptr, *comp = nullptr;
+  void* d_wave = nullptr;        // BatchWave<T>[n_wave]
+  CUtensorMap* d_maps = nullptr; // kBatchMaps per wave instance
+  void* d_line = nullptr;        // BatchLine<T>[n_line]
+  std::vector<int> wave_slot, line_slot;  // instance -> slot in d_wave / d_line (-1 if other kind)
+  int2* d_tiles_wave[3] = {nullptr, nullptr, nullptr};
+  int n_tiles_wave[3] = {0, 0, 0};
+  int2* d_tiles_line[3] = {nullptr, nullptr, nullptr};
+  int n_tiles_line[3] = {0, 0, 0};
+  int ty[3] = {0, 0, 0};
+  double* io = nullptr;
+  int* err = nullptr;
+  std::map<long long, cudaGraphExec_t> graphs;
+  long long launches = 0, points = 0;
+  std::string msg;
+};
+
+namespace {
+
+int bfail(sbp_batch* b, int code, const std::string& m) {
+  if (b) b->msg = m;
+  return code;
+}
+
+#define BCK(call)                                                                          \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return bfail(b, SBP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+  } while (0)
+
+int order_index(int order) { return order / 2 - 1; }
+
+template <typename T>
+void fill_taps(DirTaps<T>& t, int order, double scale) {
+  const ops::Operator& op = ops::get(order);
+  std::memset(&t, 0, sizeof(t));
+  for (int s = 0; s < op.width; s++) t.taps[s] = (T)(scale * op.interior[s]);
+  for (int r = 0; r < op.cls_sz; r++)
+    for (int s = 0; s < op.cls_width; s++) t.cls[r][s] = (T)(scale * op.closure[r][s]);
+}
+
+void* at(void* pool, size_t off) { return pool ? static_cast<unsigned char*>(pool) + off : nullptr; }
+
+int default_ty(bool fp32) { return fp32 ? 32 : 16; }
+
+// Encodes the 12 tensor maps of one wave instance for tile height ty.
+int encode_instance_maps(sbp_batch* b, int i, int ty, CUtensorMap* out) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return bfail(b, SBP_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const Geo& g = b->geo[i];
+  const int R = g.order / 2, hxa = 16 / (int)b->es;
+  const int HX = (R + hxa - 1) / hxa * hxa, HY = R;
+  const cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, 3};
+  const cuuint64_t strides[2] = {(cuuint64_t)(g.pitch * b->es), (cuuint64_t)(g.plane * b->es)};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const cuuint32_t boxP[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)(ty + 2 * HY), 1};
+  const cuuint32_t boxU[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)ty, 1};
+  const cuuint32_t boxV[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)(ty + 2 * HY), 1};
+  const cuuint32_t boxPt[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)ty, 3};
+  const CUtensorMapDataType dt = b->fp32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  void* inputs[3] = {at(b->un, g.off), at(b->wa, g.off), at(b->wb, g.off)};
+  struct Req { void* base; const cuuint32_t* box; } reqs[kBatchMaps] = {
+      {inputs[0], boxP}, {inputs[0], boxU}, {inputs[0], boxV}, {inputs[1], boxP}, {inputs[1], boxU},
+      {inputs[1], boxV}, {inputs[2], boxP}, {inputs[2], boxU}, {inputs[2], boxV}, {at(b->un, g.off), boxPt},
+      {at(b->acc, g.off), boxPt}, {b->comp ? at(b->comp, g.off) : at(b->acc, g.off), boxPt}};
+  for (int k = 0; k < kBatchMaps; k++)
+    if (enc(&out[k], dt, 3, reqs[k].base, dims, strides, reqs[k].box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+        CUDA_SUCCESS)
+      return bfail(b, SBP_ERR_CUDA, "cuTensorMapEncodeTiled failed for a batched instance");
+  return SBP_OK;
+}
+
+// (Re)builds the tensor maps and tile list of one order group for tile height ty.
+int build_wave_group(sbp_batch* b, int oi, int ty) {
+  const int order = 2 * (oi + 1);
+  std::vector<int2> tiles;
+  std::vector<CUtensorMap> maps;
+  std::vector<int> slots;
+  for (size_t i = 0; i < b->inst.size(); i++) {
+    const Geo& g = b->geo[i];
+    if (!g.wave || g.order != order) continue;
+    const int s = b->wave_slot[i];
+    const long long ntx = (g.nx + kWaveTX - 1) / kWaveTX, nty = (g.ny + ty - 1) / ty;
+    for (long long t = 0; t < ntx * nty; t++) tiles.push_back(make_int2(s, (int)t));
+    CUtensorMap m[kBatchMaps];
+    int rc = encode_instance_maps(b, (int)i, ty, m);
+    if (rc) return rc;
+    BCK(cudaMemcpyAsync(b->d_maps + (size_t)s * kBatchMaps, m, sizeof(m), cudaMemcpyHostToDevice, b->stream));
+  }
+  if (b->d_tiles_wave[oi]) cudaFree(b->d_tiles_wave[oi]);
+  b->d_tiles_wave[oi] = nullptr;
+  b->n_tiles_wave[oi] = (int)tiles.size();
+  if (!tiles.empty()) {
+    BCK(cudaMalloc((void**)&b->d_tiles_wave[oi], tiles.size() * sizeof(int2)));
+    BCK(cudaMemcpyAsync(b->d_tiles_wave[oi], tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                        b->stream));
+    BCK(b->fp32 ? configure_wave_batch<float>(order, ty) : configure_wave_batch<double>(order, ty));
+  }
+  b->ty[oi] = ty;
+  BCK(cudaStreamSynchronize(b->stream));
+  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  b->graphs.clear();
+  return SBP_OK;
+}
+
+template <typename T>
+int fill_params(sbp_batch* b) {
+  std::vector<BatchWave<T>> waves;
+  std::vector<BatchLine<T>> lines;
+  for (size_t i = 0; i < b->inst.size(); i++) {
+    const sbp_instance& d = b->inst[i];
+    const Geo& g = b->geo[i];
+    const double hix = (g.nx - 1) / (d.xr[0] - d.xl[0]), hiy = (g.ny - 1) / (d.xr[1] - d.xl[1]);
+    const double hi0 = ops::get(d.order).hinv0;
+    if (g.wave) {
+      BatchWave<T> w;
+      std::memset(&w, 0, sizeof(w));
+      WaveParams<T>& p = w.prm;
+      p.nx = (int)g.nx;
+      p.ny = (int)g.ny;
+      p.pitch = g.pitch;
+      p.plane = g.plane;
+      p.un = (T*)at(b->un, g.off);
+      p.acc = (T*)at(b->acc, g.off);
+      p.comp = (T*)at(b->comp, g.off);
+      fill_taps<T>(p.dx, d.order, -hix);
+      fill_taps<T>(p.dy, d.order, -hiy);
+      p.bwx = hix * hi0;
+      p.bwy = hiy * hi0;
+      p.kconst = (T)(d.c * d.c);
+      p.dt = d.dt;
+      p.bc = d.bc == SBP_BC_CHARACTERISTIC ? BC_CHARACTERISTIC : BC_FREE_SURFACE;
+      p.err = b->err;
+      w.wa = (T*)at(b->wa, g.off);
+      w.wb = (T*)at(b->wb, g.off);
+      waves.push_back(w);
+    } else {
+      BatchLine<T> l;
+      std::memset(&l, 0, sizeof(l));
+      LineParams<T>& p = l.prm;
+      p.nx = (int)g.nx;
+      p.ny = (int)g.ny;
+      p.pitch = g.pitch;
+      p.plane = g.plane;
+      p.un = (T*)at(b->un, g.off);
+      p.acc = (T*)at(b->acc, g.off);
+      p.comp = (T*)at(b->comp, g.off);
+      fill_taps<T>(p.dx, d.order, -d.a * hix);
+      fill_taps<T>(p.dy, d.order, -d.b * hiy);
+      p.sat[0] = 0.5 * (-0.5 * (d.a + std::fabs(d.a))) * (hix * hi0);
+      p.sat[1] = 0.5 * (-0.5 * (d.b + std::fabs(d.b))) * (hiy * hi0);
+      p.sat[2] = 0.5 * (0.5 * (d.a - std::fabs(d.a))) * (hix * hi0);
+      p.sat[3] = 0.5 * (0.5 * (d.b - std::fabs(d.b))) * (hiy * hi0);
+      p.bc = 1;
+      p.compensated = b->fp32 ? 1 : 0;
+      p.err = b->err;
+      l.wa = (T*)at(b->wa, g.off);
+      l.wb = (T*)at(b->wb, g.off);
+      l.dt = d.dt;
+      lines.push_back(l);
+    }
+  }
+  if (!waves.empty()) {
+    BCK(cudaMalloc(&b->d_wave, waves.size() * sizeof(BatchWave<T>)));
+    BCK(cudaMemcpy(b->d_wave, waves.data(), waves.size() * sizeof(BatchWave<T>), cudaMemcpyHostToDevice));
+    BCK(cudaMalloc((void**)&b->d_maps, waves.size() * kBatchMaps * sizeof(CUtensorMap)));
+  }
+  if (!lines.empty()) {
+    BCK(cudaMalloc(&b->d_line, lines.size() * sizeof(BatchLine<T>)));
+    BCK(cudaMemcpy(b->d_line, lines.data(), lines.size() * sizeof(BatchLine<T>), cudaMemcpyHostToDevice));
+  }
+  // advection tile lists (32 x 8 points per CTA)
+  for (int oi = 0; oi < 3; oi++) {
+    std::vector<int2> tiles;
+    for (size_t i = 0; i < b->inst.size(); i++) {
+      const Geo& g = b->geo[i];
+      if (g.wave || order_index(g.order) != oi) continue;
+      const long long ntx = (g.nx + kLineTileX - 1) / kLineTileX, nty = (g.ny + kLineTileY - 1) / kLineTileY;
+      for (long long t = 0; t < ntx * nty; t++) tiles.push_back(make_int2(b->line_slot[i], (int)t));
+    }
+    b->n_tiles_line[oi] = (int)tiles.size();
+    if (!tiles.empty()) {
+      BCK(cudaMalloc((void**)&b->d_tiles_line[oi], tiles.size() * sizeof(int2)));
+      BCK(cudaMemcpy(b->d_tiles_line[oi], tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    }
+  }
+  for (int oi = 0; oi < 3; oi++) {
+    int rc = build_wave_group(b, oi, default_ty(b->fp32));
+    if (rc) return rc;
+  }
+  return SBP_OK;
+}
+
+template <typename T>
+int launch_stage_all(sbp_batch* b, int stage, int rk) {
+  for (int oi = 0; oi < 3; oi++) {
+    const int order = 2 * (oi + 1);
+    if (b->n_tiles_wave[oi]) {
+      BCK(launch_wave_batch<T>(order, stage, b->ty[oi], (const BatchWave<T>*)b->d_wave, b->d_maps,
+                               b->d_tiles_wave[oi], b->n_tiles_wave[oi], rk, b->err, b->stream));
+      b->launches++;
+    }
+    if (b->n_tiles_line[oi]) {
+      BCK(launch_adv_batch<T>(order, stage, (const BatchLine<T>*)b->d_line, b->d_tiles_line[oi],
+                              b->n_tiles_line[oi], rk, b->stream));
+      b->launches++;
+    }
+  }
+  return SBP_OK;
+}
+
+template <typename T>
+int enqueue_step(sbp_batch* b) {
+  int rc;
+  if ((rc = launch_stage_all<T>(b, ST_FIRST, 1))) return rc;
+  if ((rc = launch_stage_all<T>(b, ST_MID, 2))) return rc;
+  if ((rc = launch_stage_all<T>(b, ST_MID, 3))) return rc;
+  return launch_stage_all<T>(b, ST_LAST, 4);
+}
+
+long long kernels_per_step(const sbp_batch* b) {
+  long long n = 0;
+  for (int oi = 0; oi < 3; oi++) n += (b->n_tiles_wave[oi] ? 1 : 0) + (b->n_tiles_line[oi] ? 1 : 0);
+  return 4 * n;
+}
+
+template <typename T>
+int run_chunk(sbp_batch* b, long long steps) {
+  auto it = b->graphs.find(steps);
+  if (it == b->graphs.end()) {
+    cudaGraph_t g = nullptr;
+    BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = b->launches;
+    int rc = SBP_OK;
+    for (long long s = 0; s < steps && rc == SBP_OK; s++) rc = enqueue_step<T>(b);
+    cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+    b->launches = before;
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    BCK(ce);
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    BCK(ie);
+    it = b->graphs.emplace(steps, ex).first;
+  }
+  BCK(cudaGraphLaunch(it->second, b->stream));
+  b->launches += kernels_per_step(b) * steps;
+  return SBP_OK;
+}
+
+// ---- tiny flat JSON cache {"key": int, ...}
+std::map<std::string, int> read_cache(const char* path) {
+  std::map<std::string, int> m;
+  if (!path) return m;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return m;
+  std::string s;
+  char buf[4096];
+  size_t n;
+  while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0) s.append(buf, n);
+  std::fclose(f);
+  size_t p = 0;
+  while ((p = s.find('"', p)) != std::string::npos) {
+    const size_t q = s.find('"', p + 1);
+    if (q == std::string::npos) break;
+    const std::string key = s.substr(p + 1, q - p - 1);
+    const size_t c = s.find(':', q);
+    if (c == std::string::npos) break;
+    m[key] = std::atoi(s.c_str() + c + 1);
+    p = s.find_first_of(",}", c);
+    if (p == std::string::npos) break;
+  }
+  return m;
+}
+
+void write_cache(const char* path, const std::map<std::string, int>& m) {
+  if (!path) return;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return;
+  std::fputs("{", f);
+  bool first = true;
+  for (const auto& kv : m) {
+    std::fprintf(f, "%s\n  \"%s\": %d", first ? "" : ",", kv.first.c_str(), kv.second);
+    first = false;
+  }
+  std::fputs("\n}\n", f);
+  std::fclose(f);
+}
+
+void release(sbp_batch* b) {
+  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  b->graphs.clear();
+  void* bufs[] = {b->un, b->acc, b->wa, b->wb, b->comp, b->d_wave, b->d_maps, b->d_line, b->io, b->err};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  for (int oi = 0; oi < 3; oi++) {
+    if (b->d_tiles_wave[oi]) cudaFree(b->d_tiles_wave[oi]);
+    if (b->d_tiles_line[oi]) cudaFree(b->d_tiles_line[oi]);
+  }
+  if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int sbp_batch_create(const sbp_instance* list, int count, int precision, int device, void* stream, sbp_batch** out) {
+  if (!list || count <= 0 || !out) {
+    g_batch_create_error = "need a non-empty instance list and an output pointer";
+    return SBP_ERR_INVALID;
+  }
+  *out = nullptr;
+  if (precision != SBP_FP64 && precision != SBP_FP32) {
+    g_batch_create_error = "unknown precision";
+    return SBP_ERR_INVALID;
+  }
+  sbp_batch* b = new (std::nothrow) sbp_batch();
+  if (!b) return SBP_ERR_INVALID;
+  b->precision = precision;
+  b->fp32 = precision == SBP_FP32;
+  b->es = b->fp32 ? 4 : 8;
+  b->device = device;
+  b->inst.assign(list, list + count);
+  size_t off = 0;
+  int nw = 0, nl = 0;
+  for (int i = 0; i < count; i++) {
+    const sbp_instance& d = list[i];
+    const bool wave = d.problem == SBP_WAVE_HOM_2D;
+    std::string bad;
+    if (!wave && d.problem != SBP_ADVECTION_2D) bad = "instances must be SBP_WAVE_HOM_2D or SBP_ADVECTION_2D";
+    else if (d.order != 2 && d.order != 4 && d.order != 6) bad = "order must be 2, 4 or 6";
+    else if (d.nx < ops::min_points(d.order) || d.ny < ops::min_points(d.order) || d.nx > (1 << 20) || d.ny > (1 << 20))
+      bad = "grid outside [operator minimum, 2^20] points per direction";
+    else if (!(d.xr[0] > d.xl[0]) || !(d.xr[1] > d.xl[1])) bad = "empty domain";
+    else if (!(d.dt > 0)) bad = "dt must be positive";
+    else if (wave && !(d.c > 0)) bad = "wave speed must be positive";
+    else if (wave && d.bc != SBP_BC_REFERENCE && d.bc != SBP_BC_CHARACTERISTIC) bad = "unknown boundary treatment";
+    if (!bad.empty()) {
+      g_batch_create_error = "instance " + std::to_string(i) + ": " + bad;
+      delete b;
+      return SBP_ERR_INVALID;
+    }
+    Geo g;
+    g.wave = wave;
+    g.order = d.order;
+    g.dofs = wave ? 3 : 1;
+    g.nx = d.nx;
+    g.ny = d.ny;
+    g.pitch = (d.nx + 63) / 64 * 64;
+    g.plane = g.pitch * d.ny;
+    g.off = off;
+    off += ((size_t)g.dofs * g.plane * b->es + 255) / 256 * 256;
+    b->geo.push_back(g);
+    b->wave_slot.push_back(wave ? nw++ : -1);
+    b->line_slot.push_back(wave ? -1 : nl++);
+    b->points += d.nx * d.ny;
+    b->max_scalars = std::max(b->max_scalars, (size_t)(g.dofs * d.nx * d.ny));
+  }
+  b->pool_bytes = off;
+  auto cuda_fail = [&](const char* what, cudaError_t e) {
+    g_batch_create_error = std::string(what) + ": " + cudaGetErrorString(e);
+    release(b);
+    delete b;
+    return SBP_ERR_CUDA;
+  };
+  cudaError_t e;
+  if ((e = cudaSetDevice(device)) != cudaSuccess) return cuda_fail("cudaSetDevice", e);
+  if (stream) {
+    b->stream = (cudaStream_t)stream;
+  } else {
+    if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess)
+      return cuda_fail("cudaStreamCreate", e);
+    b->own_stream = true;
+  }
+  void** pools[] = {&b->un, &b->acc, &b->wa, &b->wb};
+  for (void** p : pools) {
+    if ((e = cudaMalloc(p, b->pool_bytes)) != cudaSuccess) return cuda_fail("cudaMalloc(pool)", e);
+    cudaMemset(*p, 0, b->pool_bytes);
+  }
+  if (b->fp32) {
+    if ((e = cudaMalloc(&b->comp, b->pool_bytes)) != cudaSuccess) return cuda_fail("cudaMalloc(comp)", e);
+    cudaMemset(b->comp, 0, b->pool_bytes);
+  }
+  if ((e = cudaMalloc((void**)&b->io, b->max_scalars * sizeof(double))) != cudaSuccess)
+    return cuda_fail("cudaMalloc(io)", e);
+  if ((e = cudaMalloc((void**)&b->err, sizeof(int))) != cudaSuccess) return cuda_fail("cudaMalloc(err)", e);
+  cudaMemset(b->err, 0, sizeof(int));
+  const int rc = b->fp32 ? fill_params<float>(b) : fill_params<double>(b);
+  if (rc) {
+    g_batch_create_error = b->msg;
+    release(b);
+    delete b;
+    return rc;
+  }
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess) return cuda_fail("batch set-up", e);
+  *out = b;
+  return SBP_OK;
+}
+
+int sbp_batch_destroy(sbp_batch* b) {
+  if (!b) return SBP_ERR_INVALID;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  release(b);
+  delete b;
+  return SBP_OK;
+}
+
+const char* sbp_batch_last_error(const sbp_batch* b) { return b ? b->msg.c_str() : g_batch_create_error.c_str(); }
+
+int sbp_batch_set_state(sbp_batch* b, int index, const double* v, int where) {
+  if (!b || !v || index < 0 || index >= (int)b->inst.size()) return SBP_ERR_INVALID;
+  BCK(cudaSetDevice(b->device));
+  const Geo& g = b->geo[index];
+  const size_t n = (size_t)g.dofs * g.nx * g.ny;
+  const double* src = v;
+  if (where == SBP_HOST) {
+    BCK(cudaMemcpyAsync(b->io, v, n * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    src = b->io;
+  } else if (where != SBP_DEVICE) {
+    return bfail(b, SBP_ERR_INVALID, "where must be SBP_HOST or SBP_DEVICE");
+  }
+  if (b->fp32) {
+    BCK(launch_pack<float>(src, (float*)at(b->un, g.off), (int)g.nx, (int)g.ny, g.dofs, g.pitch, g.plane, b->stream));
+    BCK(cudaMemsetAsync(at(b->comp, g.off), 0, (size_t)g.dofs * g.plane * b->es, b->stream));
+  } else {
+    BCK(launch_pack<double>(src, (double*)at(b->un, g.off), (int)g.nx, (int)g.ny, g.dofs, g.pitch, g.plane,
+                            b->stream));
+  }
+  b->launches++;
+  BCK(cudaStreamSynchronize(b->stream));
+  return SBP_OK;
+}
+
+int sbp_batch_get_state(sbp_batch* b, int index, double* v, int where) {
+  if (!b || !v || index < 0 || index >= (int)b->inst.size()) return SBP_ERR_INVALID;
+  BCK(cudaSetDevice(b->device));
+  const Geo& g = b->geo[index];
+  const size_t n = (size_t)g.dofs * g.nx * g.ny;
+  double* dst = (where == SBP_DEVICE) ? v : b->io;
+  if (b->fp32)
+    BCK(launch_unpack<float>((const float*)at(b->un, g.off), dst, (int)g.nx, (int)g.ny, g.dofs, g.pitch, g.plane,
+                             b->stream));
+  else
+    BCK(launch_unpack<double>((const double*)at(b->un, g.off), dst, (int)g.nx, (int)g.ny, g.dofs, g.pitch, g.plane,
+                              b->stream));
+  b->launches++;
+  if (where != SBP_DEVICE)
+    BCK(cudaMemcpyAsync(v, b->io, n * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  return SBP_OK;
+}
+
+int sbp_batch_rk4_resident(sbp_batch* b, long long nsteps) {
+  if (!b || nsteps < 0) return SBP_ERR_INVALID;
+  BCK(cudaSetDevice(b->device));
+  const long long chunk = 100;
+  long long left = nsteps;
+  while (left > 0) {
+    const long long s = left >= chunk ? chunk : left;
+    const int rc = b->fp32 ? run_chunk<float>(b, s) : run_chunk<double>(b, s);
+    if (rc) return rc;
+    left -= s;
+  }
+  return SBP_OK;
+}
+
+int sbp_batch_synchronize(sbp_batch* b) {
+  if (!b) return SBP_ERR_INVALID;
+  BCK(cudaSetDevice(b->device));
+  BCK(cudaStreamSynchronize(b->stream));
+  int h = 0;
+  BCK(cudaMemcpy(&h, b->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    cudaMemset(b->err, 0, sizeof(int));
+    return bfail(b, SBP_ERR_DEVICE, "a TMA tile wait timed out in a batched stage kernel");
+  }
+  return SBP_OK;
+}
+
+int sbp_batch_autotune(sbp_batch* b, const char* cache_path) {
+  if (!b) return SBP_ERR_INVALID;
+  BCK(cudaSetDevice(b->device));
+  cudaDeviceProp prop;
+  BCK(cudaGetDeviceProperties(&prop, b->device));
+  std::map<std::string, int> cache = read_cache(cache_path);
+  bool dirty = false;
+  const int cand64[2] = {8, 16}, cand32[2] = {16, 32};
+  const int* cand = b->fp32 ? cand32 : cand64;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int rc = SBP_OK;
+  for (int oi = 0; oi < 3 && rc == SBP_OK; oi++) {
+    const int order = 2 * (oi + 1);
+    long long pts = 0;
+    for (size_t i = 0; i < b->inst.size(); i++)
+      if (b->geo[i].wave && b->geo[i].order == order) pts += b->geo[i].nx * b->geo[i].ny;
+    if (!pts) continue;
+    // key: device, precision, order, group size rounded to 2 significant digits
+    const double mag = std::pow(10.0, std::floor(std::log10((double)pts)) - 1);
+    const long long bucket = (long long)(std::round(pts / mag) * mag);
+    const std::string key = std::string(prop.name) + "|" + (b->fp32 ? "fp32" : "fp64") + "|order" +
+                            std::to_string(order) + "|points" + std::to_string(bucket);
+    auto hit = cache.find(key);
+    if (hit != cache.end() && (hit->second == cand[0] || hit->second == cand[1])) {
+      if (hit->second != b->ty[oi]) rc = build_wave_group(b, oi, hit->second);
+      continue;
+    }
+    float best_ms = 1e30f;
+    int best = cand[0];
+    for (int c = 0; c < 2 && rc == SBP_OK; c++) {
+      if ((rc = build_wave_group(b, oi, cand[c]))) break;
+      // time the middle stage (it writes only the accumulator and a stage buffer)
+      float ms = 0;
+      for (int rep = 0; rep < 4 && rc == SBP_OK; rep++) {
+        if (rep == 1) cudaEventRecord(e0, b->stream);
+        if (b->fp32)
+          rc = launch_wave_batch<float>(order, ST_MID, cand[c], (const BatchWave<float>*)b->d_wave, b->d_maps,
+                                        b->d_tiles_wave[oi], b->n_tiles_wave[oi], 2, b->err, b->stream) == cudaSuccess
+                   ? SBP_OK
+                   : SBP_ERR_CUDA;
+        else
+          rc = launch_wave_batch<double>(order, ST_MID, cand[c], (const BatchWave<double>*)b->d_wave, b->d_maps,
+                                         b->d_tiles_wave[oi], b->n_tiles_wave[oi], 2, b->err, b->stream) == cudaSuccess
+                   ? SBP_OK
+                   : SBP_ERR_CUDA;
+      }
+      cudaEventRecord(e1, b->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) rc = SBP_ERR_CUDA;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rc == SBP_OK && ms < best_ms) {
+        best_ms = ms;
+        best = cand[c];
+      }
+    }
+    if (rc == SBP_OK && best != b->ty[oi]) rc = build_wave_group(b, oi, best);
+    cache[key] = best;
+    dirty = true;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return bfail(b, rc, b->msg.empty() ? "autotune failed" : b->msg);
+  if (dirty) write_cache(cache_path, cache);
+  return sbp_batch_synchronize(b);
+}
+
+int sbp_batch_tile_height(const sbp_batch* b, int order) {
+  if (!b || (order != 2 && order != 4 && order != 6)) return SBP_ERR_INVALID;
+  return b->ty[order_index(order)];
+}
+
+int sbp_batch_get_stream(const sbp_batch* b, void** stream) {
+  if (!b || !stream) return SBP_ERR_INVALID;
+  *stream = (void*)b->stream;
+  return SBP_OK;
+}
+
+long long sbp_batch_points(const sbp_batch* b) { return b ? b->points : SBP_ERR_INVALID; }
+
+long long sbp_batch_launch_count(const sbp_batch* b) { return b ? b->launches : SBP_ERR_INVALID; }
+
+}  // extern "C"

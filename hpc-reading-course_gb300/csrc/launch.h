@@ -8,6 +8,7 @@
 
 #include "line_kernels.cuh"
 #include "wave2d.cuh"
+#include "wave_batch.cuh"
 
 namespace sbp {
 
@@ -58,6 +59,48 @@ int wave_smem_bytes(int order, bool fp32);
 
 template <typename T>
 cudaError_t launch_line(int order, int kind, int stage, const LineParams<T>& prm, cudaStream_t s);
+
+// Batched stage kernels (wave_batch_inst.cu, one unit per order). `ty` is the
+// tile height: 8 or 16 (FP64), 16 or 32 (FP32).
+#define SBP_DECLARE_BATCH(o)                                                                                    \
+  template <typename T> cudaError_t configure_wave_batch_o##o(int ty);                                          \
+  template <typename T>                                                                                         \
+  cudaError_t launch_wave_batch_o##o(int stage, int ty, const BatchWave<T>* insts, const CUtensorMap* maps,     \
+                                     const int2* tiles, int ntiles, int rk, int* err, unsigned grid, cudaStream_t s); \
+  template <typename T>                                                                                         \
+  cudaError_t launch_adv_batch_o##o(int stage, const BatchLine<T>* insts, const int2* tiles, int ntiles, int rk, \
+                                    cudaStream_t s);
+SBP_DECLARE_BATCH(2)
+SBP_DECLARE_BATCH(4)
+SBP_DECLARE_BATCH(6)
+#undef SBP_DECLARE_BATCH
+
+template <typename T> inline cudaError_t configure_wave_batch(int order, int ty) {
+  return order == 2 ? configure_wave_batch_o2<T>(ty)
+                    : (order == 4 ? configure_wave_batch_o4<T>(ty) : configure_wave_batch_o6<T>(ty));
+}
+template <typename T>
+inline cudaError_t launch_wave_batch(int order, int stage, int ty, const BatchWave<T>* insts, const CUtensorMap* maps,
+                                     const int2* tiles, int ntiles, int rk, int* err, cudaStream_t s) {
+  const int nsm = device_sm_count();
+  const unsigned grid = (unsigned)(ntiles < nsm ? ntiles : nsm);
+  switch (order) {
+    case 2: return launch_wave_batch_o2<T>(stage, ty, insts, maps, tiles, ntiles, rk, err, grid, s);
+    case 4: return launch_wave_batch_o4<T>(stage, ty, insts, maps, tiles, ntiles, rk, err, grid, s);
+    case 6: return launch_wave_batch_o6<T>(stage, ty, insts, maps, tiles, ntiles, rk, err, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+template <typename T>
+inline cudaError_t launch_adv_batch(int order, int stage, const BatchLine<T>* insts, const int2* tiles, int ntiles,
+                                    int rk, cudaStream_t s) {
+  switch (order) {
+    case 2: return launch_adv_batch_o2<T>(stage, insts, tiles, ntiles, rk, s);
+    case 4: return launch_adv_batch_o4<T>(stage, insts, tiles, ntiles, rk, s);
+    case 6: return launch_adv_batch_o6<T>(stage, insts, tiles, ntiles, rk, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
 
 // AoS FP64 (reference layout) <-> SoA planes of T with a row pitch.
 template <typename T>

@@ -46,29 +46,28 @@ __device__ __forceinline__ T d1_line(const T* __restrict__ line, long long st, i
   return closure_line<T, ORD>(line, st, n, i, d.cls);
 }
 
+// One grid point of a stage: RHS, boundary terms and the RK4 stage update.
 template <typename T, int ORD, int KIND, int STAGE>
-__global__ void __launch_bounds__(256) line_stage_kernel(const __grid_constant__ LineParams<T> prm) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void line_point(const LineParams<T>& prm, const T* __restrict__ in, T* wout, const T c_acc,
+                                           const T c_w, const int i, const int j) {
   const int nx = prm.nx, ny = prm.ny;
-  if (i >= nx || j >= ny) return;
   const long long pitch = prm.pitch, plane = prm.plane;
   const long long q = (long long)j * pitch + i;
   constexpr int NC = (KIND == LK_REFL1D) ? 2 : 1;
   T k[NC];
   T cen[NC];
   if constexpr (KIND == LK_ADV1D) {
-    k[0] = d1_line<T, ORD>(prm.in, 1, nx, i, prm.dx);
-    cen[0] = prm.in[q];
+    k[0] = d1_line<T, ORD>(in, 1, nx, i, prm.dx);
+    cen[0] = in[q];
     if (prm.bc) {  // SAT_bc_l / SAT_bc_r (advection_rhs.h:94-119)
       if (i == 0) k[0] = (T)((double)k[0] + prm.sat[0] * (double)cen[0]);
       if (i == nx - 1) k[0] = (T)((double)k[0] + prm.sat[2] * (double)cen[0]);
     }
   } else if constexpr (KIND == LK_ADV2D) {
-    const T* row = prm.in + (long long)j * pitch;
-    const T* col = prm.in + i;
+    const T* row = in + (long long)j * pitch;
+    const T* col = in + i;
     k[0] = d1_line<T, ORD>(row, 1, nx, i, prm.dx) + d1_line<T, ORD>(col, pitch, ny, j, prm.dy);
-    cen[0] = prm.in[q];
+    cen[0] = in[q];
     if (prm.bc) {  // SAT_bc_{west,south,east,north} (advection_rhs.h:460-528)
       double kk = (double)k[0];
       const double u = (double)cen[0];
@@ -79,10 +78,10 @@ __global__ void __launch_bounds__(256) line_stage_kernel(const __grid_constant__
       k[0] = (T)kk;
     }
   } else {  // LK_REFL1D: dst(i,1) = D1 u, dst(i,0) = D1 v
-    k[1] = d1_line<T, ORD>(prm.in, 1, nx, i, prm.dx);
-    k[0] = d1_line<T, ORD>(prm.in + plane, 1, nx, i, prm.dx);
-    cen[0] = prm.in[q];
-    cen[1] = prm.in[plane + q];
+    k[1] = d1_line<T, ORD>(in, 1, nx, i, prm.dx);
+    k[0] = d1_line<T, ORD>(in + plane, 1, nx, i, prm.dx);
+    cen[0] = in[q];
+    cen[1] = in[plane + q];
     if (prm.bc && (i == 0 || i == nx - 1)) k[0] = T(0);  // proj_dirichlet_bc_{l,r}
   }
 #pragma unroll
@@ -91,14 +90,14 @@ __global__ void __launch_bounds__(256) line_stage_kernel(const __grid_constant__
     if constexpr (STAGE == ST_RHS) {
       prm.kout[o] = k[c];
     } else if constexpr (STAGE == ST_FIRST) {
-      prm.acc[o] = prm.compensated ? prm.c_acc * k[c] : fma(prm.c_acc, k[c], cen[c]);
-      prm.wout[o] = fma(prm.c_w, k[c], cen[c]);
+      prm.acc[o] = prm.compensated ? c_acc * k[c] : fma(c_acc, k[c], cen[c]);
+      wout[o] = fma(c_w, k[c], cen[c]);
     } else if constexpr (STAGE == ST_MID) {
       const T u0 = prm.un[o];
-      prm.acc[o] = fma(prm.c_acc, k[c], prm.acc[o]);
-      prm.wout[o] = fma(prm.c_w, k[c], u0);
+      prm.acc[o] = fma(c_acc, k[c], prm.acc[o]);
+      wout[o] = fma(c_w, k[c], u0);
     } else {
-      const T d = fma(prm.c_acc, k[c], prm.acc[o]);
+      const T d = fma(c_acc, k[c], prm.acc[o]);
       if (prm.compensated) {
         const T u0 = prm.un[o], e = prm.comp[o];
         const T yv = d - e;
@@ -110,6 +109,14 @@ __global__ void __launch_bounds__(256) line_stage_kernel(const __grid_constant__
       }
     }
   }
+}
+
+template <typename T, int ORD, int KIND, int STAGE>
+__global__ void __launch_bounds__(256) line_stage_kernel(const __grid_constant__ LineParams<T> prm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= prm.nx || j >= prm.ny) return;
+  line_point<T, ORD, KIND, STAGE>(prm, prm.in, prm.wout, prm.c_acc, prm.c_w, i, j);
 }
 
 }  // namespace sbp

@@ -27,7 +27,7 @@
 
 namespace sbp {
 
-enum WaveKind : int { WK_HOM = 0, WK_VAR = 1, WK_MMS = 2 };
+enum WaveKind : int { WK_HOM = 0, WK_VAR = 1, WK_MMS = 2, WK_CONST = 3 };  // WK_CONST: rho = 1, K = kconst
 enum BcKind : int { BC_NONE = 0, BC_FREE_SURFACE = 1, BC_CHARACTERISTIC = 2 };
 enum Stage : int { ST_RHS = 0, ST_FIRST = 1, ST_MID = 2, ST_LAST = 4 };
 
@@ -48,6 +48,8 @@ template <typename T> struct WaveParams {
   DirTaps<T> dx, dy;  // -hix * stencils, -hiy * stencils
   double bwx, bwy;    // hix * HI[0], hiy * HI[0]: SAT weights (FP64)
   T c_acc, c_w;       // acc (+)= c_acc * k ; w = u^n + c_w * k
+  T kconst;           // WK_CONST: bulk modulus K (rho = 1)
+  double dt;          // batched: the instance's time step
   int bc;             // BcKind
   int ysplit;         // 0: one block; else rows [0,ysplit) and [ysplit,ny) are two blocks
                       // sharing an interface line (WK_VAR only)
@@ -66,9 +68,11 @@ template <> struct IsCompensated<float> { static constexpr bool value = true; };
 // Tile geometry and shared-memory plan for (T, order, stage). The x halo is
 // rounded up so that (tile origin - halo) * sizeof(T) is a multiple of 16
 // bytes (TMA rule for the innermost coordinate); tile origins are multiples of 64.
-template <typename T, int ORD, int STAGE> struct WaveTile {
+template <typename T> constexpr int default_wave_ty() { return sizeof(T) == 8 ? 16 : 32; }
+
+template <typename T, int ORD, int STAGE, int TY_ = default_wave_ty<T>(), int PRM_BYTES = 0> struct WaveTile {
   static constexpr bool COMP = IsCompensated<T>::value;
-  static constexpr int TY = sizeof(T) == 8 ? 16 : 32;        // tile height
+  static constexpr int TY = TY_;                              // tile height
   static constexpr int R = (OpShape<ORD>::W - 1) / 2;
   static constexpr int HXA = 16 / sizeof(T);
   static constexpr int HX = ((R + HXA - 1) / HXA) * HXA;     // x halo loaded
@@ -88,11 +92,13 @@ template <typename T, int ORD, int STAGE> struct WaveTile {
   static constexpr int OFF_N = OFF_V + align128(BYTES_V);
   static constexpr int OFF_A = OFF_N + (LOAD_UN ? BYTES_PT : 0);
   static constexpr int OFF_C = OFF_A + (LOAD_ACC ? BYTES_PT : 0);
-  static constexpr int STAGE_BYTES = align128(OFF_C + (LOAD_COMP ? BYTES_PT : 0));
+  static constexpr int OFF_PRM = align128(OFF_C + (LOAD_COMP ? BYTES_PT : 0));  // batched: instance parameters
+  static constexpr int STAGE_BYTES = OFF_PRM + align128(PRM_BYTES);
   static constexpr int OFF_BAR = 2 * STAGE_BYTES;             // full[2], empty[2]
   static constexpr int SMEM = OFF_BAR + 128;
   static constexpr uint32_t TX_BYTES = BYTES_P + BYTES_U + BYTES_V + (LOAD_UN ? BYTES_PT : 0) +
-                                       (LOAD_ACC ? BYTES_PT : 0) + (LOAD_COMP ? BYTES_PT : 0);
+                                       (LOAD_ACC ? BYTES_PT : 0) + (LOAD_COMP ? BYTES_PT : 0) + PRM_BYTES;
+  static_assert(TY % kWaveConsumerWarps == 0, "tile rows must split evenly over the consumer warps");
   static_assert(SMEM <= 227 * 1024, "wave tile pipeline exceeds shared memory");
 };
 
@@ -125,12 +131,15 @@ template <typename T> struct Rhs3 { T u, v, p; };
 // order west, south, east, north. Kept out of line so interior points branch
 // around it instead of issuing its FP64 instructions under a predicate.
 template <typename T, int KIND>
-__device__ __noinline__ Rhs3<T> apply_sat(const WaveParams<T>& prm, int i, int j, T pc, T uc, T vc, Rhs3<T> k) {
+__device__ __noinline__ Rhs3<T> apply_sat(const WaveParams<T>& prm, const T* in, int i, int j, T pc, T uc, T vc,
+                                          Rhs3<T> k) {
   const int nx = prm.nx, ny = prm.ny;
   double rho = 1.0, kk = 1.0;
   if constexpr (KIND == WK_VAR) {
     rho = prm.rho64[(long long)j * nx + i];
     kk = prm.k64[(long long)j * nx + i];
+  } else if constexpr (KIND == WK_CONST) {
+    kk = (double)prm.kconst;
   }
   const double p64 = (double)pc;
   double ku64 = (double)k.u, kv64 = (double)k.v, kp64 = (double)k.p;
@@ -160,7 +169,7 @@ __device__ __noinline__ Rhs3<T> apply_sat(const WaveParams<T>& prm, int i, int j
     if (ys > 0 && prm.bc != BC_NONE && (j == ys - 1 || j == ys)) {
       const int jo = (j == ys - 1) ? ys : ys - 1;  // the other block's copy of the line
       const long long qo = (long long)jo * prm.pitch + i;
-      const double po = (double)prm.in[2 * prm.plane + qo], vo = (double)prm.in[prm.plane + qo];
+      const double po = (double)in[2 * prm.plane + qo], vo = (double)in[prm.plane + qo];
       const double s = (j == ys - 1) ? 1.0 : -1.0;
       kv64 += s * (0.5 / rho) * (prm.bwy * (p64 - po));
       kp64 += s * (0.5 * kk) * (prm.bwy * ((double)vc - vo));
@@ -173,6 +182,156 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
+// One tile of the stage for the consumer warps: everything the tile needs is
+// in the shared-memory stage `st` (laid out as Tile), except closure-row taps
+// and coefficient fields. `in` is the stage input, `wout` the next stage input.
+template <typename T, int ORD, int KIND, int STAGE, typename Tile>
+__device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, const T* __restrict__ in, T* wout,
+                                                  const T c_acc, const T c_w, const unsigned char* st, const int i0,
+                                                  const int j0, const int warp, const int lane) {
+  constexpr bool COMP = Tile::COMP;
+  constexpr int TY = Tile::TY, W = OpShape<ORD>::W, CS = OpShape<ORD>::CS, R = Tile::R;
+  constexpr int HX = Tile::HX, HY = Tile::HY, PW = Tile::PW;
+  constexpr int ROWS = TY / kWaveConsumerWarps;
+  // FP64 is bound by the FP64 pipe: unrolling the warp's rows gives more
+  // independent FMA chains. FP32 is bound by HBM and runs faster rolled.
+  constexpr int ROW_UNROLL = sizeof(T) == 8 ? ROWS : 1;
+  constexpr int TPT = TY * kWaveTX;  // points per tile (one component)
+  const int nx = prm.nx, ny = prm.ny;
+  const long long pitch = prm.pitch, plane = prm.plane;
+  const T* sP = reinterpret_cast<const T*>(st);
+  const T* sU = reinterpret_cast<const T*>(st + Tile::OFF_U);
+  const T* sV = reinterpret_cast<const T*>(st + Tile::OFF_V);
+  const T* sN = reinterpret_cast<const T*>(st + Tile::OFF_N);
+  const T* sA = reinterpret_cast<const T*>(st + Tile::OFF_A);
+  const T* sC = reinterpret_cast<const T*>(st + Tile::OFF_C);
+  (void)sN;
+  (void)sA;
+  (void)sC;
+#pragma unroll ROW_UNROLL
+  for (int rr = 0; rr < ROWS; rr++) {
+    const int y = warp * ROWS + rr;
+    const int j = j0 + y;
+    if (j >= ny) continue;
+    // block-local row (two-block problems: the interface rows close each block)
+    const int jb0 = (prm.ysplit > 0 && j >= prm.ysplit) ? prm.ysplit : 0;
+    const int nyb = (prm.ysplit > 0) ? (j >= prm.ysplit ? ny - prm.ysplit : prm.ysplit) : ny;
+    const int jl = j - jb0;
+    const bool yint = (jl >= CS) && (jl < nyb - CS);
+#pragma unroll
+    for (int cc = 0; cc < kWaveTX / 32; cc++) {
+      const int x = lane + 32 * cc;
+      const int i = i0 + x;
+      if (i >= nx) continue;
+      const bool xint = (i >= CS) && (i < nx - CS);
+      const T* rowP = sP + (y + HY) * PW + (x + HX - R);
+      const T* rowU = sU + y * PW + (x + HX - R);
+      const T* colP = sP + y * PW + (x + HX);   // row y+HY-R
+      const T* colV = sV + y * kWaveTX + x;     // row y+HY-R
+      const T pc = rowP[R], uc = rowU[R], vc = colV[R * kWaveTX];
+
+      T dxp, dyp, kp;
+      if (xint) {
+        dxp = prm.dx.taps[0] * rowP[0];
+#pragma unroll
+        for (int s = 1; s < W; s++)
+          if (s != R) dxp = fma(prm.dx.taps[s], rowP[s], dxp);
+      } else {
+        dxp = closure_line<T, ORD>(in + 2 * plane + (long long)j * pitch, 1, nx, i, prm.dx.cls);
+      }
+      if (yint) {
+        dyp = prm.dy.taps[0] * colP[0];
+#pragma unroll
+        for (int s = 1; s < W; s++)
+          if (s != R) dyp = fma(prm.dy.taps[s], colP[s * PW], dyp);
+      } else {
+        dyp = closure_line<T, ORD>(in + 2 * plane + (long long)jb0 * pitch + i, pitch, nyb, jl, prm.dy.cls);
+      }
+      if (xint) {
+        kp = prm.dx.taps[0] * rowU[0];
+#pragma unroll
+        for (int s = 1; s < W; s++)
+          if (s != R) kp = fma(prm.dx.taps[s], rowU[s], kp);
+      } else {
+        kp = closure_line<T, ORD>(in + (long long)j * pitch, 1, nx, i, prm.dx.cls);
+      }
+      if (yint) {
+#pragma unroll
+        for (int s = 0; s < W; s++)
+          if (s != R) kp = fma(prm.dy.taps[s], colV[s * kWaveTX], kp);
+      } else {
+        kp += closure_line<T, ORD>(in + plane + (long long)jb0 * pitch + i, pitch, nyb, jl, prm.dy.cls);
+      }
+
+      const long long q = (long long)j * pitch + i;
+      T ku, kv;
+      if constexpr (KIND == WK_HOM) {
+        ku = dxp;
+        kv = dyp;
+      } else if constexpr (KIND == WK_CONST) {
+        ku = dxp;
+        kv = dyp;
+        kp = prm.kconst * kp;
+      } else if constexpr (KIND == WK_VAR) {
+        const T ri = __ldg(prm.rinv + q);
+        ku = ri * dxp;
+        kv = ri * dyp;
+        kp = __ldg(prm.kmod + q) * kp;
+      } else {  // WK_MMS (FP64): code/demo/wave/wave_eq_rhs.h:42-64
+        const double PI = 3.14159265358979323846264;
+        const double xx = mms_x(prm.xl0, i, prm.hix), yy = mms_x(prm.xl1, j, prm.hiy);
+        const double ri = 1. / (2 + xx * yy);
+        const double ct = cos(5 * PI * prm.t);
+        const double fu = -(3 * PI * ct * cos(3 * PI * xx) * sin(4 * PI * yy) * (xx * yy + 1)) / (xx * yy + 2);
+        const double fv = -(4 * PI * ct * cos(4 * PI * yy) * sin(3 * PI * xx) * (xx * yy + 1)) / (xx * yy + 2);
+        ku = (T)(ri * (double)dxp + fu);
+        kv = (T)(ri * (double)dyp + fv);
+      }
+
+      // SAT boundary terms (boundary points only)
+      const bool edge = (i == 0) || (j == 0) || (i == nx - 1) || (j == ny - 1) ||
+                        (prm.ysplit > 0 && (j == prm.ysplit - 1 || j == prm.ysplit));
+      if (prm.bc != BC_NONE && edge) {
+        const Rhs3<T> r = apply_sat<T, KIND>(prm, in, i, j, pc, uc, vc, Rhs3<T>{ku, kv, kp});
+        ku = r.u;
+        kv = r.v;
+        kp = r.p;
+      }
+
+      // RK4 stage update (classical RK4, code/include/time_stepping/time_stepping.h:127-142)
+      const T kc[3] = {ku, kv, kp};
+      const T cen[3] = {uc, vc, pc};
+      const int sp = y * kWaveTX + x;  // point within a 3-component smem box
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const long long o = c * plane + q;
+        if constexpr (STAGE == ST_RHS) {
+          prm.kout[o] = kc[c];
+        } else if constexpr (STAGE == ST_FIRST) {
+          // acc = u + dt/6 k1 (FP32 compensated: acc = dt/6 k1), w = u + dt/2 k1
+          st_stream(prm.acc + o, COMP ? c_acc * kc[c] : fma(c_acc, kc[c], cen[c]));
+          st_stream(wout + o, fma(c_w, kc[c], cen[c]));
+        } else if constexpr (STAGE == ST_MID) {
+          st_stream(prm.acc + o, fma(c_acc, kc[c], sA[c * TPT + sp]));
+          st_stream(wout + o, fma(c_w, kc[c], sN[c * TPT + sp]));
+        } else {  // ST_LAST
+          const T d = fma(c_acc, kc[c], sA[c * TPT + sp]);
+          if constexpr (COMP) {
+            // Kahan summation of the step increment into the FP32 state
+            const T u0 = sN[c * TPT + sp], e = sC[c * TPT + sp];
+            const T yv = d - e;
+            const T tv = u0 + yv;
+            st_stream(prm.comp + o, (tv - u0) - yv);
+            st_stream(prm.un + o, tv);
+          } else {
+            st_stream(prm.un + o, d);
+          }
+        }
+      }
+    }
+  }
+}
+
 template <typename T, int ORD, int KIND, int STAGE>
 __global__ void __launch_bounds__(kWaveThreads, 1)
     wave_stage_kernel(const __grid_constant__ CUtensorMap mapP, const __grid_constant__ CUtensorMap mapU,
@@ -180,9 +339,7 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
                       const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapC,
                       const __grid_constant__ WaveParams<T> prm) {
   using Tile = WaveTile<T, ORD, STAGE>;
-  constexpr bool COMP = Tile::COMP;
-  constexpr int TY = Tile::TY, W = OpShape<ORD>::W, CS = OpShape<ORD>::CS, R = Tile::R;
-  constexpr int HX = Tile::HX, HY = Tile::HY, PW = Tile::PW;
+  constexpr int TY = Tile::TY, HX = Tile::HX, HY = Tile::HY;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
   uint64_t* empty = full + 2;
@@ -229,12 +386,6 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
   }
 
   // ---------------- consumers: warps 0-7
-  const long long pitch = prm.pitch, plane = prm.plane;
-  constexpr int ROWS = TY / kWaveConsumerWarps;
-  // FP64 is bound by the FP64 pipe: unrolling the warp's rows gives more
-  // independent FMA chains. FP32 is bound by HBM and runs faster rolled.
-  constexpr int ROW_UNROLL = sizeof(T) == 8 ? ROWS : 1;
-  constexpr int TPT = TY * kWaveTX;  // points per tile (one component)
   int k = 0;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
     const int b = k & 1;
@@ -242,133 +393,9 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
       if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
       break;
     }
-    const unsigned char* st = smem + b * Tile::STAGE_BYTES;
-    const T* sP = reinterpret_cast<const T*>(st);
-    const T* sU = reinterpret_cast<const T*>(st + Tile::OFF_U);
-    const T* sV = reinterpret_cast<const T*>(st + Tile::OFF_V);
-    const T* sN = reinterpret_cast<const T*>(st + Tile::OFF_N);
-    const T* sA = reinterpret_cast<const T*>(st + Tile::OFF_A);
-    const T* sC = reinterpret_cast<const T*>(st + Tile::OFF_C);
     const int i0 = (tile % ntx) * kWaveTX, j0 = (tile / ntx) * TY;
-
-#pragma unroll ROW_UNROLL
-    for (int rr = 0; rr < ROWS; rr++) {
-      const int y = warp * ROWS + rr;
-      const int j = j0 + y;
-      if (j >= ny) continue;
-      // block-local row (two-block problems: the interface rows close each block)
-      const int jb0 = (prm.ysplit > 0 && j >= prm.ysplit) ? prm.ysplit : 0;
-      const int nyb = (prm.ysplit > 0) ? (j >= prm.ysplit ? ny - prm.ysplit : prm.ysplit) : ny;
-      const int jl = j - jb0;
-      const bool yint = (jl >= CS) && (jl < nyb - CS);
-#pragma unroll
-      for (int cc = 0; cc < kWaveTX / 32; cc++) {
-        const int x = lane + 32 * cc;
-        const int i = i0 + x;
-        if (i >= nx) continue;
-        const bool xint = (i >= CS) && (i < nx - CS);
-        const T* rowP = sP + (y + HY) * PW + (x + HX - R);
-        const T* rowU = sU + y * PW + (x + HX - R);
-        const T* colP = sP + y * PW + (x + HX);   // row y+HY-R
-        const T* colV = sV + y * kWaveTX + x;     // row y+HY-R
-        const T pc = rowP[R], uc = rowU[R], vc = colV[R * kWaveTX];
-
-        T dxp, dyp, kp;
-        if (xint) {
-          dxp = prm.dx.taps[0] * rowP[0];
-#pragma unroll
-          for (int s = 1; s < W; s++)
-            if (s != R) dxp = fma(prm.dx.taps[s], rowP[s], dxp);
-        } else {
-          dxp = closure_line<T, ORD>(prm.in + 2 * plane + (long long)j * pitch, 1, nx, i, prm.dx.cls);
-        }
-        if (yint) {
-          dyp = prm.dy.taps[0] * colP[0];
-#pragma unroll
-          for (int s = 1; s < W; s++)
-            if (s != R) dyp = fma(prm.dy.taps[s], colP[s * PW], dyp);
-        } else {
-          dyp = closure_line<T, ORD>(prm.in + 2 * plane + (long long)jb0 * pitch + i, pitch, nyb, jl, prm.dy.cls);
-        }
-        if (xint) {
-          kp = prm.dx.taps[0] * rowU[0];
-#pragma unroll
-          for (int s = 1; s < W; s++)
-            if (s != R) kp = fma(prm.dx.taps[s], rowU[s], kp);
-        } else {
-          kp = closure_line<T, ORD>(prm.in + (long long)j * pitch, 1, nx, i, prm.dx.cls);
-        }
-        if (yint) {
-#pragma unroll
-          for (int s = 0; s < W; s++)
-            if (s != R) kp = fma(prm.dy.taps[s], colV[s * kWaveTX], kp);
-        } else {
-          kp += closure_line<T, ORD>(prm.in + plane + (long long)jb0 * pitch + i, pitch, nyb, jl, prm.dy.cls);
-        }
-
-        const long long q = (long long)j * pitch + i;
-        T ku, kv;
-        if constexpr (KIND == WK_HOM) {
-          ku = dxp;
-          kv = dyp;
-        } else if constexpr (KIND == WK_VAR) {
-          const T ri = __ldg(prm.rinv + q);
-          ku = ri * dxp;
-          kv = ri * dyp;
-          kp = __ldg(prm.kmod + q) * kp;
-        } else {  // WK_MMS (FP64): code/demo/wave/wave_eq_rhs.h:42-64
-          const double PI = 3.14159265358979323846264;
-          const double xx = mms_x(prm.xl0, i, prm.hix), yy = mms_x(prm.xl1, j, prm.hiy);
-          const double ri = 1. / (2 + xx * yy);
-          const double ct = cos(5 * PI * prm.t);
-          const double fu = -(3 * PI * ct * cos(3 * PI * xx) * sin(4 * PI * yy) * (xx * yy + 1)) / (xx * yy + 2);
-          const double fv = -(4 * PI * ct * cos(4 * PI * yy) * sin(3 * PI * xx) * (xx * yy + 1)) / (xx * yy + 2);
-          ku = (T)(ri * (double)dxp + fu);
-          kv = (T)(ri * (double)dyp + fv);
-        }
-
-        // SAT boundary terms (boundary points only)
-        const bool edge = (i == 0) || (j == 0) || (i == nx - 1) || (j == ny - 1) ||
-                          (prm.ysplit > 0 && (j == prm.ysplit - 1 || j == prm.ysplit));
-        if (prm.bc != BC_NONE && edge) {
-          const Rhs3<T> r = apply_sat<T, KIND>(prm, i, j, pc, uc, vc, Rhs3<T>{ku, kv, kp});
-          ku = r.u;
-          kv = r.v;
-          kp = r.p;
-        }
-
-        // RK4 stage update (classical RK4, code/include/time_stepping/time_stepping.h:127-142)
-        const T kc[3] = {ku, kv, kp};
-        const T cen[3] = {uc, vc, pc};
-        const int sp = y * kWaveTX + x;  // point within a 3-component smem box
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          const long long o = c * plane + q;
-          if constexpr (STAGE == ST_RHS) {
-            prm.kout[o] = kc[c];
-          } else if constexpr (STAGE == ST_FIRST) {
-            // acc = u + dt/6 k1 (FP32 compensated: acc = dt/6 k1), w = u + dt/2 k1
-            st_stream(prm.acc + o, COMP ? prm.c_acc * kc[c] : fma(prm.c_acc, kc[c], cen[c]));
-            st_stream(prm.wout + o, fma(prm.c_w, kc[c], cen[c]));
-          } else if constexpr (STAGE == ST_MID) {
-            st_stream(prm.acc + o, fma(prm.c_acc, kc[c], sA[c * TPT + sp]));
-            st_stream(prm.wout + o, fma(prm.c_w, kc[c], sN[c * TPT + sp]));
-          } else {  // ST_LAST
-            const T d = fma(prm.c_acc, kc[c], sA[c * TPT + sp]);
-            if constexpr (COMP) {
-              // Kahan summation of the step increment into the FP32 state
-              const T u0 = sN[c * TPT + sp], e = sC[c * TPT + sp];
-              const T yv = d - e;
-              const T tv = u0 + yv;
-              st_stream(prm.comp + o, (tv - u0) - yv);
-              st_stream(prm.un + o, tv);
-            } else {
-              st_stream(prm.un + o, d);
-            }
-          }
-        }
-      }
-    }
+    wave_tile_compute<T, ORD, KIND, STAGE, Tile>(prm, prm.in, prm.wout, prm.c_acc, prm.c_w,
+                                                 smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[b]);
   }

@@ -1,0 +1,153 @@
+// wave_batch.cuh -- many independent wave / advection instances of uneven
+// size, order and coefficients advanced together.
+//
+// Wave instances (rho = 1, K = c^2, one constant per instance) run through a
+// persistent stage kernel per operator order: its grid walks a tile list of
+// (instance, tile) pairs. The producer warp loads each tile's state tiles
+// with TMA from the instance's own tensor maps (kept in global memory) and
+// bulk-copies the instance's parameter block (taps, SAT weights, pointers,
+// time step) into the same shared-memory stage, so consumers read every
+// per-instance constant from shared memory. The per-tile arithmetic is the
+// single-instance kernel's (wave_tile_compute).
+//
+// Advection instances (one component) use one CTA per (instance, tile) pair;
+// their per-point arithmetic is the single-instance line kernel's.
+#pragma once
+
+#include "line_kernels.cuh"
+#include "wave2d.cuh"
+
+namespace sbp {
+
+// Per-instance block of a batched wave instance; 16-byte multiple so it can
+// be bulk-copied into shared memory.
+template <typename T> struct alignas(16) BatchWave {
+  WaveParams<T> prm;  // geometry, taps, SAT weights, kconst, dt, un/acc/comp pointers
+  T* wa;              // stage-input ping-pong buffers
+  T* wb;
+};
+
+// Tensor maps of one batched wave instance, in global memory (64-byte aligned):
+// [3 * s + {0,1,2}] = stage input s (0: u^n, 1: wa, 2: wb) with the p, u, v
+// tile boxes; [9], [10], [11] = u^n, acc, comp point boxes.
+constexpr int kBatchMaps = 12;
+
+__device__ __forceinline__ void bulk_copy_g2s(void* smem_dst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(smem_dst)),
+               "l"(reinterpret_cast<uint64_t>(gsrc)), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+// Stage input and output buffers and RK4 coefficients of stage rk (1..4) of
+// the classical RK4 step sequence (see the single-instance runtime).
+template <typename T>
+__device__ __forceinline__ void batch_stage_buffers(const BatchWave<T>& I, int rk, const T*& in, T*& wout, T& c_acc,
+                                                    T& c_w) {
+  const double dt = I.prm.dt;
+  in = rk == 1 ? I.prm.un : (rk == 3 ? I.wb : I.wa);
+  wout = (rk == 1 || rk == 3) ? I.wa : I.wb;
+  c_acc = (T)((rk == 1 || rk == 4) ? dt / 6 : dt / 3);
+  c_w = (T)(rk == 3 ? dt : 0.5 * dt);
+}
+
+template <typename T, int ORD, int STAGE, int TY>
+__global__ void __launch_bounds__(kWaveThreads, 1)
+    wave_batch_stage_kernel(const BatchWave<T>* __restrict__ insts, const CUtensorMap* __restrict__ maps,
+                            const int2* __restrict__ tiles, int ntiles, int rk, int* err) {
+  using Tile = WaveTile<T, ORD, STAGE, TY, (int)sizeof(BatchWave<T>)>;
+  constexpr int HX = Tile::HX, HY = Tile::HY;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
+  uint64_t* empty = full + 2;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    mbar_init(&empty[0], kWaveConsumerWarps);
+    mbar_init(&empty[1], kWaveConsumerWarps);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  const int sel = rk == 1 ? 0 : (rk == 3 ? 2 : 1);  // which buffer is the stage input
+
+  if (warp == kWaveConsumerWarps) {
+    if (lane == 0) {
+      int k = 0;
+      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
+        const int b = k & 1;
+        if (k >= 2 && !mbar_wait_bounded(&empty[b], ((k >> 1) - 1) & 1)) {
+          atomicOr(err, ERR_TMA_TIMEOUT);
+          break;
+        }
+        const int2 tt = tiles[tile];
+        const int nx = insts[tt.x].prm.nx;
+        const int ntx = (nx + kWaveTX - 1) / kWaveTX;
+        const int i0 = (tt.y % ntx) * kWaveTX, j0 = (tt.y / ntx) * TY;
+        const CUtensorMap* m = maps + (long long)tt.x * kBatchMaps;
+        unsigned char* st = smem + b * Tile::STAGE_BYTES;
+        mbar_arrive_expect_tx(&full[b], Tile::TX_BYTES);
+        tma_load_3d(st, &m[3 * sel + 0], i0 - HX, j0 - HY, 2, &full[b]);
+        tma_load_3d(st + Tile::OFF_U, &m[3 * sel + 1], i0 - HX, j0, 0, &full[b]);
+        tma_load_3d(st + Tile::OFF_V, &m[3 * sel + 2], i0, j0 - HY, 1, &full[b]);
+        if (Tile::LOAD_UN) tma_load_3d(st + Tile::OFF_N, &m[9], i0, j0, 0, &full[b]);
+        if (Tile::LOAD_ACC) tma_load_3d(st + Tile::OFF_A, &m[10], i0, j0, 0, &full[b]);
+        if (Tile::LOAD_COMP) tma_load_3d(st + Tile::OFF_C, &m[11], i0, j0, 0, &full[b]);
+        bulk_copy_g2s(st + Tile::OFF_PRM, &insts[tt.x], (uint32_t)sizeof(BatchWave<T>), &full[b]);
+      }
+      for (int kk = (k >= 2 ? k - 2 : 0); kk < k; kk++) mbar_wait_bounded(&full[kk & 1], (kk >> 1) & 1);
+    }
+    return;
+  }
+
+  int k = 0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
+    const int b = k & 1;
+    if (!mbar_wait_bounded(&full[b], (k >> 1) & 1)) {
+      if (lane == 0) atomicOr(err, ERR_TMA_TIMEOUT);
+      break;
+    }
+    const unsigned char* st = smem + b * Tile::STAGE_BYTES;
+    const BatchWave<T>& I = *reinterpret_cast<const BatchWave<T>*>(st + Tile::OFF_PRM);
+    const int2 tt = tiles[tile];
+    const int ntx = (I.prm.nx + kWaveTX - 1) / kWaveTX;
+    const int i0 = (tt.y % ntx) * kWaveTX, j0 = (tt.y / ntx) * TY;
+    const T* in;
+    T* wout;
+    T c_acc, c_w;
+    batch_stage_buffers(I, rk, in, wout, c_acc, c_w);
+    wave_tile_compute<T, ORD, WK_CONST, STAGE, Tile>(I.prm, in, wout, c_acc, c_w, st, i0, j0, warp, lane);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[b]);
+  }
+}
+
+// Batched 2D advection: one CTA of 32 x 8 threads per (instance, tile) pair.
+template <typename T> struct alignas(16) BatchLine {
+  LineParams<T> prm;  // geometry, taps, SAT factors, un/acc/comp pointers
+  T* wa;
+  T* wb;
+  double dt;
+};
+
+constexpr int kLineTileX = 32, kLineTileY = 8;
+
+template <typename T, int ORD, int STAGE>
+__global__ void __launch_bounds__(kLineTileX * kLineTileY)
+    adv_batch_stage_kernel(const BatchLine<T>* __restrict__ insts, const int2* __restrict__ tiles, int rk) {
+  const int2 tt = tiles[blockIdx.x];
+  const BatchLine<T>& I = insts[tt.x];
+  const int ntx = (I.prm.nx + kLineTileX - 1) / kLineTileX;
+  const int i = (tt.y % ntx) * kLineTileX + threadIdx.x;
+  const int j = (tt.y / ntx) * kLineTileY + threadIdx.y;
+  if (i >= I.prm.nx || j >= I.prm.ny) return;
+  const double dt = I.dt;
+  const T* in = rk == 1 ? I.prm.un : (rk == 3 ? I.wb : I.wa);
+  T* wout = (rk == 1 || rk == 3) ? I.wa : I.wb;
+  const T c_acc = (T)((rk == 1 || rk == 4) ? dt / 6 : dt / 3);
+  const T c_w = (T)(rk == 3 ? dt : 0.5 * dt);
+  line_point<T, ORD, LK_ADV2D, STAGE>(I.prm, in, wout, c_acc, c_w, i, j);
+}
+
+}  // namespace sbp

@@ -34,7 +34,10 @@ DOFS = {WAVE_HOM_2D: 3, WAVE_MMS_2D: 3, WAVE_VAR_2D: 3, ADVECTION_1D: 1, ADVECTI
 EXPORTS = ("sbp_create", "sbp_destroy", "sbp_last_error", "sbp_dofs", "sbp_rhs", "sbp_apply", "sbp_rk4_nsteps",
            "sbp_ts_rk4", "sbp_rk4", "sbp_set_state", "sbp_get_state", "sbp_rk4_resident", "sbp_synchronize",
            "sbp_error_norms", "sbp_hnorm", "sbp_get_stream", "sbp_launch_count", "sbp_probe_dfma_rate",
-           "sbp_wave_rhs_noalloc", "sbp_write_petsc_vec", "sbp_read_petsc_vec")
+           "sbp_wave_rhs_noalloc", "sbp_write_petsc_vec", "sbp_read_petsc_vec",
+           "sbp_batch_create", "sbp_batch_destroy", "sbp_batch_last_error", "sbp_batch_set_state",
+           "sbp_batch_get_state", "sbp_batch_rk4_resident", "sbp_batch_synchronize", "sbp_batch_autotune",
+           "sbp_batch_tile_height", "sbp_batch_get_stream", "sbp_batch_points", "sbp_batch_launch_count")
 
 _dp = C.POINTER(C.c_double)
 
@@ -46,6 +49,14 @@ class Desc(C.Structure):
                 ("a", C.c_double), ("b", C.c_double),
                 ("rho", _dp), ("K", _dp),
                 ("stream", C.c_void_p), ("device", C.c_int)]
+
+
+class Instance(C.Structure):
+    """One member of a batch (sbp_instance)."""
+    _fields_ = [("problem", C.c_int), ("order", C.c_int), ("bc", C.c_int),
+                ("nx", C.c_longlong), ("ny", C.c_longlong),
+                ("xl", C.c_double * 2), ("xr", C.c_double * 2),
+                ("c", C.c_double), ("a", C.c_double), ("b", C.c_double), ("dt", C.c_double)]
 
 
 class SbpError(RuntimeError):
@@ -89,6 +100,21 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.sbp_launch_count.restype = C.c_longlong
     L.sbp_probe_dfma_rate.argtypes = [C.c_int, _dp]
     L.sbp_wave_rhs_noalloc.argtypes = [C.POINTER(Desc), C.c_double, C.c_void_p, C.c_void_p]
+    L.sbp_batch_create.argtypes = [C.POINTER(Instance), C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(P)]
+    L.sbp_batch_destroy.argtypes = [P]
+    L.sbp_batch_last_error.argtypes = [P]
+    L.sbp_batch_last_error.restype = C.c_char_p
+    L.sbp_batch_set_state.argtypes = [P, C.c_int, C.c_void_p, C.c_int]
+    L.sbp_batch_get_state.argtypes = [P, C.c_int, C.c_void_p, C.c_int]
+    L.sbp_batch_rk4_resident.argtypes = [P, C.c_longlong]
+    L.sbp_batch_synchronize.argtypes = [P]
+    L.sbp_batch_autotune.argtypes = [P, C.c_char_p]
+    L.sbp_batch_tile_height.argtypes = [P, C.c_int]
+    L.sbp_batch_get_stream.argtypes = [P, C.POINTER(C.c_void_p)]
+    L.sbp_batch_points.argtypes = [P]
+    L.sbp_batch_points.restype = C.c_longlong
+    L.sbp_batch_launch_count.argtypes = [P]
+    L.sbp_batch_launch_count.restype = C.c_longlong
     L.sbp_write_petsc_vec.argtypes = [C.c_char_p, C.c_void_p, C.c_longlong]
     L.sbp_read_petsc_vec.argtypes = [C.c_char_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     _lib = L
@@ -277,3 +303,83 @@ class Context:
     @property
     def launches(self) -> int:
         return self._L.sbp_launch_count(self._h)
+
+
+class Batch:
+    """Many independent wave / advection instances advanced together (sbp_batch_*).
+
+    instances: dicts with problem (WAVE_HOM_2D or ADVECTION_2D), order, nx, ny,
+    dt and c (wave speed) or a, b (advection velocity); optional bc, xl, xr.
+    """
+
+    def __init__(self, instances, *, precision: int = FP64, device: int = 0, stream: int | None = None):
+        L = load()
+        self._L = L
+        arr = (Instance * len(instances))()
+        self.shapes = []
+        for k, d in enumerate(instances):
+            xl, xr = d.get("xl", (-1.0, -1.0)), d.get("xr", (1.0, 1.0))
+            arr[k] = Instance(d["problem"], d["order"], d.get("bc", BC_REFERENCE), d["nx"], d["ny"],
+                              (C.c_double * 2)(*xl), (C.c_double * 2)(*xr), d.get("c", 1.0), d.get("a", 0.0),
+                              d.get("b", 0.0), d["dt"])
+            self.shapes.append((d["ny"], d["nx"], 3 if d["problem"] == WAVE_HOM_2D else 1))
+        h = C.c_void_p()
+        rc = L.sbp_batch_create(arr, len(instances), precision, device, stream, C.byref(h))
+        if rc:
+            raise SbpError(rc, L.sbp_batch_last_error(None).decode())
+        self._h = h
+
+    def _check(self, rc):
+        if rc:
+            raise SbpError(rc, self._L.sbp_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.sbp_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_state(self, index: int, v: np.ndarray):
+        self._check(self._L.sbp_batch_set_state(self._h, index, _host(v).ctypes.data, HOST))
+
+    def get_state(self, index: int) -> np.ndarray:
+        out = np.empty(int(np.prod(self.shapes[index])))
+        self._check(self._L.sbp_batch_get_state(self._h, index, out.ctypes.data, HOST))
+        return out
+
+    def step_resident(self, nsteps: int):
+        self._check(self._L.sbp_batch_rk4_resident(self._h, nsteps))
+
+    def synchronize(self):
+        self._check(self._L.sbp_batch_synchronize(self._h))
+
+    def autotune(self, cache_path: str | None = None):
+        self._check(self._L.sbp_batch_autotune(self._h, cache_path.encode() if cache_path else None))
+
+    def tile_height(self, order: int) -> int:
+        return self._L.sbp_batch_tile_height(self._h, order)
+
+    @property
+    def points(self) -> int:
+        return self._L.sbp_batch_points(self._h)
+
+    @property
+    def launches(self) -> int:
+        return self._L.sbp_batch_launch_count(self._h)
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(self._L.sbp_batch_get_stream(self._h, C.byref(s)))
+        return s.value or 0

@@ -143,6 +143,46 @@ long long sbp_launch_count(const sbp_ctx* ctx);
  * FP64 ALU roof beside the HBM roof. */
 int sbp_probe_dfma_rate(int device, double* dfma_per_s);
 
+/* ---------------------------------------------------------------- batches
+ * Many independent instances of uneven size, order and coefficients
+ * advanced together: 2D waves (rho = 1, K = c^2) and 2D advection. No
+ * counterpart in the reference, which runs one grid per process; each
+ * instance computes what a single-instance context of the same problem
+ * computes (the same per-point arithmetic). Per order, one persistent stage
+ * kernel walks a tile list over all wave instances; the step loop runs in
+ * CUDA graphs of 100 steps; each instance has its own time step. */
+typedef struct sbp_batch sbp_batch;
+typedef struct {
+  int problem;        /* SBP_WAVE_HOM_2D (wave speed c) or SBP_ADVECTION_2D (velocity a, b) */
+  int order;          /* 2, 4 or 6 */
+  int bc;             /* wave: SBP_BC_REFERENCE (free surface) or SBP_BC_CHARACTERISTIC */
+  long long nx, ny;
+  double xl[2], xr[2];
+  double c;           /* wave speed (rho = 1, K = c^2) */
+  double a, b;        /* advection velocity */
+  double dt;          /* this instance's time step */
+} sbp_instance;
+
+int sbp_batch_create(const sbp_instance* list, int count, int precision, int device, void* stream,
+                     sbp_batch** batch);
+int sbp_batch_destroy(sbp_batch* batch);
+const char* sbp_batch_last_error(const sbp_batch* batch); /* NULL: last failed sbp_batch_create */
+/* State of instance `index` in the reference's AoS layout (host or device). */
+int sbp_batch_set_state(sbp_batch* batch, int index, const double* v, int where);
+int sbp_batch_get_state(sbp_batch* batch, int index, double* v, int where);
+/* nsteps RK4 steps of every instance (each with its own dt); enqueues only. */
+int sbp_batch_rk4_resident(sbp_batch* batch, long long nsteps);
+int sbp_batch_synchronize(sbp_batch* batch);
+/* Picks each order group's tile height (FP64: 8 or 16 rows, FP32: 16 or 32)
+ * by timing the stage kernel on this batch; results are cached in the flat
+ * JSON file cache_path (NULL: no cache). Call between steps: it writes only
+ * the stage scratch buffers, never the states. */
+int sbp_batch_autotune(sbp_batch* batch, const char* cache_path);
+int sbp_batch_tile_height(const sbp_batch* batch, int order);
+int sbp_batch_get_stream(const sbp_batch* batch, void** stream);
+long long sbp_batch_points(const sbp_batch* batch);       /* grid points over all instances */
+long long sbp_batch_launch_count(const sbp_batch* batch); /* kernels launched so far */
+
 /* PETSc binary Vec files (host-side I/O): the format VecView writes on a
  * binary viewer, as the reference's write_vector_to_binary does
  * (code/src/util/io_util.cpp:4-14): big-endian int32 classid 1211214,

@@ -1,0 +1,97 @@
+"""Batched form: every instance of a batch must evolve exactly as a
+single-instance context of the same problem does (same per-point arithmetic),
+for uneven sizes, orders, speeds and time steps, FP64 and FP32."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import fields
+
+
+def _instances(sbp, seed, count):
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        order = int(rng.choice([2, 4, 6]))
+        nx = int(rng.integers(12, 150))
+        ny = int(rng.integers(12, 150))
+        c = float(rng.uniform(0.5, 2.0))
+        h = min(2.0 / (nx - 1), 2.0 / (ny - 1))
+        if k % 2 == 0:
+            out.append(dict(problem=sbp.WAVE_HOM_2D, order=order, nx=nx, ny=ny, c=c, dt=0.2 * h / c,
+                            bc=int(rng.integers(0, 2))))
+        else:
+            ang = rng.uniform(0, 2 * np.pi)
+            out.append(dict(problem=sbp.ADVECTION_2D, order=order, nx=nx, ny=ny, a=c * np.cos(ang),
+                            b=c * np.sin(ang), dt=0.2 * h / c))
+    return out
+
+
+def _state(d, seed):
+    if d["problem"] == 1:
+        x0, y0 = np.random.default_rng(seed).uniform(-0.5, 0.5, 2)
+        return fields.gaussian_pulse(d["nx"], d["ny"], x0, y0, 0.2, 1.0)
+    x = np.linspace(-1, 1, d["nx"])
+    y = np.linspace(-1, 1, d["ny"])
+    return np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / 0.1).ravel()
+
+
+def _single(sbp, d, v0, steps, precision):
+    if d["problem"] == sbp.WAVE_HOM_2D:
+        ones = np.ones(d["nx"] * d["ny"])
+        ctx = sbp.Context(sbp.WAVE_VAR_2D, d["order"], d["nx"], d["ny"], rho=ones, K=ones * d["c"] ** 2,
+                          bc=d["bc"], precision=precision)
+    else:
+        ctx = sbp.Context(sbp.ADVECTION_2D, d["order"], d["nx"], d["ny"], a=d["a"], b=d["b"], precision=precision)
+    with ctx:
+        return ctx.rk4(v0, 0.0, d["dt"], steps)
+
+
+def test_batch_rejects_bad_instances(sbp):
+    with pytest.raises(sbp.SbpError) as ei:
+        sbp.Batch([dict(problem=sbp.WAVE_HOM_2D, order=5, nx=40, ny=40, c=1.0, dt=0.01)])
+    assert "order" in str(ei.value)
+    with pytest.raises(sbp.SbpError):
+        sbp.Batch([dict(problem=sbp.WAVE_MMS_2D, order=4, nx=40, ny=40, c=1.0, dt=0.01)])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_matches_single_instances(sbp, precision):
+    insts = _instances(sbp, 11 + precision, 12)
+    steps = 130  # one 100-step graph chunk and a 30-step chunk
+    with sbp.Batch(insts, precision=precision) as b:
+        v0 = [_state(d, k) for k, d in enumerate(insts)]
+        for k, v in enumerate(v0):
+            b.set_state(k, v)
+        b.step_resident(steps)
+        b.synchronize()
+        got = [b.get_state(k) for k in range(len(insts))]
+    tol = 1e-12 if precision == 0 else 1e-6
+    for k, d in enumerate(insts):
+        ref = _single(sbp, d, v0[k], steps, precision)
+        err = np.max(np.abs(got[k] - ref)) / np.max(np.abs(ref))
+        assert err <= tol, (k, d, err)
+
+
+@pytest.mark.gpu
+def test_batch_autotune_keeps_states_and_caches(sbp, tmp_path):
+    insts = _instances(sbp, 5, 8)
+    cache = os.path.join(tmp_path, "tiles.json")
+    with sbp.Batch(insts) as b:
+        v0 = [_state(d, k) for k, d in enumerate(insts)]
+        for k, v in enumerate(v0):
+            b.set_state(k, v)
+        b.autotune(cache)
+        for order in (2, 4, 6):
+            assert b.tile_height(order) in (0, 8, 16)
+        b.step_resident(20)
+        b.synchronize()
+        got = [b.get_state(k) for k in range(len(insts))]
+    entries = json.load(open(cache))
+    assert entries and all(v in (8, 16) for v in entries.values())
+    for k, d in enumerate(insts):
+        ref = _single(sbp, d, v0[k], 20, 0)
+        assert np.max(np.abs(got[k] - ref)) <= 1e-12 * np.max(np.abs(ref))
