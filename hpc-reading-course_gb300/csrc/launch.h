@@ -15,10 +15,13 @@ namespace sbp {
 struct WaveMaps {
   CUtensorMap p, u, v;  // the stage input seen with the p, u and v tile boxes (with halos)
   CUtensorMap n, a, c;  // u^n, acc and the FP32 Kahan term as 3-component point boxes
+  CUtensorMap k;        // variable coefficients [1/rho | K] as a 2-component point box
 };
 
-// Tile height of the wave stage kernel for an element size (bytes).
-inline int wave_tile_height(int elem_bytes) { return elem_bytes == 8 ? 16 : 32; }
+// Tile height of the single-instance wave stage kernel (see wave_ty).
+inline int wave_tile_height(int elem_bytes, int kind = WK_HOM) {
+  return elem_bytes == 8 ? 16 : (kind == WK_VAR ? 24 : 32);
+}
 
 // Streaming multiprocessors of the current device (cached per device).
 int device_sm_count();
@@ -42,7 +45,7 @@ template <typename T>
 inline cudaError_t launch_wave(int order, int kind, int stage, const WaveMaps& m, const WaveParams<T>& prm,
                                cudaStream_t s) {
   // persistent grid: one CTA per SM, each walking the tiles with a fixed stride
-  const int ty = wave_tile_height((int)sizeof(T));
+  const int ty = wave_tile_height((int)sizeof(T), kind);
   const long long ntiles = (long long)((prm.nx + kWaveTX - 1) / kWaveTX) * ((prm.ny + ty - 1) / ty);
   const int nsm = device_sm_count();
   const dim3 grid((unsigned)(ntiles < nsm ? ntiles : nsm));

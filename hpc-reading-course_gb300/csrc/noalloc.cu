@@ -138,7 +138,7 @@ extern "C" int sbp_wave_rhs_noalloc(const sbp_desc* d, double t, const double* s
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return reject(SBP_ERR_CUDA, "cuTensorMapEncodeTiled failed");
-  maps.n = maps.a = maps.c = maps.p;  // the RHS-only stage loads no per-point operands
+  maps.n = maps.a = maps.c = maps.k = maps.p;  // the RHS-only stage loads no per-point operands
 
   WaveParams<double> p;
   std::memset(&p, 0, sizeof(p));

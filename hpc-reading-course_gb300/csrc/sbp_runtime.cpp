@@ -100,6 +100,11 @@ void fill_taps(DirTaps<T>& t, int order, double scale) {
     for (int s = 0; s < op.cls_width; s++) t.cls[r][s] = (T)(scale * op.closure[r][s]);
 }
 
+int wave_kind(const sbp_ctx* ctx) {
+  if (ctx->d.problem == SBP_WAVE_HOM_2D) return WK_HOM;
+  return has_fields(ctx->d.problem) ? WK_VAR : WK_MMS;
+}
+
 // Encodes one 3D tensor map (x, y, component) over a state buffer of the context.
 int encode_map(sbp_ctx* ctx, void* base, const cuuint32_t box[3], CUtensorMap* out) {
   EncodeTiledFn enc = encode_tiled();
@@ -120,7 +125,7 @@ int make_maps(sbp_ctx* ctx, void* base, WaveMaps& m) {
   const int R = ctx->d.order / 2;
   const int hxa = 16 / (int)ctx->es;
   const int HX = (R + hxa - 1) / hxa * hxa, HY = R;
-  const int TY = wave_tile_height((int)ctx->es);
+  const int TY = wave_tile_height((int)ctx->es, wave_kind(ctx));
   const cuuint32_t boxP[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)(TY + 2 * HY), 1};
   const cuuint32_t boxU[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)TY, 1};
   const cuuint32_t boxV[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)(TY + 2 * HY), 1};
@@ -128,9 +133,24 @@ int make_maps(sbp_ctx* ctx, void* base, WaveMaps& m) {
   int rc;
   if ((rc = encode_map(ctx, base, boxP, &m.p)) || (rc = encode_map(ctx, base, boxU, &m.u)) ||
       (rc = encode_map(ctx, base, boxV, &m.v)) || (rc = encode_map(ctx, ctx->un, boxPt, &m.n)) ||
-      (rc = encode_map(ctx, ctx->acc, boxPt, &m.a)))
+      (rc = encode_map(ctx, ctx->acc, boxPt, &m.a)) ||
+      (rc = encode_map(ctx, ctx->comp ? ctx->comp : ctx->acc, boxPt, &m.c)))
     return rc;
-  return encode_map(ctx, ctx->comp ? ctx->comp : ctx->acc, boxPt, &m.c);
+  if (!ctx->rinv) {
+    m.k = m.p;  // no coefficient fields: the map is never used
+    return SBP_OK;
+  }
+  // [1/rho | K]: two planes at rinv (kmod follows it), as a 2-component point box
+  EncodeTiledFn enc = encode_tiled();
+  const cuuint64_t dims[3] = {(cuuint64_t)ctx->nx, (cuuint64_t)ctx->ny, 2};
+  const cuuint64_t strides[2] = {(cuuint64_t)(ctx->pitch * ctx->es), (cuuint64_t)(ctx->plane * ctx->es)};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const cuuint32_t boxK[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)TY, 2};
+  const CUtensorMapDataType dt = ctx->fp32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  if (enc(&m.k, dt, 3, ctx->rinv, dims, strides, boxK, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return fail(ctx, SBP_ERR_CUDA, "cuTensorMapEncodeTiled failed for the coefficient planes");
+  return SBP_OK;
 }
 
 // Stage-independent kernel parameters.
@@ -159,11 +179,6 @@ WaveParams<T> wave_params(sbp_ctx* ctx) {
   p.hiy = ctx->hiy;
   p.err = ctx->err;
   return p;
-}
-
-int wave_kind(const sbp_ctx* ctx) {
-  if (ctx->d.problem == SBP_WAVE_HOM_2D) return WK_HOM;
-  return has_fields(ctx->d.problem) ? WK_VAR : WK_MMS;
 }
 
 template <typename T>
@@ -384,7 +399,7 @@ void release(sbp_ctx* ctx) {
   if (!ctx) return;
   drop_graphs(ctx);
   void* bufs[] = {ctx->un, ctx->acc, ctx->wa, ctx->wb, ctx->comp, ctx->io, ctx->partial, ctx->red,
-                  ctx->rinv, ctx->kmod, ctx->rho64, ctx->k64, ctx->err};
+                  ctx->rinv, ctx->rho64, ctx->k64, ctx->err};  // kmod lives inside the rinv allocation
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -483,11 +498,12 @@ int sbp_create(const sbp_desc* desc, sbp_ctx** out) {
     for (size_t q = 0; q < np; q++) rinv_h[q] = 1.0 / d.rho[q];
     if ((e = cudaMalloc((void**)&ctx->rho64, np * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc((void**)&ctx->k64, np * sizeof(double))) != cudaSuccess ||
-        (e = cudaMalloc(&ctx->rinv, ctx->plane * ctx->es)) != cudaSuccess ||
-        (e = cudaMalloc(&ctx->kmod, ctx->plane * ctx->es)) != cudaSuccess) {
+        (e = cudaMalloc(&ctx->rinv, 2 * ctx->plane * ctx->es)) != cudaSuccess) {
       delete[] rinv_h;
       return cuda_fail("cudaMalloc(coefficients)", e);
     }
+    cudaMemset(ctx->rinv, 0, 2 * ctx->plane * ctx->es);
+    ctx->kmod = static_cast<unsigned char*>(ctx->rinv) + ctx->plane * ctx->es;  // second plane
     cudaMemcpy(ctx->rho64, d.rho, np * sizeof(double), cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->k64, d.K, np * sizeof(double), cudaMemcpyHostToDevice);
     // pack 1/rho and K into padded planes of T via the AoS->SoA kernel (dofs = 1)

@@ -69,8 +69,14 @@ template <> struct IsCompensated<float> { static constexpr bool value = true; };
 // rounded up so that (tile origin - halo) * sizeof(T) is a multiple of 16
 // bytes (TMA rule for the innermost coordinate); tile origins are multiples of 64.
 template <typename T> constexpr int default_wave_ty() { return sizeof(T) == 8 ? 16 : 32; }
+// Tile height of the single-instance kernel: the variable-coefficient FP32
+// kind also stages 1/rho and K, so it uses 24 rows to keep two stages in 227 KB.
+template <typename T, int KIND> constexpr int wave_ty() {
+  return (sizeof(T) == 4 && KIND == WK_VAR) ? 24 : default_wave_ty<T>();
+}
 
-template <typename T, int ORD, int STAGE, int TY_ = default_wave_ty<T>(), int PRM_BYTES = 0> struct WaveTile {
+template <typename T, int ORD, int STAGE, int TY_ = default_wave_ty<T>(), int PRM_BYTES = 0, bool COEF = false>
+struct WaveTile {
   static constexpr bool COMP = IsCompensated<T>::value;
   static constexpr int TY = TY_;                              // tile height
   static constexpr int R = (OpShape<ORD>::W - 1) / 2;
@@ -82,6 +88,7 @@ template <typename T, int ORD, int STAGE, int TY_ = default_wave_ty<T>(), int PR
   static constexpr bool LOAD_UN = (STAGE == ST_MID) || (STAGE == ST_LAST && COMP);
   static constexpr bool LOAD_ACC = (STAGE == ST_MID) || (STAGE == ST_LAST);
   static constexpr bool LOAD_COMP = (STAGE == ST_LAST && COMP);
+  static constexpr bool LOAD_COEF = COEF;  // 1/rho and K planes as one 2-component point box
   static constexpr int align128(int b) { return (b + 127) / 128 * 128; }
   static constexpr int BYTES_P = PH * PW * (int)sizeof(T);
   static constexpr int BYTES_U = TY * PW * (int)sizeof(T);
@@ -92,12 +99,15 @@ template <typename T, int ORD, int STAGE, int TY_ = default_wave_ty<T>(), int PR
   static constexpr int OFF_N = OFF_V + align128(BYTES_V);
   static constexpr int OFF_A = OFF_N + (LOAD_UN ? BYTES_PT : 0);
   static constexpr int OFF_C = OFF_A + (LOAD_ACC ? BYTES_PT : 0);
-  static constexpr int OFF_PRM = align128(OFF_C + (LOAD_COMP ? BYTES_PT : 0));  // batched: instance parameters
+  static constexpr int BYTES_K = 2 * TY * kWaveTX * (int)sizeof(T);
+  static constexpr int OFF_K = align128(OFF_C + (LOAD_COMP ? BYTES_PT : 0));
+  static constexpr int OFF_PRM = align128(OFF_K + (LOAD_COEF ? BYTES_K : 0));  // batched: instance parameters
   static constexpr int STAGE_BYTES = OFF_PRM + align128(PRM_BYTES);
   static constexpr int OFF_BAR = 2 * STAGE_BYTES;             // full[2], empty[2]
   static constexpr int SMEM = OFF_BAR + 128;
   static constexpr uint32_t TX_BYTES = BYTES_P + BYTES_U + BYTES_V + (LOAD_UN ? BYTES_PT : 0) +
-                                       (LOAD_ACC ? BYTES_PT : 0) + (LOAD_COMP ? BYTES_PT : 0) + PRM_BYTES;
+                                       (LOAD_ACC ? BYTES_PT : 0) + (LOAD_COMP ? BYTES_PT : 0) +
+                                       (LOAD_COEF ? BYTES_K : 0) + PRM_BYTES;
   static_assert(TY % kWaveConsumerWarps == 0, "tile rows must split evenly over the consumer warps");
   static_assert(SMEM <= 227 * 1024, "wave tile pipeline exceeds shared memory");
 };
@@ -205,9 +215,11 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
   const T* sN = reinterpret_cast<const T*>(st + Tile::OFF_N);
   const T* sA = reinterpret_cast<const T*>(st + Tile::OFF_A);
   const T* sC = reinterpret_cast<const T*>(st + Tile::OFF_C);
+  const T* sK = reinterpret_cast<const T*>(st + Tile::OFF_K);  // [1/rho | K] when Tile::LOAD_COEF
   (void)sN;
   (void)sA;
   (void)sC;
+  (void)sK;
 #pragma unroll ROW_UNROLL
   for (int rr = 0; rr < ROWS; rr++) {
     const int y = warp * ROWS + rr;
@@ -337,8 +349,8 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
     wave_stage_kernel(const __grid_constant__ CUtensorMap mapP, const __grid_constant__ CUtensorMap mapU,
                       const __grid_constant__ CUtensorMap mapV, const __grid_constant__ CUtensorMap mapN,
                       const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapC,
-                      const __grid_constant__ WaveParams<T> prm) {
-  using Tile = WaveTile<T, ORD, STAGE>;
+                      const __grid_constant__ CUtensorMap mapK, const __grid_constant__ WaveParams<T> prm) {
+  using Tile = WaveTile<T, ORD, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR>;
   constexpr int TY = Tile::TY, HX = Tile::HX, HY = Tile::HY;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
@@ -378,6 +390,7 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
         if (Tile::LOAD_UN) tma_load_3d(st + Tile::OFF_N, &mapN, i0, j0, 0, &full[b]);
         if (Tile::LOAD_ACC) tma_load_3d(st + Tile::OFF_A, &mapA, i0, j0, 0, &full[b]);
         if (Tile::LOAD_COMP) tma_load_3d(st + Tile::OFF_C, &mapC, i0, j0, 0, &full[b]);
+        if (Tile::LOAD_COEF) tma_load_3d(st + Tile::OFF_K, &mapK, i0, j0, 0, &full[b]);
       }
       // the CTA must not exit with copies in flight: wait for the last two stages
       for (int kk = (k >= 2 ? k - 2 : 0); kk < k; kk++) mbar_wait_bounded(&full[kk & 1], (kk >> 1) & 1);
