@@ -74,9 +74,9 @@ struct sbp_batch {
   CUtensorMap* d_maps = nullptr; // kBatchMaps per wave instance
   void* d_line = nullptr;        // BatchLine<T>[n_line]
   std::vector<int> wave_slot, line_slot;  // instance -> slot in d_wave / d_line (-1 if other kind)
-  int2* d_tiles_wave[3] = {nullptr, nullptr, nullptr};
+  BatchTile* d_tiles_wave[3] = {nullptr, nullptr, nullptr};
   int n_tiles_wave[3] = {0, 0, 0};
-  int2* d_tiles_line[3] = {nullptr, nullptr, nullptr};
+  BatchTile* d_tiles_line[3] = {nullptr, nullptr, nullptr};
   int n_tiles_line[3] = {0, 0, 0};
   int ty[3] = {0, 0, 0};
   double* io = nullptr;
@@ -146,15 +146,13 @@ int encode_instance_maps(sbp_batch* b, int i, int ty, CUtensorMap* out) {
 // (Re)builds the tensor maps and tile list of one order group for tile height ty.
 int build_wave_group(sbp_batch* b, int oi, int ty) {
   const int order = 2 * (oi + 1);
-  std::vector<int2> tiles;
-  std::vector<CUtensorMap> maps;
-  std::vector<int> slots;
+  std::vector<BatchTile> tiles;
   for (size_t i = 0; i < b->inst.size(); i++) {
     const Geo& g = b->geo[i];
     if (!g.wave || g.order != order) continue;
     const int s = b->wave_slot[i];
-    const long long ntx = (g.nx + kWaveTX - 1) / kWaveTX, nty = (g.ny + ty - 1) / ty;
-    for (long long t = 0; t < ntx * nty; t++) tiles.push_back(make_int2(s, (int)t));
+    for (long long j0 = 0; j0 < g.ny; j0 += ty)
+      for (long long i0 = 0; i0 < g.nx; i0 += kWaveTX) tiles.push_back(BatchTile{s, (int)i0, (int)j0, 0});
     CUtensorMap m[kBatchMaps];
     int rc = encode_instance_maps(b, (int)i, ty, m);
     if (rc) return rc;
@@ -164,8 +162,8 @@ int build_wave_group(sbp_batch* b, int oi, int ty) {
   b->d_tiles_wave[oi] = nullptr;
   b->n_tiles_wave[oi] = (int)tiles.size();
   if (!tiles.empty()) {
-    BCK(cudaMalloc((void**)&b->d_tiles_wave[oi], tiles.size() * sizeof(int2)));
-    BCK(cudaMemcpyAsync(b->d_tiles_wave[oi], tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice,
+    BCK(cudaMalloc((void**)&b->d_tiles_wave[oi], tiles.size() * sizeof(BatchTile)));
+    BCK(cudaMemcpyAsync(b->d_tiles_wave[oi], tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice,
                         b->stream));
     BCK(b->fp32 ? configure_wave_batch<float>(order, ty) : configure_wave_batch<double>(order, ty));
   }
@@ -244,17 +242,18 @@ int fill_params(sbp_batch* b) {
   }
   // advection tile lists (32 x 8 points per CTA)
   for (int oi = 0; oi < 3; oi++) {
-    std::vector<int2> tiles;
+    std::vector<BatchTile> tiles;
     for (size_t i = 0; i < b->inst.size(); i++) {
       const Geo& g = b->geo[i];
       if (g.wave || order_index(g.order) != oi) continue;
-      const long long ntx = (g.nx + kLineTileX - 1) / kLineTileX, nty = (g.ny + kLineTileY - 1) / kLineTileY;
-      for (long long t = 0; t < ntx * nty; t++) tiles.push_back(make_int2(b->line_slot[i], (int)t));
+      for (long long j0 = 0; j0 < g.ny; j0 += kLineTileY)
+        for (long long i0 = 0; i0 < g.nx; i0 += kLineTileX)
+          tiles.push_back(BatchTile{b->line_slot[i], (int)i0, (int)j0, 0});
     }
     b->n_tiles_line[oi] = (int)tiles.size();
     if (!tiles.empty()) {
-      BCK(cudaMalloc((void**)&b->d_tiles_line[oi], tiles.size() * sizeof(int2)));
-      BCK(cudaMemcpy(b->d_tiles_line[oi], tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
+      BCK(cudaMalloc((void**)&b->d_tiles_line[oi], tiles.size() * sizeof(BatchTile)));
+      BCK(cudaMemcpy(b->d_tiles_line[oi], tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice));
     }
   }
   for (int oi = 0; oi < 3; oi++) {

@@ -69,9 +69,10 @@ cudaError_t launch_line(int order, int kind, int stage, const LineParams<T>& prm
   template <typename T> cudaError_t configure_wave_batch_o##o(int ty);                                          \
   template <typename T>                                                                                         \
   cudaError_t launch_wave_batch_o##o(int stage, int ty, const BatchWave<T>* insts, const CUtensorMap* maps,     \
-                                     const int2* tiles, int ntiles, int rk, int* err, unsigned grid, cudaStream_t s); \
+                                     const BatchTile* tiles, int ntiles, int rk, int* err, unsigned grid,          \
+                                     cudaStream_t s);                                                              \
   template <typename T>                                                                                         \
-  cudaError_t launch_adv_batch_o##o(int stage, const BatchLine<T>* insts, const int2* tiles, int ntiles, int rk, \
+  cudaError_t launch_adv_batch_o##o(int stage, const BatchLine<T>* insts, const BatchTile* tiles, int ntiles, int rk, \
                                     cudaStream_t s);
 SBP_DECLARE_BATCH(2)
 SBP_DECLARE_BATCH(4)
@@ -84,7 +85,7 @@ template <typename T> inline cudaError_t configure_wave_batch(int order, int ty)
 }
 template <typename T>
 inline cudaError_t launch_wave_batch(int order, int stage, int ty, const BatchWave<T>* insts, const CUtensorMap* maps,
-                                     const int2* tiles, int ntiles, int rk, int* err, cudaStream_t s) {
+                                     const BatchTile* tiles, int ntiles, int rk, int* err, cudaStream_t s) {
   const int nsm = device_sm_count();
   const unsigned grid = (unsigned)(ntiles < nsm ? ntiles : nsm);
   switch (order) {
@@ -95,7 +96,7 @@ inline cudaError_t launch_wave_batch(int order, int stage, int ty, const BatchWa
   }
 }
 template <typename T>
-inline cudaError_t launch_adv_batch(int order, int stage, const BatchLine<T>* insts, const int2* tiles, int ntiles,
+inline cudaError_t launch_adv_batch(int order, int stage, const BatchLine<T>* insts, const BatchTile* tiles, int ntiles,
                                     int rk, cudaStream_t s) {
   switch (order) {
     case 2: return launch_adv_batch_o2<T>(stage, insts, tiles, ntiles, rk, s);

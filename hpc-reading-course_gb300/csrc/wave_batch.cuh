@@ -51,10 +51,16 @@ __device__ __forceinline__ void batch_stage_buffers(const BatchWave<T>& I, int r
   c_w = (T)(rk == 3 ? dt : 0.5 * dt);
 }
 
+// A tile-list entry: the instance's slot and the tile's origin, so the
+// producer issues its loads without first reading the instance block.
+struct BatchTile {
+  int slot, i0, j0, pad;
+};
+
 template <typename T, int ORD, int STAGE, int TY>
 __global__ void __launch_bounds__(kWaveThreads, 1)
     wave_batch_stage_kernel(const BatchWave<T>* __restrict__ insts, const CUtensorMap* __restrict__ maps,
-                            const int2* __restrict__ tiles, int ntiles, int rk, int* err) {
+                            const BatchTile* __restrict__ tiles, int ntiles, int rk, int* err) {
   using Tile = WaveTile<T, ORD, STAGE, TY, (int)sizeof(BatchWave<T>)>;
   constexpr int HX = Tile::HX, HY = Tile::HY;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -75,17 +81,17 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
   if (warp == kWaveConsumerWarps) {
     if (lane == 0) {
       int k = 0;
+      BatchTile next = blockIdx.x < ntiles ? tiles[blockIdx.x] : BatchTile{0, 0, 0, 0};
       for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
+        const BatchTile tt = next;
+        if (tile + (int)gridDim.x < ntiles) next = tiles[tile + gridDim.x];  // prefetch the next descriptor
         const int b = k & 1;
         if (k >= 2 && !mbar_wait_bounded(&empty[b], ((k >> 1) - 1) & 1)) {
           atomicOr(err, ERR_TMA_TIMEOUT);
           break;
         }
-        const int2 tt = tiles[tile];
-        const int nx = insts[tt.x].prm.nx;
-        const int ntx = (nx + kWaveTX - 1) / kWaveTX;
-        const int i0 = (tt.y % ntx) * kWaveTX, j0 = (tt.y / ntx) * TY;
-        const CUtensorMap* m = maps + (long long)tt.x * kBatchMaps;
+        const int i0 = tt.i0, j0 = tt.j0;
+        const CUtensorMap* m = maps + (long long)tt.slot * kBatchMaps;
         unsigned char* st = smem + b * Tile::STAGE_BYTES;
         mbar_arrive_expect_tx(&full[b], Tile::TX_BYTES);
         tma_load_3d(st, &m[3 * sel + 0], i0 - HX, j0 - HY, 2, &full[b]);
@@ -94,7 +100,7 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
         if (Tile::LOAD_UN) tma_load_3d(st + Tile::OFF_N, &m[9], i0, j0, 0, &full[b]);
         if (Tile::LOAD_ACC) tma_load_3d(st + Tile::OFF_A, &m[10], i0, j0, 0, &full[b]);
         if (Tile::LOAD_COMP) tma_load_3d(st + Tile::OFF_C, &m[11], i0, j0, 0, &full[b]);
-        bulk_copy_g2s(st + Tile::OFF_PRM, &insts[tt.x], (uint32_t)sizeof(BatchWave<T>), &full[b]);
+        bulk_copy_g2s(st + Tile::OFF_PRM, &insts[tt.slot], (uint32_t)sizeof(BatchWave<T>), &full[b]);
       }
       for (int kk = (k >= 2 ? k - 2 : 0); kk < k; kk++) mbar_wait_bounded(&full[kk & 1], (kk >> 1) & 1);
     }
@@ -110,9 +116,8 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
     }
     const unsigned char* st = smem + b * Tile::STAGE_BYTES;
     const BatchWave<T>& I = *reinterpret_cast<const BatchWave<T>*>(st + Tile::OFF_PRM);
-    const int2 tt = tiles[tile];
-    const int ntx = (I.prm.nx + kWaveTX - 1) / kWaveTX;
-    const int i0 = (tt.y % ntx) * kWaveTX, j0 = (tt.y / ntx) * TY;
+    const BatchTile tt = tiles[tile];
+    const int i0 = tt.i0, j0 = tt.j0;
     const T* in;
     T* wout;
     T c_acc, c_w;
@@ -135,12 +140,11 @@ constexpr int kLineTileX = 32, kLineTileY = 8;
 
 template <typename T, int ORD, int STAGE>
 __global__ void __launch_bounds__(kLineTileX * kLineTileY)
-    adv_batch_stage_kernel(const BatchLine<T>* __restrict__ insts, const int2* __restrict__ tiles, int rk) {
-  const int2 tt = tiles[blockIdx.x];
-  const BatchLine<T>& I = insts[tt.x];
-  const int ntx = (I.prm.nx + kLineTileX - 1) / kLineTileX;
-  const int i = (tt.y % ntx) * kLineTileX + threadIdx.x;
-  const int j = (tt.y / ntx) * kLineTileY + threadIdx.y;
+    adv_batch_stage_kernel(const BatchLine<T>* __restrict__ insts, const BatchTile* __restrict__ tiles, int rk) {
+  const BatchTile tt = tiles[blockIdx.x];
+  const BatchLine<T>& I = insts[tt.slot];
+  const int i = tt.i0 + threadIdx.x;
+  const int j = tt.j0 + threadIdx.y;
   if (i >= I.prm.nx || j >= I.prm.ny) return;
   const double dt = I.dt;
   const T* in = rk == 1 ? I.prm.un : (rk == 3 ? I.wb : I.wa);

@@ -35,7 +35,7 @@ cudaError_t configure_ty() {
 }
 
 template <typename T, int TY>
-cudaError_t launch_ty(int stage, const BatchWave<T>* insts, const CUtensorMap* maps, const int2* tiles, int ntiles,
+cudaError_t launch_ty(int stage, const BatchWave<T>* insts, const CUtensorMap* maps, const BatchTile* tiles, int ntiles,
                       int rk, int* err, unsigned grid, cudaStream_t s) {
   switch (stage) {
     case ST_FIRST:
@@ -68,7 +68,7 @@ cudaError_t CAT(configure_wave_batch_o, SBP_ORDER)<float>(int ty) {
 
 template <>
 cudaError_t CAT(launch_wave_batch_o, SBP_ORDER)<double>(int stage, int ty, const BatchWave<double>* insts,
-                                                        const CUtensorMap* maps, const int2* tiles, int ntiles, int rk,
+                                                        const CUtensorMap* maps, const BatchTile* tiles, int ntiles, int rk,
                                                         int* err, unsigned grid, cudaStream_t s) {
   if (ty == 8) return launch_ty<double, 8>(stage, insts, maps, tiles, ntiles, rk, err, grid, s);
   if (ty == 16) return launch_ty<double, 16>(stage, insts, maps, tiles, ntiles, rk, err, grid, s);
@@ -76,7 +76,7 @@ cudaError_t CAT(launch_wave_batch_o, SBP_ORDER)<double>(int stage, int ty, const
 }
 template <>
 cudaError_t CAT(launch_wave_batch_o, SBP_ORDER)<float>(int stage, int ty, const BatchWave<float>* insts,
-                                                       const CUtensorMap* maps, const int2* tiles, int ntiles, int rk,
+                                                       const CUtensorMap* maps, const BatchTile* tiles, int ntiles, int rk,
                                                        int* err, unsigned grid, cudaStream_t s) {
   if (ty == 16) return launch_ty<float, 16>(stage, insts, maps, tiles, ntiles, rk, err, grid, s);
   if (ty == 32) return launch_ty<float, 32>(stage, insts, maps, tiles, ntiles, rk, err, grid, s);
@@ -84,7 +84,7 @@ cudaError_t CAT(launch_wave_batch_o, SBP_ORDER)<float>(int stage, int ty, const 
 }
 
 template <typename T>
-static cudaError_t adv_launch(int stage, const BatchLine<T>* insts, const int2* tiles, int ntiles, int rk,
+static cudaError_t adv_launch(int stage, const BatchLine<T>* insts, const BatchTile* tiles, int ntiles, int rk,
                               cudaStream_t s) {
   const dim3 block(kLineTileX, kLineTileY);
   switch (stage) {
@@ -97,12 +97,12 @@ static cudaError_t adv_launch(int stage, const BatchLine<T>* insts, const int2* 
 }
 
 template <>
-cudaError_t CAT(launch_adv_batch_o, SBP_ORDER)<double>(int stage, const BatchLine<double>* insts, const int2* tiles,
+cudaError_t CAT(launch_adv_batch_o, SBP_ORDER)<double>(int stage, const BatchLine<double>* insts, const BatchTile* tiles,
                                                        int ntiles, int rk, cudaStream_t s) {
   return adv_launch<double>(stage, insts, tiles, ntiles, rk, s);
 }
 template <>
-cudaError_t CAT(launch_adv_batch_o, SBP_ORDER)<float>(int stage, const BatchLine<float>* insts, const int2* tiles,
+cudaError_t CAT(launch_adv_batch_o, SBP_ORDER)<float>(int stage, const BatchLine<float>* insts, const BatchTile* tiles,
                                                       int ntiles, int rk, cudaStream_t s) {
   return adv_launch<float>(stage, insts, tiles, ntiles, rk, s);
 }
