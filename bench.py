@@ -133,14 +133,14 @@ def measured_peaks():
 
 
 def profiled_traffic(order: int, precision: str):
-    """DRAM bytes per launch of the stage kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", f"wave_stage_{precision}_o{order}_traffic.txt")
+    """DRAM bytes per point of one middle-stage launch, from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"wave_stage_{precision}_o{order}_4096.md")
     try:
         with open(path) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_point_stage:"):
-                    return float(line.split(":", 1)[1])
-    except OSError:
+                if line.startswith("| traffic_bytes_per_point_stage |"):
+                    return float(line.split("|")[2].split()[0])
+    except (OSError, ValueError, IndexError):
         pass
     return None
 
@@ -417,8 +417,12 @@ def main():
     achieved = bytes_per_launch / (kernel_ms * 1e-3) / 1e9
     peak, peak_src = measured_peaks()
     traffic_pp = profiled_traffic(order, args.precision)
+    mid_alg = (5 * 3 * es) * n * n  # algorithmic bytes of one middle-stage launch
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": (traffic_pp * n * n if traffic_pp else None), "peak_source": peak_src,
+                "traffic": (traffic_pp * n * n if traffic_pp else None),
+                "traffic_note": "DRAM bytes of one middle-stage (stage 2/3) launch from the committed ncu capture "
+                                "(2560^2, scaled by points); its algorithmic bytes: %d" % mid_alg,
+                "peak_source": peak_src,
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "kernel": "wave_stage_kernel (fused RHS + SAT + RK4 stage)", "avg_launch_ms": kernel_ms}
     if args.precision == "fp64":
