@@ -46,6 +46,7 @@ def units():
     out.append(("noalloc.o", "noalloc.cu", []))
     out.append(("petsc_io.o", "petsc_io.cpp", []))
     out.append(("batch_runtime.o", "batch_runtime.cpp", ["-x", "cu"]))
+    out.append(("cnn.o", "cnn.cu", []))
     return out
 
 

@@ -1,0 +1,665 @@
+// cnn.cu -- the learned correction: a 4-layer 3x3 convolutional network
+// (4 -> 32 -> 32 -> 32 -> 3 channels, ReLU between layers) trained and run on
+// the GPU by the kernels in this file. No counterpart in the reference.
+//
+// Tensors are NHWC. Activations and weights are BF16; every product is
+// accumulated in FP32 on the tensor cores (mma.sync m16n8k16, BF16 inputs,
+// FP32 accumulators); master weights, biases and Adam moments are FP32.
+// Channel counts are padded to multiples of 16 (the MMA K step): input 4 -> 16,
+// output 3 -> 16; the padding carries zeros.
+//
+//   conv3x3_fwd_kernel    implicit GEMM, M = pixels, N = output channels,
+//                         K = 9 taps x input channels; also computes the input
+//                         gradient (dgrad) with the spatially flipped,
+//                         transposed weights.
+//   conv3x3_wgrad_kernel  GEMM, M = output channels, N = input channels per
+//                         tap, K = pixels (split over CTAs, FP32 atomics).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/sbpgpu.h"
+
+namespace sbp {
+namespace cnn {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int kLayers = 4;
+constexpr int kCin[kLayers] = {16, 32, 32, 32};   // padded input channels
+constexpr int kCout[kLayers] = {32, 32, 32, 16};  // padded output channels
+constexpr int kInReal = 4, kOutReal = 3;
+
+__device__ __forceinline__ uint32_t ld_pair(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+__device__ __forceinline__ uint32_t pack_pair(bf16 lo, bf16 hi) {
+  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+// D += A * B, A 16x16 (row), B 16x8 (col), BF16 in, FP32 accumulate.
+__device__ __forceinline__ void mma_16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// y[p][n] = act(bias[n] + sum_{tap,c} x[p + off(tap)][c] * w[n][tap][c]), zero padding outside
+// the image. One warp computes 16 pixels x COUT channels; 4 warps per CTA.
+template <int CIN, int COUT, bool RELU, bool OUT_F32>
+__global__ void __launch_bounds__(128) conv3x3_fwd_kernel(const bf16* __restrict__ x, const bf16* __restrict__ w,
+                                                          const float* __restrict__ bias, void* __restrict__ y, int B,
+                                                          int H, int W) {
+  static_assert(CIN % 16 == 0 && COUT % 8 == 0, "channel padding");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const long long P = (long long)B * H * W;
+  const long long p0 = ((long long)blockIdx.x * 4 + warp) * 16;
+  if (p0 >= P) return;
+  long long pr[2];
+  int pb[2], ph[2], pw[2];
+  bool pv[2];
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    pr[r] = p0 + g + 8 * r;
+    pv[r] = pr[r] < P;
+    const long long q = pv[r] ? pr[r] : 0;
+    pw[r] = (int)(q % W);
+    ph[r] = (int)((q / W) % H);
+    pb[r] = (int)(q / ((long long)W * H));
+  }
+  float acc[COUT / 8][4];
+#pragma unroll
+  for (int nb = 0; nb < COUT / 8; nb++) acc[nb][0] = acc[nb][1] = acc[nb][2] = acc[nb][3] = 0.f;
+#pragma unroll 1
+  for (int tap = 0; tap < 9; tap++) {
+    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+    const bf16* src[2];
+    bool ok[2];
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      const int hh = ph[r] + dy, ww = pw[r] + dx;
+      ok[r] = pv[r] && hh >= 0 && hh < H && ww >= 0 && ww < W;
+      src[r] = x + (((long long)pb[r] * H + (ok[r] ? hh : 0)) * W + (ok[r] ? ww : 0)) * CIN;
+    }
+#pragma unroll
+    for (int c0 = 0; c0 < CIN; c0 += 16) {
+      uint32_t a[4];
+      a[0] = ok[0] ? ld_pair(src[0] + c0 + 2 * t) : 0u;
+      a[1] = ok[1] ? ld_pair(src[1] + c0 + 2 * t) : 0u;
+      a[2] = ok[0] ? ld_pair(src[0] + c0 + 8 + 2 * t) : 0u;
+      a[3] = ok[1] ? ld_pair(src[1] + c0 + 8 + 2 * t) : 0u;
+#pragma unroll
+      for (int nb = 0; nb < COUT / 8; nb++) {
+        const bf16* wp = w + ((long long)(nb * 8 + g) * 9 + tap) * CIN + c0;
+        const uint32_t b[2] = {ld_pair(wp + 2 * t), ld_pair(wp + 8 + 2 * t)};
+        mma_16816(acc[nb], a, b);
+      }
+    }
+  }
+#pragma unroll
+  for (int nb = 0; nb < COUT / 8; nb++) {
+    const int n = nb * 8 + 2 * t;
+    const float b0 = bias ? bias[n] : 0.f, b1 = bias ? bias[n + 1] : 0.f;
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      if (!pv[r]) continue;
+      float v0 = acc[nb][2 * r] + b0, v1 = acc[nb][2 * r + 1] + b1;
+      if (RELU) {
+        v0 = fmaxf(v0, 0.f);
+        v1 = fmaxf(v1, 0.f);
+      }
+      if (OUT_F32) {
+        float* yp = static_cast<float*>(y) + pr[r] * COUT + n;
+        yp[0] = v0;
+        yp[1] = v1;
+      } else {
+        bf16* yp = static_cast<bf16*>(y) + pr[r] * COUT + n;
+        *reinterpret_cast<uint32_t*>(yp) = pack_pair(__float2bfloat16(v0), __float2bfloat16(v1));
+      }
+    }
+  }
+}
+
+// dw[n][tap][c] += sum_p dy[p][n] * x[p + off(tap)][c]. Grid (pixel chunks, 9 taps); each warp
+// accumulates its pixel range in registers and adds its partial sums atomically.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) conv3x3_wgrad_kernel(const bf16* __restrict__ x, const bf16* __restrict__ dy,
+                                                            float* __restrict__ dw, int B, int H, int W,
+                                                            int pix_per_warp) {
+  static_assert(CIN % 8 == 0 && COUT % 16 == 0, "channel padding");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int tap = blockIdx.y, ddy = tap / 3 - 1, ddx = tap % 3 - 1;
+  const long long P = (long long)B * H * W;
+  const long long pbeg = ((long long)blockIdx.x * 4 + warp) * pix_per_warp;
+  if (pbeg >= P) return;
+  const long long pend = pbeg + pix_per_warp < P ? pbeg + pix_per_warp : P;
+  float acc[COUT / 16][CIN / 8][4];
+#pragma unroll
+  for (int mb = 0; mb < COUT / 16; mb++)
+#pragma unroll
+    for (int cb = 0; cb < CIN / 8; cb++) acc[mb][cb][0] = acc[mb][cb][1] = acc[mb][cb][2] = acc[mb][cb][3] = 0.f;
+  const bf16 zero = __float2bfloat16(0.f);
+  for (long long p0 = pbeg; p0 < pend; p0 += 16) {
+    // the four pixels this thread reads: k = 2t, 2t+1, 2t+8, 2t+9
+    const bf16* dyp[4];
+    const bf16* xp[4];
+    bool vy[4], vx[4];
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+      const long long p = p0 + 2 * t + (s & 1) + 8 * (s >> 1);
+      vy[s] = p < pend;
+      const long long q = vy[s] ? p : 0;
+      const int pw_ = (int)(q % W), ph_ = (int)((q / W) % H), pb_ = (int)(q / ((long long)W * H));
+      const int hh = ph_ + ddy, ww = pw_ + ddx;
+      vx[s] = vy[s] && hh >= 0 && hh < H && ww >= 0 && ww < W;
+      dyp[s] = dy + q * COUT;
+      xp[s] = x + (((long long)pb_ * H + (vx[s] ? hh : 0)) * W + (vx[s] ? ww : 0)) * CIN;
+    }
+#pragma unroll
+    for (int mb = 0; mb < COUT / 16; mb++) {
+      uint32_t a[4];
+      const int m0 = mb * 16 + g, m1 = m0 + 8;
+      a[0] = pack_pair(vy[0] ? dyp[0][m0] : zero, vy[1] ? dyp[1][m0] : zero);
+      a[1] = pack_pair(vy[0] ? dyp[0][m1] : zero, vy[1] ? dyp[1][m1] : zero);
+      a[2] = pack_pair(vy[2] ? dyp[2][m0] : zero, vy[3] ? dyp[3][m0] : zero);
+      a[3] = pack_pair(vy[2] ? dyp[2][m1] : zero, vy[3] ? dyp[3][m1] : zero);
+#pragma unroll
+      for (int cb = 0; cb < CIN / 8; cb++) {
+        const int c = cb * 8 + g;
+        const uint32_t b[2] = {pack_pair(vx[0] ? xp[0][c] : zero, vx[1] ? xp[1][c] : zero),
+                               pack_pair(vx[2] ? xp[2][c] : zero, vx[3] ? xp[3][c] : zero)};
+        mma_16816(acc[mb][cb], a, b);
+      }
+    }
+  }
+#pragma unroll
+  for (int mb = 0; mb < COUT / 16; mb++)
+#pragma unroll
+    for (int cb = 0; cb < CIN / 8; cb++)
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        const int n = mb * 16 + g + 8 * (e >> 1), c = cb * 8 + 2 * t + (e & 1);
+        atomicAdd(&dw[((long long)n * 9 + tap) * CIN + c], acc[mb][cb][e]);
+      }
+}
+
+// db[n] += sum_p dy[p][n]
+template <int COUT>
+__global__ void bias_grad_kernel(const bf16* __restrict__ dy, float* __restrict__ db, long long P) {
+  __shared__ float sh[COUT];
+  for (int n = threadIdx.x; n < COUT; n += blockDim.x) sh[n] = 0.f;
+  __syncthreads();
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < P * COUT; e += (long long)gridDim.x * blockDim.x)
+    atomicAdd(&sh[e % COUT], __bfloat162float(dy[e]));
+  __syncthreads();
+  for (int n = threadIdx.x; n < COUT; n += blockDim.x) atomicAdd(&db[n], sh[n]);
+}
+
+// d[e] = (y[e] > 0) ? d[e] : 0   (ReLU backward through the post-activation output y)
+__global__ void relu_back_kernel(bf16* __restrict__ d, const bf16* __restrict__ y, long long n) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+    if (!(__bfloat162float(y[e]) > 0.f)) d[e] = __float2bfloat16(0.f);
+}
+
+// wT[c][tap][n] = w[n][8 - tap][c]: the weights of the input-gradient convolution.
+__global__ void flip_weights_kernel(const bf16* __restrict__ w, bf16* __restrict__ wT, int cin, int cout) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= cin * 9 * cout) return;
+  const int n = e % cout, tap = (e / cout) % 9, c = e / (cout * 9);
+  wT[e] = w[((long long)n * 9 + (8 - tap)) * cin + c];
+}
+
+// x16[p][c] = c < 4 ? bf16(x[p][c]) : 0
+__global__ void pack_input_kernel(const float* __restrict__ x, bf16* __restrict__ x16, long long P) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < P * 16; e += (long long)gridDim.x * blockDim.x) {
+    const long long p = e / 16;
+    const int c = (int)(e % 16);
+    x16[e] = __float2bfloat16(c < kInReal ? x[p * kInReal + c] : 0.f);
+  }
+}
+
+// out3[p][c] = out16[p][c], c < 3
+__global__ void unpack_output_kernel(const float* __restrict__ out16, float* __restrict__ out3, long long P) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < P * kOutReal;
+       e += (long long)gridDim.x * blockDim.x)
+    out3[e] = out16[(e / kOutReal) * 16 + e % kOutReal];
+}
+
+// Mean squared error over the 3 real channels; gradient (bf16, 16 channels) and the loss sum.
+__global__ void mse_kernel(const float* __restrict__ out16, const float* __restrict__ target, bf16* __restrict__ d16,
+                           float* __restrict__ loss, long long P) {
+  __shared__ float sh[256];
+  float s = 0.f;
+  const float scale = 2.f / (float)(P * kOutReal);
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < P * 16; e += (long long)gridDim.x * blockDim.x) {
+    const long long p = e / 16;
+    const int c = (int)(e % 16);
+    float g = 0.f;
+    if (c < kOutReal) {
+      const float r = out16[e] - target[p * kOutReal + c];
+      s += r * r;
+      g = scale * r;
+    }
+    d16[e] = __float2bfloat16(g);
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(loss, sh[0]);
+}
+
+// Adam on FP32 master parameters; writes the BF16 copy used by the kernels.
+__global__ void adam_kernel(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v,
+                            const float* __restrict__ g, bf16* __restrict__ p16, int n, float lr, float b1, float b2,
+                            float eps, float c1, float c2) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const float gg = g[e];
+  const float mm = b1 * m[e] + (1.f - b1) * gg;
+  const float vv = b2 * v[e] + (1.f - b2) * gg * gg;
+  m[e] = mm;
+  v[e] = vv;
+  const float upd = lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+  p[e] -= upd;
+  if (p16) p16[e] = __float2bfloat16(p[e]);
+}
+
+__global__ void f32_to_bf16_kernel(const float* __restrict__ a, bf16* __restrict__ b, int n) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) b[e] = __float2bfloat16(a[e]);
+}
+
+// Features of a two-block wave state (AoS FP64 u, v, p) for the network:
+// x[p] = (u/s, v/s, p/s, log(rho)/log(4)) with the state scale s.
+__global__ void features_kernel(const double* __restrict__ state, const double* __restrict__ rho,
+                                float* __restrict__ x, long long P, double inv_scale) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
+    x[4 * p + 0] = (float)(state[3 * p + 0] * inv_scale);
+    x[4 * p + 1] = (float)(state[3 * p + 1] * inv_scale);
+    x[4 * p + 2] = (float)(state[3 * p + 2] * inv_scale);
+    x[4 * p + 3] = (float)(log(rho[p]) / log(4.0));
+  }
+}
+
+// state[p][c] += scale * delta[p][c] (AoS FP64 state, network output in units of `scale`)
+__global__ void correct_kernel(double* __restrict__ state, const float* __restrict__ delta, long long P, double scale) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < 3 * P; e += (long long)gridDim.x * blockDim.x)
+    state[e] += scale * (double)delta[e];
+}
+
+inline int blocks_for(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  return (int)(b > 4096 ? 4096 : (b < 1 ? 1 : b));
+}
+
+}  // namespace cnn
+}  // namespace sbp
+
+using namespace sbp::cnn;
+
+struct sbp_cnn {
+  int H = 0, W = 0, maxB = 0, device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  long long step = 0;
+  float* wm[kLayers] = {};   // FP32 master weights [cout][9][cin]
+  bf16* wb[kLayers] = {};    // BF16 copies
+  bf16* wT[kLayers] = {};    // flipped, transposed (input-gradient) weights
+  float* bias[kLayers] = {};
+  float *mw[kLayers] = {}, *vw[kLayers] = {}, *mbias[kLayers] = {}, *vbias[kLayers] = {};
+  float *gw[kLayers] = {}, *gb[kLayers] = {};
+  bf16* act[kLayers] = {};   // layer inputs: act[0] = packed input, act[l] = output of layer l-1
+  bf16* dact = nullptr;      // gradient buffers (two, ping-pong)
+  bf16* dact2 = nullptr;
+  float* out16 = nullptr;    // last layer output (FP32, 16 channels)
+  float* loss = nullptr;
+  long long launches = 0;
+  std::string msg;
+};
+
+namespace {
+
+thread_local std::string g_cnn_error;
+
+int cfail(sbp_cnn* c, int code, const std::string& m) {
+  if (c) c->msg = m;
+  else g_cnn_error = m;
+  return code;
+}
+
+#define CCK(call)                                                                        \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return cfail(c, SBP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+long long wcount(int l) { return (long long)kCout[l] * 9 * kCin[l]; }
+
+void cnn_release(sbp_cnn* c) {
+  for (int l = 0; l < kLayers; l++) {
+    void* ps[] = {c->wm[l], c->wb[l], c->wT[l], c->bias[l], c->mw[l], c->vw[l], c->mbias[l], c->vbias[l],
+                  c->gw[l], c->gb[l], c->act[l]};
+    for (void* p : ps)
+      if (p) cudaFree(p);
+  }
+  void* ps[] = {c->dact, c->dact2, c->out16, c->loss};
+  for (void* p : ps)
+    if (p) cudaFree(p);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+}
+
+// Launch one conv of layer l (forward) or its input-gradient conv.
+cudaError_t conv_fwd(int l, const bf16* x, void* y, const sbp_cnn* c, int batch, cudaStream_t s) {
+  const long long P = (long long)batch * c->H * c->W;
+  const int grid = (int)((P + 63) / 64);
+  switch (l) {
+    case 0: conv3x3_fwd_kernel<16, 32, true, false><<<grid, 128, 0, s>>>(x, c->wb[0], c->bias[0], y, batch, c->H, c->W); break;
+    case 1: conv3x3_fwd_kernel<32, 32, true, false><<<grid, 128, 0, s>>>(x, c->wb[1], c->bias[1], y, batch, c->H, c->W); break;
+    case 2: conv3x3_fwd_kernel<32, 32, true, false><<<grid, 128, 0, s>>>(x, c->wb[2], c->bias[2], y, batch, c->H, c->W); break;
+    default: conv3x3_fwd_kernel<32, 16, false, true><<<grid, 128, 0, s>>>(x, c->wb[3], c->bias[3], y, batch, c->H, c->W); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t conv_dgrad(int l, const bf16* dy, bf16* dx, const sbp_cnn* c, int batch, cudaStream_t s) {
+  const long long P = (long long)batch * c->H * c->W;
+  const int grid = (int)((P + 63) / 64);
+  if (l == 3)
+    conv3x3_fwd_kernel<16, 32, false, false><<<grid, 128, 0, s>>>(dy, c->wT[3], nullptr, dx, batch, c->H, c->W);
+  else
+    conv3x3_fwd_kernel<32, 32, false, false><<<grid, 128, 0, s>>>(dy, c->wT[l], nullptr, dx, batch, c->H, c->W);
+  return cudaGetLastError();
+}
+
+cudaError_t conv_wgrad(int l, const bf16* x, const bf16* dy, float* dw, const sbp_cnn* c, int batch, cudaStream_t s) {
+  const long long P = (long long)batch * c->H * c->W;
+  const int ppw = 1024;
+  const dim3 grid((unsigned)((P + 4LL * ppw - 1) / (4LL * ppw)), 9);
+  switch (l) {
+    case 0: conv3x3_wgrad_kernel<16, 32><<<grid, 128, 0, s>>>(x, dy, dw, batch, c->H, c->W, ppw); break;
+    case 1:
+    case 2: conv3x3_wgrad_kernel<32, 32><<<grid, 128, 0, s>>>(x, dy, dw, batch, c->H, c->W, ppw); break;
+    default: conv3x3_wgrad_kernel<32, 16><<<grid, 128, 0, s>>>(x, dy, dw, batch, c->H, c->W, ppw); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t bias_grad(int l, const bf16* dy, float* db, int batch, const sbp_cnn* c, cudaStream_t s) {
+  const long long P = (long long)batch * c->H * c->W;
+  if (kCout[l] == 32)
+    bias_grad_kernel<32><<<blocks_for(P * 32, 256), 256, 0, s>>>(dy, db, P);
+  else
+    bias_grad_kernel<16><<<blocks_for(P * 16, 256), 256, 0, s>>>(dy, db, P);
+  return cudaGetLastError();
+}
+
+int refresh_weights(sbp_cnn* c) {
+  for (int l = 0; l < kLayers; l++) {
+    const int n = (int)wcount(l);
+    f32_to_bf16_kernel<<<(n + 255) / 256, 256, 0, c->stream>>>(c->wm[l], c->wb[l], n);
+    flip_weights_kernel<<<(n + 255) / 256, 256, 0, c->stream>>>(c->wb[l], c->wT[l], kCin[l], kCout[l]);
+    c->launches += 2;
+  }
+  CCK(cudaGetLastError());
+  return SBP_OK;
+}
+
+int run_forward(sbp_cnn* c, const float* x, int batch) {
+  const long long P = (long long)batch * c->H * c->W;
+  pack_input_kernel<<<blocks_for(P * 16, 256), 256, 0, c->stream>>>(x, c->act[0], P);
+  c->launches++;
+  for (int l = 0; l < kLayers; l++) {
+    void* y = (l == kLayers - 1) ? (void*)c->out16 : (void*)c->act[l + 1];
+    CCK(conv_fwd(l, c->act[l], y, c, batch, c->stream));
+    c->launches++;
+  }
+  return SBP_OK;
+}
+
+// Masks that keep padded channels of parameters at zero (never trained).
+bool weight_is_real(int l, long long e) {
+  const int cin = kCin[l];
+  const int ci = (int)(e % cin);
+  const int n = (int)(e / (9LL * cin));
+  if (l == 0 && ci >= kInReal) return false;
+  if (l == kLayers - 1 && n >= kOutReal) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sbp_cnn_create(int height, int width, int max_batch, int device, void* stream, sbp_cnn** out) {
+  if (!out || height < 1 || width < 1 || max_batch < 1) return cfail(nullptr, SBP_ERR_INVALID, "bad network size");
+  *out = nullptr;
+  sbp_cnn* c = new sbp_cnn();
+  c->H = height;
+  c->W = width;
+  c->maxB = max_batch;
+  c->device = device;
+  auto bad = [&](const std::string& m) {
+    g_cnn_error = m;
+    cnn_release(c);
+    delete c;
+    return SBP_ERR_CUDA;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return bad("cudaSetDevice failed");
+  if (stream) {
+    c->stream = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bad("stream");
+    c->own_stream = true;
+  }
+  const long long P = (long long)max_batch * height * width;
+  for (int l = 0; l < kLayers; l++) {
+    const size_t nw = (size_t)wcount(l), nb = (size_t)kCout[l];
+    if (cudaMalloc(&c->wm[l], nw * 4) || cudaMalloc(&c->wb[l], nw * 2) || cudaMalloc(&c->wT[l], nw * 2) ||
+        cudaMalloc(&c->bias[l], nb * 4) || cudaMalloc(&c->mw[l], nw * 4) || cudaMalloc(&c->vw[l], nw * 4) ||
+        cudaMalloc(&c->mbias[l], nb * 4) || cudaMalloc(&c->vbias[l], nb * 4) || cudaMalloc(&c->gw[l], nw * 4) ||
+        cudaMalloc(&c->gb[l], nb * 4) || cudaMalloc(&c->act[l], (size_t)P * kCin[l] * 2))
+      return bad("cudaMalloc(network)");
+    cudaMemset(c->mw[l], 0, nw * 4);
+    cudaMemset(c->vw[l], 0, nw * 4);
+    cudaMemset(c->mbias[l], 0, nb * 4);
+    cudaMemset(c->vbias[l], 0, nb * 4);
+  }
+  if (cudaMalloc(&c->dact, (size_t)P * 32 * 2) || cudaMalloc(&c->dact2, (size_t)P * 32 * 2) ||
+      cudaMalloc(&c->out16, (size_t)P * 16 * 4) || cudaMalloc(&c->loss, 4))
+    return bad("cudaMalloc(activations)");
+  *out = c;
+  return sbp_cnn_init(c, 1234);
+}
+
+int sbp_cnn_destroy(sbp_cnn* c) {
+  if (!c) return SBP_ERR_INVALID;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  cnn_release(c);
+  delete c;
+  return SBP_OK;
+}
+
+const char* sbp_cnn_last_error(const sbp_cnn* c) { return c ? c->msg.c_str() : g_cnn_error.c_str(); }
+
+long long sbp_cnn_param_count(void) {
+  long long n = 0;
+  for (int l = 0; l < kLayers; l++) n += wcount(l) + kCout[l];
+  return n;
+}
+
+int sbp_cnn_init(sbp_cnn* c, unsigned long long seed) {
+  if (!c) return SBP_ERR_INVALID;
+  CCK(cudaSetDevice(c->device));
+  std::mt19937_64 rng(seed);
+  for (int l = 0; l < kLayers; l++) {
+    const long long n = wcount(l);
+    const int fan_in = 9 * (l == 0 ? kInReal : kCin[l]);
+    std::normal_distribution<double> nd(0.0, std::sqrt(2.0 / fan_in) * (l == kLayers - 1 ? 0.1 : 1.0));
+    std::vector<float> w(n);
+    for (long long e = 0; e < n; e++) w[e] = weight_is_real(l, e) ? (float)nd(rng) : 0.f;
+    std::vector<float> b(kCout[l], 0.f);
+    CCK(cudaMemcpyAsync(c->wm[l], w.data(), n * 4, cudaMemcpyHostToDevice, c->stream));
+    CCK(cudaMemcpyAsync(c->bias[l], b.data(), b.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    CCK(cudaMemsetAsync(c->mw[l], 0, n * 4, c->stream));
+    CCK(cudaMemsetAsync(c->vw[l], 0, n * 4, c->stream));
+    CCK(cudaMemsetAsync(c->mbias[l], 0, kCout[l] * 4, c->stream));
+    CCK(cudaMemsetAsync(c->vbias[l], 0, kCout[l] * 4, c->stream));
+  }
+  c->step = 0;
+  int rc = refresh_weights(c);
+  if (rc) return rc;
+  CCK(cudaStreamSynchronize(c->stream));
+  return SBP_OK;
+}
+
+// Parameters as one FP32 vector: per layer, weights [cout][9][cin] then bias [cout].
+int sbp_cnn_get_params(sbp_cnn* c, float* host, long long n) {
+  if (!c || !host || n != sbp_cnn_param_count()) return SBP_ERR_INVALID;
+  CCK(cudaSetDevice(c->device));
+  long long o = 0;
+  for (int l = 0; l < kLayers; l++) {
+    CCK(cudaMemcpyAsync(host + o, c->wm[l], wcount(l) * 4, cudaMemcpyDeviceToHost, c->stream));
+    o += wcount(l);
+    CCK(cudaMemcpyAsync(host + o, c->bias[l], kCout[l] * 4, cudaMemcpyDeviceToHost, c->stream));
+    o += kCout[l];
+  }
+  CCK(cudaStreamSynchronize(c->stream));
+  return SBP_OK;
+}
+
+int sbp_cnn_set_params(sbp_cnn* c, const float* host, long long n) {
+  if (!c || !host || n != sbp_cnn_param_count()) return SBP_ERR_INVALID;
+  CCK(cudaSetDevice(c->device));
+  long long o = 0;
+  for (int l = 0; l < kLayers; l++) {
+    CCK(cudaMemcpyAsync(c->wm[l], host + o, wcount(l) * 4, cudaMemcpyHostToDevice, c->stream));
+    o += wcount(l);
+    CCK(cudaMemcpyAsync(c->bias[l], host + o, kCout[l] * 4, cudaMemcpyHostToDevice, c->stream));
+    o += kCout[l];
+  }
+  int rc = refresh_weights(c);
+  if (rc) return rc;
+  CCK(cudaStreamSynchronize(c->stream));
+  return SBP_OK;
+}
+
+// out = network(x): x, out device arrays, NHWC FP32, 4 and 3 channels.
+int sbp_cnn_forward(sbp_cnn* c, const float* x, int batch, float* out) {
+  if (!c || !x || !out || batch < 1 || batch > c->maxB) return SBP_ERR_INVALID;
+  CCK(cudaSetDevice(c->device));
+  int rc = run_forward(c, x, batch);
+  if (rc) return rc;
+  const long long P = (long long)batch * c->H * c->W;
+  unpack_output_kernel<<<blocks_for(P * 3, 256), 256, 0, c->stream>>>(c->out16, out, P);
+  c->launches++;
+  CCK(cudaStreamSynchronize(c->stream));
+  return SBP_OK;
+}
+
+// Gradients of the mean squared error of network(x) against target (both device, NHWC FP32,
+// 4 and 3 channels), without updating the parameters; written as one FP32 vector in the
+// layout of sbp_cnn_get_params (host `grad`, may be NULL). Returns the loss in *loss.
+static int backward(sbp_cnn* c, const float* x, const float* target, int batch, float* loss) {
+  const long long P = (long long)batch * c->H * c->W;
+  int rc = run_forward(c, x, batch);
+  if (rc) return rc;
+  CCK(cudaMemsetAsync(c->loss, 0, 4, c->stream));
+  mse_kernel<<<blocks_for(P * 16, 256), 256, 0, c->stream>>>(c->out16, target, c->dact, c->loss, P);
+  c->launches++;
+  for (int l = 0; l < kLayers; l++) {
+    CCK(cudaMemsetAsync(c->gw[l], 0, wcount(l) * 4, c->stream));
+    CCK(cudaMemsetAsync(c->gb[l], 0, kCout[l] * 4, c->stream));
+  }
+  bf16* dcur = c->dact;   // gradient w.r.t. the output of layer l (pre-activation once masked)
+  bf16* dnext = c->dact2;
+  for (int l = kLayers - 1; l >= 0; l--) {
+    CCK(conv_wgrad(l, c->act[l], dcur, c->gw[l], c, batch, c->stream));
+    CCK(bias_grad(l, dcur, c->gb[l], batch, c, c->stream));
+    c->launches += 2;
+    if (l == 0) break;
+    CCK(conv_dgrad(l, dcur, dnext, c, batch, c->stream));
+    relu_back_kernel<<<blocks_for(P * kCin[l], 256), 256, 0, c->stream>>>(dnext, c->act[l], P * kCin[l]);
+    c->launches += 2;
+    bf16* tmp = dcur;
+    dcur = dnext;
+    dnext = tmp;
+  }
+  float h = 0;
+  CCK(cudaMemcpyAsync(&h, c->loss, 4, cudaMemcpyDeviceToHost, c->stream));
+  CCK(cudaStreamSynchronize(c->stream));
+  if (loss) *loss = h / (float)(P * kOutReal);
+  return SBP_OK;
+}
+
+int sbp_cnn_gradients(sbp_cnn* c, const float* x, const float* target, int batch, float* grad, long long n,
+                      float* loss) {
+  if (!c || !x || !target || batch < 1 || batch > c->maxB) return SBP_ERR_INVALID;
+  if (grad && n != sbp_cnn_param_count()) return SBP_ERR_INVALID;
+  CCK(cudaSetDevice(c->device));
+  int rc = backward(c, x, target, batch, loss);
+  if (rc || !grad) return rc;
+  long long o = 0;
+  for (int l = 0; l < kLayers; l++) {
+    CCK(cudaMemcpyAsync(grad + o, c->gw[l], wcount(l) * 4, cudaMemcpyDeviceToHost, c->stream));
+    o += wcount(l);
+    CCK(cudaMemcpyAsync(grad + o, c->gb[l], kCout[l] * 4, cudaMemcpyDeviceToHost, c->stream));
+    o += kCout[l];
+  }
+  CCK(cudaStreamSynchronize(c->stream));
+  return SBP_OK;
+}
+
+// One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the mean squared error.
+int sbp_cnn_train_step(sbp_cnn* c, const float* x, const float* target, int batch, float lr, float* loss) {
+  if (!c || !x || !target || batch < 1 || batch > c->maxB || !(lr > 0)) return SBP_ERR_INVALID;
+  CCK(cudaSetDevice(c->device));
+  int rc = backward(c, x, target, batch, loss);
+  if (rc) return rc;
+  c->step++;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, (float)c->step), c2 = 1.f - std::pow(b2, (float)c->step);
+  for (int l = 0; l < kLayers; l++) {
+    const int n = (int)wcount(l);
+    adam_kernel<<<(n + 255) / 256, 256, 0, c->stream>>>(c->wm[l], c->mw[l], c->vw[l], c->gw[l], nullptr, n, lr, b1, b2,
+                                                        1e-8f, c1, c2);
+    adam_kernel<<<1, 256, 0, c->stream>>>(c->bias[l], c->mbias[l], c->vbias[l], c->gb[l], nullptr, kCout[l], lr, b1,
+                                          b2, 1e-8f, c1, c2);
+    c->launches += 2;
+  }
+  // padded channels stay zero: their gradients are zero (zero inputs / zero targets) and
+  // Adam leaves zero-gradient entries unchanged.
+  rc = refresh_weights(c);
+  if (rc) return rc;
+  CCK(cudaStreamSynchronize(c->stream));
+  return SBP_OK;
+}
+
+int sbp_cnn_features(const double* state, const double* rho, long long npts, double inv_scale, float* x,
+                     void* stream) {
+  if (!state || !rho || !x || npts < 1) return SBP_ERR_INVALID;
+  features_kernel<<<blocks_for(npts, 256), 256, 0, (cudaStream_t)stream>>>(state, rho, x, npts, inv_scale);
+  return cudaGetLastError() == cudaSuccess ? SBP_OK : SBP_ERR_CUDA;
+}
+
+int sbp_cnn_correct(double* state, const float* delta, long long npts, double scale, void* stream) {
+  if (!state || !delta || npts < 1) return SBP_ERR_INVALID;
+  correct_kernel<<<blocks_for(3 * npts, 256), 256, 0, (cudaStream_t)stream>>>(state, delta, npts, scale);
+  return cudaGetLastError() == cudaSuccess ? SBP_OK : SBP_ERR_CUDA;
+}
+
+long long sbp_cnn_launch_count(const sbp_cnn* c) { return c ? c->launches : SBP_ERR_INVALID; }
+
+}  // extern "C"

@@ -37,7 +37,10 @@ EXPORTS = ("sbp_create", "sbp_destroy", "sbp_last_error", "sbp_dofs", "sbp_rhs",
            "sbp_wave_rhs_noalloc", "sbp_write_petsc_vec", "sbp_read_petsc_vec",
            "sbp_batch_create", "sbp_batch_destroy", "sbp_batch_last_error", "sbp_batch_set_state",
            "sbp_batch_get_state", "sbp_batch_rk4_resident", "sbp_batch_synchronize", "sbp_batch_autotune",
-           "sbp_batch_tile_height", "sbp_batch_get_stream", "sbp_batch_points", "sbp_batch_launch_count")
+           "sbp_batch_tile_height", "sbp_batch_get_stream", "sbp_batch_points", "sbp_batch_launch_count",
+           "sbp_cnn_create", "sbp_cnn_destroy", "sbp_cnn_last_error", "sbp_cnn_param_count", "sbp_cnn_init",
+           "sbp_cnn_get_params", "sbp_cnn_set_params", "sbp_cnn_forward", "sbp_cnn_gradients", "sbp_cnn_train_step",
+           "sbp_cnn_features", "sbp_cnn_correct", "sbp_cnn_launch_count")
 
 _dp = C.POINTER(C.c_double)
 
@@ -115,6 +118,22 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.sbp_batch_points.restype = C.c_longlong
     L.sbp_batch_launch_count.argtypes = [P]
     L.sbp_batch_launch_count.restype = C.c_longlong
+    L.sbp_cnn_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(P)]
+    L.sbp_cnn_destroy.argtypes = [P]
+    L.sbp_cnn_last_error.argtypes = [P]
+    L.sbp_cnn_last_error.restype = C.c_char_p
+    L.sbp_cnn_param_count.restype = C.c_longlong
+    L.sbp_cnn_init.argtypes = [P, C.c_ulonglong]
+    L.sbp_cnn_get_params.argtypes = [P, C.c_void_p, C.c_longlong]
+    L.sbp_cnn_set_params.argtypes = [P, C.c_void_p, C.c_longlong]
+    L.sbp_cnn_forward.argtypes = [P, C.c_void_p, C.c_int, C.c_void_p]
+    L.sbp_cnn_gradients.argtypes = [P, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_longlong,
+                                    C.POINTER(C.c_float)]
+    L.sbp_cnn_train_step.argtypes = [P, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.POINTER(C.c_float)]
+    L.sbp_cnn_features.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong, C.c_double, C.c_void_p, C.c_void_p]
+    L.sbp_cnn_correct.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong, C.c_double, C.c_void_p]
+    L.sbp_cnn_launch_count.argtypes = [P]
+    L.sbp_cnn_launch_count.restype = C.c_longlong
     L.sbp_write_petsc_vec.argtypes = [C.c_char_p, C.c_void_p, C.c_longlong]
     L.sbp_read_petsc_vec.argtypes = [C.c_char_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     _lib = L
@@ -383,3 +402,86 @@ class Batch:
         s = C.c_void_p()
         self._check(self._L.sbp_batch_get_stream(self._h, C.byref(s)))
         return s.value or 0
+
+
+class Cnn:
+    """The learned-correction network (sbp_cnn_*). Device arrays are passed by address
+    (e.g. torch CUDA tensors' data_ptr()): features NHWC FP32 with 4 channels, outputs 3."""
+
+    def __init__(self, height: int, width: int, max_batch: int, *, device: int = 0, stream: int | None = None,
+                 seed: int = 1234):
+        L = load()
+        self._L = L
+        self.height, self.width, self.max_batch = height, width, max_batch
+        h = C.c_void_p()
+        rc = L.sbp_cnn_create(height, width, max_batch, device, stream, C.byref(h))
+        if rc:
+            raise SbpError(rc, L.sbp_cnn_last_error(None).decode())
+        self._h = h
+        if seed != 1234:
+            self._check(L.sbp_cnn_init(h, seed))
+
+    def _check(self, rc):
+        if rc:
+            raise SbpError(rc, self._L.sbp_cnn_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.sbp_cnn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @staticmethod
+    def param_count() -> int:
+        return load().sbp_cnn_param_count()
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.param_count(), dtype=np.float32)
+        self._check(self._L.sbp_cnn_get_params(self._h, out.ctypes.data, out.size))
+        return out
+
+    def set_params(self, v: np.ndarray):
+        v = np.ascontiguousarray(v, dtype=np.float32)
+        self._check(self._L.sbp_cnn_set_params(self._h, v.ctypes.data, v.size))
+
+    def forward(self, x_ptr: int, batch: int, out_ptr: int):
+        self._check(self._L.sbp_cnn_forward(self._h, x_ptr, batch, out_ptr))
+
+    def gradients(self, x_ptr: int, target_ptr: int, batch: int):
+        g = np.empty(self.param_count(), dtype=np.float32)
+        loss = C.c_float()
+        self._check(self._L.sbp_cnn_gradients(self._h, x_ptr, target_ptr, batch, g.ctypes.data, g.size,
+                                              C.byref(loss)))
+        return loss.value, g
+
+    def train_step(self, x_ptr: int, target_ptr: int, batch: int, lr: float) -> float:
+        loss = C.c_float()
+        self._check(self._L.sbp_cnn_train_step(self._h, x_ptr, target_ptr, batch, lr, C.byref(loss)))
+        return loss.value
+
+    @property
+    def launches(self) -> int:
+        return self._L.sbp_cnn_launch_count(self._h)
+
+
+def cnn_features(state_ptr: int, rho_ptr: int, npts: int, inv_scale: float, x_ptr: int, stream: int | None = None):
+    rc = load().sbp_cnn_features(state_ptr, rho_ptr, npts, inv_scale, x_ptr, stream)
+    if rc:
+        raise SbpError(rc, "sbp_cnn_features failed")
+
+
+def cnn_correct(state_ptr: int, delta_ptr: int, npts: int, scale: float, stream: int | None = None):
+    rc = load().sbp_cnn_correct(state_ptr, delta_ptr, npts, scale, stream)
+    if rc:
+        raise SbpError(rc, "sbp_cnn_correct failed")

@@ -183,6 +183,37 @@ int sbp_batch_get_stream(const sbp_batch* batch, void** stream);
 long long sbp_batch_points(const sbp_batch* batch);       /* grid points over all instances */
 long long sbp_batch_launch_count(const sbp_batch* batch); /* kernels launched so far */
 
+/* ---------------------------------------------------------------- learned correction
+ * A 4-layer 3x3 convolutional network (4 -> 32 -> 32 -> 32 -> 3 channels,
+ * ReLU) that corrects a coarse solve; no counterpart in the reference.
+ * Inputs and outputs are device arrays, NHWC FP32 (features: u, v, p scaled,
+ * log(rho)/log(4); outputs: corrections of u, v, p in the same scale).
+ * Inside: BF16 activations and weights, FP32 accumulation on the tensor
+ * cores, FP32 master weights, Adam. Parameters as one FP32 vector: per layer
+ * the weights [cout][9][cin] (channels padded: layer 1 cin 16 of which 4
+ * real, layer 4 cout 16 of which 3 real) then the bias [cout]. */
+typedef struct sbp_cnn sbp_cnn;
+int sbp_cnn_create(int height, int width, int max_batch, int device, void* stream, sbp_cnn** cnn);
+int sbp_cnn_destroy(sbp_cnn* cnn);
+const char* sbp_cnn_last_error(const sbp_cnn* cnn); /* NULL: last failed sbp_cnn_create */
+long long sbp_cnn_param_count(void);
+int sbp_cnn_init(sbp_cnn* cnn, unsigned long long seed);
+int sbp_cnn_get_params(sbp_cnn* cnn, float* host, long long n);
+int sbp_cnn_set_params(sbp_cnn* cnn, const float* host, long long n);
+int sbp_cnn_forward(sbp_cnn* cnn, const float* x, int batch, float* out);
+/* Gradients of the mean squared error (host vector in the parameter layout, may be NULL). */
+int sbp_cnn_gradients(sbp_cnn* cnn, const float* x, const float* target, int batch, float* grad, long long n,
+                      float* loss);
+/* One Adam step (beta 0.9 / 0.999) on the mean squared error of a batch. */
+int sbp_cnn_train_step(sbp_cnn* cnn, const float* x, const float* target, int batch, float lr, float* loss);
+/* Device helpers of the corrected solve: features of an AoS FP64 wave state
+ * (x[p] = u/s, v/s, p/s, log(rho)/log(4) with inv_scale = 1/s), and
+ * state += scale * delta. */
+int sbp_cnn_features(const double* state, const double* rho, long long npts, double inv_scale, float* x,
+                     void* stream);
+int sbp_cnn_correct(double* state, const float* delta, long long npts, double scale, void* stream);
+long long sbp_cnn_launch_count(const sbp_cnn* cnn);
+
 /* PETSc binary Vec files (host-side I/O): the format VecView writes on a
  * binary viewer, as the reference's write_vector_to_binary does
  * (code/src/util/io_util.cpp:4-14): big-endian int32 classid 1211214,
