@@ -56,11 +56,13 @@ def parse():
     ap.add_argument("--bc", default="characteristic", choices=["characteristic", "free_surface"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--study", default=None, choices=["precision", "batched"],
+    ap.add_argument("--study", default=None, choices=["precision", "batched", "learned"],
                     help="precision: variable rho, K (seeded Fourier fields) to --t-end in FP64 and in "
                          "compensated FP32; prints errors of FP32 against FP64 and both wall times. "
                          "batched: 512 uneven wave/advection instances in one batch, FP64 and FP32")
     ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--trajectories", type=int, default=2000, help="learned: training trajectories")
+    ap.add_argument("--epochs", type=int, default=3, help="learned: training epochs")
     ap.add_argument("--t-end", type=float, default=1.0)
     return ap.parse_args()
 
@@ -326,8 +328,48 @@ def run_batched_study(args):
     print(json.dumps(out), flush=True)
 
 
+def run_learned_study(args):
+    """Two-layer problem (rho, K x4 across y = 0): coarse 257 x 2*129 order-4 solve corrected by the
+    network every 4 steps, trained on restricted fine (1025 x 2*513, FP64) trajectories with seeded
+    pulse position U[-0.5,0.5]^2, width U[0.02,0.1], amplitude U[0.5,2] (seeds 1000..), two windows
+    per trajectory; judged against the fine solve on 100 held-out trajectories (seeds 5000..5099)."""
+    import numpy as np
+    import torch
+
+    import build as gpu_build
+    import learned
+    import sbpgpu
+
+    gpu_build.build()
+    s = learned.Setup()
+    sv = learned.Solvers(s)
+    t0 = time.perf_counter()
+    X, Y, scale = learned.make_dataset(sv, range(1000, 1000 + args.trajectories), windows=2)
+    t_data = time.perf_counter() - t0
+    with sbpgpu.Cnn(2 * s.nbc, s.nxc, 8) as net:
+        t0 = time.perf_counter()
+        losses = learned.train(net, X, Y, epochs=args.epochs, batch=8, lr=1e-3)
+        torch.cuda.synchronize()
+        t_train = time.perf_counter() - t0
+        del X, Y
+        solver = learned.LearnedSolver(sv, net, scale)
+        res = learned.evaluate(sv, solver, range(5000, 5100), windows=16)
+    out = {"study": "learned", "coarse_grid": [s.nxc, 2 * s.nbc], "fine_grid": [s.nxf, 2 * s.nbf],
+           "params": sbpgpu.Cnn.param_count(), "training_samples": 2 * args.trajectories, "epochs": args.epochs,
+           "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-20:])),
+           "seconds_data": t_data, "seconds_train": t_train,
+           "eval_windows": 16, "eval_t_end": 16 * s.window * s.dtc,
+           "rel_l2_coarse": float(np.mean(res["coarse"])), "rel_l2_learned": float(np.mean(res["learned"])),
+           "seconds_fine": res["t_fine"], "seconds_coarse": res["t_coarse"], "seconds_learned": res["t_learned"],
+           "fallbacks": solver.fallbacks, "held_out": 100}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.study == "learned":
+        run_learned_study(args)
+        return
     if args.study == "precision":
         run_precision_study(args)
         return

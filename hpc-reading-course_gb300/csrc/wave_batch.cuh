@@ -128,7 +128,8 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
   }
 }
 
-// Batched 2D advection: one CTA of 32 x 8 threads per (instance, tile) pair.
+// Batched 2D advection: one CTA of 32 x 8 threads per 32 x 32 (instance, tile)
+// pair, 4 rows per thread; the instance block is staged in shared memory once.
 template <typename T> struct alignas(16) BatchLine {
   LineParams<T> prm;  // geometry, taps, SAT factors, un/acc/comp pointers
   T* wa;
@@ -136,22 +137,34 @@ template <typename T> struct alignas(16) BatchLine {
   double dt;
 };
 
-constexpr int kLineTileX = 32, kLineTileY = 8;
+constexpr int kLineTileX = 32, kLineTileY = 32, kLineThreadsY = 8;
 
 template <typename T, int ORD, int STAGE>
-__global__ void __launch_bounds__(kLineTileX * kLineTileY)
+__global__ void __launch_bounds__(kLineTileX * kLineThreadsY)
     adv_batch_stage_kernel(const BatchLine<T>* __restrict__ insts, const BatchTile* __restrict__ tiles, int rk) {
+  __shared__ __align__(16) unsigned char blk[sizeof(BatchLine<T>)];
   const BatchTile tt = tiles[blockIdx.x];
-  const BatchLine<T>& I = insts[tt.slot];
-  const int i = tt.i0 + threadIdx.x;
-  const int j = tt.j0 + threadIdx.y;
-  if (i >= I.prm.nx || j >= I.prm.ny) return;
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(&insts[tt.slot]);
+    uint4* dst = reinterpret_cast<uint4*>(blk);
+    for (int k = threadIdx.y * kLineTileX + threadIdx.x; k < (int)(sizeof(BatchLine<T>) / 16);
+         k += kLineTileX * kLineThreadsY)
+      dst[k] = src[k];
+  }
+  __syncthreads();
+  const BatchLine<T>& I = *reinterpret_cast<const BatchLine<T>*>(blk);
   const double dt = I.dt;
   const T* in = rk == 1 ? I.prm.un : (rk == 3 ? I.wb : I.wa);
   T* wout = (rk == 1 || rk == 3) ? I.wa : I.wb;
   const T c_acc = (T)((rk == 1 || rk == 4) ? dt / 6 : dt / 3);
   const T c_w = (T)(rk == 3 ? dt : 0.5 * dt);
-  line_point<T, ORD, LK_ADV2D, STAGE>(I.prm, in, wout, c_acc, c_w, i, j);
+  const int i = tt.i0 + threadIdx.x;
+  if (i >= I.prm.nx) return;
+#pragma unroll
+  for (int r = 0; r < kLineTileY / kLineThreadsY; r++) {
+    const int j = tt.j0 + threadIdx.y + kLineThreadsY * r;
+    if (j < I.prm.ny) line_point<T, ORD, LK_ADV2D, STAGE>(I.prm, in, wout, c_acc, c_w, i, j);
+  }
 }
 
 }  // namespace sbp

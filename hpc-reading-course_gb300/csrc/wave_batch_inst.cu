@@ -86,7 +86,7 @@ cudaError_t CAT(launch_wave_batch_o, SBP_ORDER)<float>(int stage, int ty, const 
 template <typename T>
 static cudaError_t adv_launch(int stage, const BatchLine<T>* insts, const BatchTile* tiles, int ntiles, int rk,
                               cudaStream_t s) {
-  const dim3 block(kLineTileX, kLineTileY);
+  const dim3 block(kLineTileX, kLineThreadsY);
   switch (stage) {
     case ST_FIRST: adv_batch_stage_kernel<T, SBP_ORDER, ST_FIRST><<<ntiles, block, 0, s>>>(insts, tiles, rk); break;
     case ST_MID: adv_batch_stage_kernel<T, SBP_ORDER, ST_MID><<<ntiles, block, 0, s>>>(insts, tiles, rk); break;

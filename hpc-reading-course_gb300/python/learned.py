@@ -1,0 +1,236 @@
+"""Learned correction of a coarse two-layer wave solve.
+
+The problem: the two-block acoustic wave system (libsbpgpu's SBP_WAVE_2BLOCK_2D)
+with rho = K = 1 below y = 0 and rho = K = 4 above (impedance ratio 4, equal
+speeds), characteristic SAT on the outer boundary, energy-conserving interface
+SAT, SBP order 4. A fine grid (nx_f = 4 (nx_c - 1) + 1 points per row, the same
+in y per block) is nested in a 4x coarser one, so restriction is injection.
+
+Every `window` coarse RK4 steps (4 by default) the network (libsbpgpu's
+sbp_cnn_*, BF16 tensor-core convolutions) maps the coarse state to a
+correction towards the restricted fine solution. A correction that raises
+the coarse state's H-norm by more than `guard` (relative) is rejected: that
+window is recomputed by the fine solver from the interpolated coarse state and
+restricted back (the fallback). The fine solve is also the judge: errors are
+measured against the restricted fine solution.
+
+Device memory and small glue operations (restriction by slicing, bilinear
+prolongation for the fallback, target differences) use torch on the GPU; the
+solves and the network run in libsbpgpu.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+import sbpgpu
+
+
+@dataclass
+class Setup:
+    nxc: int = 257          # coarse points per row
+    nbc: int = 129          # coarse points per block column (2 blocks)
+    order: int = 4
+    ratio: float = 4.0      # rho and K above y = 0 (1 below)
+    cfl: float = 0.2
+    window: int = 4         # coarse steps between corrections
+
+    @property
+    def nxf(self):
+        return 4 * (self.nxc - 1) + 1
+
+    @property
+    def nbf(self):
+        return 4 * (self.nbc - 1) + 1
+
+    @property
+    def hc(self):
+        return 2.0 / (self.nxc - 1)
+
+    @property
+    def hf(self):
+        return 2.0 / (self.nxf - 1)
+
+    @property
+    def dtc(self):
+        return self.cfl * min(self.hc, 1.0 / (self.nbc - 1))
+
+    @property
+    def dtf(self):
+        return self.dtc / 4
+
+
+def two_layer_fields(nx: int, nb: int, ratio: float):
+    rho = np.ones((2 * nb, nx))
+    rho[nb:] = ratio
+    return rho.ravel(), rho.ravel().copy()
+
+
+def pulse_state(nx: int, nb: int, x0: float, y0: float, width: float, amp: float):
+    """Gaussian pressure pulse on the two-block grid (AoS u, v, p; the interface line in both blocks)."""
+    x = np.linspace(-1, 1, nx)
+    y = np.concatenate([np.linspace(-1, 0, nb), np.linspace(0, 1, nb)])
+    v = np.zeros((2 * nb, nx, 3))
+    v[:, :, 2] = amp * np.exp(-((x[None, :] - x0) ** 2 + (y[:, None] - y0) ** 2) / width**2)
+    return v.ravel()
+
+
+def trajectory_params(seed: int):
+    """Pulse position U[-0.5, 0.5]^2, width U[0.02, 0.1], amplitude U[0.5, 2] from `seed`."""
+    rng = np.random.default_rng(seed)
+    x0, y0 = rng.uniform(-0.5, 0.5, 2)
+    return float(x0), float(y0), float(rng.uniform(0.02, 0.1)), float(rng.uniform(0.5, 2.0))
+
+
+class Solvers:
+    """The fine and coarse two-block contexts plus device buffers."""
+
+    def __init__(self, s: Setup, device: int = 0):
+        self.s = s
+        self.dev = torch.device(f"cuda:{device}")
+        rf, kf = two_layer_fields(s.nxf, s.nbf, s.ratio)
+        rc, kc = two_layer_fields(s.nxc, s.nbc, s.ratio)
+        bc = sbpgpu.BC_CHARACTERISTIC
+        self.fine = sbpgpu.Context(sbpgpu.WAVE_2BLOCK_2D, s.order, s.nxf, 2 * s.nbf, rho=rf, K=kf, bc=bc,
+                                   device=device)
+        self.coarse = sbpgpu.Context(sbpgpu.WAVE_2BLOCK_2D, s.order, s.nxc, 2 * s.nbc, rho=rc, K=kc, bc=bc,
+                                     device=device)
+        self.rho_c = torch.from_numpy(rc).to(self.dev)
+        self.npc = s.nxc * 2 * s.nbc
+
+    # -- state movement (AoS FP64 device tensors)
+    def fine_state(self):
+        out = torch.empty(self.s.nxf * 2 * self.s.nbf * 3, dtype=torch.float64, device=self.dev)
+        self.fine.get_state_ptr(out.data_ptr(), sbpgpu.DEVICE)
+        return out
+
+    def coarse_state(self):
+        out = torch.empty(self.npc * 3, dtype=torch.float64, device=self.dev)
+        self.coarse.get_state_ptr(out.data_ptr(), sbpgpu.DEVICE)
+        return out
+
+    def restrict(self, fine_aos):
+        s = self.s
+        f = fine_aos.view(2, s.nbf, s.nxf, 3)
+        return f[:, ::4, ::4, :].contiguous().view(-1)
+
+    def prolong(self, coarse_aos):
+        s = self.s
+        c = coarse_aos.view(2, s.nbc, s.nxc, 3).permute(0, 3, 1, 2)
+        f = torch.nn.functional.interpolate(c, size=(s.nbf, s.nxf), mode="bilinear", align_corners=True)
+        return f.permute(0, 2, 3, 1).contiguous().view(-1)
+
+    def coarse_steps(self, state, n):
+        self.coarse.set_state_ptr(state.data_ptr(), sbpgpu.DEVICE)
+        self.coarse.step_resident(0.0, self.s.dtc, n)
+        self.coarse.synchronize()
+        return self.coarse_state()
+
+    def fine_steps_from(self, fine_state, n):
+        self.fine.set_state_ptr(fine_state.data_ptr(), sbpgpu.DEVICE)
+        self.fine.step_resident(0.0, self.s.dtf, n)
+        self.fine.synchronize()
+        return self.fine_state()
+
+    def features(self, coarse_aos):
+        x = torch.empty(self.npc * 4, dtype=torch.float32, device=self.dev)
+        torch.cuda.synchronize()
+        sbpgpu.cnn_features(coarse_aos.data_ptr(), self.rho_c.data_ptr(), self.npc, 1.0, x.data_ptr())
+        return x
+
+
+def make_dataset(sv: Solvers, seeds, windows: int):
+    """Pairs (features of the coarse state after `window` coarse steps from the restricted fine
+    state, restricted fine state minus that coarse state) over `windows` windows per trajectory."""
+    s = sv.s
+    xs, ys = [], []
+    fine_steps = 4 * s.window
+    for seed in seeds:
+        x0, y0, w, a = trajectory_params(seed)
+        fine = torch.from_numpy(pulse_state(s.nxf, s.nbf, x0, y0, w, a)).to(sv.dev)
+        for _ in range(windows):
+            start = sv.restrict(fine)
+            pred = sv.coarse_steps(start, s.window)
+            fine = sv.fine_steps_from(fine, fine_steps)
+            target = sv.restrict(fine)
+            xs.append(sv.features(pred))
+            ys.append((target - pred).to(torch.float32))
+    X = torch.stack(xs)
+    Y = torch.stack(ys)
+    scale = float(Y.abs().max().item()) or 1.0
+    return X, Y / scale, scale
+
+
+def train(net: sbpgpu.Cnn, X, Y, *, epochs: int, batch: int, lr: float, seed: int = 0):
+    """Adam over shuffled minibatches; returns the loss history (one entry per step)."""
+    n = X.shape[0]
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    losses = []
+    for _ in range(epochs):
+        perm = torch.randperm(n, generator=g)
+        for k in range(0, n - batch + 1, batch):
+            idx = perm[k:k + batch].to(X.device)
+            xb = X.index_select(0, idx).contiguous()
+            yb = Y.index_select(0, idx).contiguous()
+            losses.append(net.train_step(xb.data_ptr(), yb.data_ptr(), batch, lr))
+    return losses
+
+
+class LearnedSolver:
+    """Coarse solve corrected by the network every window, with the energy guard."""
+
+    def __init__(self, sv: Solvers, net: sbpgpu.Cnn, scale: float, guard: float = 0.01):
+        self.sv, self.net, self.scale, self.guard = sv, net, scale, guard
+        self.delta = torch.empty(sv.npc * 3, dtype=torch.float32, device=sv.dev)
+        self.fallbacks = 0
+
+    def hnorm(self, state):
+        self.sv.coarse.set_state_ptr(state.data_ptr(), sbpgpu.DEVICE)
+        return self.sv.coarse.hnorm()
+
+    def advance_window(self, state, correct: bool = True):
+        sv, s = self.sv, self.sv.s
+        pred = sv.coarse_steps(state, s.window)
+        if not correct:
+            return pred
+        x = sv.features(pred)
+        self.net.forward(x.data_ptr(), 1, self.delta.data_ptr())
+        e0 = self.hnorm(pred)
+        corrected = pred.clone()
+        sbpgpu.cnn_correct(corrected.data_ptr(), self.delta.data_ptr(), sv.npc, self.scale)
+        torch.cuda.synchronize()
+        e1 = self.hnorm(corrected)
+        if not np.isfinite(e1) or e1 > e0 * (1.0 + self.guard):
+            # fallback: recompute the window with the fine solver
+            self.fallbacks += 1
+            fine = sv.fine_steps_from(sv.prolong(state), 4 * s.window)
+            return sv.restrict(fine)
+        return corrected
+
+
+def evaluate(sv: Solvers, solver: LearnedSolver, seeds, windows: int):
+    """Relative L2 errors against the restricted fine solution after `windows` windows, for
+    the plain coarse solve and the corrected one, and the wall time of each form."""
+    s = sv.s
+    out = {"coarse": [], "learned": [], "t_fine": 0.0, "t_coarse": 0.0, "t_learned": 0.0}
+    for seed in seeds:
+        x0, y0, w, a = trajectory_params(seed)
+        fine0 = torch.from_numpy(pulse_state(s.nxf, s.nbf, x0, y0, w, a)).to(sv.dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fine = sv.fine_steps_from(fine0, 4 * s.window * windows)
+        out["t_fine"] += time.perf_counter() - t0
+        ref = sv.restrict(fine)
+        start = sv.restrict(fine0)
+        for key, corr in (("coarse", False), ("learned", True)):
+            st = start.clone()
+            t0 = time.perf_counter()
+            for _ in range(windows):
+                st = solver.advance_window(st, correct=corr)
+            torch.cuda.synchronize()
+            out["t_" + key] += time.perf_counter() - t0
+            out[key].append(float(torch.linalg.norm(st - ref) / torch.linalg.norm(ref)))
+    return out

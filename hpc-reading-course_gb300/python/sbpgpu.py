@@ -297,6 +297,9 @@ class Context:
         self._check(self._L.sbp_get_state(self._h, out.ctypes.data, HOST))
         return out
 
+    def get_state_ptr(self, ptr: int, where: int):
+        self._check(self._L.sbp_get_state(self._h, ptr, where))
+
     def step_resident(self, t0: float, dt: float, nsteps: int):
         self._check(self._L.sbp_rk4_resident(self._h, t0, dt, nsteps))
 

@@ -1,0 +1,43 @@
+"""The learned correction of the coarse two-layer solve: trained on fine
+trajectories this solver generates, it must beat the plain coarse solve on
+held-out trajectories; with corrupted weights the energy guard must reject its
+corrections and fall back to the fine solve."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _small():
+    import learned
+
+    return learned.Setup(nxc=65, nbc=33)
+
+
+def test_learned_correction_beats_plain_coarse_solve(sbp):
+    import learned
+
+    s = _small()
+    sv = learned.Solvers(s)
+    X, Y, scale = learned.make_dataset(sv, range(1000, 1024), windows=6)
+    with sbp.Cnn(2 * s.nbc, s.nxc, 8) as net:
+        losses = learned.train(net, X, Y, epochs=25, batch=8, lr=2e-3)
+        assert np.mean(losses[-10:]) < 0.5 * np.mean(losses[:10])
+        solver = learned.LearnedSolver(sv, net, scale)
+        res = learned.evaluate(sv, solver, range(5000, 5004), windows=6)
+    assert np.mean(res["learned"]) < np.mean(res["coarse"])
+
+
+def test_energy_guard_falls_back_to_fine_solve(sbp):
+    import learned
+
+    s = _small()
+    sv = learned.Solvers(s)
+    with sbp.Cnn(2 * s.nbc, s.nxc, 1) as net:
+        p = net.get_params()
+        rng = np.random.default_rng(0)
+        net.set_params((p + 5.0 * rng.standard_normal(p.size)).astype(np.float32))  # corrupted weights
+        solver = learned.LearnedSolver(sv, net, scale=1.0)
+        res = learned.evaluate(sv, solver, [5000], windows=3)
+    assert solver.fallbacks >= 3
+    assert res["learned"][0] < res["coarse"][0]  # the fallback windows are fine-solver accurate
