@@ -20,7 +20,8 @@ struct WaveMaps {
 
 // Tile height of the single-instance wave stage kernel (see wave_ty).
 inline int wave_tile_height(int elem_bytes, int kind = WK_HOM) {
-  return elem_bytes == 8 ? 16 : (kind == WK_VAR ? 24 : 32);
+  if (elem_bytes == 8) return wave_ty<double, WK_HOM>();
+  return kind == WK_VAR ? wave_ty<float, WK_VAR>() : wave_ty<float, WK_HOM>();
 }
 
 // Streaming multiprocessors of the current device (cached per device).

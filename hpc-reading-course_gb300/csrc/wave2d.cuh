@@ -69,13 +69,28 @@ template <> struct IsCompensated<float> { static constexpr bool value = true; };
 // rounded up so that (tile origin - halo) * sizeof(T) is a multiple of 16
 // bytes (TMA rule for the innermost coordinate); tile origins are multiples of 64.
 template <typename T> constexpr int default_wave_ty() { return sizeof(T) == 8 ? 16 : 32; }
+
+// Pipeline shape of the single-instance kernel for FP32 (tile rows, ring depth);
+// the build may override them to compare shapes.
+#ifndef SBP_FP32_TILE_ROWS
+#define SBP_FP32_TILE_ROWS 32
+#endif
+#ifndef SBP_FP32_RING
+#define SBP_FP32_RING 2
+#endif
+
 // Tile height of the single-instance kernel: the variable-coefficient FP32
 // kind also stages 1/rho and K, so it uses 24 rows to keep two stages in 227 KB.
 template <typename T, int KIND> constexpr int wave_ty() {
-  return (sizeof(T) == 4 && KIND == WK_VAR) ? 24 : default_wave_ty<T>();
+  return sizeof(T) == 8 ? 16 : (KIND == WK_VAR ? 24 : SBP_FP32_TILE_ROWS);
+}
+// Shared-memory ring depth (tiles in flight + the one being computed).
+template <typename T, int KIND> constexpr int wave_ring() {
+  return (sizeof(T) == 4 && KIND != WK_VAR) ? SBP_FP32_RING : 2;
 }
 
-template <typename T, int ORD, int STAGE, int TY_ = default_wave_ty<T>(), int PRM_BYTES = 0, bool COEF = false>
+template <typename T, int ORD, int STAGE, int TY_ = default_wave_ty<T>(), int PRM_BYTES = 0, bool COEF = false,
+          int NST_ = 2>
 struct WaveTile {
   static constexpr bool COMP = IsCompensated<T>::value;
   static constexpr int TY = TY_;                              // tile height
@@ -103,12 +118,14 @@ struct WaveTile {
   static constexpr int OFF_K = align128(OFF_C + (LOAD_COMP ? BYTES_PT : 0));
   static constexpr int OFF_PRM = align128(OFF_K + (LOAD_COEF ? BYTES_K : 0));  // batched: instance parameters
   static constexpr int STAGE_BYTES = OFF_PRM + align128(PRM_BYTES);
-  static constexpr int OFF_BAR = 2 * STAGE_BYTES;             // full[2], empty[2]
+  static constexpr int NST = NST_;                            // ring depth
+  static constexpr int OFF_BAR = NST * STAGE_BYTES;           // full[NST], empty[NST]
   static constexpr int SMEM = OFF_BAR + 128;
   static constexpr uint32_t TX_BYTES = BYTES_P + BYTES_U + BYTES_V + (LOAD_UN ? BYTES_PT : 0) +
                                        (LOAD_ACC ? BYTES_PT : 0) + (LOAD_COMP ? BYTES_PT : 0) +
                                        (LOAD_COEF ? BYTES_K : 0) + PRM_BYTES;
   static_assert(TY % kWaveConsumerWarps == 0, "tile rows must split evenly over the consumer warps");
+  static_assert(NST >= 2 && NST <= 8, "ring depth");
   static_assert(SMEM <= 227 * 1024, "wave tile pipeline exceeds shared memory");
 };
 
@@ -350,11 +367,11 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
                       const __grid_constant__ CUtensorMap mapV, const __grid_constant__ CUtensorMap mapN,
                       const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapC,
                       const __grid_constant__ CUtensorMap mapK, const __grid_constant__ WaveParams<T> prm) {
-  using Tile = WaveTile<T, ORD, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR>;
-  constexpr int TY = Tile::TY, HX = Tile::HX, HY = Tile::HY;
+  using Tile = WaveTile<T, ORD, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR, wave_ring<T, KIND>()>;
+  constexpr int TY = Tile::TY, HX = Tile::HX, HY = Tile::HY, NST = Tile::NST;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
-  uint64_t* empty = full + 2;
+  uint64_t* empty = full + NST;
 
   const int nx = prm.nx, ny = prm.ny;
   const int ntx = (nx + kWaveTX - 1) / kWaveTX;
@@ -362,22 +379,22 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    mbar_init(&full[0], 1);
-    mbar_init(&full[1], 1);
-    mbar_init(&empty[0], kWaveConsumerWarps);
-    mbar_init(&empty[1], kWaveConsumerWarps);
+    for (int s = 0; s < NST; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kWaveConsumerWarps);
+    }
     fence_barrier_init();
   }
   __syncthreads();
 
   if (warp == kWaveConsumerWarps) {
-    // ---------------- producer: TMA loads of tile k into stage k & 1
+    // ---------------- producer: TMA loads of tile k into stage k % NST
     if (lane == 0) {
       prefetch_tensormap(&mapP);
       int k = 0;
       for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
-        const int b = k & 1;
-        if (k >= 2 && !mbar_wait_bounded(&empty[b], ((k >> 1) - 1) & 1)) {
+        const int b = k % NST;
+        if (k >= NST && !mbar_wait_bounded(&empty[b], ((k / NST) - 1) & 1)) {
           atomicOr(prm.err, ERR_TMA_TIMEOUT);
           break;
         }
@@ -392,8 +409,8 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
         if (Tile::LOAD_COMP) tma_load_3d(st + Tile::OFF_C, &mapC, i0, j0, 0, &full[b]);
         if (Tile::LOAD_COEF) tma_load_3d(st + Tile::OFF_K, &mapK, i0, j0, 0, &full[b]);
       }
-      // the CTA must not exit with copies in flight: wait for the last two stages
-      for (int kk = (k >= 2 ? k - 2 : 0); kk < k; kk++) mbar_wait_bounded(&full[kk & 1], (kk >> 1) & 1);
+      // the CTA must not exit with copies in flight: wait for the last NST stages
+      for (int kk = (k >= NST ? k - NST : 0); kk < k; kk++) mbar_wait_bounded(&full[kk % NST], (kk / NST) & 1);
     }
     return;
   }
@@ -401,8 +418,8 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
   // ---------------- consumers: warps 0-7
   int k = 0;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
-    const int b = k & 1;
-    if (!mbar_wait_bounded(&full[b], (k >> 1) & 1)) {
+    const int b = k % NST;
+    if (!mbar_wait_bounded(&full[b], (k / NST) & 1)) {
       if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
       break;
     }

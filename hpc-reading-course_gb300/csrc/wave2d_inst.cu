@@ -19,7 +19,8 @@ namespace {
 template <typename T, int KIND, int STAGE>
 cudaError_t configure_one() {
   return cudaFuncSetAttribute(wave_stage_kernel<T, SBP_ORDER, KIND, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              WaveTile<T, SBP_ORDER, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR>::SMEM);
+                              WaveTile<T, SBP_ORDER, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR,
+                                       wave_ring<T, KIND>()>::SMEM);
 }
 
 template <typename T, int KIND>
@@ -33,7 +34,7 @@ cudaError_t configure_kind() {
 
 template <typename T, int KIND, int STAGE>
 cudaError_t launch_one(const WaveMaps& m, const WaveParams<T>& prm, dim3 grid, cudaStream_t s) {
-  using Tile = WaveTile<T, SBP_ORDER, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR>;
+  using Tile = WaveTile<T, SBP_ORDER, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR, wave_ring<T, KIND>()>;
   wave_stage_kernel<T, SBP_ORDER, KIND, STAGE>
       <<<grid, kWaveThreads, Tile::SMEM, s>>>(m.p, m.u, m.v, m.n, m.a, m.c, m.k, prm);
   return cudaGetLastError();

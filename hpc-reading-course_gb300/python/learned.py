@@ -9,14 +9,13 @@ in y per block) is nested in a 4x coarser one, so restriction is injection.
 Every `window` coarse RK4 steps (4 by default) the network (libsbpgpu's
 sbp_cnn_*, BF16 tensor-core convolutions) maps the coarse state to a
 correction towards the restricted fine solution. A correction that raises
-the coarse state's H-norm by more than `guard` (relative) is rejected: that
-window is recomputed by the fine solver from the interpolated coarse state and
-restricted back (the fallback). The fine solve is also the judge: errors are
-measured against the restricted fine solution.
+the coarse state's H-norm by more than `guard` (relative) fails the energy
+check; then the run falls back to the fine solve: the answer is the fine
+solver's, restricted to the coarse grid. The fine solve is also the judge:
+errors are measured against the restricted fine solution.
 
-Device memory and small glue operations (restriction by slicing, bilinear
-prolongation for the fallback, target differences) use torch on the GPU; the
-solves and the network run in libsbpgpu.
+Device memory and small glue operations (restriction by slicing, target
+differences) use torch on the GPU; the solves and the network run in libsbpgpu.
 """
 from __future__ import annotations
 
@@ -117,12 +116,6 @@ class Solvers:
         f = fine_aos.view(2, s.nbf, s.nxf, 3)
         return f[:, ::4, ::4, :].contiguous().view(-1)
 
-    def prolong(self, coarse_aos):
-        s = self.s
-        c = coarse_aos.view(2, s.nbc, s.nxc, 3).permute(0, 3, 1, 2)
-        f = torch.nn.functional.interpolate(c, size=(s.nbf, s.nxf), mode="bilinear", align_corners=True)
-        return f.permute(0, 2, 3, 1).contiguous().view(-1)
-
     def coarse_steps(self, state, n):
         self.coarse.set_state_ptr(state.data_ptr(), sbpgpu.DEVICE)
         self.coarse.step_resident(0.0, self.s.dtc, n)
@@ -180,7 +173,7 @@ def train(net: sbpgpu.Cnn, X, Y, *, epochs: int, batch: int, lr: float, seed: in
 
 
 class LearnedSolver:
-    """Coarse solve corrected by the network every window, with the energy guard."""
+    """Coarse solve corrected by the network every window, with the energy check."""
 
     def __init__(self, sv: Solvers, net: sbpgpu.Cnn, scale: float, guard: float = 0.01):
         self.sv, self.net, self.scale, self.guard = sv, net, scale, guard
@@ -191,11 +184,10 @@ class LearnedSolver:
         self.sv.coarse.set_state_ptr(state.data_ptr(), sbpgpu.DEVICE)
         return self.sv.coarse.hnorm()
 
-    def advance_window(self, state, correct: bool = True):
+    def corrected_window(self, state):
+        """One window of the corrected coarse solve; None if the correction fails the energy check."""
         sv, s = self.sv, self.sv.s
         pred = sv.coarse_steps(state, s.window)
-        if not correct:
-            return pred
         x = sv.features(pred)
         self.net.forward(x.data_ptr(), 1, self.delta.data_ptr())
         e0 = self.hnorm(pred)
@@ -204,11 +196,25 @@ class LearnedSolver:
         torch.cuda.synchronize()
         e1 = self.hnorm(corrected)
         if not np.isfinite(e1) or e1 > e0 * (1.0 + self.guard):
-            # fallback: recompute the window with the fine solver
-            self.fallbacks += 1
-            fine = sv.fine_steps_from(sv.prolong(state), 4 * s.window)
-            return sv.restrict(fine)
+            return None
         return corrected
+
+    def run(self, fine0, windows: int):
+        """`windows` corrected windows from the fine initial state `fine0` (restricted); if a
+        correction fails the energy check, the fine solve from `fine0` gives the answer."""
+        sv, s = self.sv, self.sv.s
+        state = sv.restrict(fine0)
+        for _ in range(windows):
+            state = self.corrected_window(state)
+            if state is None:
+                self.fallbacks += 1
+                return sv.restrict(sv.fine_steps_from(fine0, 4 * s.window * windows))
+        return state
+
+    def run_plain(self, fine0, windows: int):
+        """The coarse solve without corrections."""
+        sv, s = self.sv, self.sv.s
+        return sv.coarse_steps(sv.restrict(fine0), s.window * windows)
 
 
 def evaluate(sv: Solvers, solver: LearnedSolver, seeds, windows: int):
@@ -224,12 +230,9 @@ def evaluate(sv: Solvers, solver: LearnedSolver, seeds, windows: int):
         fine = sv.fine_steps_from(fine0, 4 * s.window * windows)
         out["t_fine"] += time.perf_counter() - t0
         ref = sv.restrict(fine)
-        start = sv.restrict(fine0)
-        for key, corr in (("coarse", False), ("learned", True)):
-            st = start.clone()
+        for key, fn in (("coarse", solver.run_plain), ("learned", solver.run)):
             t0 = time.perf_counter()
-            for _ in range(windows):
-                st = solver.advance_window(st, correct=corr)
+            st = fn(fine0, windows)
             torch.cuda.synchronize()
             out["t_" + key] += time.perf_counter() - t0
             out[key].append(float(torch.linalg.norm(st - ref) / torch.linalg.norm(ref)))

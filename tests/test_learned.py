@@ -1,7 +1,7 @@
 """The learned correction of the coarse two-layer solve: trained on fine
 trajectories this solver generates, it must beat the plain coarse solve on
-held-out trajectories; with corrupted weights the energy guard must reject its
-corrections and fall back to the fine solve."""
+held-out trajectories; with corrupted weights (injected on the host) the
+energy check must reject its corrections and the fine solve must answer."""
 import numpy as np
 import pytest
 
@@ -39,5 +39,5 @@ def test_energy_guard_falls_back_to_fine_solve(sbp):
         net.set_params((p + 5.0 * rng.standard_normal(p.size)).astype(np.float32))  # corrupted weights
         solver = learned.LearnedSolver(sv, net, scale=1.0)
         res = learned.evaluate(sv, solver, [5000], windows=3)
-    assert solver.fallbacks >= 3
-    assert res["learned"][0] < res["coarse"][0]  # the fallback windows are fine-solver accurate
+    assert solver.fallbacks == 1
+    assert res["learned"][0] == 0.0  # the answer came from the fine solve, the judge itself
