@@ -157,7 +157,7 @@ def cpu_baseline(n: int, order: int, precision: str, bc: str, budget_s: float, r
     import oracle as O
 
     O.build()
-    port = O.Port()
+    port = O.Port(O.PORT_OPT_SO)  # built with the reference's -O3 -ffast-math
     threads = os.cpu_count() or 1
     port.set_threads(threads)
     v = initial_state(n)
@@ -180,7 +180,7 @@ def cpu_baseline(n: int, order: int, precision: str, bc: str, budget_s: float, r
     kind = "port"
     sample = (f"{steps} RK4 steps of the {n}x{n} order-{order} FP64 wave workload "
               f"({'characteristic' if bc == 'characteristic' else 'free-surface'} SAT), oracle restatement "
-              f"(oracle/sbp_oracle.c, -O2, OpenMP) on {threads} threads")
+              f"(oracle/sbp_oracle.c with the reference's -O3 -ffast-math, OpenMP) on {threads} threads")
     return rates, kind, threads, sample
 
 
@@ -332,7 +332,8 @@ def run_learned_study(args):
     """Two-layer problem (rho, K x4 across y = 0): coarse 257 x 2*129 order-4 solve corrected by the
     network every 4 steps, trained on restricted fine (1025 x 2*513, FP64) trajectories with seeded
     pulse position U[-0.5,0.5]^2, width U[0.02,0.1], amplitude U[0.5,2] (seeds 1000..), two windows
-    per trajectory; judged against the fine solve on 100 held-out trajectories (seeds 5000..5099)."""
+    drawn from the 16-window horizon per trajectory; judged against the fine solve on 100 held-out
+    trajectories (seeds 5000..5099) after 16 windows."""
     import numpy as np
     import torch
 
@@ -344,7 +345,7 @@ def run_learned_study(args):
     s = learned.Setup()
     sv = learned.Solvers(s)
     t0 = time.perf_counter()
-    X, Y, scale = learned.make_dataset(sv, range(1000, 1000 + args.trajectories), windows=2)
+    X, Y, scale = learned.make_dataset(sv, range(1000, 1000 + args.trajectories), windows=16, keep=2)
     t_data = time.perf_counter() - t0
     with sbpgpu.Cnn(2 * s.nbc, s.nxc, 8) as net:
         t0 = time.perf_counter()

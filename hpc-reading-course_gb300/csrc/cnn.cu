@@ -281,14 +281,17 @@ __global__ void f32_to_bf16_kernel(const float* __restrict__ a, bf16* __restrict
 }
 
 // Features of a two-block wave state (AoS FP64 u, v, p) for the network:
-// x[p] = (u/s, v/s, p/s, log(rho)/log(4)) with the state scale s.
+// x[p] = (u/s, v/s, p/s, (p/s) log(rho)/log(4)) with the state scale s. Every
+// feature vanishes where the state does, so with zero biases the network maps
+// a zero state to a zero correction (the coarse solve's error is linear in
+// the state).
 __global__ void features_kernel(const double* __restrict__ state, const double* __restrict__ rho,
                                 float* __restrict__ x, long long P, double inv_scale) {
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
     x[4 * p + 0] = (float)(state[3 * p + 0] * inv_scale);
     x[4 * p + 1] = (float)(state[3 * p + 1] * inv_scale);
     x[4 * p + 2] = (float)(state[3 * p + 2] * inv_scale);
-    x[4 * p + 3] = (float)(log(rho[p]) / log(4.0));
+    x[4 * p + 3] = (float)(state[3 * p + 2] * inv_scale * (log(rho[p]) / log(4.0)));
   }
 }
 
@@ -623,6 +626,8 @@ int sbp_cnn_gradients(sbp_cnn* c, const float* x, const float* target, int batch
 }
 
 // One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the mean squared error.
+// Weights are trained; biases keep their values (zero from sbp_cnn_init), so
+// the trained network maps zero features to zero outputs.
 int sbp_cnn_train_step(sbp_cnn* c, const float* x, const float* target, int batch, float lr, float* loss) {
   if (!c || !x || !target || batch < 1 || batch > c->maxB || !(lr > 0)) return SBP_ERR_INVALID;
   CCK(cudaSetDevice(c->device));
@@ -635,9 +640,7 @@ int sbp_cnn_train_step(sbp_cnn* c, const float* x, const float* target, int batc
     const int n = (int)wcount(l);
     adam_kernel<<<(n + 255) / 256, 256, 0, c->stream>>>(c->wm[l], c->mw[l], c->vw[l], c->gw[l], nullptr, n, lr, b1, b2,
                                                         1e-8f, c1, c2);
-    adam_kernel<<<1, 256, 0, c->stream>>>(c->bias[l], c->mbias[l], c->vbias[l], c->gb[l], nullptr, kCout[l], lr, b1,
-                                          b2, 1e-8f, c1, c2);
-    c->launches += 2;
+    c->launches += 1;
   }
   // padded channels stay zero: their gradients are zero (zero inputs / zero targets) and
   // Adam leaves zero-gradient entries unchanged.

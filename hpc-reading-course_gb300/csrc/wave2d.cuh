@@ -73,10 +73,10 @@ template <typename T> constexpr int default_wave_ty() { return sizeof(T) == 8 ? 
 // Pipeline shape of the single-instance kernel for FP32 (tile rows, ring depth);
 // the build may override them to compare shapes.
 #ifndef SBP_FP32_TILE_ROWS
-#define SBP_FP32_TILE_ROWS 32
+#define SBP_FP32_TILE_ROWS 16
 #endif
 #ifndef SBP_FP32_RING
-#define SBP_FP32_RING 2
+#define SBP_FP32_RING 4
 #endif
 
 // Tile height of the single-instance kernel: the variable-coefficient FP32

@@ -135,22 +135,28 @@ class Solvers:
         return x
 
 
-def make_dataset(sv: Solvers, seeds, windows: int):
-    """Pairs (features of the coarse state after `window` coarse steps from the restricted fine
-    state, restricted fine state minus that coarse state) over `windows` windows per trajectory."""
+def make_dataset(sv: Solvers, seeds, windows: int, keep: int | None = None):
+    """Pairs (features of the coarse state after one window of coarse steps from the restricted
+    fine state, restricted fine state minus that coarse state). Each trajectory runs `windows`
+    windows of the fine solve; `keep` of them (drawn from the trajectory's seed; all if None)
+    become samples, so the samples cover the whole horizon the solver is used on."""
     s = sv.s
     xs, ys = [], []
     fine_steps = 4 * s.window
     for seed in seeds:
         x0, y0, w, a = trajectory_params(seed)
+        picks = set(range(windows)) if keep is None else set(
+            np.random.default_rng(seed + 7).choice(windows, size=keep, replace=False).tolist())
         fine = torch.from_numpy(pulse_state(s.nxf, s.nbf, x0, y0, w, a)).to(sv.dev)
-        for _ in range(windows):
-            start = sv.restrict(fine)
-            pred = sv.coarse_steps(start, s.window)
+        for k in range(windows):
+            if k in picks:
+                start = sv.restrict(fine)
+                pred = sv.coarse_steps(start, s.window)
             fine = sv.fine_steps_from(fine, fine_steps)
-            target = sv.restrict(fine)
-            xs.append(sv.features(pred))
-            ys.append((target - pred).to(torch.float32))
+            if k in picks:
+                target = sv.restrict(fine)
+                xs.append(sv.features(pred))
+                ys.append((target - pred).to(torch.float32))
     X = torch.stack(xs)
     Y = torch.stack(ys)
     scale = float(Y.abs().max().item()) or 1.0

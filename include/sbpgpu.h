@@ -187,7 +187,7 @@ long long sbp_batch_launch_count(const sbp_batch* batch); /* kernels launched so
  * A 4-layer 3x3 convolutional network (4 -> 32 -> 32 -> 32 -> 3 channels,
  * ReLU) that corrects a coarse solve; no counterpart in the reference.
  * Inputs and outputs are device arrays, NHWC FP32 (features: u, v, p scaled,
- * log(rho)/log(4); outputs: corrections of u, v, p in the same scale).
+ * p log(rho)/log(4); outputs: corrections of u, v, p in the same scale).
  * Inside: BF16 activations and weights, FP32 accumulation on the tensor
  * cores, FP32 master weights, Adam. Parameters as one FP32 vector: per layer
  * the weights [cout][9][cin] (channels padded: layer 1 cin 16 of which 4
@@ -204,10 +204,11 @@ int sbp_cnn_forward(sbp_cnn* cnn, const float* x, int batch, float* out);
 /* Gradients of the mean squared error (host vector in the parameter layout, may be NULL). */
 int sbp_cnn_gradients(sbp_cnn* cnn, const float* x, const float* target, int batch, float* grad, long long n,
                       float* loss);
-/* One Adam step (beta 0.9 / 0.999) on the mean squared error of a batch. */
+/* One Adam step (beta 0.9 / 0.999) on the mean squared error of a batch;
+ * weights are trained, biases keep their values (zero after sbp_cnn_init). */
 int sbp_cnn_train_step(sbp_cnn* cnn, const float* x, const float* target, int batch, float lr, float* loss);
 /* Device helpers of the corrected solve: features of an AoS FP64 wave state
- * (x[p] = u/s, v/s, p/s, log(rho)/log(4) with inv_scale = 1/s), and
+ * (x[p] = u/s, v/s, p/s, (p/s) log(rho)/log(4) with inv_scale = 1/s), and
  * state += scale * delta. */
 int sbp_cnn_features(const double* state, const double* rho, long long npts, double inv_scale, float* x,
                      void* stream);

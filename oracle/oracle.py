@@ -21,6 +21,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libsbporacle.so")
+PORT_OPT_SO = os.path.join(HERE, "_build", "libsbporacle_opt.so")  # -O3 -ffast-math: timing only
 REF_SO = os.path.join(HERE, "_ref", "libsbpref.so")
 
 WAVE_HOM_2D, WAVE_MMS_2D, ADVECTION_1D, ADVECTION_2D, REFLECTION_1D, WAVE_VAR_2D = 1, 2, 3, 4, 5, 6
