@@ -1,11 +1,11 @@
 // cnn.cu -- the learned correction: a 4-layer 3x3 convolutional network
-// (4 -> 32 -> 32 -> 32 -> 3 channels, ReLU between layers) trained and run on
+// (24 -> 32 -> 32 -> 32 -> 3 channels, ReLU between layers) trained and run on
 // the GPU by the kernels in this file. No counterpart in the reference.
 //
 // Tensors are NHWC. Activations and weights are BF16; every product is
 // accumulated in FP32 on the tensor cores (mma.sync m16n8k16, BF16 inputs,
 // FP32 accumulators); master weights, biases and Adam moments are FP32.
-// Channel counts are padded to multiples of 16 (the MMA K step): input 4 -> 16,
+// Channel counts are padded to multiples of 16 (the MMA K step): input 24 -> 32,
 // output 3 -> 16; the padding carries zeros.
 //
 //   conv3x3_fwd_kernel    implicit GEMM, M = pixels, N = output channels,
@@ -32,9 +32,9 @@ namespace cnn {
 typedef __nv_bfloat16 bf16;
 
 constexpr int kLayers = 4;
-constexpr int kCin[kLayers] = {16, 32, 32, 32};   // padded input channels
+constexpr int kCin[kLayers] = {32, 32, 32, 32};   // padded input channels
 constexpr int kCout[kLayers] = {32, 32, 32, 16};  // padded output channels
-constexpr int kInReal = 4, kOutReal = 3;
+constexpr int kInReal = 24, kOutReal = 3;
 
 __device__ __forceinline__ uint32_t ld_pair(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
 
@@ -217,11 +217,12 @@ __global__ void flip_weights_kernel(const bf16* __restrict__ w, bf16* __restrict
   wT[e] = w[((long long)n * 9 + (8 - tap)) * cin + c];
 }
 
-// x16[p][c] = c < 4 ? bf16(x[p][c]) : 0
+// x16[p][c] = c < 24 ? bf16(x[p][c]) : 0, c < 32
 __global__ void pack_input_kernel(const float* __restrict__ x, bf16* __restrict__ x16, long long P) {
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < P * 16; e += (long long)gridDim.x * blockDim.x) {
-    const long long p = e / 16;
-    const int c = (int)(e % 16);
+  constexpr int CP = kCin[0];
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < P * CP; e += (long long)gridDim.x * blockDim.x) {
+    const long long p = e / CP;
+    const int c = (int)(e % CP);
     x16[e] = __float2bfloat16(c < kInReal ? x[p * kInReal + c] : 0.f);
   }
 }
@@ -280,25 +281,88 @@ __global__ void f32_to_bf16_kernel(const float* __restrict__ a, bf16* __restrict
   if (e < n) b[e] = __float2bfloat16(a[e]);
 }
 
-// Features of a two-block wave state (AoS FP64 u, v, p) for the network:
-// x[p] = (u/s, v/s, p/s, (p/s) log(rho)/log(4)) with the state scale s. Every
-// feature vanishes where the state does, so with zero biases the network maps
-// a zero state to a zero correction (the coarse solve's error is linear in
-// the state).
-__global__ void features_kernel(const double* __restrict__ state, const double* __restrict__ rho,
-                                float* __restrict__ x, long long P, double inv_scale) {
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
-    x[4 * p + 0] = (float)(state[3 * p + 0] * inv_scale);
-    x[4 * p + 1] = (float)(state[3 * p + 1] * inv_scale);
-    x[4 * p + 2] = (float)(state[3 * p + 2] * inv_scale);
-    x[4 * p + 3] = (float)(state[3 * p + 2] * inv_scale * (log(rho[p]) / log(4.0)));
+// Features of a layered wave state (AoS FP64 u, v, p on ny = blocks x block_rows
+// rows of nx points) for the network. In the impedance-scaled variables
+// q = (Z u, Z v, p), Z = sqrt(rho K), the coarse solve's error does not depend
+// on the layer away from the interface (equal wave speeds). Per point, divided
+// by the feature scale s (inv_scale = 1/s):
+//   x[0..2]   = d2x q    undivided second differences along x,
+//   x[3..5]   = d2y q    along y, within the point's block (no differencing
+//                        across the interface line, which both blocks hold),
+//   x[6..8]   = d4x q    undivided fourth differences along x,
+//   x[9..11]  = d4y q    along y, within the block,
+//   x[12..23] = t x[0..11]   t = +1 in block 0, -1 above (the layer tag),
+// with each centre clamped one (two, for d4) point(s) in from an edge, so the
+// difference is one-sided there. The differences are taken in FP64 before the
+// network's BF16 rounding. The features are high-pass and linear in the state;
+// the network's ReLU layers without biases are positively homogeneous, so a
+// smooth or zero state gets a proportionally small or zero correction.
+__device__ __forceinline__ void zq(const double* __restrict__ state, const double* __restrict__ rho,
+                                   const double* __restrict__ K, long long p, double (&q)[3]) {
+  const double z = sqrt(rho[p] * K[p]);
+  q[0] = z * state[3 * p + 0];
+  q[1] = z * state[3 * p + 1];
+  q[2] = state[3 * p + 2];
+}
+
+// Second (D4 = false) or fourth (D4 = true) undivided difference of q at point p0 with stride st.
+template <bool D4>
+__device__ __forceinline__ void diff_q(const double* __restrict__ state, const double* __restrict__ rho,
+                                       const double* __restrict__ K, long long p0, long long st, double (&d)[3]) {
+  double a[3], b[3], m[3];
+  zq(state, rho, K, p0, m);
+  if (!D4) {
+    zq(state, rho, K, p0 - st, a);
+    zq(state, rho, K, p0 + st, b);
+    for (int c = 0; c < 3; c++) d[c] = a[c] - 2.0 * m[c] + b[c];
+  } else {
+    double a2[3], b2[3];
+    zq(state, rho, K, p0 - 2 * st, a2);
+    zq(state, rho, K, p0 - st, a);
+    zq(state, rho, K, p0 + st, b);
+    zq(state, rho, K, p0 + 2 * st, b2);
+    for (int c = 0; c < 3; c++) d[c] = a2[c] - 4.0 * a[c] + 6.0 * m[c] - 4.0 * b[c] + b2[c];
   }
 }
 
-// state[p][c] += scale * delta[p][c] (AoS FP64 state, network output in units of `scale`)
-__global__ void correct_kernel(double* __restrict__ state, const float* __restrict__ delta, long long P, double scale) {
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < 3 * P; e += (long long)gridDim.x * blockDim.x)
-    state[e] += scale * (double)delta[e];
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__global__ void features_kernel(const double* __restrict__ state, const double* __restrict__ rho,
+                                const double* __restrict__ K, float* __restrict__ x, int nx, int ny, int block_rows,
+                                double inv_scale) {
+  const long long P = (long long)nx * ny;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(p / nx), i = (int)(p % nx);
+    const int b = j / block_rows, r = j % block_rows;
+    const long long row0 = (long long)b * block_rows;
+    double f[12], d[3];
+    diff_q<false>(state, rho, K, (long long)j * nx + clampi(i, 1, nx - 2), 1, d);
+    for (int c = 0; c < 3; c++) f[c] = d[c];
+    diff_q<false>(state, rho, K, (row0 + clampi(r, 1, block_rows - 2)) * nx + i, nx, d);
+    for (int c = 0; c < 3; c++) f[3 + c] = d[c];
+    diff_q<true>(state, rho, K, (long long)j * nx + clampi(i, 2, nx - 3), 1, d);
+    for (int c = 0; c < 3; c++) f[6 + c] = d[c];
+    diff_q<true>(state, rho, K, (row0 + clampi(r, 2, block_rows - 3)) * nx + i, nx, d);
+    for (int c = 0; c < 3; c++) f[9 + c] = d[c];
+    const double t = b == 0 ? 1.0 : -1.0;
+    for (int c = 0; c < 12; c++) {
+      x[(long long)kInReal * p + c] = (float)(f[c] * inv_scale);
+      x[(long long)kInReal * p + 12 + c] = (float)(t * f[c] * inv_scale);
+    }
+  }
+}
+
+// The network's output is a correction of q = (Z u, Z v, p) in units of `scale`:
+// state[p] += scale * (delta[p][0] / Z, delta[p][1] / Z, delta[p][2]).
+__global__ void correct_kernel(double* __restrict__ state, const float* __restrict__ delta,
+                               const double* __restrict__ rho, const double* __restrict__ K, long long P,
+                               double scale) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
+    const double zi = scale / sqrt(rho[p] * K[p]);
+    state[3 * p + 0] += zi * (double)delta[3 * p + 0];
+    state[3 * p + 1] += zi * (double)delta[3 * p + 1];
+    state[3 * p + 2] += scale * (double)delta[3 * p + 2];
+  }
 }
 
 inline int blocks_for(long long n, int threads) {
@@ -368,7 +432,7 @@ cudaError_t conv_fwd(int l, const bf16* x, void* y, const sbp_cnn* c, int batch,
   const long long P = (long long)batch * c->H * c->W;
   const int grid = (int)((P + 63) / 64);
   switch (l) {
-    case 0: conv3x3_fwd_kernel<16, 32, true, false><<<grid, 128, 0, s>>>(x, c->wb[0], c->bias[0], y, batch, c->H, c->W); break;
+    case 0: conv3x3_fwd_kernel<32, 32, true, false><<<grid, 128, 0, s>>>(x, c->wb[0], c->bias[0], y, batch, c->H, c->W); break;
     case 1: conv3x3_fwd_kernel<32, 32, true, false><<<grid, 128, 0, s>>>(x, c->wb[1], c->bias[1], y, batch, c->H, c->W); break;
     case 2: conv3x3_fwd_kernel<32, 32, true, false><<<grid, 128, 0, s>>>(x, c->wb[2], c->bias[2], y, batch, c->H, c->W); break;
     default: conv3x3_fwd_kernel<32, 16, false, true><<<grid, 128, 0, s>>>(x, c->wb[3], c->bias[3], y, batch, c->H, c->W); break;
@@ -391,7 +455,7 @@ cudaError_t conv_wgrad(int l, const bf16* x, const bf16* dy, float* dw, const sb
   const int ppw = 1024;
   const dim3 grid((unsigned)((P + 4LL * ppw - 1) / (4LL * ppw)), 9);
   switch (l) {
-    case 0: conv3x3_wgrad_kernel<16, 32><<<grid, 128, 0, s>>>(x, dy, dw, batch, c->H, c->W, ppw); break;
+    case 0:
     case 1:
     case 2: conv3x3_wgrad_kernel<32, 32><<<grid, 128, 0, s>>>(x, dy, dw, batch, c->H, c->W, ppw); break;
     default: conv3x3_wgrad_kernel<32, 16><<<grid, 128, 0, s>>>(x, dy, dw, batch, c->H, c->W, ppw); break;
@@ -421,7 +485,7 @@ int refresh_weights(sbp_cnn* c) {
 
 int run_forward(sbp_cnn* c, const float* x, int batch) {
   const long long P = (long long)batch * c->H * c->W;
-  pack_input_kernel<<<blocks_for(P * 16, 256), 256, 0, c->stream>>>(x, c->act[0], P);
+  pack_input_kernel<<<blocks_for(P * kCin[0], 256), 256, 0, c->stream>>>(x, c->act[0], P);
   c->launches++;
   for (int l = 0; l < kLayers; l++) {
     void* y = (l == kLayers - 1) ? (void*)c->out16 : (void*)c->act[l + 1];
@@ -510,7 +574,9 @@ int sbp_cnn_init(sbp_cnn* c, unsigned long long seed) {
   for (int l = 0; l < kLayers; l++) {
     const long long n = wcount(l);
     const int fan_in = 9 * (l == 0 ? kInReal : kCin[l]);
-    std::normal_distribution<double> nd(0.0, std::sqrt(2.0 / fan_in) * (l == kLayers - 1 ? 0.1 : 1.0));
+    // He-normal hidden layers; the output layer starts at zero, so the untrained network is the
+    // zero correction and training moves away from it only where that lowers the error.
+    std::normal_distribution<double> nd(0.0, std::sqrt(2.0 / fan_in) * (l == kLayers - 1 ? 0.0 : 1.0));
     std::vector<float> w(n);
     for (long long e = 0; e < n; e++) w[e] = weight_is_real(l, e) ? (float)nd(rng) : 0.f;
     std::vector<float> b(kCout[l], 0.f);
@@ -650,16 +716,20 @@ int sbp_cnn_train_step(sbp_cnn* c, const float* x, const float* target, int batc
   return SBP_OK;
 }
 
-int sbp_cnn_features(const double* state, const double* rho, long long npts, double inv_scale, float* x,
-                     void* stream) {
-  if (!state || !rho || !x || npts < 1) return SBP_ERR_INVALID;
-  features_kernel<<<blocks_for(npts, 256), 256, 0, (cudaStream_t)stream>>>(state, rho, x, npts, inv_scale);
+int sbp_cnn_features(const double* state, const double* rho, const double* K, int nx, int ny, int block_rows,
+                     double inv_scale, float* x, void* stream) {
+  if (!state || !rho || !K || !x || nx < 5 || block_rows < 5 || ny < block_rows || ny % block_rows)
+    return SBP_ERR_INVALID;
+  const long long P = (long long)nx * ny;
+  features_kernel<<<blocks_for(P, 256), 256, 0, (cudaStream_t)stream>>>(state, rho, K, x, nx, ny, block_rows,
+                                                                        inv_scale);
   return cudaGetLastError() == cudaSuccess ? SBP_OK : SBP_ERR_CUDA;
 }
 
-int sbp_cnn_correct(double* state, const float* delta, long long npts, double scale, void* stream) {
-  if (!state || !delta || npts < 1) return SBP_ERR_INVALID;
-  correct_kernel<<<blocks_for(3 * npts, 256), 256, 0, (cudaStream_t)stream>>>(state, delta, npts, scale);
+int sbp_cnn_correct(double* state, const float* delta, const double* rho, const double* K, long long npts,
+                    double scale, void* stream) {
+  if (!state || !delta || !rho || !K || npts < 1) return SBP_ERR_INVALID;
+  correct_kernel<<<blocks_for(npts, 256), 256, 0, (cudaStream_t)stream>>>(state, delta, rho, K, npts, scale);
   return cudaGetLastError() == cudaSuccess ? SBP_OK : SBP_ERR_CUDA;
 }
 

@@ -7,8 +7,20 @@ SAT, SBP order 4. A fine grid (nx_f = 4 (nx_c - 1) + 1 points per row, the same
 in y per block) is nested in a 4x coarser one, so restriction is injection.
 
 Every `window` coarse RK4 steps (4 by default) the network (libsbpgpu's
-sbp_cnn_*, BF16 tensor-core convolutions) maps the coarse state to a
-correction towards the restricted fine solution. A correction that raises
+sbp_cnn_*, BF16 tensor-core convolutions) maps high-pass features of the
+coarse state (undivided second and fourth differences of Z u, Z v, p,
+Z = sqrt(rho K), computed in FP64) to a correction of Z u, Z v, p towards the
+restricted fine solution.
+
+Training: pairs (features of a coarse window's result, restricted fine state
+minus that result) from seeded pulse trajectories, first from windows started
+on the restricted fine state, then from windows started on the corrected
+solve's own states (rollout rounds: the states the solver actually meets,
+with targets that pull back to the fine solution). The network has no biases
+and ReLU activations, so it is positively homogeneous: scaling a sample's
+features and target by the same factor leaves the function to learn
+unchanged. Each sample is scaled to unit target RMS, so every trajectory
+counts equally in relative terms, as in the relative error it is judged by. A correction that raises
 the coarse state's H-norm by more than `guard` (relative) fails the energy
 check; then the run falls back to the fine solve: the answer is the fine
 solver's, restricted to the coarse grid. The fine solve is also the judge:
@@ -16,6 +28,9 @@ errors are measured against the restricted fine solution.
 
 Device memory and small glue operations (restriction by slicing, target
 differences) use torch on the GPU; the solves and the network run in libsbpgpu.
+The library's contexts and network run on their own streams, so every hand-off
+of a device array between torch and the library waits for the producer
+(`_ready`).
 """
 from __future__ import annotations
 
@@ -84,6 +99,12 @@ def trajectory_params(seed: int):
     return float(x0), float(y0), float(rng.uniform(0.02, 0.1)), float(rng.uniform(0.5, 2.0))
 
 
+def _ready():
+    """Wait for all work on the device (the hand-off point between torch's stream and the
+    library's streams)."""
+    torch.cuda.synchronize()
+
+
 class Solvers:
     """The fine and coarse two-block contexts plus device buffers."""
 
@@ -98,6 +119,7 @@ class Solvers:
         self.coarse = sbpgpu.Context(sbpgpu.WAVE_2BLOCK_2D, s.order, s.nxc, 2 * s.nbc, rho=rc, K=kc, bc=bc,
                                      device=device)
         self.rho_c = torch.from_numpy(rc).to(self.dev)
+        self.K_c = torch.from_numpy(kc).to(self.dev)
         self.npc = s.nxc * 2 * s.nbc
 
     # -- state movement (AoS FP64 device tensors)
@@ -117,29 +139,51 @@ class Solvers:
         return f[:, ::4, ::4, :].contiguous().view(-1)
 
     def coarse_steps(self, state, n):
+        _ready()
         self.coarse.set_state_ptr(state.data_ptr(), sbpgpu.DEVICE)
         self.coarse.step_resident(0.0, self.s.dtc, n)
         self.coarse.synchronize()
         return self.coarse_state()
 
     def fine_steps_from(self, fine_state, n):
+        _ready()
         self.fine.set_state_ptr(fine_state.data_ptr(), sbpgpu.DEVICE)
         self.fine.step_resident(0.0, self.s.dtf, n)
         self.fine.synchronize()
         return self.fine_state()
 
-    def features(self, coarse_aos):
-        x = torch.empty(self.npc * 4, dtype=torch.float32, device=self.dev)
-        torch.cuda.synchronize()
-        sbpgpu.cnn_features(coarse_aos.data_ptr(), self.rho_c.data_ptr(), self.npc, 1.0, x.data_ptr())
+    def features(self, coarse_aos, inv_scale: float = 1.0):
+        s = self.s
+        x = torch.empty(self.npc * 24, dtype=torch.float32, device=self.dev)
+        _ready()
+        sbpgpu.cnn_features(coarse_aos.data_ptr(), self.rho_c.data_ptr(), self.K_c.data_ptr(), s.nxc, 2 * s.nbc,
+                            s.nbc, inv_scale, x.data_ptr())
+        _ready()
         return x
 
+    def to_q(self, coarse_aos):
+        """(Z u, Z v, p) of an AoS coarse state, Z = sqrt(rho K): the variables the network corrects."""
+        z = (self.rho_c * self.K_c).sqrt()
+        q = coarse_aos.view(-1, 3).clone()
+        q[:, 0] *= z
+        q[:, 1] *= z
+        return q.view(-1)
 
-def make_dataset(sv: Solvers, seeds, windows: int, keep: int | None = None):
-    """Pairs (features of the coarse state after one window of coarse steps from the restricted
-    fine state, restricted fine state minus that coarse state). Each trajectory runs `windows`
-    windows of the fine solve; `keep` of them (drawn from the trajectory's seed; all if None)
-    become samples, so the samples cover the whole horizon the solver is used on."""
+
+@dataclass
+class Scales:
+    """Feature scale (features are divided by it) and correction scale (outputs are in its units)."""
+    inp: float = 1.0
+    out: float = 1.0
+
+
+def collect(sv: Solvers, seeds, windows: int, keep: int | None = None, solver: "LearnedSolver | None" = None):
+    """Raw pairs (features of the coarse state after one window, restricted fine state minus that
+    coarse state in Z u, Z v, p). Each trajectory runs `windows` windows of the fine solve; `keep`
+    of them (drawn from the trajectory's seed; all if None) become samples, so the samples cover
+    the whole horizon the solver is used on. Without `solver` every window starts on the
+    restricted fine state; with one, windows start on the corrected solve's own state (the
+    restricted fine state again where a correction fails the energy check)."""
     s = sv.s
     xs, ys = [], []
     fine_steps = 4 * s.window
@@ -148,25 +192,49 @@ def make_dataset(sv: Solvers, seeds, windows: int, keep: int | None = None):
         picks = set(range(windows)) if keep is None else set(
             np.random.default_rng(seed + 7).choice(windows, size=keep, replace=False).tolist())
         fine = torch.from_numpy(pulse_state(s.nxf, s.nbf, x0, y0, w, a)).to(sv.dev)
-        for k in range(windows):
-            if k in picks:
-                start = sv.restrict(fine)
-                pred = sv.coarse_steps(start, s.window)
+        state = sv.restrict(fine)
+        last = max(picks) if picks else -1
+        for k in range(last + 1):
+            if solver is None and k not in picks:
+                fine = sv.fine_steps_from(fine, fine_steps)
+                continue
+            start = sv.restrict(fine) if solver is None else state
+            pred = sv.coarse_steps(start, s.window)
             fine = sv.fine_steps_from(fine, fine_steps)
+            target = sv.restrict(fine)
             if k in picks:
-                target = sv.restrict(fine)
                 xs.append(sv.features(pred))
-                ys.append((target - pred).to(torch.float32))
-    X = torch.stack(xs)
-    Y = torch.stack(ys)
-    scale = float(Y.abs().max().item()) or 1.0
-    return X, Y / scale, scale
+                ys.append((sv.to_q(target) - sv.to_q(pred)).to(torch.float32))
+            if solver is not None:
+                corrected = solver.correct(pred)
+                state = target if corrected is None else corrected
+    return torch.stack(xs), torch.stack(ys)
+
+
+def normalize(X, Y, scales: Scales | None = None):
+    """Scale each sample to unit target RMS (valid for the homogeneous network; the floor keeps
+    near-zero targets from dominating), then features and targets by the set's RMS (`scales`,
+    computed when None). Returns (X, Y, scales)."""
+    a = Y.square().mean(dim=1).sqrt()
+    a = torch.clamp(a, min=max(1e-3 * float(a.median()), 1e-30))[:, None]
+    X = X / a
+    Y = Y / a
+    if scales is None:
+        scales = Scales(inp=float(X.square().mean().sqrt()) or 1.0, out=float(Y.square().mean().sqrt()) or 1.0)
+    return X / scales.inp, Y / scales.out, scales
+
+
+def make_dataset(sv: Solvers, seeds, windows: int, keep: int | None = None):
+    """Windows started on the restricted fine state, normalized: (X, Y, Scales)."""
+    return normalize(*collect(sv, seeds, windows, keep))
 
 
 def train(net: sbpgpu.Cnn, X, Y, *, epochs: int, batch: int, lr: float, seed: int = 0):
-    """Adam over shuffled minibatches; returns the loss history (one entry per step)."""
+    """Adam over shuffled minibatches, learning rate decayed from `lr` to `lr`/10 on a cosine;
+    returns the loss history (one entry per step)."""
     n = X.shape[0]
     g = torch.Generator(device="cpu").manual_seed(seed)
+    total = epochs * (n // batch)
     losses = []
     for _ in range(epochs):
         perm = torch.randperm(n, generator=g)
@@ -174,31 +242,40 @@ def train(net: sbpgpu.Cnn, X, Y, *, epochs: int, batch: int, lr: float, seed: in
             idx = perm[k:k + batch].to(X.device)
             xb = X.index_select(0, idx).contiguous()
             yb = Y.index_select(0, idx).contiguous()
-            losses.append(net.train_step(xb.data_ptr(), yb.data_ptr(), batch, lr))
+            _ready()
+            frac = len(losses) / max(total, 1)
+            step_lr = lr * (0.1 + 0.45 * (1.0 + np.cos(np.pi * frac)))
+            losses.append(net.train_step(xb.data_ptr(), yb.data_ptr(), batch, step_lr))
     return losses
 
 
 class LearnedSolver:
     """Coarse solve corrected by the network every window, with the energy check."""
 
-    def __init__(self, sv: Solvers, net: sbpgpu.Cnn, scale: float, guard: float = 0.01):
-        self.sv, self.net, self.scale, self.guard = sv, net, scale, guard
+    def __init__(self, sv: Solvers, net: sbpgpu.Cnn, scales: Scales, guard: float = 0.01):
+        self.sv, self.net, self.scales, self.guard = sv, net, scales, guard
         self.delta = torch.empty(sv.npc * 3, dtype=torch.float32, device=sv.dev)
         self.fallbacks = 0
 
     def hnorm(self, state):
+        _ready()
         self.sv.coarse.set_state_ptr(state.data_ptr(), sbpgpu.DEVICE)
         return self.sv.coarse.hnorm()
 
     def corrected_window(self, state):
         """One window of the corrected coarse solve; None if the correction fails the energy check."""
-        sv, s = self.sv, self.sv.s
-        pred = sv.coarse_steps(state, s.window)
-        x = sv.features(pred)
+        return self.correct(self.sv.coarse_steps(state, self.sv.s.window))
+
+    def correct(self, pred):
+        """The network's correction of a coarse window's result; None if it fails the energy check."""
+        sv = self.sv
+        x = sv.features(pred, 1.0 / self.scales.inp)
         self.net.forward(x.data_ptr(), 1, self.delta.data_ptr())
         e0 = self.hnorm(pred)
         corrected = pred.clone()
-        sbpgpu.cnn_correct(corrected.data_ptr(), self.delta.data_ptr(), sv.npc, self.scale)
+        _ready()
+        sbpgpu.cnn_correct(corrected.data_ptr(), self.delta.data_ptr(), sv.rho_c.data_ptr(), sv.K_c.data_ptr(), sv.npc,
+                           self.scales.out)
         torch.cuda.synchronize()
         e1 = self.hnorm(corrected)
         if not np.isfinite(e1) or e1 > e0 * (1.0 + self.guard):

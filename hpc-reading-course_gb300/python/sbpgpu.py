@@ -130,8 +130,10 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.sbp_cnn_gradients.argtypes = [P, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_longlong,
                                     C.POINTER(C.c_float)]
     L.sbp_cnn_train_step.argtypes = [P, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.POINTER(C.c_float)]
-    L.sbp_cnn_features.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong, C.c_double, C.c_void_p, C.c_void_p]
-    L.sbp_cnn_correct.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong, C.c_double, C.c_void_p]
+    L.sbp_cnn_features.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
+                                   C.c_void_p, C.c_void_p]
+    L.sbp_cnn_correct.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.c_double,
+                                  C.c_void_p]
     L.sbp_cnn_launch_count.argtypes = [P]
     L.sbp_cnn_launch_count.restype = C.c_longlong
     L.sbp_write_petsc_vec.argtypes = [C.c_char_p, C.c_void_p, C.c_longlong]
@@ -409,7 +411,7 @@ class Batch:
 
 class Cnn:
     """The learned-correction network (sbp_cnn_*). Device arrays are passed by address
-    (e.g. torch CUDA tensors' data_ptr()): features NHWC FP32 with 4 channels, outputs 3."""
+    (e.g. torch CUDA tensors' data_ptr()): features NHWC FP32 with 24 channels, outputs 3."""
 
     def __init__(self, height: int, width: int, max_batch: int, *, device: int = 0, stream: int | None = None,
                  seed: int = 1234):
@@ -478,13 +480,15 @@ class Cnn:
         return self._L.sbp_cnn_launch_count(self._h)
 
 
-def cnn_features(state_ptr: int, rho_ptr: int, npts: int, inv_scale: float, x_ptr: int, stream: int | None = None):
-    rc = load().sbp_cnn_features(state_ptr, rho_ptr, npts, inv_scale, x_ptr, stream)
+def cnn_features(state_ptr: int, rho_ptr: int, K_ptr: int, nx: int, ny: int, block_rows: int, inv_scale: float,
+                 x_ptr: int, stream: int | None = None):
+    rc = load().sbp_cnn_features(state_ptr, rho_ptr, K_ptr, nx, ny, block_rows, inv_scale, x_ptr, stream)
     if rc:
         raise SbpError(rc, "sbp_cnn_features failed")
 
 
-def cnn_correct(state_ptr: int, delta_ptr: int, npts: int, scale: float, stream: int | None = None):
-    rc = load().sbp_cnn_correct(state_ptr, delta_ptr, npts, scale, stream)
+def cnn_correct(state_ptr: int, delta_ptr: int, rho_ptr: int, K_ptr: int, npts: int, scale: float,
+                stream: int | None = None):
+    rc = load().sbp_cnn_correct(state_ptr, delta_ptr, rho_ptr, K_ptr, npts, scale, stream)
     if rc:
         raise SbpError(rc, "sbp_cnn_correct failed")

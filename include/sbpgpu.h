@@ -10,7 +10,9 @@
  * never throws; sbp_last_error() gives the message of the last failure on a
  * context. A context is bound to one CUDA stream and one device; calls on one
  * context must not run concurrently (as the reference's callbacks, which run
- * one per MPI rank).
+ * one per MPI rank). Device arrays passed in are read and written on that
+ * stream: a caller that produces or consumes them on another stream orders
+ * the two first (an event, or a synchronize).
  *
  * Array format at the boundary is the reference's: FP64, array-of-structs,
  * element (j, i, comp) at dofs*(i + nx*j) + comp (code/include/grids/layout.h:124-127;
@@ -184,19 +186,20 @@ long long sbp_batch_points(const sbp_batch* batch);       /* grid points over al
 long long sbp_batch_launch_count(const sbp_batch* batch); /* kernels launched so far */
 
 /* ---------------------------------------------------------------- learned correction
- * A 4-layer 3x3 convolutional network (4 -> 32 -> 32 -> 32 -> 3 channels,
+ * A 4-layer 3x3 convolutional network (24 -> 32 -> 32 -> 32 -> 3 channels,
  * ReLU) that corrects a coarse solve; no counterpart in the reference.
- * Inputs and outputs are device arrays, NHWC FP32 (features: u, v, p scaled,
- * p log(rho)/log(4); outputs: corrections of u, v, p in the same scale).
+ * Inputs and outputs are device arrays, NHWC FP32 (features: sbp_cnn_features;
+ * outputs: corrections of Z u, Z v, p in units of a scale, sbp_cnn_correct).
  * Inside: BF16 activations and weights, FP32 accumulation on the tensor
  * cores, FP32 master weights, Adam. Parameters as one FP32 vector: per layer
- * the weights [cout][9][cin] (channels padded: layer 1 cin 16 of which 4
+ * the weights [cout][9][cin] (channels padded: layer 1 cin 32 of which 24
  * real, layer 4 cout 16 of which 3 real) then the bias [cout]. */
 typedef struct sbp_cnn sbp_cnn;
 int sbp_cnn_create(int height, int width, int max_batch, int device, void* stream, sbp_cnn** cnn);
 int sbp_cnn_destroy(sbp_cnn* cnn);
 const char* sbp_cnn_last_error(const sbp_cnn* cnn); /* NULL: last failed sbp_cnn_create */
 long long sbp_cnn_param_count(void);
+/* He-normal weights for layers 1-3 from `seed`, zero output layer, zero biases, Adam reset. */
 int sbp_cnn_init(sbp_cnn* cnn, unsigned long long seed);
 int sbp_cnn_get_params(sbp_cnn* cnn, float* host, long long n);
 int sbp_cnn_set_params(sbp_cnn* cnn, const float* host, long long n);
@@ -207,12 +210,19 @@ int sbp_cnn_gradients(sbp_cnn* cnn, const float* x, const float* target, int bat
 /* One Adam step (beta 0.9 / 0.999) on the mean squared error of a batch;
  * weights are trained, biases keep their values (zero after sbp_cnn_init). */
 int sbp_cnn_train_step(sbp_cnn* cnn, const float* x, const float* target, int batch, float lr, float* loss);
-/* Device helpers of the corrected solve: features of an AoS FP64 wave state
- * (x[p] = u/s, v/s, p/s, (p/s) log(rho)/log(4) with inv_scale = 1/s), and
- * state += scale * delta. */
-int sbp_cnn_features(const double* state, const double* rho, long long npts, double inv_scale, float* x,
-                     void* stream);
-int sbp_cnn_correct(double* state, const float* delta, long long npts, double scale, void* stream);
+/* Device helpers of the corrected solve on a layered grid (ny = blocks x
+ * block_rows rows of nx points, nx and block_rows >= 5, AoS FP64 u, v, p;
+ * rho, K per point). Features (24 per point, inv_scale = 1/s), with
+ * q = (Z u, Z v, p), Z = sqrt(rho K), computed in FP64 and divided by s:
+ * undivided second differences of q along x (3) and along y within the
+ * point's block (3), fourth differences along x (3) and y (3), then the same
+ * twelve times +1 in block 0 and -1 above. Centres are clamped one (second
+ * differences) or two (fourth) points in from an edge.
+ * sbp_cnn_correct: state += scale * (delta_0 / Z, delta_1 / Z, delta_2). */
+int sbp_cnn_features(const double* state, const double* rho, const double* K, int nx, int ny, int block_rows,
+                     double inv_scale, float* x, void* stream);
+int sbp_cnn_correct(double* state, const float* delta, const double* rho, const double* K, long long npts,
+                    double scale, void* stream);
 long long sbp_cnn_launch_count(const sbp_cnn* cnn);
 
 /* PETSc binary Vec files (host-side I/O): the format VecView writes on a

@@ -2,8 +2,8 @@
 
 The checker for the GPU network kernels in hpc-reading-course_gb300/csrc/cnn.cu
 (the network has no counterpart in the reference). Same architecture,
-parameter layout and padding: 4 conv3x3 layers, channels (16 -> 32 -> 32 ->
-32 -> 16) of which 4 inputs and 3 outputs are real, zero padding at the image
+parameter layout and padding: 4 conv3x3 layers, channels (32 -> 32 -> 32 ->
+32 -> 16) of which 24 inputs and 3 outputs are real, zero padding at the image
 border, ReLU after layers 1-3, mean squared error over the 3 real outputs.
 
 `bf16=True` rounds every tensor the GPU stores in BF16 (inputs, weights,
@@ -14,8 +14,8 @@ from __future__ import annotations
 
 import numpy as np
 
-LAYERS = [(16, 32, True), (32, 32, True), (32, 32, True), (32, 16, False)]  # (cin, cout, relu)
-IN_REAL, OUT_REAL = 4, 3
+LAYERS = [(32, 32, True), (32, 32, True), (32, 32, True), (32, 16, False)]  # (cin, cout, relu)
+IN_REAL, OUT_REAL = 24, 3
 
 
 def param_count() -> int:
@@ -83,7 +83,7 @@ def conv3x3_weight_grad(x, d):
 
 
 def _pad_input(x4):
-    x = np.zeros(x4.shape[:3] + (16,))
+    x = np.zeros(x4.shape[:3] + (LAYERS[0][0],))
     x[..., :IN_REAL] = x4
     return x
 

@@ -53,7 +53,7 @@ def test_gpu_forward_and_gradients_match_oracle(sbp):
 
     B, H, W = 2, 19, 23
     rng = np.random.default_rng(3)
-    x = rng.standard_normal((B, H, W, 4)).astype(np.float32)
+    x = rng.standard_normal((B, H, W, N.IN_REAL)).astype(np.float32)
     t = rng.standard_normal((B, H, W, 3)).astype(np.float32)
     with sbp.Cnn(H, W, B) as net:
         vec = _small_params(7).astype(np.float32)
@@ -81,7 +81,7 @@ def test_gpu_training_fits_a_batch(sbp):
 
     B, H, W = 4, 24, 24
     rng = np.random.default_rng(5)
-    x = rng.standard_normal((B, H, W, 4)).astype(np.float32)
+    x = rng.standard_normal((B, H, W, N.IN_REAL)).astype(np.float32)
     # a target the network can represent: a smoothed function of the inputs
     t = (0.3 * x[..., :3] + 0.1 * np.roll(x[..., 1:4], 1, axis=1)).astype(np.float32)
     with sbp.Cnn(H, W, B) as net:

@@ -19,11 +19,11 @@ def test_learned_correction_beats_plain_coarse_solve(sbp):
 
     s = _small()
     sv = learned.Solvers(s)
-    X, Y, scale = learned.make_dataset(sv, range(1000, 1024), windows=6, keep=3)
+    X, Y, scales = learned.make_dataset(sv, range(1000, 1024), windows=6, keep=3)
     with sbp.Cnn(2 * s.nbc, s.nxc, 8) as net:
         losses = learned.train(net, X, Y, epochs=25, batch=8, lr=2e-3)
         assert np.mean(losses[-10:]) < 0.5 * np.mean(losses[:10])
-        solver = learned.LearnedSolver(sv, net, scale)
+        solver = learned.LearnedSolver(sv, net, scales)
         res = learned.evaluate(sv, solver, range(5000, 5004), windows=6)
     assert np.mean(res["learned"]) < np.mean(res["coarse"])
 
@@ -37,32 +37,52 @@ def test_energy_guard_falls_back_to_fine_solve(sbp):
         p = net.get_params()
         rng = np.random.default_rng(0)
         net.set_params((p + 5.0 * rng.standard_normal(p.size)).astype(np.float32))  # corrupted weights
-        solver = learned.LearnedSolver(sv, net, scale=1.0)
+        solver = learned.LearnedSolver(sv, net, learned.Scales())
         res = learned.evaluate(sv, solver, [5000], windows=3)
     assert solver.fallbacks == 1
     assert res["learned"][0] == 0.0  # the answer came from the fine solve, the judge itself
 
 
+def _features_np(q_aos, rho, K, nx, ny, nb):
+    """Numpy restatement of sbp_cnn_features (inv_scale 1)."""
+    st = q_aos.reshape(ny, nx, 3)
+    z = np.sqrt(rho * K).reshape(ny, nx)
+    q = np.stack([z * st[..., 0], z * st[..., 1], st[..., 2]], axis=-1)
+    f = np.zeros((ny, nx, 24))
+    i1 = np.clip(np.arange(nx), 1, nx - 2)
+    i2 = np.clip(np.arange(nx), 2, nx - 3)
+    f[:, :, 0:3] = q[:, i1 - 1] - 2 * q[:, i1] + q[:, i1 + 1]
+    f[:, :, 6:9] = q[:, i2 - 2] - 4 * q[:, i2 - 1] + 6 * q[:, i2] - 4 * q[:, i2 + 1] + q[:, i2 + 2]
+    for b in range(ny // nb):
+        rows = slice(b * nb, (b + 1) * nb)
+        r1 = np.clip(np.arange(nb), 1, nb - 2) + b * nb
+        r2 = np.clip(np.arange(nb), 2, nb - 3) + b * nb
+        f[rows, :, 3:6] = q[r1 - 1] - 2 * q[r1] + q[r1 + 1]
+        f[rows, :, 9:12] = q[r2 - 2] - 4 * q[r2 - 1] + 6 * q[r2] - 4 * q[r2 + 1] + q[r2 + 2]
+        f[rows, :, 12:24] = (1.0 if b == 0 else -1.0) * f[rows, :, 0:12]
+    return f.reshape(-1, 24)
+
+
 def test_features_and_zero_state_gives_zero_correction(sbp):
-    """Features are (u, v, p, p log(rho)/log 4) / s; a trained network (biases held at zero)
-    maps the zero state to an exactly zero correction."""
+    """Features are undivided second and fourth differences of (Z u, Z v, p) within each block
+    plus a layer-tagged copy; a trained network (biases held at zero) maps the zero state to an
+    exactly zero correction."""
     import learned
     import torch
 
     s = _small()
     sv = learned.Solvers(s)
-    x0, y0, w, a = learned.trajectory_params(5000)
-    st = torch.from_numpy(learned.pulse_state(s.nxc, s.nbc, x0, y0, w, a)).to(sv.dev)
-    x = sv.features(st).view(-1, 4).cpu().numpy()
-    q = st.view(-1, 3).cpu().numpy()
-    rho = sv.rho_c.cpu().numpy()
-    expect = np.concatenate([q, (q[:, 2] * np.log(rho) / np.log(4.0))[:, None]], axis=1)
-    np.testing.assert_allclose(x, expect.astype(np.float32), rtol=1e-6, atol=1e-30)
-    X, Y, scale = learned.make_dataset(sv, range(1000, 1004), windows=4, keep=2)
+    rng = np.random.default_rng(3)
+    st = torch.from_numpy(rng.standard_normal(sv.npc * 3)).to(sv.dev)
+    x = sv.features(st).view(-1, 24).cpu().numpy()
+    expect = _features_np(st.cpu().numpy(), sv.rho_c.cpu().numpy(), sv.K_c.cpu().numpy(), s.nxc, 2 * s.nbc, s.nbc)
+    np.testing.assert_allclose(x, expect.astype(np.float32), rtol=1e-5, atol=1e-5)
+    X, Y, scales = learned.make_dataset(sv, range(1000, 1004), windows=4, keep=2)
     with sbp.Cnn(2 * s.nbc, s.nxc, 2) as net:
         learned.train(net, X, Y, epochs=3, batch=2, lr=2e-3)
-        zero = torch.zeros(sv.npc * 4, dtype=torch.float32, device=sv.dev)
+        zero = torch.zeros(sv.npc * 24, dtype=torch.float32, device=sv.dev)
         out = torch.full((sv.npc * 3,), 7.0, dtype=torch.float32, device=sv.dev)
+        torch.cuda.synchronize()
         net.forward(zero.data_ptr(), 1, out.data_ptr())
         torch.cuda.synchronize()
     assert float(out.abs().max()) == 0.0
