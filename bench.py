@@ -56,16 +56,18 @@ def parse():
     ap.add_argument("--bc", default="characteristic", choices=["characteristic", "free_surface"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--study", default=None, choices=["precision", "batched", "learned"],
+    ap.add_argument("--study", default=None, choices=["precision", "batched", "learned", "rk45"],
                     help="precision: variable rho, K (seeded Fourier fields) to --t-end in FP64 and in "
                          "compensated FP32; prints errors of FP32 against FP64 and both wall times. "
-                         "batched: 512 uneven wave/advection instances in one batch, FP64 and FP32")
+                         "batched: 512 uneven wave/advection instances in one batch, FP64 and FP32. "
+                         "rk45: adaptive RKF45 (ts_rk45) on the bench's wave problem to --rk45-t-end")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--trajectories", type=int, default=2000, help="learned: training trajectories")
     ap.add_argument("--epochs", type=int, default=30, help="learned: training epochs per round")
     ap.add_argument("--rollout-rounds", type=int, default=2,
                     help="learned: rounds of training on windows started on the corrected solve's states")
     ap.add_argument("--t-end", type=float, default=1.0)
+    ap.add_argument("--rk45-t-end", type=float, default=0.25, help="rk45: final time")
     return ap.parse_args()
 
 
@@ -330,6 +332,75 @@ def run_batched_study(args):
     print(json.dumps(out), flush=True)
 
 
+def run_rk45_study(args):
+    """Adaptive RKF45 (the reference's ts_rk45: PETSc TSRK5F + TSADAPTBASIC) on the bench's
+    problem: 2D wave, rho = K = 1, characteristic SAT, Gaussian pulse w = 0.05 at the origin,
+    --grid^2 points, order --order, FP64, default tolerances (atol = rtol = 1e-4), dt0 = 0.2 h,
+    from t = 0 to --rk45-t-end. Reports the attempts, the wall time (host loop included), RHS
+    point-evaluations/s and the bytes an attempt moves against measured HBM bandwidth; beside it
+    fixed-step RK4 at dt = 0.2 h over the same interval, and the oracle's restatement on all host
+    cores for a bounded number of attempts of the same run (its step limit)."""
+    import numpy as np
+
+    import build as gpu_build
+    import sbpgpu
+
+    gpu_build.build()
+    n, order, t_end = args.grid, args.order, args.rk45_t_end
+    h = 2.0 / (n - 1)
+    v0 = initial_state(n)
+    with sbpgpu.Context(sbpgpu.WAVE_HOM_2D, order, n, n, bc=sbpgpu.BC_CHARACTERISTIC) as ctx:
+        ctx.set_state(v0)
+        ctx.rk45_resident(0.0, 4 * 0.2 * h, 0.2 * h)  # warm-up: graph capture
+        ctx.set_state(v0)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        st = ctx.rk45_resident(0.0, t_end, 0.2 * h)
+        t_rk45 = time.perf_counter() - t0
+        nsteps, dt = sbpgpu.rk4_nsteps(t_end, 0.2 * h)
+        ctx.set_state(v0)
+        ctx.step_resident(0.0, dt, 2)  # warm-up
+        ctx.set_state(v0)
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.step_resident(0.0, dt, nsteps)
+        ctx.synchronize()
+        t_rk4 = time.perf_counter() - t0
+    attempts = st["accepted"] + st["rejected"]
+    evals = 6.0 * n * n * attempts
+    # scalars moved per point and attempt: 6 RHS (input + k), 5 stage combinations (u, k1..ks, w),
+    # candidate (u, k1..k6, unew) and, when accepted, the copy unew -> u
+    vectors = 12 + sum(s + 2 for s in range(1, 6)) + 8 + 2.0 * st["accepted"] / max(attempts, 1)
+    bytes_attempt = vectors * 3 * 8 * n * n
+    peak, src = measured_peaks()
+    line = {"study": "rk45", "grid": [n, n], "order": order, "t_end": t_end, "dt0": 0.2 * h,
+            "tolerances": {"atol": 1e-4, "rtol": 1e-4}, "accepted": st["accepted"], "rejected": st["rejected"],
+            "dt_last": st["dt_next"], "seconds": t_rk45, "rhs_point_evals_per_s": evals / t_rk45,
+            "bytes_per_point_attempt": vectors * 24,
+            "achieved_gbs": bytes_attempt * attempts / t_rk45 / 1e9, "peak_gbs": peak, "peak_source": src,
+            "frac": bytes_attempt * attempts / t_rk45 / 1e9 / peak,
+            "rk4_fixed": {"dt": dt, "steps": nsteps, "seconds": t_rk4}}
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        O.build()
+        port = O.Port(O.PORT_OPT_SO)
+        threads = os.cpu_count() or 1
+        port.set_threads(threads)
+        ones = np.ones(n * n)
+        pb = O.Problem(O.WAVE_VAR_2D, order, n, n, rho=ones, K=ones, bc=O.BC_CHARACTERISTIC)
+        k = max(1, min(attempts, 8))
+        t0 = time.perf_counter()
+        _, cst = port.rk45(pb, v0, 0.0, t_end, 0.2 * h, max_steps=k)
+        t_cpu = time.perf_counter() - t0
+        done = cst["accepted"] + cst["rejected"]
+        line["cpu"] = {"rhs_point_evals_per_s": 6.0 * n * n * done / t_cpu, "attempts": done, "seconds": t_cpu,
+                       "cores": threads, "kind": "port",
+                       "sample": f"the first {done} attempts of the same run (oracle step limit)"}
+    print(json.dumps(line), flush=True)
+
+
 def run_learned_study(args):
     """Two-layer problem (rho, K x4 across y = 0): coarse 257 x 2*129 order-4 solve corrected by the
     network every 4 steps, trained on restricted fine (1025 x 2*513, FP64) trajectories with seeded
@@ -346,7 +417,7 @@ def run_learned_study(args):
 
     gpu_build.build()
     s = learned.Setup()
-    sv = learned.Solvers(s)
+    sv = learned.Solvers(s, mid=True)
     t0 = time.perf_counter()
     seeds = range(1000, 1000 + args.trajectories)
     X, Y, scales = learned.normalize(*learned.collect(sv, seeds, 16, keep=2))
@@ -382,7 +453,10 @@ def run_learned_study(args):
            "rel_l2_coarse_median": float(np.median(res["coarse"])),
            "rel_l2_learned_median": float(np.median(res["learned"])),
            "learned_better": int(np.sum(np.array(res["learned"]) < np.array(res["coarse"]))),
+           "mid_grid": [2 * s.nxc - 1, 2 * (2 * s.nbc - 1)], "rel_l2_mid": float(np.mean(res["mid"])),
+           "rel_l2_mid_median": float(np.median(res["mid"])),
            "seconds_fine": res["t_fine"], "seconds_coarse": res["t_coarse"], "seconds_learned": res["t_learned"],
+           "seconds_mid": res["t_mid"],
            "fallbacks": solver.fallbacks, "held_out": 100}
     print(json.dumps(out), flush=True)
 
@@ -397,6 +471,9 @@ def main():
         return
     if args.study == "batched":
         run_batched_study(args)
+        return
+    if args.study == "rk45":
+        run_rk45_study(args)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

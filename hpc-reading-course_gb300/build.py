@@ -47,6 +47,7 @@ def units():
     out.append(("petsc_io.o", "petsc_io.cpp", []))
     out.append(("batch_runtime.o", "batch_runtime.cpp", ["-x", "cu"]))
     out.append(("cnn.o", "cnn.cu", []))
+    out.append(("rk45.o", "rk45.cu", []))
     return out
 
 

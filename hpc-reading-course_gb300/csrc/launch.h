@@ -130,6 +130,40 @@ template <typename T>
 cudaError_t launch_hnorm(const T* soa, int nx, int ny, int dofs, long long pitch, long long plane, int order,
                          double hx, double hy, int ysplit, double* partial, double* out, cudaStream_t s);
 
+// ---------------------------------------------------------------- RK45 (rk45.cu)
+// Buffers of the adaptive Runge-Kutta-Fehlberg 4(5) integrator (FP64 SoA planes
+// of the context's layout).
+struct Rk45Buffers {
+  int nx, ny, dofs;
+  long long pitch, plane;
+  double* u;        // current solution
+  double* w;        // stage input
+  double* k[6];     // stage derivatives
+  double* unew;     // candidate solution of the attempt
+  double* partial;  // kReduceBlocks partial sums of the weighted error
+};
+
+enum Rk45Status : int { RK45_OK = 0, RK45_STEP_LIMIT = 1, RK45_NONFINITE = 2, RK45_REJECTED = 3 };
+
+// Controller state in device memory; the stage kernels read t and h (adjacent,
+// in this order) for time-dependent forcing, and `done` to skip their work.
+struct Rk45Ctrl {
+  double t, h;  // time reached, step of the next attempt
+  double t_end, atol, rtol, safety, reject_safety, clip_lo, clip_hi, dt_min, dt_max;
+  double wlte;  // weighted error of the last attempt
+  double n;     // scalars in the error norm
+  long long accepted, rejected, max_steps;
+  int max_reject, rejects_in_row;
+  int done;          // stop: every kernel of later attempts returns at entry
+  int copy_pending;  // the last attempt was accepted: its solution replaces u
+  int last_accepted, final_step, status;
+};
+
+// w = u + h sum_{j<=stage} a[stage][j] k_j (the input of stage `stage` + 1).
+cudaError_t launch_rk45_combine(int stage, const Rk45Buffers& b, const Rk45Ctrl* ctrl, cudaStream_t s);
+// Candidate solution and error partial sums, the controller, and the accept copy.
+cudaError_t launch_rk45_finish(const Rk45Buffers& b, Rk45Ctrl* ctrl, cudaStream_t s);
+
 // FP64 fused-multiply-add throughput probe: each thread runs `iters`
 // iterations of 8 independent DFMA chains; result written to out[0].
 cudaError_t launch_dfma_probe(double* out, int blocks, int threads, int iters, cudaStream_t s);

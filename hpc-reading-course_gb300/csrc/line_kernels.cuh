@@ -28,6 +28,7 @@ template <typename T> struct LineParams {
   int bc;             // 0: none, 1: the reference's boundary treatment
   int compensated;
   T c_acc, c_w;
+  const int* skip;  // non-null and set: the kernel returns at entry
   int* err;
 };
 
@@ -113,6 +114,7 @@ __device__ __forceinline__ void line_point(const LineParams<T>& prm, const T* __
 
 template <typename T, int ORD, int KIND, int STAGE>
 __global__ void __launch_bounds__(256) line_stage_kernel(const __grid_constant__ LineParams<T> prm) {
+  if (prm.skip && *prm.skip) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= prm.nx || j >= prm.ny) return;

@@ -68,6 +68,11 @@ struct sbp_ctx {
   double *rho64 = nullptr, *k64 = nullptr;   // WAVE_VAR: nx*ny FP64
   int* err = nullptr;
   WaveMaps maps_un{}, maps_wa{}, maps_wb{};
+  // adaptive RK45 (FP64; allocated on first use)
+  double* rk_k[6] = {};
+  double* rk_unew = nullptr;
+  Rk45Ctrl* rk_ctrl = nullptr;
+  cudaGraphExec_t rk_graph = nullptr;
   std::map<long long, cudaGraphExec_t> graphs;
   double graph_dt = 0.0;
   long long launches = 0;
@@ -216,7 +221,7 @@ int line_kind(const sbp_ctx* ctx) {
 // evaluated on; `in_maps` its TMA descriptors (2D wave only).
 template <typename T>
 int launch_stage(sbp_ctx* ctx, int stage, int rk, double t, double dt, void* in, const WaveMaps* in_maps,
-                 void* kout, int bc_on) {
+                 void* kout, int bc_on, const Rk45Ctrl* ctl = nullptr, double tc = 0.0) {
   T c_acc = 0, c_w = 0;
   if (stage == ST_FIRST) {
     c_acc = (T)(dt / 6);
@@ -239,6 +244,11 @@ int launch_stage(sbp_ctx* ctx, int stage, int rk, double t, double dt, void* in,
     p.c_acc = c_acc;
     p.c_w = c_w;
     p.t = t;
+    if (ctl) {  // adaptive integrator: stage time and stop flag from device memory
+      p.tctl = &ctl->t;
+      p.tc = tc;
+      p.skip = &ctl->done;
+    }
     if (!bc_on) p.bc = BC_NONE;
     CK(launch_wave<T>(ctx->d.order, wave_kind(ctx), stage, *in_maps, p, ctx->stream));
   } else {
@@ -252,6 +262,7 @@ int launch_stage(sbp_ctx* ctx, int stage, int rk, double t, double dt, void* in,
     p.c_acc = c_acc;
     p.c_w = c_w;
     p.bc = bc_on;
+    if (ctl) p.skip = &ctl->done;
     CK(launch_line<T>(ctx->d.order, line_kind(ctx), stage, p, ctx->stream));
   }
   ctx->launches++;
@@ -395,9 +406,103 @@ int rhs_impl(sbp_ctx* ctx, double t, const double* src, double* dst, int where, 
   return check_device_errors(ctx);
 }
 
+// ---------------------------------------------------------------- adaptive RK45
+Rk45Buffers rk45_buffers(sbp_ctx* ctx) {
+  Rk45Buffers b;
+  std::memset(&b, 0, sizeof(b));
+  b.nx = (int)ctx->nx;
+  b.ny = (int)ctx->ny;
+  b.dofs = ctx->dofs;
+  b.pitch = ctx->pitch;
+  b.plane = ctx->plane;
+  b.u = (double*)ctx->un;
+  b.w = (double*)ctx->wa;
+  for (int s = 0; s < 6; s++) b.k[s] = ctx->rk_k[s];
+  b.unew = ctx->rk_unew;
+  b.partial = ctx->partial;
+  return b;
+}
+
+int rk45_prepare(sbp_ctx* ctx) {
+  if (ctx->rk_ctrl) return SBP_OK;
+  const size_t bytes = (size_t)ctx->dofs * ctx->plane * sizeof(double);
+  for (int s = 0; s < 6; s++) CK(cudaMalloc((void**)&ctx->rk_k[s], bytes));
+  CK(cudaMalloc((void**)&ctx->rk_unew, bytes));
+  CK(cudaMemsetAsync(ctx->rk_unew, 0, bytes, ctx->stream));  // row padding stays zero
+  CK(cudaMalloc((void**)&ctx->rk_ctrl, sizeof(Rk45Ctrl)));
+  return SBP_OK;
+}
+
+// Fehlberg stage times c_s (the abscissae of the tableau in rk45.cu).
+constexpr double kRkfC[6] = {0.0, 1.0 / 4, 3.0 / 8, 12.0 / 13, 1.0, 1.0 / 2};
+
+// One attempted step: six RHS evaluations with the stage combinations between
+// them, then the candidate solution, the controller and the accept copy.
+int enqueue_rk45_attempt(sbp_ctx* ctx) {
+  const Rk45Buffers b = rk45_buffers(ctx);
+  for (int s = 0; s < 6; s++) {
+    void* in = s == 0 ? ctx->un : ctx->wa;
+    const WaveMaps* m = s == 0 ? &ctx->maps_un : &ctx->maps_wa;
+    int rc = launch_stage<double>(ctx, ST_RHS, 0, 0.0, 0.0, in, m, ctx->rk_k[s], 1, ctx->rk_ctrl, kRkfC[s]);
+    if (rc) return rc;
+    if (s < 5) {
+      CK(launch_rk45_combine(s + 1, b, ctx->rk_ctrl, ctx->stream));
+      ctx->launches++;
+    }
+  }
+  CK(launch_rk45_finish(b, ctx->rk_ctrl, ctx->stream));
+  ctx->launches += 3;
+  return SBP_OK;
+}
+
+constexpr int kRk45Chunk = 8;            // attempts per graph launch
+constexpr int kRk45LaunchesPerTry = 14;  // 6 RHS + 5 combine + final, control, accept
+
+int rk45_chunk_graph(sbp_ctx* ctx) {
+  if (ctx->rk_graph) return SBP_OK;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  const long long before = ctx->launches;
+  int rc = SBP_OK;
+  for (int a = 0; a < kRk45Chunk && rc == SBP_OK; a++) rc = enqueue_rk45_attempt(ctx);
+  cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+  ctx->launches = before;  // captured, not yet run
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  CK(ce);
+  cudaError_t ie = cudaGraphInstantiate(&ctx->rk_graph, g, 0);
+  cudaGraphDestroy(g);
+  CK(ie);
+  return SBP_OK;
+}
+
+// First step under the landing rule of the controller (rk45.cu).
+void rk45_first_step(double t0, double t_end, double dt0, double* h, int* fin) {
+  const double hmax = t_end - t0;
+  *h = dt0;
+  *fin = 0;
+  if (dt0 >= hmax) {
+    *h = hmax;
+    *fin = 1;
+    return;
+  }
+  if (2.0 * dt0 > hmax) *h = 0.5 * hmax;
+  if (1.01 * dt0 > hmax) {
+    *h = hmax;
+    *fin = 1;
+  }
+}
+
 void release(sbp_ctx* ctx) {
   if (!ctx) return;
   drop_graphs(ctx);
+  if (ctx->rk_graph) cudaGraphExecDestroy(ctx->rk_graph);
+  for (int s = 0; s < 6; s++)
+    if (ctx->rk_k[s]) cudaFree(ctx->rk_k[s]);
+  if (ctx->rk_unew) cudaFree(ctx->rk_unew);
+  if (ctx->rk_ctrl) cudaFree(ctx->rk_ctrl);
   void* bufs[] = {ctx->un, ctx->acc, ctx->wa, ctx->wb, ctx->comp, ctx->io, ctx->partial, ctx->red,
                   ctx->rinv, ctx->rho64, ctx->k64, ctx->err};  // kmod lives inside the rinv allocation
   for (void* b : bufs)
@@ -657,6 +762,89 @@ int sbp_hnorm(sbp_ctx* ctx, double* hn) {
   CK(cudaStreamSynchronize(ctx->stream));
   *hn = std::sqrt(h);
   return SBP_OK;
+}
+
+void sbp_rk45_default_opts(sbp_rk45_opts* o) {
+  if (!o) return;
+  o->atol = 1e-4;
+  o->rtol = 1e-4;
+  o->safety = 0.9;
+  o->reject_safety = 0.5;
+  o->clip_lo = 0.1;
+  o->clip_hi = 10.0;
+  o->dt_min = 1e-20;
+  o->dt_max = 1e50;
+  o->max_steps = 10000000;
+  o->max_reject = 10;
+}
+
+int sbp_rk45_resident(sbp_ctx* ctx, double t0, double t_end, double dt0, const sbp_rk45_opts* opts,
+                      sbp_rk45_stats* stats) {
+  if (!ctx) return SBP_ERR_INVALID;
+  if (ctx->fp32) return fail(ctx, SBP_ERR_UNSUPPORTED, "the adaptive RK45 integrator runs on FP64 contexts");
+  if (!(dt0 > 0) || !(t_end >= t0)) return fail(ctx, SBP_ERR_INVALID, "need dt0 > 0 and t_end >= t0");
+  sbp_rk45_opts o;
+  sbp_rk45_default_opts(&o);
+  if (opts) o = *opts;
+  if (!(o.atol >= 0 && o.rtol >= 0 && o.atol + o.rtol > 0) || !(o.safety > 0) || !(o.reject_safety > 0) ||
+      !(o.clip_lo > 0 && o.clip_hi >= o.clip_lo) || !(o.dt_min > 0 && o.dt_max >= o.dt_min) || o.max_steps < 1 ||
+      o.max_reject < 1)
+    return fail(ctx, SBP_ERR_INVALID, "invalid RK45 options");
+  CK(cudaSetDevice(ctx->d.device));
+  int rc;
+  if ((rc = rk45_prepare(ctx))) return rc;
+  if ((rc = rk45_chunk_graph(ctx))) return rc;
+  Rk45Ctrl c;
+  std::memset(&c, 0, sizeof(c));
+  c.t = t0;
+  c.t_end = t_end;
+  c.atol = o.atol;
+  c.rtol = o.rtol;
+  c.safety = o.safety;
+  c.reject_safety = o.reject_safety;
+  c.clip_lo = o.clip_lo;
+  c.clip_hi = o.clip_hi;
+  c.dt_min = o.dt_min;
+  c.dt_max = o.dt_max;
+  c.max_steps = o.max_steps;
+  c.max_reject = o.max_reject;
+  c.n = (double)(ctx->dofs * ctx->nx * ctx->ny);
+  c.last_accepted = 1;
+  c.status = RK45_OK;
+  rk45_first_step(t0, t_end, std::fmin(dt0, o.dt_max), &c.h, &c.final_step);
+  c.done = (t_end > t0) ? 0 : 1;
+  CK(cudaMemcpyAsync(ctx->rk_ctrl, &c, sizeof(c), cudaMemcpyHostToDevice, ctx->stream));
+  // every chunk advances the attempt count by kRk45Chunk until the controller stops
+  const long long max_chunks = o.max_steps / kRk45Chunk + 2;
+  for (long long chunk = 0; !c.done; chunk++) {
+    if (chunk >= max_chunks) return fail(ctx, SBP_ERR_DEVICE, "the RK45 controller did not stop");
+    CK(cudaGraphLaunch(ctx->rk_graph, ctx->stream));
+    ctx->launches += (long long)kRk45Chunk * kRk45LaunchesPerTry;
+    CK(cudaMemcpyAsync(&c, ctx->rk_ctrl, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
+    if ((rc = check_device_errors(ctx))) return rc;  // synchronizes the stream
+  }
+  if (stats) {
+    stats->accepted = c.accepted;
+    stats->rejected = c.rejected;
+    stats->t = c.t;
+    stats->dt_next = c.h;
+    stats->wlte = c.wlte;
+    stats->status = c.status;
+  }
+  if (c.status != RK45_OK) {
+    static const char* why[] = {"", "the RK45 step limit was reached", "the RK45 error norm was not finite",
+                                "too many RK45 rejections in a row"};
+    return fail(ctx, SBP_ERR_DIVERGED, why[c.status]);
+  }
+  return SBP_OK;
+}
+
+int sbp_ts_rk45(sbp_ctx* ctx, double t_end, double dt, double* v, int where) {
+  if (!ctx) return SBP_ERR_INVALID;
+  int rc;
+  if ((rc = sbp_set_state(ctx, v, where))) return rc;
+  if ((rc = sbp_rk45_resident(ctx, 0.0, t_end, dt, nullptr, nullptr))) return rc;
+  return sbp_get_state(ctx, v, where);
 }
 
 int sbp_get_stream(const sbp_ctx* ctx, void** stream) {

@@ -54,6 +54,9 @@ template <typename T> struct WaveParams {
   int ysplit;         // 0: one block; else rows [0,ysplit) and [ysplit,ny) are two blocks
                       // sharing an interface line (WK_VAR only)
   double t, xl0, xl1, hix, hiy;  // WK_MMS: stage time and grid geometry
+  const double* tctl;  // WK_MMS under the adaptive integrator: stage time tctl[0] + tc * tctl[1]
+  double tc;
+  const int* skip;     // non-null and set: the kernel returns at entry
   int* err;
 };
 
@@ -310,7 +313,8 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
         const double PI = 3.14159265358979323846264;
         const double xx = mms_x(prm.xl0, i, prm.hix), yy = mms_x(prm.xl1, j, prm.hiy);
         const double ri = 1. / (2 + xx * yy);
-        const double ct = cos(5 * PI * prm.t);
+        const double ts = prm.tctl ? __dadd_rn(prm.tctl[0], __dmul_rn(prm.tc, prm.tctl[1])) : prm.t;
+        const double ct = cos(5 * PI * ts);
         const double fu = -(3 * PI * ct * cos(3 * PI * xx) * sin(4 * PI * yy) * (xx * yy + 1)) / (xx * yy + 2);
         const double fv = -(4 * PI * ct * cos(4 * PI * yy) * sin(3 * PI * xx) * (xx * yy + 1)) / (xx * yy + 2);
         ku = (T)(ri * (double)dxp + fu);
@@ -370,6 +374,7 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
   using Tile = WaveTile<T, ORD, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR, wave_ring<T, KIND>()>;
   constexpr int TY = Tile::TY, HX = Tile::HX, HY = Tile::HY, NST = Tile::NST;
   extern __shared__ __align__(128) unsigned char smem[];
+  if (prm.skip && *prm.skip) return;  // uniform over the grid: set before this launch
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
   uint64_t* empty = full + NST;
 

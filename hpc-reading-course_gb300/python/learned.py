@@ -106,9 +106,10 @@ def _ready():
 
 
 class Solvers:
-    """The fine and coarse two-block contexts plus device buffers."""
+    """The fine and coarse two-block contexts plus device buffers; with `mid`, also a plain solve
+    at twice the coarse resolution (for the time-against-error comparison)."""
 
-    def __init__(self, s: Setup, device: int = 0):
+    def __init__(self, s: Setup, device: int = 0, mid: bool = False):
         self.s = s
         self.dev = torch.device(f"cuda:{device}")
         rf, kf = two_layer_fields(s.nxf, s.nbf, s.ratio)
@@ -118,6 +119,13 @@ class Solvers:
                                    device=device)
         self.coarse = sbpgpu.Context(sbpgpu.WAVE_2BLOCK_2D, s.order, s.nxc, 2 * s.nbc, rho=rc, K=kc, bc=bc,
                                      device=device)
+        self.mid = None
+        if mid:
+            nxm, nbm = 2 * (s.nxc - 1) + 1, 2 * (s.nbc - 1) + 1
+            rm, km = two_layer_fields(nxm, nbm, s.ratio)
+            self.mid = sbpgpu.Context(sbpgpu.WAVE_2BLOCK_2D, s.order, nxm, 2 * nbm, rho=rm, K=km, bc=bc,
+                                      device=device)
+            self.mid_shape = (nxm, nbm)
         self.rho_c = torch.from_numpy(rc).to(self.dev)
         self.K_c = torch.from_numpy(kc).to(self.dev)
         self.npc = s.nxc * 2 * s.nbc
@@ -151,6 +159,20 @@ class Solvers:
         self.fine.step_resident(0.0, self.s.dtf, n)
         self.fine.synchronize()
         return self.fine_state()
+
+    def mid_solve(self, fine_aos, windows: int):
+        """Plain solve at twice the coarse resolution from the fine state (restricted by 2), over
+        `windows` coarse windows, restricted to the coarse grid."""
+        s = self.s
+        nxm, nbm = self.mid_shape
+        st = fine_aos.view(2, s.nbf, s.nxf, 3)[:, ::2, ::2, :].contiguous().view(-1)
+        _ready()
+        self.mid.set_state_ptr(st.data_ptr(), sbpgpu.DEVICE)
+        self.mid.step_resident(0.0, s.dtc / 2, 2 * s.window * windows)
+        self.mid.synchronize()
+        out = torch.empty(nxm * 2 * nbm * 3, dtype=torch.float64, device=self.dev)
+        self.mid.get_state_ptr(out.data_ptr(), sbpgpu.DEVICE)
+        return out.view(2, nbm, nxm, 3)[:, ::2, ::2, :].contiguous().view(-1)
 
     def features(self, coarse_aos, inv_scale: float = 1.0):
         s = self.s
@@ -302,9 +324,13 @@ class LearnedSolver:
 
 def evaluate(sv: Solvers, solver: LearnedSolver, seeds, windows: int):
     """Relative L2 errors against the restricted fine solution after `windows` windows, for
-    the plain coarse solve and the corrected one, and the wall time of each form."""
+    the plain coarse solve and the corrected one (and the plain solve at twice the coarse
+    resolution, if `sv` has it), and the wall time of each form."""
     s = sv.s
-    out = {"coarse": [], "learned": [], "t_fine": 0.0, "t_coarse": 0.0, "t_learned": 0.0}
+    out = {"coarse": [], "learned": [], "mid": [], "t_fine": 0.0, "t_coarse": 0.0, "t_learned": 0.0, "t_mid": 0.0}
+    forms = [("coarse", solver.run_plain), ("learned", solver.run)]
+    if sv.mid is not None:
+        forms.append(("mid", sv.mid_solve))
     for seed in seeds:
         x0, y0, w, a = trajectory_params(seed)
         fine0 = torch.from_numpy(pulse_state(s.nxf, s.nbf, x0, y0, w, a)).to(sv.dev)
@@ -313,7 +339,7 @@ def evaluate(sv: Solvers, solver: LearnedSolver, seeds, windows: int):
         fine = sv.fine_steps_from(fine0, 4 * s.window * windows)
         out["t_fine"] += time.perf_counter() - t0
         ref = sv.restrict(fine)
-        for key, fn in (("coarse", solver.run_plain), ("learned", solver.run)):
+        for key, fn in forms:
             t0 = time.perf_counter()
             st = fn(fine0, windows)
             torch.cuda.synchronize()

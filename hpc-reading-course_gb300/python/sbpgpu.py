@@ -40,9 +40,22 @@ EXPORTS = ("sbp_create", "sbp_destroy", "sbp_last_error", "sbp_dofs", "sbp_rhs",
            "sbp_batch_tile_height", "sbp_batch_get_stream", "sbp_batch_points", "sbp_batch_launch_count",
            "sbp_cnn_create", "sbp_cnn_destroy", "sbp_cnn_last_error", "sbp_cnn_param_count", "sbp_cnn_init",
            "sbp_cnn_get_params", "sbp_cnn_set_params", "sbp_cnn_forward", "sbp_cnn_gradients", "sbp_cnn_train_step",
-           "sbp_cnn_features", "sbp_cnn_correct", "sbp_cnn_launch_count")
+           "sbp_cnn_features", "sbp_cnn_correct", "sbp_cnn_launch_count",
+           "sbp_rk45_default_opts", "sbp_rk45_resident", "sbp_ts_rk45")
 
 _dp = C.POINTER(C.c_double)
+ERR_DIVERGED = -6
+
+
+class Rk45Opts(C.Structure):
+    _fields_ = [("atol", C.c_double), ("rtol", C.c_double), ("safety", C.c_double), ("reject_safety", C.c_double),
+                ("clip_lo", C.c_double), ("clip_hi", C.c_double), ("dt_min", C.c_double), ("dt_max", C.c_double),
+                ("max_steps", C.c_longlong), ("max_reject", C.c_int)]
+
+
+class Rk45Stats(C.Structure):
+    _fields_ = [("accepted", C.c_longlong), ("rejected", C.c_longlong), ("t", C.c_double), ("dt_next", C.c_double),
+                ("wlte", C.c_double), ("status", C.c_int)]
 
 
 class Desc(C.Structure):
@@ -95,6 +108,11 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.sbp_set_state.argtypes = [P, C.c_void_p, C.c_int]
     L.sbp_get_state.argtypes = [P, C.c_void_p, C.c_int]
     L.sbp_rk4_resident.argtypes = [P, C.c_double, C.c_double, C.c_longlong]
+    L.sbp_rk45_default_opts.argtypes = [C.POINTER(Rk45Opts)]
+    L.sbp_rk45_default_opts.restype = None
+    L.sbp_rk45_resident.argtypes = [P, C.c_double, C.c_double, C.c_double, C.POINTER(Rk45Opts),
+                                    C.POINTER(Rk45Stats)]
+    L.sbp_ts_rk45.argtypes = [P, C.c_double, C.c_double, C.c_void_p, C.c_int]
     L.sbp_synchronize.argtypes = [P]
     L.sbp_error_norms.argtypes = [P, C.c_void_p, C.c_int, _dp, _dp]
     L.sbp_hnorm.argtypes = [P, _dp]
@@ -304,6 +322,26 @@ class Context:
 
     def step_resident(self, t0: float, dt: float, nsteps: int):
         self._check(self._L.sbp_rk4_resident(self._h, t0, dt, nsteps))
+
+    def rk45_resident(self, t0: float, t_end: float, dt0: float, check: bool = True, **opts) -> dict:
+        """Adaptive RKF45 on the resident state (sbp_rk45_resident); opts override the defaults.
+        Returns the stats as a dict; with check=False a stopped run returns its stats too."""
+        o = Rk45Opts()
+        self._L.sbp_rk45_default_opts(C.byref(o))
+        for k, val in opts.items():
+            setattr(o, k, val)
+        st = Rk45Stats()
+        rc = self._L.sbp_rk45_resident(self._h, t0, t_end, dt0, C.byref(o), C.byref(st))
+        if rc and (check or rc != ERR_DIVERGED):
+            self._check(rc)
+        out = {f: getattr(st, f) for f, _ in Rk45Stats._fields_}
+        out["rc"] = rc
+        return out
+
+    def ts_rk45(self, v: np.ndarray, t_end: float, dt: float) -> np.ndarray:
+        out = np.array(_host(v), copy=True)
+        self._check(self._L.sbp_ts_rk45(self._h, t_end, dt, out.ctypes.data, HOST))
+        return out
 
     def synchronize(self):
         self._check(self._L.sbp_synchronize(self._h))

@@ -34,6 +34,7 @@ extern "C" {
 #define SBP_ERR_DEVICE (-3)      /* a kernel reported an error (e.g. a bounded wait gave up) */
 #define SBP_ERR_UNSUPPORTED (-4) /* combination not provided (e.g. FP32 manufactured-solution problem) */
 #define SBP_ERR_TOO_LARGE (-5)   /* grid exceeds the static scratch of sbp_wave_rhs_noalloc */
+#define SBP_ERR_DIVERGED (-6)    /* the adaptive integrator stopped before t_end (see sbp_rk45_stats) */
 
 /* Problems: the reference demos plus the variable-coefficient wave system. */
 typedef enum {
@@ -134,6 +135,44 @@ int sbp_error_norms(sbp_ctx* ctx, const double* exact, int where, double* error_
  * single rank applies the left closure weights only; the 2D form is
  * get_norm_2D, a TODO returning -1 in the reference (H_central.h:177-183). */
 int sbp_hnorm(sbp_ctx* ctx, double* hnorm);
+
+/* ---------------------------------------------------------------- adaptive RK45
+ * Runge-Kutta-Fehlberg 4(5) with a basic step-size controller on the
+ * context's device-resident state (FP64 contexts). Replaces ts_rk45
+ * (code/include/time_stepping/ts_rk.h:15, code/src/time_stepping/ts_rk.cpp:41-52),
+ * which runs PETSc's TSRK5F (Fehlberg's pair, advanced with the 5th-order
+ * weights) under TSADAPTBASIC with TS_EXACTFINALTIME_MATCHSTEP and PETSc's
+ * default options. The controller per attempted step h from time t:
+ *   wlte = sqrt(mean over all scalars of ((u5 - u4) / (atol + rtol max(|u5|, |u4|)))^2)
+ *   accept iff wlte <= 1; h' = h clip(safety' wlte^(-1/5), clip_lo, clip_hi)
+ *   (safety' = safety, times reject_safety when this and the previous attempt
+ *   failed), h' in [dt_min, dt_max]; with hmax = t_end - t: h' >= hmax -> hmax,
+ *   otherwise 2 h' > hmax -> hmax/2 and 1.01 h' > hmax -> hmax.
+ * The first attempt uses dt0 under the same landing rule. The run stops when
+ * the attempt that lands on t_end is accepted (t = t_end exactly). */
+typedef struct {
+  double atol, rtol;            /* error tolerances (1e-4, 1e-4) */
+  double safety, reject_safety; /* 0.9, 0.5 */
+  double clip_lo, clip_hi;      /* bounds of the step change factor: 0.1, 10 */
+  double dt_min, dt_max;        /* 1e-20, 1e50 */
+  long long max_steps;          /* attempts (accepted + rejected) allowed: 1e7 */
+  int max_reject;               /* rejections in a row allowed: 10 */
+} sbp_rk45_opts;
+typedef struct {
+  long long accepted, rejected;
+  double t;       /* time reached */
+  double dt_next; /* step the controller proposes next */
+  double wlte;    /* weighted error of the last attempt */
+  int status;     /* 0 done; 1 step limit; 2 non-finite error; 3 rejections in a row */
+} sbp_rk45_stats;
+void sbp_rk45_default_opts(sbp_rk45_opts* opts);
+/* From t0 to t_end on the resident state; opts NULL = defaults, stats may be
+ * NULL. Synchronous. SBP_ERR_DIVERGED when the controller stopped early (the
+ * state then holds the last accepted step). */
+int sbp_rk45_resident(sbp_ctx* ctx, double t0, double t_end, double dt0, const sbp_rk45_opts* opts,
+                      sbp_rk45_stats* stats);
+/* ts_rk45(da, t_end, dt, v, rhs, ctx): from t = 0, default options, in place on v. */
+int sbp_ts_rk45(sbp_ctx* ctx, double t_end, double dt, double* v, int where);
 
 /* The context's CUDA stream (cudaStream_t) and the number of kernels the
  * context has launched so far (graph replays count each kernel node). */

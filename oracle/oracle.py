@@ -86,6 +86,17 @@ class Problem:
         return s
 
 
+class Rk45Opts(C.Structure):
+    _fields_ = [("atol", C.c_double), ("rtol", C.c_double), ("safety", C.c_double), ("reject_safety", C.c_double),
+                ("clip_lo", C.c_double), ("clip_hi", C.c_double), ("dt_min", C.c_double), ("dt_max", C.c_double),
+                ("max_steps", C.c_longlong), ("max_reject", C.c_int)]
+
+
+class Rk45Stats(C.Structure):
+    _fields_ = [("accepted", C.c_longlong), ("rejected", C.c_longlong), ("t", C.c_double), ("dt_next", C.c_double),
+                ("wlte", C.c_double), ("status", C.c_int)]
+
+
 class Port:
     """The C restatement (oracle/sbp_oracle.c)."""
 
@@ -99,6 +110,10 @@ class Port:
             getattr(L, name).restype = C.c_int
         L.orc_bc.argtypes = [P, _dp, _dp]
         L.orc_rk4.argtypes = [P, C.c_double, C.c_double, C.c_longlong, _dp]
+        L.orc_rk45_default_opts.argtypes = [C.POINTER(Rk45Opts)]
+        L.orc_rk45_default_opts.restype = None
+        L.orc_rk45.argtypes = [P, C.c_double, C.c_double, C.c_double, C.POINTER(Rk45Opts), _dp,
+                               C.POINTER(Rk45Stats)]
         L.orc_rk4_nsteps.argtypes = [C.c_double, _dp]
         L.orc_rk4_nsteps.restype = C.c_longlong
         L.orc_hnorm1d_reference.argtypes = [_dp, C.c_longlong, C.c_longlong, C.c_double, C.c_int]
@@ -150,6 +165,21 @@ class Port:
         if rc:
             raise ValueError(f"oracle rejected the problem (code {rc})")
         return out
+
+    def rk45(self, pb: Problem, v, t0: float, t_end: float, dt0: float, **opts):
+        """Adaptive RKF45 from t0 to t_end (orc_rk45); opts override the defaults.
+        Returns (state, stats dict)."""
+        o = Rk45Opts()
+        self.lib.orc_rk45_default_opts(C.byref(o))
+        for k, val in opts.items():
+            setattr(o, k, val)
+        out = np.array(v, dtype=np.float64, copy=True)
+        st = Rk45Stats()
+        s = pb.c_struct()
+        rc = self.lib.orc_rk45(C.byref(s), t0, t_end, dt0, C.byref(o), _ptr(out), C.byref(st))
+        if rc:
+            raise ValueError(f"oracle rejected the problem (code {rc})")
+        return out, {f: getattr(st, f) for f, _ in Rk45Stats._fields_}
 
     def rk4_nsteps(self, t_end: float, dt: float):
         d = C.c_double(dt)

@@ -164,6 +164,152 @@ int orc_rhs(const orc_problem* p, double t, const double* src, double* dst) {
   return orc_bc(p, src, dst);
 }
 
+void orc_rk45_default_opts(orc_rk45_opts* o) {
+  o->atol = 1e-4;
+  o->rtol = 1e-4;
+  o->safety = 0.9;
+  o->reject_safety = 0.5;
+  o->clip_lo = 0.1;
+  o->clip_hi = 10.0;
+  o->dt_min = 1e-20;
+  o->dt_max = 1e50;
+  o->max_steps = 10000000;
+  o->max_reject = 10;
+}
+
+/* Fehlberg's 4(5) pair. */
+static const double RKF_C[6] = {0.0, 1.0 / 4, 3.0 / 8, 12.0 / 13, 1.0, 1.0 / 2};
+static const double RKF_A[6][5] = {{0, 0, 0, 0, 0},
+                                   {1.0 / 4, 0, 0, 0, 0},
+                                   {3.0 / 32, 9.0 / 32, 0, 0, 0},
+                                   {1932.0 / 2197, -7200.0 / 2197, 7296.0 / 2197, 0, 0},
+                                   {439.0 / 216, -8.0, 3680.0 / 513, -845.0 / 4104, 0},
+                                   {-8.0 / 27, 2.0, -3544.0 / 2565, 1859.0 / 4104, -11.0 / 40}};
+static const double RKF_B5[6] = {16.0 / 135, 0.0, 6656.0 / 12825, 28561.0 / 56430, -9.0 / 50, 2.0 / 55};
+static const double RKF_B4[6] = {25.0 / 216, 0.0, 1408.0 / 2565, 2197.0 / 4104, -1.0 / 5, 0.0};
+
+/* Landing rule on t_end for a candidate step h0 from t; sets *fin on the last step. */
+static double rk45_land(double t, double t_end, double h0, int* fin) {
+  const double hmax = t_end - t;
+  double h = h0;
+  *fin = 0;
+  if (h0 >= hmax) {
+    *fin = 1;
+    return hmax;
+  }
+  if (2.0 * h0 > hmax) h = 0.5 * hmax;
+  if (1.01 * h0 > hmax) {
+    h = hmax;
+    *fin = 1;
+  }
+  return h;
+}
+
+int orc_rk45(const orc_problem* p, double t0, double t_end, double dt0, const orc_rk45_opts* opts, double* v,
+             orc_rk45_stats* st) {
+  int rc = check(p);
+  if (rc) return rc;
+  orc_rk45_opts o;
+  if (opts) o = *opts; else orc_rk45_default_opts(&o);
+  const long long n = p->nx * (is_2d(p->problem) ? p->ny : 1) * orc_dofs(p->problem);
+  double* k[6];
+  double* w = (double*)malloc(sizeof(double) * n);
+  double* u5 = (double*)malloc(sizeof(double) * n);
+  int ok = w && u5;
+  for (int s = 0; s < 6; s++) {
+    k[s] = (double*)malloc(sizeof(double) * n);
+    ok = ok && k[s];
+  }
+  if (!ok) {
+    free(w); free(u5);
+    for (int s = 0; s < 6; s++) free(k[s]);
+    return -5;
+  }
+  double t = t0, wlte = 0.0;
+  long long acc = 0, rej = 0;
+  int last_ok = 1, in_row = 0, fin = 0, status = 0, done = !(t_end > t0);
+  double h = rk45_land(t0, t_end, fmin(dt0, o.dt_max), &fin);
+  while (!done) {
+    for (int s = 0; s < 6; s++) {
+      const double* in = v;
+      if (s > 0) {
+#pragma omp parallel for schedule(static) if (n > 65536)
+        for (long long i = 0; i < n; i++) {
+          double a = RKF_A[s][0] * k[0][i];
+          for (int j = 1; j < s; j++) a = fma(RKF_A[s][j], k[j][i], a);
+          w[i] = fma(h, a, v[i]);
+        }
+        in = w;
+      }
+      orc_rhs(p, t + RKF_C[s] * h, in, k[s]);
+    }
+    double sum = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : sum) if (n > 65536)
+    for (long long i = 0; i < n; i++) {
+      double s5 = RKF_B5[0] * k[0][i], s4 = RKF_B4[0] * k[0][i];
+      for (int j = 1; j < 6; j++) {
+        s5 = fma(RKF_B5[j], k[j][i], s5);
+        s4 = fma(RKF_B4[j], k[j][i], s4);
+      }
+      const double a5 = fma(h, s5, v[i]), a4 = fma(h, s4, v[i]);
+      u5[i] = a5;
+      const double tol = o.atol + o.rtol * fmax(fabs(a5), fabs(a4));
+      const double e = (a5 - a4) / tol;
+      sum += e * e;
+    }
+    wlte = sqrt(sum / (double)n);
+    if (!(wlte <= 1e300)) {
+      rej++;
+      status = 2;
+      break;
+    }
+    double safety = o.safety;
+    int accept = 1;
+    if (wlte > 1.0) {
+      if (!last_ok) safety *= o.reject_safety;
+      accept = h < (1.0 + 1.4901161193847656e-08) * o.dt_min;
+    }
+    double hfac = wlte > 0.0 ? safety * pow(wlte, -0.2) : o.clip_hi;
+    hfac = fmin(fmax(hfac, o.clip_lo), o.clip_hi);
+    double hn = fmin(fmax(h * hfac, o.dt_min), o.dt_max);
+    last_ok = accept;
+    if (accept) {
+      memcpy(v, u5, sizeof(double) * n);
+      acc++;
+      in_row = 0;
+      if (fin) {
+        t = t_end;
+        h = hn;
+        break;
+      }
+      t = t + h;
+    } else {
+      rej++;
+      in_row++;
+    }
+    h = rk45_land(t, t_end, hn, &fin);
+    if (in_row >= o.max_reject) {
+      status = 3;
+      break;
+    }
+    if (acc + rej >= o.max_steps) {
+      status = 1;
+      break;
+    }
+  }
+  if (st) {
+    st->accepted = acc;
+    st->rejected = rej;
+    st->t = t;
+    st->dt_next = h;
+    st->wlte = wlte;
+    st->status = status;
+  }
+  free(w); free(u5);
+  for (int s = 0; s < 6; s++) free(k[s]);
+  return 0;
+}
+
 long long orc_rk4_nsteps(double t_end, double* dt_inout) {
   const double dt = *dt_inout;
   const long long n = llround(t_end / dt);

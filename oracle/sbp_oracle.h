@@ -70,6 +70,37 @@ int orc_rhs(const orc_problem* p, double t, const double* src, double* dst);
  * (code/include/time_stepping/time_stepping.h:127-142). */
 int orc_rk4(const orc_problem* p, double t0, double dt, long long nsteps, double* v);
 
+/* Adaptive Runge-Kutta-Fehlberg 4(5) with the basic step-size controller, from
+ * t0 to t_end in place on v. Restates what the reference's ts_rk45
+ * (code/src/time_stepping/ts_rk.cpp:41-52) asks of PETSc: TSRK5F (Fehlberg's
+ * published pair, E. Fehlberg, NASA TR R-315, 1969, advanced with the 5th-order
+ * weights) under TSADAPTBASIC with TS_EXACTFINALTIME_MATCHSTEP and default
+ * options. PETSc is an unpinned dependency absent from the reference tree; the
+ * controller is restated from its documented behaviour:
+ *   wlte = sqrt(mean_i (|u5_i - u4_i| / (atol + rtol max(|u5_i|, |u4_i|)))^2)
+ *   accept iff wlte <= 1 (or h < (1 + sqrt(eps)) dt_min)
+ *   safety' = safety * reject_safety if this and the previous attempt failed
+ *   h' = clamp(h * clamp(safety' wlte^(-1/5), clip_lo, clip_hi), dt_min, dt_max)
+ *   with hmax = t_end - t: h' >= hmax -> hmax (last step); otherwise
+ *   2 h' > hmax -> hmax / 2, then 1.01 h' > hmax -> hmax (last step).
+ * The first attempt is dt0 under the same landing rule. Stops when the last
+ * step is accepted (t = t_end), after max_reject rejections in a row (status
+ * 3), after max_steps attempts (status 1) or on a non-finite wlte (status 2).
+ * Stage inputs w = u + h * (a_s1 k1 + ...), sums left to right with fma. */
+typedef struct {
+  double atol, rtol, safety, reject_safety, clip_lo, clip_hi, dt_min, dt_max;
+  long long max_steps;
+  int max_reject;
+} orc_rk45_opts;
+typedef struct {
+  long long accepted, rejected;
+  double t, dt_next, wlte;
+  int status;
+} orc_rk45_stats;
+void orc_rk45_default_opts(orc_rk45_opts* o);
+int orc_rk45(const orc_problem* p, double t0, double t_end, double dt0, const orc_rk45_opts* o, double* v,
+             orc_rk45_stats* st);
+
 /* Step count rule of the reference's RK4: round(t_end/dt) steps, and dt is
  * replaced by t_end/steps when they do not match (time_stepping.h:104-109). */
 long long orc_rk4_nsteps(double t_end, double* dt_inout);
