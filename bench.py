@@ -368,9 +368,10 @@ def run_rk45_study(args):
         t_rk4 = time.perf_counter() - t0
     attempts = st["accepted"] + st["rejected"]
     evals = 6.0 * n * n * attempts
-    # scalars moved per point and attempt: 6 RHS (input + k), 5 stage combinations (u, k1..ks, w),
-    # candidate (u, k1..k6, unew) and, when accepted, the copy unew -> u
-    vectors = 12 + sum(s + 2 for s in range(1, 6)) + 8 + 2.0 * st["accepted"] / max(attempts, 1)
+    # state vectors moved per point and attempt by the fused wave stages: stage 1 reads u and
+    # writes k1, w2; stage s = 2..5 reads w_s, u, k_1..k_{s-1} and writes k_s, w_{s+1}; stage 6
+    # reads w6, u, k1, k3, k4, k5 and writes the candidate; an accepted attempt copies it to u
+    vectors = 3 + sum(s + 3 for s in range(2, 6)) + 7 + 2.0 * st["accepted"] / max(attempts, 1)
     bytes_attempt = vectors * 3 * 8 * n * n
     peak, src = measured_peaks()
     line = {"study": "rk45", "grid": [n, n], "order": order, "t_end": t_end, "dt0": 0.2 * h,

@@ -163,6 +163,9 @@ struct Rk45Ctrl {
 cudaError_t launch_rk45_combine(int stage, const Rk45Buffers& b, const Rk45Ctrl* ctrl, cudaStream_t s);
 // Candidate solution and error partial sums, the controller, and the accept copy.
 cudaError_t launch_rk45_finish(const Rk45Buffers& b, Rk45Ctrl* ctrl, cudaStream_t s);
+// The controller over `nparts` partial sums already in b.partial, and the accept copy
+// (after the fused wave stage ST_RKF6 wrote the candidate and one partial per CTA).
+cudaError_t launch_rk45_control(const Rk45Buffers& b, int nparts, Rk45Ctrl* ctrl, cudaStream_t s);
 
 // FP64 fused-multiply-add throughput probe: each thread runs `iters`
 // iterations of 8 independent DFMA chains; result written to out[0].

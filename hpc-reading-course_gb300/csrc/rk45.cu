@@ -18,19 +18,9 @@
 #include <cmath>
 
 #include "launch.h"
+#include "rkf_tableau.cuh"
 
 namespace sbp {
-
-// Fehlberg's 4(5) pair (Fehlberg 1969, NASA TR R-315, table III).
-__constant__ double kRkfA[6][5] = {
-    {0, 0, 0, 0, 0},
-    {1.0 / 4, 0, 0, 0, 0},
-    {3.0 / 32, 9.0 / 32, 0, 0, 0},
-    {1932.0 / 2197, -7200.0 / 2197, 7296.0 / 2197, 0, 0},
-    {439.0 / 216, -8.0, 3680.0 / 513, -845.0 / 4104, 0},
-    {-8.0 / 27, 2.0, -3544.0 / 2565, 1859.0 / 4104, -11.0 / 40}};
-__constant__ double kRkfB5[6] = {16.0 / 135, 0.0, 6656.0 / 12825, 28561.0 / 56430, -9.0 / 50, 2.0 / 55};
-__constant__ double kRkfB4[6] = {25.0 / 216, 0.0, 1408.0 / 2565, 2197.0 / 4104, -1.0 / 5, 0.0};
 
 constexpr int kRkfThreads = 256;
 
@@ -61,7 +51,8 @@ __global__ void __launch_bounds__(kRkfThreads) rkf_combine_kernel(Rk45Buffers b,
 }
 
 // u5 = u + h * sum b5_j k_j (written to unew), u4 = u + h * sum b4_j k_j, and the
-// per-block partial sum of ((u5 - u4) / (atol + rtol * max(|u5|, |u4|)))^2.
+// per-block partial sum of ((u5 - u4) / (atol + rtol * max(|u5|, |u4|)))^2
+// (rkf_candidate, rkf_err_term).
 __global__ void __launch_bounds__(kRkfThreads) rkf_final_kernel(Rk45Buffers b, Rk45Ctrl* __restrict__ ctrl) {
   __shared__ double red[kRkfThreads];
   if (ctrl->done) return;
@@ -72,20 +63,10 @@ __global__ void __launch_bounds__(kRkfThreads) rkf_final_kernel(Rk45Buffers b, R
     const long long o0 = rkf_row(r, b.ny, b.pitch, b.plane);
     for (int i = threadIdx.x; i < b.nx; i += blockDim.x) {
       const long long o = o0 + i;
-      const double k0 = b.k[0][o];
-      double s5 = kRkfB5[0] * k0, s4 = kRkfB4[0] * k0;
-#pragma unroll
-      for (int j = 1; j < 6; j++) {
-        const double kj = b.k[j][o];
-        s5 = fma(kRkfB5[j], kj, s5);
-        s4 = fma(kRkfB4[j], kj, s4);
-      }
-      const double u = b.u[o];
-      const double u5 = fma(h, s5, u), u4 = fma(h, s4, u);
+      double u5, u4;
+      rkf_candidate(b.u[o], h, b.k[0][o], b.k[2][o], b.k[3][o], b.k[4][o], b.k[5][o], u5, u4);
       b.unew[o] = u5;
-      const double tol = atol + rtol * fmax(fabs(u5), fabs(u4));
-      const double e = (u5 - u4) / tol;
-      acc = fma(e, e, acc);
+      acc += rkf_err_term(u5, u4, atol, rtol);
     }
   }
   red[threadIdx.x] = acc;
@@ -212,7 +193,11 @@ cudaError_t launch_rk45_combine(int stage, const Rk45Buffers& b, const Rk45Ctrl*
 cudaError_t launch_rk45_finish(const Rk45Buffers& b, Rk45Ctrl* ctrl, cudaStream_t s) {
   // the partial-sum count is fixed (kReduceBlocks) so the sum order is the same every attempt
   rkf_final_kernel<<<kReduceBlocks, kRkfThreads, 0, s>>>(b, ctrl);
-  rkf_control_kernel<<<1, kRkfThreads, 0, s>>>(b.partial, kReduceBlocks, ctrl);
+  return launch_rk45_control(b, kReduceBlocks, ctrl, s);
+}
+
+cudaError_t launch_rk45_control(const Rk45Buffers& b, int nparts, Rk45Ctrl* ctrl, cudaStream_t s) {
+  rkf_control_kernel<<<1, kRkfThreads, 0, s>>>(b.partial, nparts, ctrl);
   rkf_accept_kernel<<<kReduceBlocks, kRkfThreads, 0, s>>>(b, ctrl);
   return cudaGetLastError();
 }

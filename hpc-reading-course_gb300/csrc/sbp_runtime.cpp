@@ -72,6 +72,7 @@ struct sbp_ctx {
   double* rk_k[6] = {};
   double* rk_unew = nullptr;
   Rk45Ctrl* rk_ctrl = nullptr;
+  double rk_atol = 0, rk_rtol = 0;  // tolerances baked into the fused wave stages
   cudaGraphExec_t rk_graph = nullptr;
   std::map<long long, cudaGraphExec_t> graphs;
   double graph_dt = 0.0;
@@ -436,10 +437,56 @@ int rk45_prepare(sbp_ctx* ctx) {
 // Fehlberg stage times c_s (the abscissae of the tableau in rk45.cu).
 constexpr double kRkfC[6] = {0.0, 1.0 / 4, 3.0 / 8, 12.0 / 13, 1.0, 1.0 / 2};
 
+// Fused Fehlberg stage s (1..6) of the 2D wave kernel: k_s from the stage input
+// `in`, then the next stage input into `wout` (s < 6) or the candidate solution
+// and one error partial per CTA (s = 6). Inputs alternate un -> wa -> wb -> wa ...
+// so that no CTA overwrites halo rows another CTA is still reading.
+int launch_rkf_wave_stage(sbp_ctx* ctx, int s, void* in, const WaveMaps* in_maps, void* wout) {
+  WaveParams<double> p = wave_params<double>(ctx);
+  const Rk45Ctrl* ctl = ctx->rk_ctrl;
+  p.in = (const double*)in;
+  p.wout = (double*)wout;
+  p.tctl = &ctl->t;
+  p.tc = kRkfC[s - 1];
+  p.skip = &ctl->done;
+  for (int j = 0; j < 6; j++) p.rkk[j] = ctx->rk_k[j];
+  p.rku = (const double*)ctx->un;
+  p.rkunew = ctx->rk_unew;
+  p.rkpart = ctx->partial;
+  p.rkatol = ctx->rk_atol;
+  p.rkrtol = ctx->rk_rtol;
+  CK(launch_wave<double>(ctx->d.order, wave_kind(ctx), ST_RKF1 + s - 1, *in_maps, p, ctx->stream));
+  ctx->launches++;
+  return SBP_OK;
+}
+
+// CTAs of the persistent wave kernel (as launch_wave sizes its grid).
+int wave_grid(const sbp_ctx* ctx) {
+  const int ty = wave_tile_height(8, wave_kind(ctx));
+  const long long ntiles = ((ctx->nx + kWaveTX - 1) / kWaveTX) * ((ctx->ny + ty - 1) / ty);
+  const int nsm = device_sm_count();
+  return (int)(ntiles < nsm ? ntiles : nsm);
+}
+
 // One attempted step: six RHS evaluations with the stage combinations between
-// them, then the candidate solution, the controller and the accept copy.
+// them, then the candidate solution, the controller and the accept copy. The 2D
+// wave problems fuse each combination into the stage kernel.
 int enqueue_rk45_attempt(sbp_ctx* ctx) {
   const Rk45Buffers b = rk45_buffers(ctx);
+  if (ctx->wave) {
+    int rc;
+    void* bufs[2] = {ctx->wa, ctx->wb};
+    const WaveMaps* maps[2] = {&ctx->maps_wa, &ctx->maps_wb};
+    for (int s = 1; s <= 6; s++) {
+      void* in = s == 1 ? ctx->un : bufs[s % 2];           // s = 2: wa, 3: wb, 4: wa, ...
+      const WaveMaps* m = s == 1 ? &ctx->maps_un : maps[s % 2];
+      void* wout = s == 6 ? nullptr : bufs[(s + 1) % 2];  // s = 1: wa, 2: wb, ...
+      if ((rc = launch_rkf_wave_stage(ctx, s, in, m, wout))) return rc;
+    }
+    CK(launch_rk45_control(b, wave_grid(ctx), ctx->rk_ctrl, ctx->stream));
+    ctx->launches += 2;
+    return SBP_OK;
+  }
   for (int s = 0; s < 6; s++) {
     void* in = s == 0 ? ctx->un : ctx->wa;
     const WaveMaps* m = s == 0 ? &ctx->maps_un : &ctx->maps_wa;
@@ -455,8 +502,10 @@ int enqueue_rk45_attempt(sbp_ctx* ctx) {
   return SBP_OK;
 }
 
-constexpr int kRk45Chunk = 8;            // attempts per graph launch
-constexpr int kRk45LaunchesPerTry = 14;  // 6 RHS + 5 combine + final, control, accept
+constexpr int kRk45Chunk = 8;  // attempts per graph launch
+// kernels per attempt: 6 fused stages + control + accept (2D wave), or
+// 6 RHS + 5 combinations + final, control, accept
+int rk45_launches_per_try(const sbp_ctx* ctx) { return ctx->wave ? 8 : 14; }
 
 int rk45_chunk_graph(sbp_ctx* ctx) {
   if (ctx->rk_graph) return SBP_OK;
@@ -793,6 +842,12 @@ int sbp_rk45_resident(sbp_ctx* ctx, double t0, double t_end, double dt0, const s
   CK(cudaSetDevice(ctx->d.device));
   int rc;
   if ((rc = rk45_prepare(ctx))) return rc;
+  if (ctx->rk_graph && (ctx->rk_atol != o.atol || ctx->rk_rtol != o.rtol)) {
+    cudaGraphExecDestroy(ctx->rk_graph);
+    ctx->rk_graph = nullptr;
+  }
+  ctx->rk_atol = o.atol;
+  ctx->rk_rtol = o.rtol;
   if ((rc = rk45_chunk_graph(ctx))) return rc;
   Rk45Ctrl c;
   std::memset(&c, 0, sizeof(c));
@@ -819,7 +874,7 @@ int sbp_rk45_resident(sbp_ctx* ctx, double t0, double t_end, double dt0, const s
   for (long long chunk = 0; !c.done; chunk++) {
     if (chunk >= max_chunks) return fail(ctx, SBP_ERR_DEVICE, "the RK45 controller did not stop");
     CK(cudaGraphLaunch(ctx->rk_graph, ctx->stream));
-    ctx->launches += (long long)kRk45Chunk * kRk45LaunchesPerTry;
+    ctx->launches += (long long)kRk45Chunk * rk45_launches_per_try(ctx);
     CK(cudaMemcpyAsync(&c, ctx->rk_ctrl, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
     if ((rc = check_device_errors(ctx))) return rc;  // synchronizes the stream
   }

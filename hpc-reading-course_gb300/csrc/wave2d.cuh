@@ -23,13 +23,18 @@
 // each ny rows of `pitch` elements (pitch a multiple of 64).
 #pragma once
 
+#include "rkf_tableau.cuh"
 #include "sbp_device.cuh"
 
 namespace sbp {
 
 enum WaveKind : int { WK_HOM = 0, WK_VAR = 1, WK_MMS = 2, WK_CONST = 3 };  // WK_CONST: rho = 1, K = kconst
 enum BcKind : int { BC_NONE = 0, BC_FREE_SURFACE = 1, BC_CHARACTERISTIC = 2 };
-enum Stage : int { ST_RHS = 0, ST_FIRST = 1, ST_MID = 2, ST_LAST = 4 };
+enum Stage : int { ST_RHS = 0, ST_FIRST = 1, ST_MID = 2, ST_LAST = 4, ST_RKF1 = 11, ST_RKF6 = 16 };
+// ST_RKF1 + s - 1 (s = 1..6): stage s of the Runge-Kutta-Fehlberg 4(5) attempt (FP64):
+// k_s, then the input of stage s+1 (s < 6) or the candidate solution and the
+// error partial sum (s = 6).
+constexpr bool is_rkf_stage(int stage) { return stage >= ST_RKF1 && stage <= ST_RKF6; }
 
 template <typename T> struct WaveParams {
   int nx, ny;
@@ -54,9 +59,14 @@ template <typename T> struct WaveParams {
   int ysplit;         // 0: one block; else rows [0,ysplit) and [ysplit,ny) are two blocks
                       // sharing an interface line (WK_VAR only)
   double t, xl0, xl1, hix, hiy;  // WK_MMS: stage time and grid geometry
-  const double* tctl;  // WK_MMS under the adaptive integrator: stage time tctl[0] + tc * tctl[1]
+  const double* tctl;  // the adaptive integrator's (t, h); WK_MMS stage time tctl[0] + tc * tctl[1]
   double tc;
   const int* skip;     // non-null and set: the kernel returns at entry
+  T* rkk[6];           // ST_RKF*: stage derivatives k_1..k_6 (3 planes each)
+  const T* rku;        // ST_RKF*: the attempt's starting state u
+  T* rkunew;           // ST_RKF6: candidate solution u5
+  double* rkpart;      // ST_RKF6: one error partial sum per CTA
+  double rkatol, rkrtol;
   int* err;
 };
 
@@ -218,7 +228,8 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 template <typename T, int ORD, int KIND, int STAGE, typename Tile>
 __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, const T* __restrict__ in, T* wout,
                                                   const T c_acc, const T c_w, const unsigned char* st, const int i0,
-                                                  const int j0, const int warp, const int lane) {
+                                                  const int j0, const int warp, const int lane,
+                                                  double* errsq = nullptr) {
   constexpr bool COMP = Tile::COMP;
   constexpr int TY = Tile::TY, W = OpShape<ORD>::W, CS = OpShape<ORD>::CS, R = Tile::R;
   constexpr int HX = Tile::HX, HY = Tile::HY, PW = Tile::PW;
@@ -261,6 +272,22 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
       const T* colP = sP + y * PW + (x + HX);   // row y+HY-R
       const T* colV = sV + y * kWaveTX + x;     // row y+HY-R
       const T pc = rowP[R], uc = rowU[R], vc = colV[R * kWaveTX];
+      // Fehlberg stages: the point's u and k_1..k_{S-1} are loaded here, ahead of
+      // the stencil arithmetic, so that their latency overlaps it (stage 6 does
+      // not need k2: its weights are zero).
+      constexpr int RKS = is_rkf_stage(STAGE) ? STAGE - ST_RKF1 + 1 : 1;
+      double rkpre[3][RKS];  // [c][0..RKS-2] = k_1..k_{RKS-1}, [c][RKS-1] = u (RKS > 1)
+      if constexpr (RKS > 1) {
+        const long long q0 = (long long)j * pitch + i;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+#pragma unroll
+          for (int jj = 0; jj < RKS - 1; jj++)
+            if (RKS < 6 || jj != 1) rkpre[c][jj] = __ldg(prm.rkk[jj] + c * plane + q0);
+          rkpre[c][RKS - 1] = __ldg(prm.rku + c * plane + q0);
+        }
+      }
+      (void)rkpre;
 
       T dxp, dyp, kp;
       if (xint) {
@@ -340,6 +367,25 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
         const long long o = c * plane + q;
         if constexpr (STAGE == ST_RHS) {
           prm.kout[o] = kc[c];
+        } else if constexpr (is_rkf_stage(STAGE)) {
+          // Fehlberg stage S: the same sums, in the same order, as the unfused
+          // combination kernels (rk45.cu); k_S is the register value.
+          constexpr int S = RKS;
+          const double h = prm.tctl[1];
+          const double kS = kc[c];
+          if constexpr (S < 6) {
+            prm.rkk[S - 1][o] = kS;
+            double s = kRkfA[S][0] * (S == 1 ? kS : rkpre[c][0]);
+#pragma unroll
+            for (int jj = 1; jj < S; jj++) s = fma(kRkfA[S][jj], jj == S - 1 ? kS : rkpre[c][jj], s);
+            const double u0 = S == 1 ? (double)cen[c] : rkpre[c][S - 1];
+            st_stream(wout + o, fma(h, s, u0));
+          } else {
+            double u5, u4;
+            rkf_candidate(rkpre[c][5], h, rkpre[c][0], rkpre[c][2], rkpre[c][3], rkpre[c][4], kS, u5, u4);
+            st_stream(prm.rkunew + o, u5);
+            *errsq += rkf_err_term(u5, u4, prm.rkatol, prm.rkrtol);
+          }
         } else if constexpr (STAGE == ST_FIRST) {
           // acc = u + dt/6 k1 (FP32 compensated: acc = dt/6 k1), w = u + dt/2 k1
           st_stream(prm.acc + o, COMP ? c_acc * kc[c] : fma(c_acc, kc[c], cen[c]));
@@ -421,6 +467,7 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
   }
 
   // ---------------- consumers: warps 0-7
+  double errsq = 0.0;  // ST_RKF6: this thread's share of the weighted error sum
   int k = 0;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
     const int b = k % NST;
@@ -430,9 +477,22 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
     }
     const int i0 = (tile % ntx) * kWaveTX, j0 = (tile / ntx) * TY;
     wave_tile_compute<T, ORD, KIND, STAGE, Tile>(prm, prm.in, prm.wout, prm.c_acc, prm.c_w,
-                                                 smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane);
+                                                 smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane, &errsq);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[b]);
+  }
+  if constexpr (STAGE == ST_RKF6) {
+    // fixed-order sum over the 256 consumer threads -> one partial per CTA
+    __shared__ double warp_sum[kWaveConsumerWarps];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) errsq += __shfl_down_sync(0xffffffffu, errsq, off);
+    if (lane == 0) warp_sum[warp] = errsq;
+    asm volatile("bar.sync 1, %0;" ::"n"(32 * kWaveConsumerWarps) : "memory");  // consumer warps only
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int q = 0; q < kWaveConsumerWarps; q++) s += warp_sum[q];
+      prm.rkpart[blockIdx.x] = s;
+    }
   }
 }
 

@@ -29,7 +29,16 @@ cudaError_t configure_kind() {
   if ((e = configure_one<T, KIND, ST_RHS>()) != cudaSuccess) return e;
   if ((e = configure_one<T, KIND, ST_FIRST>()) != cudaSuccess) return e;
   if ((e = configure_one<T, KIND, ST_MID>()) != cudaSuccess) return e;
-  return configure_one<T, KIND, ST_LAST>();
+  if ((e = configure_one<T, KIND, ST_LAST>()) != cudaSuccess) return e;
+  if constexpr (sizeof(T) == 8) {  // the Fehlberg stages (FP64 only)
+    if ((e = configure_one<T, KIND, ST_RKF1>()) != cudaSuccess) return e;
+    if ((e = configure_one<T, KIND, ST_RKF1 + 1>()) != cudaSuccess) return e;
+    if ((e = configure_one<T, KIND, ST_RKF1 + 2>()) != cudaSuccess) return e;
+    if ((e = configure_one<T, KIND, ST_RKF1 + 3>()) != cudaSuccess) return e;
+    if ((e = configure_one<T, KIND, ST_RKF1 + 4>()) != cudaSuccess) return e;
+    if ((e = configure_one<T, KIND, ST_RKF6>()) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 template <typename T, int KIND, int STAGE>
@@ -47,8 +56,20 @@ cudaError_t launch_kind(int stage, const WaveMaps& m, const WaveParams<T>& prm, 
     case ST_FIRST: return launch_one<T, KIND, ST_FIRST>(m, prm, grid, s);
     case ST_MID: return launch_one<T, KIND, ST_MID>(m, prm, grid, s);
     case ST_LAST: return launch_one<T, KIND, ST_LAST>(m, prm, grid, s);
-    default: return cudaErrorInvalidValue;
+    default: break;
   }
+  if constexpr (sizeof(T) == 8) {
+    switch (stage) {
+      case ST_RKF1: return launch_one<T, KIND, ST_RKF1>(m, prm, grid, s);
+      case ST_RKF1 + 1: return launch_one<T, KIND, ST_RKF1 + 1>(m, prm, grid, s);
+      case ST_RKF1 + 2: return launch_one<T, KIND, ST_RKF1 + 2>(m, prm, grid, s);
+      case ST_RKF1 + 3: return launch_one<T, KIND, ST_RKF1 + 3>(m, prm, grid, s);
+      case ST_RKF1 + 4: return launch_one<T, KIND, ST_RKF1 + 4>(m, prm, grid, s);
+      case ST_RKF6: return launch_one<T, KIND, ST_RKF6>(m, prm, grid, s);
+      default: break;
+    }
+  }
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace

@@ -143,7 +143,8 @@ int sbp_hnorm(sbp_ctx* ctx, double* hnorm);
  * which runs PETSc's TSRK5F (Fehlberg's pair, advanced with the 5th-order
  * weights) under TSADAPTBASIC with TS_EXACTFINALTIME_MATCHSTEP and PETSc's
  * default options. The controller per attempted step h from time t:
- *   wlte = sqrt(mean over all scalars of ((u5 - u4) / (atol + rtol max(|u5|, |u4|)))^2)
+ *   wlte = sqrt(mean over all scalars of ((u5 - u4) / (atol + rtol max(|u5|, |u4|)))^2),
+ *   an entry with a zero tolerance contributing 0
  *   accept iff wlte <= 1; h' = h clip(safety' wlte^(-1/5), clip_lo, clip_hi)
  *   (safety' = safety, times reject_safety when this and the previous attempt
  *   failed), h' in [dt_min, dt_max]; with hmax = t_end - t: h' >= hmax -> hmax,

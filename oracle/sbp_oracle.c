@@ -254,8 +254,10 @@ int orc_rk45(const orc_problem* p, double t0, double t_end, double dt0, const or
       const double a5 = fma(h, s5, v[i]), a4 = fma(h, s4, v[i]);
       u5[i] = a5;
       const double tol = o.atol + o.rtol * fmax(fabs(a5), fabs(a4));
-      const double e = (a5 - a4) / tol;
-      sum += e * e;
+      if (tol != 0.0) { /* a zero tolerance contributes 0 */
+        const double e = (a5 - a4) / tol;
+        sum += e * e;
+      }
     }
     wlte = sqrt(sum / (double)n);
     if (!(wlte <= 1e300)) {

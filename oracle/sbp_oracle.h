@@ -77,7 +77,8 @@ int orc_rk4(const orc_problem* p, double t0, double dt, long long nsteps, double
  * weights) under TSADAPTBASIC with TS_EXACTFINALTIME_MATCHSTEP and default
  * options. PETSc is an unpinned dependency absent from the reference tree; the
  * controller is restated from its documented behaviour:
- *   wlte = sqrt(mean_i (|u5_i - u4_i| / (atol + rtol max(|u5_i|, |u4_i|)))^2)
+ *   wlte = sqrt(mean_i (|u5_i - u4_i| / (atol + rtol max(|u5_i|, |u4_i|)))^2),
+ *   an entry with a zero tolerance contributing 0
  *   accept iff wlte <= 1 (or h < (1 + sqrt(eps)) dt_min)
  *   safety' = safety * reject_safety if this and the previous attempt failed
  *   h' = clamp(h * clamp(safety' wlte^(-1/5), clip_lo, clip_hi), dt_min, dt_max)

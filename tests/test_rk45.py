@@ -215,3 +215,24 @@ def test_gpu_rk45_step_limit_and_unsupported(sbp, port):
         c32.set_state(_case_state(O.WAVE_HOM_2D, 33, 33))
         with pytest.raises(sbp.SbpError):
             c32.rk45_resident(0.0, 0.1, 0.01)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,problem,order,nx,ny,kw,t_end,dt0", [CASES[1], CASES[4], CASES[6], CASES[10]],
+                         ids=[CASES[i][0] for i in (1, 4, 6, 10)])
+def test_gpu_rk45_error_norm_of_one_attempt(sbp, port, name, problem, order, nx, ny, kw, t_end, dt0):
+    """The weighted error of a single attempt (its 1/tol from a refined FP32 reciprocal, the
+    sum in per-CTA partials) against the oracle's (FP64 division, sequential sum). Each
+    difference u5 - u4 inherits the last-bit differences of the stage derivatives (a couple
+    of ulps of u), which moves wlte by up to about 4 eps max|u| / tol; the rest must agree
+    to 1e-13 relative (an FP32-accurate reciprocal would be off by about 1e-7)."""
+    v0 = _case_state(problem, nx, ny)
+    for tol in (1e-4, 1e-9):
+        ctx, pb = _pair(sbp, problem, order, nx, ny, kw)
+        with ctx:
+            ctx.set_state(v0)
+            st = ctx.rk45_resident(0.0, t_end, dt0, check=False, max_steps=1, atol=tol, rtol=tol)
+        _, rst = port.rk45(pb, v0, 0.0, t_end, dt0, max_steps=1, atol=tol, rtol=tol)
+        assert st["accepted"] + st["rejected"] == 1
+        bound = 1e-13 * rst["wlte"] + 4 * np.finfo(float).eps * np.abs(v0).max() / tol
+        assert abs(st["wlte"] - rst["wlte"]) <= bound
