@@ -7,9 +7,9 @@ namespace sbp {
 
 int wave_smem_bytes(int order, bool fp32) {
   switch (order) {
-    case 2: return fp32 ? WaveTile<float, 2, ST_MID>::SMEM : WaveTile<double, 2, ST_MID>::SMEM;
-    case 4: return fp32 ? WaveTile<float, 4, ST_MID>::SMEM : WaveTile<double, 4, ST_MID>::SMEM;
-    case 6: return fp32 ? WaveTile<float, 6, ST_MID>::SMEM : WaveTile<double, 6, ST_MID>::SMEM;
+    case 2: return fp32 ? WaveStageTile<float, 2, WK_HOM, ST_MID>::SMEM : WaveStageTile<double, 2, WK_HOM, ST_MID>::SMEM;
+    case 4: return fp32 ? WaveStageTile<float, 4, WK_HOM, ST_MID>::SMEM : WaveStageTile<double, 4, WK_HOM, ST_MID>::SMEM;
+    case 6: return fp32 ? WaveStageTile<float, 6, WK_HOM, ST_MID>::SMEM : WaveStageTile<double, 6, WK_HOM, ST_MID>::SMEM;
     default: return -1;
   }
 }

@@ -71,7 +71,7 @@ template <typename T> struct WaveParams {
 };
 
 constexpr int kWaveTX = 64;            // tile width (x, contiguous)
-constexpr int kWaveConsumerWarps = 8;  // compute warps
+constexpr int kWaveConsumerWarps = 8;  // compute warps (FP64, variable-coefficient FP32, batched)
 constexpr int kWaveThreads = 32 * (kWaveConsumerWarps + 1);
 
 // FP32 keeps the state with a Kahan-compensated final update.
@@ -86,10 +86,10 @@ template <typename T> constexpr int default_wave_ty() { return sizeof(T) == 8 ? 
 // Pipeline shape of the single-instance kernel for FP32 (tile rows, ring depth);
 // the build may override them to compare shapes.
 #ifndef SBP_FP32_TILE_ROWS
-#define SBP_FP32_TILE_ROWS 16
+#define SBP_FP32_TILE_ROWS 32
 #endif
 #ifndef SBP_FP32_RING
-#define SBP_FP32_RING 4
+#define SBP_FP32_RING 2
 #endif
 
 // Tile height of the single-instance kernel: the variable-coefficient FP32
@@ -101,10 +101,21 @@ template <typename T, int KIND> constexpr int wave_ty() {
 template <typename T, int KIND> constexpr int wave_ring() {
   return (sizeof(T) == 4 && KIND != WK_VAR) ? SBP_FP32_RING : 2;
 }
+// Consumer warps of the single-instance kernel. The FP64 kernels need 120-166
+// registers a thread, which leaves room for 8 warps; the constant-coefficient
+// FP32 kernels run 16 (two tile rows each), which hides more load latency.
+#ifndef SBP_FP32_WARPS
+#define SBP_FP32_WARPS 16
+#endif
+template <typename T, int KIND> constexpr int wave_warps() {
+  return (sizeof(T) == 4 && KIND != WK_VAR) ? SBP_FP32_WARPS : kWaveConsumerWarps;
+}
 
 template <typename T, int ORD, int STAGE, int TY_ = default_wave_ty<T>(), int PRM_BYTES = 0, bool COEF = false,
-          int NST_ = 2>
+          int NST_ = 2, int WARPS_ = kWaveConsumerWarps>
 struct WaveTile {
+  static constexpr int WARPS = WARPS_;                        // consumer warps
+  static constexpr int THREADS = 32 * (WARPS_ + 1);           // + the producer warp
   static constexpr bool COMP = IsCompensated<T>::value;
   static constexpr int TY = TY_;                              // tile height
   static constexpr int R = (OpShape<ORD>::W - 1) / 2;
@@ -137,7 +148,7 @@ struct WaveTile {
   static constexpr uint32_t TX_BYTES = BYTES_P + BYTES_U + BYTES_V + (LOAD_UN ? BYTES_PT : 0) +
                                        (LOAD_ACC ? BYTES_PT : 0) + (LOAD_COMP ? BYTES_PT : 0) +
                                        (LOAD_COEF ? BYTES_K : 0) + PRM_BYTES;
-  static_assert(TY % kWaveConsumerWarps == 0, "tile rows must split evenly over the consumer warps");
+  static_assert(TY % WARPS == 0, "tile rows must split evenly over the consumer warps");
   static_assert(NST >= 2 && NST <= 8, "ring depth");
   static_assert(SMEM <= 227 * 1024, "wave tile pipeline exceeds shared memory");
 };
@@ -233,7 +244,7 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
   constexpr bool COMP = Tile::COMP;
   constexpr int TY = Tile::TY, W = OpShape<ORD>::W, CS = OpShape<ORD>::CS, R = Tile::R;
   constexpr int HX = Tile::HX, HY = Tile::HY, PW = Tile::PW;
-  constexpr int ROWS = TY / kWaveConsumerWarps;
+  constexpr int ROWS = TY / Tile::WARPS;
   // FP64 is bound by the FP64 pipe: unrolling the warp's rows gives more
   // independent FMA chains. FP32 is bound by HBM and runs faster rolled.
   constexpr int ROW_UNROLL = sizeof(T) == 8 ? ROWS : 1;
@@ -411,14 +422,19 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
   }
 }
 
+// The Tile type of the single-instance kernel for (T, order, kind, stage).
 template <typename T, int ORD, int KIND, int STAGE>
-__global__ void __launch_bounds__(kWaveThreads, 1)
+using WaveStageTile = WaveTile<T, ORD, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR, wave_ring<T, KIND>(),
+                               wave_warps<T, KIND>()>;
+
+template <typename T, int ORD, int KIND, int STAGE>
+__global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
     wave_stage_kernel(const __grid_constant__ CUtensorMap mapP, const __grid_constant__ CUtensorMap mapU,
                       const __grid_constant__ CUtensorMap mapV, const __grid_constant__ CUtensorMap mapN,
                       const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapC,
                       const __grid_constant__ CUtensorMap mapK, const __grid_constant__ WaveParams<T> prm) {
-  using Tile = WaveTile<T, ORD, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR, wave_ring<T, KIND>()>;
-  constexpr int TY = Tile::TY, HX = Tile::HX, HY = Tile::HY, NST = Tile::NST;
+  using Tile = WaveStageTile<T, ORD, KIND, STAGE>;
+  constexpr int TY = Tile::TY, HX = Tile::HX, HY = Tile::HY, NST = Tile::NST, WARPS = Tile::WARPS;
   extern __shared__ __align__(128) unsigned char smem[];
   if (prm.skip && *prm.skip) return;  // uniform over the grid: set before this launch
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
@@ -432,13 +448,13 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < NST; s++) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], kWaveConsumerWarps);
+      mbar_init(&empty[s], WARPS);
     }
     fence_barrier_init();
   }
   __syncthreads();
 
-  if (warp == kWaveConsumerWarps) {
+  if (warp == WARPS) {
     // ---------------- producer: TMA loads of tile k into stage k % NST
     if (lane == 0) {
       prefetch_tensormap(&mapP);
@@ -483,14 +499,14 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
   }
   if constexpr (STAGE == ST_RKF6) {
     // fixed-order sum over the 256 consumer threads -> one partial per CTA
-    __shared__ double warp_sum[kWaveConsumerWarps];
+    __shared__ double warp_sum[WARPS];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) errsq += __shfl_down_sync(0xffffffffu, errsq, off);
     if (lane == 0) warp_sum[warp] = errsq;
-    asm volatile("bar.sync 1, %0;" ::"n"(32 * kWaveConsumerWarps) : "memory");  // consumer warps only
+    asm volatile("bar.sync 1, %0;" ::"n"(32 * WARPS) : "memory");  // consumer warps only
     if (threadIdx.x == 0) {
       double s = 0.0;
-      for (int q = 0; q < kWaveConsumerWarps; q++) s += warp_sum[q];
+      for (int q = 0; q < WARPS; q++) s += warp_sum[q];
       prm.rkpart[blockIdx.x] = s;
     }
   }

@@ -19,8 +19,7 @@ namespace {
 template <typename T, int KIND, int STAGE>
 cudaError_t configure_one() {
   return cudaFuncSetAttribute(wave_stage_kernel<T, SBP_ORDER, KIND, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              WaveTile<T, SBP_ORDER, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR,
-                                       wave_ring<T, KIND>()>::SMEM);
+                              WaveStageTile<T, SBP_ORDER, KIND, STAGE>::SMEM);
 }
 
 template <typename T, int KIND>
@@ -43,9 +42,9 @@ cudaError_t configure_kind() {
 
 template <typename T, int KIND, int STAGE>
 cudaError_t launch_one(const WaveMaps& m, const WaveParams<T>& prm, dim3 grid, cudaStream_t s) {
-  using Tile = WaveTile<T, SBP_ORDER, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR, wave_ring<T, KIND>()>;
+  using Tile = WaveStageTile<T, SBP_ORDER, KIND, STAGE>;
   wave_stage_kernel<T, SBP_ORDER, KIND, STAGE>
-      <<<grid, kWaveThreads, Tile::SMEM, s>>>(m.p, m.u, m.v, m.n, m.a, m.c, m.k, prm);
+      <<<grid, Tile::THREADS, Tile::SMEM, s>>>(m.p, m.u, m.v, m.n, m.a, m.c, m.k, prm);
   return cudaGetLastError();
 }
 
