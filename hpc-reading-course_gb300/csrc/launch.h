@@ -20,7 +20,7 @@ struct WaveMaps {
 
 // Tile height of the single-instance wave stage kernel (see wave_ty).
 inline int wave_tile_height(int elem_bytes, int kind = WK_HOM) {
-  if (elem_bytes == 8) return wave_ty<double, WK_HOM>();
+  if (elem_bytes == 8) return kind == WK_HOM ? wave_ty<double, WK_HOM>() : wave_ty<double, WK_VAR>();
   return kind == WK_VAR ? wave_ty<float, WK_VAR>() : wave_ty<float, WK_HOM>();
 }
 

@@ -92,23 +92,35 @@ template <typename T> constexpr int default_wave_ty() { return sizeof(T) == 8 ? 
 #define SBP_FP32_RING 2
 #endif
 
+// Pipeline shape of the constant-coefficient FP64 kernel (tile rows, consumer
+// warps); the build may override them to compare shapes.
+#ifndef SBP_FP64_TILE_ROWS
+#define SBP_FP64_TILE_ROWS 12
+#endif
+#ifndef SBP_FP64_WARPS
+#define SBP_FP64_WARPS 12
+#endif
+
 // Tile height of the single-instance kernel: the variable-coefficient FP32
 // kind also stages 1/rho and K, so it uses 24 rows to keep two stages in 227 KB.
 template <typename T, int KIND> constexpr int wave_ty() {
-  return sizeof(T) == 8 ? 16 : (KIND == WK_VAR ? 24 : SBP_FP32_TILE_ROWS);
+  return sizeof(T) == 8 ? (KIND == WK_HOM ? SBP_FP64_TILE_ROWS : 16) : (KIND == WK_VAR ? 24 : SBP_FP32_TILE_ROWS);
 }
 // Shared-memory ring depth (tiles in flight + the one being computed).
 template <typename T, int KIND> constexpr int wave_ring() {
   return (sizeof(T) == 4 && KIND != WK_VAR) ? SBP_FP32_RING : 2;
 }
-// Consumer warps of the single-instance kernel. The FP64 kernels need 120-166
-// registers a thread, which leaves room for 8 warps; the constant-coefficient
-// FP32 kernels run 16 (two tile rows each), which hides more load latency.
+// Consumer warps of the single-instance kernel. The variable-coefficient and
+// manufactured-solution FP64 kernels need up to 166 registers a thread, which
+// leaves room for 8 warps; the constant-coefficient FP64 kernels (at most 128)
+// run 12 with one tile row each, the constant-coefficient FP32 kernels 16 with
+// two rows each (more warps hide more load latency).
 #ifndef SBP_FP32_WARPS
 #define SBP_FP32_WARPS 16
 #endif
 template <typename T, int KIND> constexpr int wave_warps() {
-  return (sizeof(T) == 4 && KIND != WK_VAR) ? SBP_FP32_WARPS : kWaveConsumerWarps;
+  return sizeof(T) == 4 ? (KIND != WK_VAR ? SBP_FP32_WARPS : kWaveConsumerWarps)
+                        : (KIND == WK_HOM ? SBP_FP64_WARPS : kWaveConsumerWarps);
 }
 
 template <typename T, int ORD, int STAGE, int TY_ = default_wave_ty<T>(), int PRM_BYTES = 0, bool COEF = false,
