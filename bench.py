@@ -56,11 +56,12 @@ def parse():
     ap.add_argument("--bc", default="characteristic", choices=["characteristic", "free_surface"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--study", default=None, choices=["precision", "batched", "learned", "rk45"],
+    ap.add_argument("--study", default=None, choices=["precision", "batched", "learned", "rk45", "wave3d"],
                     help="precision: variable rho, K (seeded Fourier fields) to --t-end in FP64 and in "
                          "compensated FP32; prints errors of FP32 against FP64 and both wall times. "
                          "batched: 512 uneven wave/advection instances in one batch, FP64 and FP32. "
-                         "rk45: adaptive RKF45 (ts_rk45) on the bench's wave problem to --rk45-t-end")
+                         "rk45: adaptive RKF45 (ts_rk45) on the bench's wave problem to --rk45-t-end. "
+                         "wave3d: the 3D wave system on --grid3d^3 points, FP64 and FP32")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--trajectories", type=int, default=2000, help="learned: training trajectories")
     ap.add_argument("--epochs", type=int, default=30, help="learned: training epochs per round")
@@ -68,6 +69,7 @@ def parse():
                     help="learned: rounds of training on windows started on the corrected solve's states")
     ap.add_argument("--t-end", type=float, default=1.0)
     ap.add_argument("--rk45-t-end", type=float, default=0.25, help="rk45: final time")
+    ap.add_argument("--grid3d", type=int, default=256, help="wave3d: points per direction")
     return ap.parse_args()
 
 
@@ -402,6 +404,73 @@ def run_rk45_study(args):
     print(json.dumps(line), flush=True)
 
 
+def run_wave3d_study(args):
+    """3D wave (u, v, w, p), rho = K = 1, characteristic SAT on the six faces, Gaussian pulse
+    w = 0.2 at the origin, --grid3d^3 points, order --order, dt = 0.2 h, 100 RK4 steps per timed run,
+    FP64 and compensated FP32, state resident in HBM, timed with CUDA events on the context's stream.
+    Roofs: HBM with 16 c s bytes per point and RK4 step (c = 4), and for FP64 the FP64 pipe at
+    about 33 FP64 instructions per point-stage (order 4: six derivatives of 4 instructions, two adds,
+    7 for the stage update on average). CPU: the oracle restatement on all host cores, a bounded
+    number of steps."""
+    import numpy as np
+    import torch
+
+    import build as gpu_build
+    import sbpgpu
+
+    gpu_build.build()
+    n, order, steps = args.grid3d, args.order, 100
+    h = 2.0 / (n - 1)
+    dt = 0.2 * h
+    x = np.linspace(-1, 1, n)
+    v0 = np.zeros((n, n, n, 4))
+    v0[..., 3] = np.exp(-(x[None, None, :] ** 2 + x[None, :, None] ** 2 + x[:, None, None] ** 2) / 0.2**2)
+    v0 = v0.ravel()
+    peak, src = measured_peaks()
+    dfma = sbpgpu.probe_dfma_rate() if hasattr(sbpgpu, "probe_dfma_rate") else None
+    out = {"study": "wave3d", "grid": [n, n, n], "order": order, "rk4_steps": steps, "dt": dt,
+           "bc": "characteristic", "peak_gbs": peak, "peak_source": src}
+    for name, prec, s in (("fp64", sbpgpu.FP64, 8), ("fp32", sbpgpu.FP32, 4)):
+        with sbpgpu.Context(sbpgpu.WAVE_3D, order, n, n, n, bc=sbpgpu.BC_CHARACTERISTIC, precision=prec) as ctx:
+            ctx.set_state(v0)
+            ctx.step_resident(0.0, dt, 3)  # warm-up (graph capture)
+            ctx.synchronize()
+            stream = torch.cuda.ExternalStream(ctx.stream)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            ctx.step_resident(0.0, dt, steps)
+            ev1.record(stream)
+            ctx.synchronize()
+            sec = ev0.elapsed_time(ev1) / 1e3
+        rate = 4.0 * n**3 * steps / sec
+        bytes_step = (16 * 4 * s + (2 * 4 * s if prec == sbpgpu.FP32 else 0)) * n**3
+        line = {"point_stage_per_s": rate, "seconds": sec, "achieved_gbs": bytes_step * steps / sec / 1e9}
+        line["hbm_frac"] = line["achieved_gbs"] / peak
+        if prec == sbpgpu.FP64 and dfma:
+            line["fp64_alu_bound_point_stage_per_s"] = dfma / 33.0
+            line["fp64_alu_frac"] = rate / (dfma / 33.0)
+        out[name] = line
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        O.build()
+        port = O.Port(O.PORT_OPT_SO)
+        threads = os.cpu_count() or 1
+        port.set_threads(threads)
+        pb = O.Problem(O.WAVE_3D, order, n, n, n, bc=O.BC_CHARACTERISTIC)
+        t0 = time.perf_counter()
+        port.rk4(pb, v0, 0.0, dt, 1)
+        t1 = time.perf_counter() - t0
+        k = max(1, min(steps, int(10.0 / max(t1, 1e-6))))
+        t0 = time.perf_counter()
+        port.rk4(pb, v0, 0.0, dt, k)
+        sec = time.perf_counter() - t0
+        out["cpu"] = {"point_stage_per_s": 4.0 * n**3 * k / sec, "cores": threads, "kind": "port",
+                      "sample": f"{k} RK4 steps of the same run"}
+    print(json.dumps(out), flush=True)
+
+
 def run_learned_study(args):
     """Two-layer problem (rho, K x4 across y = 0): coarse 257 x 2*129 order-4 solve corrected by the
     network every 4 steps, trained on restricted fine (1025 x 2*513, FP64) trajectories with seeded
@@ -475,6 +544,9 @@ def main():
         return
     if args.study == "rk45":
         run_rk45_study(args)
+        return
+    if args.study == "wave3d":
+        run_wave3d_study(args)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

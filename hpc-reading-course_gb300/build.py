@@ -48,6 +48,7 @@ def units():
     out.append(("batch_runtime.o", "batch_runtime.cpp", ["-x", "cu"]))
     out.append(("cnn.o", "cnn.cu", []))
     out.append(("rk45.o", "rk45.cu", []))
+    out.append(("wave3d.o", "wave3d.cu", []))
     return out
 
 

@@ -207,20 +207,23 @@ __device__ __forceinline__ double hweight(int n, int i, int cs, int oi) {
 template <typename T>
 __global__ void __launch_bounds__(kReduceThreads)
     hnorm_partial_kernel(const T* __restrict__ soa, int nx, int ny, int dofs, long long pitch, long long plane,
-                         int order, double hx, double hy, int ysplit, double* __restrict__ partial) {
+                         int order, double hx, double hy, int ysplit, double* __restrict__ partial, int nz,
+                         double hz) {
   __shared__ double sh[64];
   const int oi = order / 2 - 1, cs = (order == 2) ? 1 : (order == 4 ? 4 : 6);
   double sum = 0.0, mx = 0.0;
-  const long long n = (long long)nx * ny;
+  const long long n = (long long)nx * ny * nz;
   for (long long pt = blockIdx.x * (long long)blockDim.x + threadIdx.x; pt < n; pt += (long long)gridDim.x * blockDim.x) {
-    const long long j = pt / nx, i = pt - j * nx;
+    const long long r = pt / nx, i = pt - r * nx;  // row r = j + ny * k
+    const long long kz = r / ny, j = r - kz * ny;
     // two-block grids: each block has its own quadrature in y
     const int jb0 = (ysplit > 0 && j >= ysplit) ? ysplit : 0;
     const int nyb = (ysplit > 0) ? (j >= ysplit ? ny - ysplit : ysplit) : ny;
-    const double w = hx * hweight(nx, (int)i, cs, oi) * (ny > 1 ? hy * hweight(nyb, (int)j - jb0, cs, oi) : 1.0);
+    double w = hx * hweight(nx, (int)i, cs, oi) * (ny > 1 ? hy * hweight(nyb, (int)j - jb0, cs, oi) : 1.0);
+    if (nz > 1) w *= hz * hweight(nz, (int)kz, cs, oi);
     double s = 0.0;
     for (int c = 0; c < dofs; c++) {
-      const double x = (double)soa[c * plane + j * pitch + i];
+      const double x = (double)soa[c * plane + r * pitch + i];
       s += x * x;
     }
     sum += w * s;
@@ -234,16 +237,17 @@ __global__ void __launch_bounds__(kReduceThreads)
 
 template <typename T>
 cudaError_t launch_hnorm(const T* soa, int nx, int ny, int dofs, long long pitch, long long plane, int order,
-                         double hx, double hy, int ysplit, double* partial, double* out, cudaStream_t s) {
+                         double hx, double hy, int ysplit, double* partial, double* out, cudaStream_t s, int nz,
+                         double hz) {
   hnorm_partial_kernel<T><<<kReduceBlocks, kReduceThreads, 0, s>>>(soa, nx, ny, dofs, pitch, plane, order, hx, hy,
-                                                                   ysplit, partial);
+                                                                   ysplit, partial, nz, hz);
   final_reduce_kernel<<<1, kReduceThreads, 0, s>>>(partial, kReduceBlocks, out);
   return cudaGetLastError();
 }
 template cudaError_t launch_hnorm<double>(const double*, int, int, int, long long, long long, int, double, double,
-                                          int, double*, double*, cudaStream_t);
+                                          int, double*, double*, cudaStream_t, int, double);
 template cudaError_t launch_hnorm<float>(const float*, int, int, int, long long, long long, int, double, double, int,
-                                         double*, double*, cudaStream_t);
+                                         double*, double*, cudaStream_t, int, double);
 
 // ---------------------------------------------------------------- FP64 probe
 __global__ void dfma_probe_kernel(double* out, int iters) {

@@ -8,6 +8,7 @@
 
 #include "line_kernels.cuh"
 #include "wave2d.cuh"
+#include "wave3d.cuh"
 #include "wave_batch.cuh"
 
 namespace sbp {
@@ -63,6 +64,10 @@ int wave_smem_bytes(int order, bool fp32);
 
 template <typename T>
 cudaError_t launch_line(int order, int kind, int stage, const LineParams<T>& prm, cudaStream_t s);
+
+// The 3D wave stage kernel (wave3d.cu).
+template <typename T>
+cudaError_t launch_wave3d(int order, int stage, const Wave3Params<T>& prm, cudaStream_t s);
 
 // Batched stage kernels (wave_batch_inst.cu, one unit per order). `ty` is the
 // tile height: 8 or 16 (FP64), 16 or 32 (FP32).
@@ -126,9 +131,11 @@ cudaError_t launch_error_norms(const T* soa, const double* aos, int nx, int ny, 
 // Energy norm squared sum_c sum_j sum_i hy*wy_j * hx*wx_i * v^2 with the
 // closure quadrature at both ends of each direction (of each block when
 // ysplit > 0): out[0].
+// 3D (nz > 1): ny*nz rows, the z quadrature weight hz * w_k of slab k = row / ny as a third factor.
 template <typename T>
 cudaError_t launch_hnorm(const T* soa, int nx, int ny, int dofs, long long pitch, long long plane, int order,
-                         double hx, double hy, int ysplit, double* partial, double* out, cudaStream_t s);
+                         double hx, double hy, int ysplit, double* partial, double* out, cudaStream_t s,
+                         int nz = 1, double hz = 1.0);
 
 // ---------------------------------------------------------------- RK45 (rk45.cu)
 // Buffers of the adaptive Runge-Kutta-Fehlberg 4(5) integrator (FP64 SoA planes

@@ -43,6 +43,7 @@ bool is_wave(int problem) {
 bool has_fields(int problem) { return problem == SBP_WAVE_VAR_2D || problem == SBP_WAVE_2BLOCK_2D; }
 bool is_2d(int problem) { return is_wave(problem) || problem == SBP_ADVECTION_2D; }
 int dofs_of(int problem) {
+  if (problem == SBP_WAVE_3D) return 4;
   if (is_wave(problem)) return 3;
   return problem == SBP_REFLECTION_1D ? 2 : 1;
 }
@@ -53,10 +54,11 @@ struct sbp_ctx {
   sbp_desc d{};
   int dofs = 0;
   bool fp32 = false, two_d = false, wave = false, time_dependent = false;
-  long long nx = 0, ny = 1, pitch = 0, plane = 0, npts = 0, nscalar = 0;
+  bool three_d = false;  // SBP_WAVE_3D: nz slabs of ny rows; row-generic kernels see ny * nz rows
+  long long nx = 0, ny = 1, nz = 1, pitch = 0, plane = 0, npts = 0, nscalar = 0;
   int ysplit = 0;  // two-block problems: first row of the upper block
   size_t es = 8;
-  double hix = 1, hiy = 1, hx = 1, hy = 1;
+  double hix = 1, hiy = 1, hx = 1, hy = 1, hiz = 1, hz = 1;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   // device buffers: SoA planes (dofs * plane elements of T each)
@@ -252,6 +254,34 @@ int launch_stage(sbp_ctx* ctx, int stage, int rk, double t, double dt, void* in,
     }
     if (!bc_on) p.bc = BC_NONE;
     CK(launch_wave<T>(ctx->d.order, wave_kind(ctx), stage, *in_maps, p, ctx->stream));
+  } else if (ctx->three_d) {
+    Wave3Params<T> p;
+    std::memset(&p, 0, sizeof(p));
+    p.nx = (int)ctx->nx;
+    p.ny = (int)ctx->ny;
+    p.nz = (int)ctx->nz;
+    p.pitch = ctx->pitch;
+    p.slab = ctx->pitch * ctx->ny;
+    p.plane = ctx->plane;
+    p.in = (const T*)in;
+    p.un = (T*)ctx->un;
+    p.acc = (T*)ctx->acc;
+    p.wout = (T*)wout;
+    p.kout = (T*)kout;
+    p.comp = (T*)ctx->comp;
+    fill_taps<T>(p.dx, ctx->d.order, -ctx->hix);
+    fill_taps<T>(p.dy, ctx->d.order, -ctx->hiy);
+    fill_taps<T>(p.dz, ctx->d.order, -ctx->hiz);
+    const double hi0 = ops::get(ctx->d.order).hinv0;
+    p.bw[0] = ctx->hix * hi0;
+    p.bw[1] = ctx->hiy * hi0;
+    p.bw[2] = ctx->hiz * hi0;
+    p.bc = !bc_on ? BC_NONE : (ctx->d.bc == SBP_BC_CHARACTERISTIC ? BC_CHARACTERISTIC : BC_FREE_SURFACE);
+    p.compensated = ctx->fp32 ? 1 : 0;
+    p.c_acc = c_acc;
+    p.c_w = c_w;
+    if (ctl) p.skip = &ctl->done;
+    CK(launch_wave3d<T>(ctx->d.order, stage, p, ctx->stream));
   } else {
     LineParams<T> p = line_params<T>(ctx);
     p.in = (const T*)in;
@@ -368,9 +398,10 @@ int stage_in(sbp_ctx* ctx, const double* src, int where, const double** dev) {
 
 int pack_into(sbp_ctx* ctx, const double* aos, void* soa) {
   if (ctx->fp32)
-    CK(launch_pack<float>(aos, (float*)soa, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane, ctx->stream));
+    CK(launch_pack<float>(aos, (float*)soa, (int)ctx->nx, (int)(ctx->ny * ctx->nz), ctx->dofs, ctx->pitch, ctx->plane,
+                          ctx->stream));
   else
-    CK(launch_pack<double>(aos, (double*)soa, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane,
+    CK(launch_pack<double>(aos, (double*)soa, (int)ctx->nx, (int)(ctx->ny * ctx->nz), ctx->dofs, ctx->pitch, ctx->plane,
                            ctx->stream));
   ctx->launches++;
   return SBP_OK;
@@ -380,10 +411,12 @@ int unpack_to(sbp_ctx* ctx, const void* soa, double* dst, int where) {
   if (!dst) return fail(ctx, SBP_ERR_INVALID, "null array");
   double* out = (where == SBP_DEVICE) ? dst : ctx->io;
   if (ctx->fp32)
-    CK(launch_unpack<float>((const float*)soa, out, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane,
+    CK(launch_unpack<float>((const float*)soa, out, (int)ctx->nx, (int)(ctx->ny * ctx->nz), ctx->dofs, ctx->pitch,
+                            ctx->plane,
                             ctx->stream));
   else
-    CK(launch_unpack<double>((const double*)soa, out, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane,
+    CK(launch_unpack<double>((const double*)soa, out, (int)ctx->nx, (int)(ctx->ny * ctx->nz), ctx->dofs, ctx->pitch,
+                             ctx->plane,
                              ctx->stream));
   ctx->launches++;
   if (where != SBP_DEVICE)
@@ -412,7 +445,7 @@ Rk45Buffers rk45_buffers(sbp_ctx* ctx) {
   Rk45Buffers b;
   std::memset(&b, 0, sizeof(b));
   b.nx = (int)ctx->nx;
-  b.ny = (int)ctx->ny;
+  b.ny = (int)(ctx->ny * ctx->nz);  // rows per component plane
   b.dofs = ctx->dofs;
   b.pitch = ctx->pitch;
   b.plane = ctx->plane;
@@ -575,27 +608,35 @@ int sbp_create(const sbp_desc* desc, sbp_ctx** out) {
     delete ctx;
     return SBP_ERR_INVALID;
   };
-  if (d.problem < SBP_WAVE_HOM_2D || d.problem > SBP_WAVE_2BLOCK_2D) return bad("unknown problem");
+  if (d.problem < SBP_WAVE_HOM_2D || d.problem > SBP_WAVE_3D) return bad("unknown problem");
   if (d.order != 2 && d.order != 4 && d.order != 6) return bad("order must be 2, 4 or 6");
   if (d.precision != SBP_FP64 && d.precision != SBP_FP32) return bad("unknown precision");
   if (d.bc != SBP_BC_REFERENCE && d.bc != SBP_BC_CHARACTERISTIC) return bad("unknown boundary treatment");
   ctx->two_d = is_2d(d.problem);
+  ctx->three_d = d.problem == SBP_WAVE_3D;
   ctx->wave = is_wave(d.problem);
   ctx->dofs = dofs_of(d.problem);
   ctx->fp32 = d.precision == SBP_FP32;
   ctx->es = ctx->fp32 ? 4 : 8;
   ctx->nx = d.nx;
-  ctx->ny = ctx->two_d ? d.ny : 1;
+  ctx->ny = (ctx->two_d || ctx->three_d) ? d.ny : 1;
+  ctx->nz = ctx->three_d ? d.nz : 1;
   const long long m = ops::min_points(d.order);
-  if (ctx->nx < m || (ctx->two_d && ctx->ny < m)) return bad("grid smaller than the operator's minimum size");
-  if (ctx->nx > (1LL << 30) || ctx->ny > (1LL << 30)) return bad("grid too large");
-  if (d.bc == SBP_BC_CHARACTERISTIC && !(d.problem == SBP_WAVE_HOM_2D || has_fields(d.problem)))
+  if (ctx->nx < m || ((ctx->two_d || ctx->three_d) && ctx->ny < m) || (ctx->three_d && ctx->nz < m))
+    return bad("grid smaller than the operator's minimum size");
+  if (ctx->nx > (1LL << 30) || ctx->ny > (1LL << 30) || ctx->nz > (1LL << 20) ||
+      (ctx->three_d && ctx->ny * ctx->nz > (1LL << 30)))
+    return bad("grid too large");
+  if (d.bc == SBP_BC_CHARACTERISTIC && !(d.problem == SBP_WAVE_HOM_2D || d.problem == SBP_WAVE_3D ||
+                                          has_fields(d.problem)))
     return bad("characteristic boundary terms exist for the wave problems with rho, K fields only");
   if (d.problem == SBP_WAVE_MMS_2D && ctx->fp32) return bad("the manufactured-solution problem is FP64 only");
   if (has_fields(d.problem) && (!d.rho || !d.K)) return bad("rho and K are required");
   if (d.problem == SBP_WAVE_2BLOCK_2D && (ctx->ny % 2 || ctx->ny / 2 < m))
     return bad("two-block grids need an even ny with ny/2 at least the operator's minimum size");
-  if (!(d.xr[0] > d.xl[0]) || (ctx->two_d && !(d.xr[1] > d.xl[1]))) return bad("empty domain");
+  if (!(d.xr[0] > d.xl[0]) || ((ctx->two_d || ctx->three_d) && !(d.xr[1] > d.xl[1])) ||
+      (ctx->three_d && !(d.xr2 > d.xl2)))
+    return bad("empty domain");
   ctx->time_dependent = d.problem == SBP_WAVE_MMS_2D;
   ctx->hix = (ctx->nx - 1) / (d.xr[0] - d.xl[0]);
   ctx->hx = 1.0 / ctx->hix;
@@ -607,9 +648,15 @@ int sbp_create(const sbp_desc* desc, sbp_ctx** out) {
     }
     ctx->hy = 1.0 / ctx->hiy;
   }
+  if (ctx->three_d) {
+    ctx->hiy = (ctx->ny - 1) / (d.xr[1] - d.xl[1]);
+    ctx->hy = 1.0 / ctx->hiy;
+    ctx->hiz = (ctx->nz - 1) / (d.xr2 - d.xl2);
+    ctx->hz = 1.0 / ctx->hiz;
+  }
   ctx->pitch = (ctx->nx + 63) / 64 * 64;
-  ctx->plane = ctx->pitch * ctx->ny;
-  ctx->npts = ctx->nx * ctx->ny;
+  ctx->plane = ctx->pitch * ctx->ny * ctx->nz;
+  ctx->npts = ctx->nx * ctx->ny * ctx->nz;
   ctx->nscalar = ctx->npts * ctx->dofs;
 
   if (cudaSetDevice(d.device) != cudaSuccess) return bad("cudaSetDevice failed");
@@ -781,16 +828,18 @@ int sbp_error_norms(sbp_ctx* ctx, const double* exact, int where, double* l2, do
   int rc;
   if ((rc = stage_in(ctx, exact, where, &dev))) return rc;
   if (ctx->fp32)
-    CK(launch_error_norms<float>((const float*)ctx->un, dev, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch,
+    CK(launch_error_norms<float>((const float*)ctx->un, dev, (int)ctx->nx, (int)(ctx->ny * ctx->nz), ctx->dofs,
+                                 ctx->pitch,
                                  ctx->plane, ctx->partial, ctx->red, ctx->stream));
   else
-    CK(launch_error_norms<double>((const double*)ctx->un, dev, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch,
+    CK(launch_error_norms<double>((const double*)ctx->un, dev, (int)ctx->nx, (int)(ctx->ny * ctx->nz), ctx->dofs,
+                                  ctx->pitch,
                                   ctx->plane, ctx->partial, ctx->red, ctx->stream));
   ctx->launches += 2;
   double h[2];
   CK(cudaMemcpyAsync(h, ctx->red, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  const double hprod = ctx->two_d ? ctx->hx * ctx->hy : ctx->hx;
+  const double hprod = (ctx->two_d || ctx->three_d) ? ctx->hx * ctx->hy * (ctx->three_d ? ctx->hz : 1.0) : ctx->hx;
   *l2 = std::sqrt(hprod) * std::sqrt(h[0]);
   *linf = h[1];
   return SBP_OK;
@@ -801,10 +850,12 @@ int sbp_hnorm(sbp_ctx* ctx, double* hn) {
   CK(cudaSetDevice(ctx->d.device));
   if (ctx->fp32)
     CK(launch_hnorm<float>((const float*)ctx->un, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane,
-                           ctx->d.order, ctx->hx, ctx->hy, ctx->ysplit, ctx->partial, ctx->red, ctx->stream));
+                           ctx->d.order, ctx->hx, ctx->hy, ctx->ysplit, ctx->partial, ctx->red, ctx->stream,
+                           (int)ctx->nz, ctx->hz));
   else
     CK(launch_hnorm<double>((const double*)ctx->un, (int)ctx->nx, (int)ctx->ny, ctx->dofs, ctx->pitch, ctx->plane,
-                            ctx->d.order, ctx->hx, ctx->hy, ctx->ysplit, ctx->partial, ctx->red, ctx->stream));
+                            ctx->d.order, ctx->hx, ctx->hy, ctx->ysplit, ctx->partial, ctx->red, ctx->stream,
+                            (int)ctx->nz, ctx->hz));
   ctx->launches += 2;
   double h = 0;
   CK(cudaMemcpyAsync(&h, ctx->red, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));

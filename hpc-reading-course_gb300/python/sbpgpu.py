@@ -23,12 +23,13 @@ OK, ERR_INVALID, ERR_CUDA, ERR_DEVICE, ERR_UNSUPPORTED, ERR_TOO_LARGE = 0, -1, -
 NOALLOC_MAX_PLANE = 65536
 WAVE_HOM_2D, WAVE_MMS_2D, ADVECTION_1D, ADVECTION_2D, REFLECTION_1D, WAVE_VAR_2D = 1, 2, 3, 4, 5, 6
 WAVE_2BLOCK_2D = 7
+WAVE_3D = 8
 BC_REFERENCE, BC_CHARACTERISTIC = 0, 1
 FP64, FP32 = 0, 1
 HOST, DEVICE = 0, 1
 TWO_D = {WAVE_HOM_2D, WAVE_MMS_2D, WAVE_VAR_2D, ADVECTION_2D, WAVE_2BLOCK_2D}
 DOFS = {WAVE_HOM_2D: 3, WAVE_MMS_2D: 3, WAVE_VAR_2D: 3, ADVECTION_1D: 1, ADVECTION_2D: 1, REFLECTION_1D: 2,
-        WAVE_2BLOCK_2D: 3}
+        WAVE_2BLOCK_2D: 3, WAVE_3D: 4}
 
 # Every exported entry point of include/sbpgpu.h.
 EXPORTS = ("sbp_create", "sbp_destroy", "sbp_last_error", "sbp_dofs", "sbp_rhs", "sbp_apply", "sbp_rk4_nsteps",
@@ -64,7 +65,8 @@ class Desc(C.Structure):
                 ("xl", C.c_double * 2), ("xr", C.c_double * 2),
                 ("a", C.c_double), ("b", C.c_double),
                 ("rho", _dp), ("K", _dp),
-                ("stream", C.c_void_p), ("device", C.c_int)]
+                ("stream", C.c_void_p), ("device", C.c_int),
+                ("nz", C.c_longlong), ("xl2", C.c_double), ("xr2", C.c_double)]
 
 
 class Instance(C.Structure):
@@ -215,20 +217,23 @@ def _host(a: np.ndarray) -> np.ndarray:
 class Context:
     """One problem instance on one device (sbp_create / sbp_destroy)."""
 
-    def __init__(self, problem: int, order: int, nx: int, ny: int = 1, *, bc: int = BC_REFERENCE,
-                 precision: int = FP64, xl=(-1.0, -1.0), xr=(1.0, 1.0), a: float = 1.0, b: float = 0.0,
+    def __init__(self, problem: int, order: int, nx: int, ny: int = 1, nz: int = 1, *, bc: int = BC_REFERENCE,
+                 precision: int = FP64, xl=(-1.0, -1.0, -1.0), xr=(1.0, 1.0, 1.0), a: float = 1.0, b: float = 0.0,
                  rho=None, K=None, stream: int | None = None, device: int = 0):
         L = load()
         self._L = L
         self.problem, self.order, self.nx = problem, order, nx
-        self.ny = ny if problem in TWO_D else 1
+        self.ny = ny if problem in TWO_D or problem == WAVE_3D else 1
+        self.nz = nz if problem == WAVE_3D else 1
         self.dofs = DOFS.get(problem, 0)
         self.precision = precision
-        self.xl, self.xr = tuple(xl), tuple(xr)
+        xl = tuple(xl) + (-1.0,) * (3 - len(xl))
+        xr = tuple(xr) + (1.0,) * (3 - len(xr))
+        self.xl, self.xr = xl, xr
         self._rho = None if rho is None else np.ascontiguousarray(rho, dtype=np.float64).ravel()
         self._K = None if K is None else np.ascontiguousarray(K, dtype=np.float64).ravel()
-        d = Desc(problem, order, bc, precision, nx, self.ny, (C.c_double * 2)(*xl), (C.c_double * 2)(*xr), a, b,
-                 None, None, stream, device)
+        d = Desc(problem, order, bc, precision, nx, self.ny, (C.c_double * 2)(*xl[:2]), (C.c_double * 2)(*xr[:2]),
+                 a, b, None, None, stream, device, self.nz, xl[2], xr[2])
         if self._rho is not None:
             d.rho = self._rho.ctypes.data_as(_dp)
             d.K = self._K.ctypes.data_as(_dp)
@@ -241,7 +246,7 @@ class Context:
     # -- helpers
     @property
     def size(self) -> int:
-        return self.nx * self.ny * self.dofs
+        return self.nx * self.ny * self.nz * self.dofs
 
     @property
     def hx(self) -> float:
@@ -251,7 +256,11 @@ class Context:
     def hy(self) -> float:
         if self.problem == WAVE_2BLOCK_2D:
             return 0.5 * (self.xr[1] - self.xl[1]) / (self.ny // 2 - 1)
-        return (self.xr[1] - self.xl[1]) / (self.ny - 1) if self.problem in TWO_D else 1.0
+        return (self.xr[1] - self.xl[1]) / (self.ny - 1) if self.problem in TWO_D or self.problem == WAVE_3D else 1.0
+
+    @property
+    def hz(self) -> float:
+        return (self.xr[2] - self.xl[2]) / (self.nz - 1) if self.problem == WAVE_3D else 1.0
 
     def _check(self, rc: int):
         if rc:

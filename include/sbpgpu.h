@@ -44,9 +44,14 @@ typedef enum {
   SBP_ADVECTION_2D = 4,  /* code/demo/advection, u_t + a u_x + b u_y = 0 */
   SBP_REFLECTION_1D = 5, /* code/demo/reflection, [u;v]_t = [v_x;u_x] */
   SBP_WAVE_VAR_2D = 6,   /* (u,v,p) with rho(x,y), K(x,y) fields; no reference counterpart */
-  SBP_WAVE_2BLOCK_2D = 7 /* two SBP_WAVE_VAR_2D blocks, rows [0,ny/2) and [ny/2,ny), sharing the
+  SBP_WAVE_2BLOCK_2D = 7,/* two SBP_WAVE_VAR_2D blocks, rows [0,ny/2) and [ny/2,ny), sharing the
                             line y = (xl[1]+xr[1])/2 (stored in both blocks), coupled by an
                             energy-conserving interface SAT; no reference counterpart */
+  SBP_WAVE_3D = 8        /* (u,v,w,p), rho = K = 1, on nx x ny x nz points: the wave_hom system with a
+                            third direction (the reference leaves 3D as a TODO,
+                            code/include/partitioned_rhs/rhs.h:400-402); free-surface or
+                            characteristic SAT on the six faces. Arrays: element (k, j, i, comp)
+                            at 4*(i + nx*(j + ny*k)) + comp */
 } sbp_problem;
 
 typedef enum {
@@ -77,6 +82,8 @@ typedef struct {
   const double* K;    /* SBP_WAVE_VAR_2D: host array of nx*ny bulk moduli */
   void* stream;       /* cudaStream_t to run on, or NULL for a private stream */
   int device;         /* CUDA device ordinal */
+  long long nz;       /* SBP_WAVE_3D: grid points in z (ignored otherwise) */
+  double xl2, xr2;    /* SBP_WAVE_3D: z extent of the domain */
 } sbp_desc;
 
 /* Creates a context: validates the description (N >= max(closure width,
@@ -86,7 +93,7 @@ typedef struct {
 int sbp_create(const sbp_desc* desc, sbp_ctx** ctx);
 int sbp_destroy(sbp_ctx* ctx);
 const char* sbp_last_error(const sbp_ctx* ctx);
-/* Scalars per grid point of the context's problem (3, 2 or 1). */
+/* Scalars per grid point of the context's problem (4, 3, 2 or 1). */
 int sbp_dofs(const sbp_ctx* ctx);
 
 /* RHS callback body: dst = F(t, src) = matrix-free apply + boundary terms.

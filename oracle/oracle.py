@@ -26,9 +26,10 @@ REF_SO = os.path.join(HERE, "_ref", "libsbpref.so")
 
 WAVE_HOM_2D, WAVE_MMS_2D, ADVECTION_1D, ADVECTION_2D, REFLECTION_1D, WAVE_VAR_2D = 1, 2, 3, 4, 5, 6
 WAVE_2BLOCK_2D = 7
+WAVE_3D = 8
 BC_REFERENCE, BC_CHARACTERISTIC = 0, 1
 DOFS = {WAVE_HOM_2D: 3, WAVE_MMS_2D: 3, WAVE_VAR_2D: 3, ADVECTION_1D: 1, ADVECTION_2D: 1, REFLECTION_1D: 2,
-        WAVE_2BLOCK_2D: 3}
+        WAVE_2BLOCK_2D: 3, WAVE_3D: 4}
 TWO_D = {WAVE_HOM_2D, WAVE_MMS_2D, WAVE_VAR_2D, ADVECTION_2D, WAVE_2BLOCK_2D}
 
 _dp = C.POINTER(C.c_double)
@@ -45,7 +46,8 @@ class _Problem(C.Structure):
                 ("hix", C.c_double), ("hiy", C.c_double),
                 ("xl0", C.c_double), ("xl1", C.c_double),
                 ("a", C.c_double), ("b", C.c_double),
-                ("rho", _dp), ("K", _dp)]
+                ("rho", _dp), ("K", _dp),
+                ("nz", C.c_longlong), ("hiz", C.c_double), ("xl2", C.c_double)]
 
 
 def build(ref_dir: str | None = None, quiet: bool = True) -> None:
@@ -59,13 +61,16 @@ def build(ref_dir: str | None = None, quiet: bool = True) -> None:
 class Problem:
     """A grid problem on [xl, xr]^d with N points per direction, h = (xr-xl)/(N-1)."""
 
-    def __init__(self, problem: int, order: int, nx: int, ny: int = 1, *, xl=(-1.0, -1.0), xr=(1.0, 1.0),
-                 a: float = 1.0, b: float = 0.0, bc: int = BC_REFERENCE, rho=None, K=None):
+    def __init__(self, problem: int, order: int, nx: int, ny: int = 1, nz: int = 1, *, xl=(-1.0, -1.0, -1.0),
+                 xr=(1.0, 1.0, 1.0), a: float = 1.0, b: float = 0.0, bc: int = BC_REFERENCE, rho=None, K=None):
         self.problem, self.order, self.bc = problem, order, bc
-        self.nx, self.ny = nx, (ny if problem in TWO_D else 1)
-        self.xl, self.xr = tuple(xl), tuple(xr)
+        self.nx, self.ny = nx, (ny if problem in TWO_D or problem == WAVE_3D else 1)
+        self.nz = nz if problem == WAVE_3D else 1
+        xl, xr = tuple(xl) + (-1.0,) * (3 - len(xl)), tuple(xr) + (1.0,) * (3 - len(xr))
+        self.xl, self.xr = xl, xr
         self.hix = (nx - 1) / (xr[0] - xl[0])
-        self.hiy = (self.ny - 1) / (xr[1] - xl[1]) if problem in TWO_D else 1.0
+        self.hiy = (self.ny - 1) / (xr[1] - xl[1]) if problem in TWO_D or problem == WAVE_3D else 1.0
+        self.hiz = (self.nz - 1) / (xr[2] - xl[2]) if problem == WAVE_3D else 1.0
         if problem == WAVE_2BLOCK_2D:  # each block: ny/2 points over half of [xl1, xr1]
             self.hiy = (self.ny // 2 - 1) / ((xr[1] - xl[1]) / 2)
         self.a, self.b = a, b
@@ -75,11 +80,11 @@ class Problem:
 
     @property
     def size(self) -> int:
-        return self.nx * self.ny * self.dofs
+        return self.nx * self.ny * self.nz * self.dofs
 
     def c_struct(self) -> _Problem:
         s = _Problem(self.problem, self.order, self.bc, self.nx, self.ny, self.hix, self.hiy,
-                     self.xl[0], self.xl[1], self.a, self.b, None, None)
+                     self.xl[0], self.xl[1], self.a, self.b, None, None, self.nz, self.hiz, self.xl[2])
         if self.rho is not None:
             s.rho = _ptr(self.rho)
             s.K = _ptr(self.K)
@@ -121,6 +126,10 @@ class Port:
         L.orc_hnorm.argtypes = [_dp, C.c_longlong, C.c_longlong, C.c_longlong, C.c_double, C.c_double, C.c_int]
         L.orc_hnorm.restype = C.c_double
         L.orc_hnorm_2block.argtypes = L.orc_hnorm.argtypes
+        L.orc_hnorm3d.argtypes = [_dp] + [C.c_longlong] * 4 + [C.c_double] * 3 + [C.c_int]
+        L.orc_hnorm3d.restype = C.c_double
+        L.orc_init_wave3d_mode.argtypes = [_dp] + [C.c_longlong] * 3 + [C.c_double] * 6 + [C.c_int] * 3 + \
+            [C.c_double]
         L.orc_hnorm_2block.restype = C.c_double
         L.orc_error_l2.argtypes = [_dp, _dp, C.c_longlong, C.c_double]
         L.orc_error_l2.restype = C.c_double
@@ -194,6 +203,10 @@ class Port:
         v = np.ascontiguousarray(v, dtype=np.float64)
         return self.lib.orc_hnorm(_ptr(v), nx, ny, dofs, hx, hy, order)
 
+    def hnorm3d(self, v, nx, ny, nz, dofs, hx, hy, hz, order):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        return self.lib.orc_hnorm3d(_ptr(v), nx, ny, nz, dofs, hx, hy, hz, order)
+
     def hnorm_2block(self, v, nx, ny, dofs, hx, hy, order):
         v = np.ascontiguousarray(v, dtype=np.float64)
         return self.lib.orc_hnorm_2block(_ptr(v), nx, ny, dofs, hx, hy, order)
@@ -232,6 +245,13 @@ class Port:
     def init_wave_pulse(self, nx, ny, x0=0.0, y0=0.0, w=0.05, amp=1.0):
         v = np.zeros(nx * ny * 3)
         self.lib.orc_init_wave_pulse(_ptr(v), nx, ny, -1.0, -1.0, 2.0 / (nx - 1), 2.0 / (ny - 1), x0, y0, w, amp)
+        return v
+
+    def init_wave3d_mode(self, nx, ny, nz, t, a=1, b=2, c=2):
+        """Standing mode on [-1, 1]^3 with p = 0 on the faces (orc_init_wave3d_mode)."""
+        v = np.zeros(nx * ny * nz * 4)
+        self.lib.orc_init_wave3d_mode(_ptr(v), nx, ny, nz, -1.0, -1.0, -1.0, 2.0 / (nx - 1), 2.0 / (ny - 1),
+                                      2.0 / (nz - 1), a, b, c, t)
         return v
 
     def set_threads(self, n: int):

@@ -86,6 +86,7 @@ int orc_dofs(int problem) {
     case ORC_WAVE_MMS_2D:
     case ORC_WAVE_VAR_2D:
     case ORC_WAVE_2BLOCK_2D: return 3;
+    case ORC_WAVE_3D: return 4;
     case ORC_ADVECTION_1D:
     case ORC_ADVECTION_2D: return 1;
     case ORC_REFLECTION_1D: return 2;
@@ -107,12 +108,20 @@ static int is_2d(int problem) {
          problem == ORC_ADVECTION_2D || problem == ORC_WAVE_2BLOCK_2D;
 }
 
+/* Scalars of a state of problem p. */
+static long long nscalars(const orc_problem* p) {
+  const long long pts = p->nx * (is_2d(p->problem) || p->problem == ORC_WAVE_3D ? p->ny : 1) *
+                        (p->problem == ORC_WAVE_3D ? p->nz : 1);
+  return pts * orc_dofs(p->problem);
+}
+
 static int check(const orc_problem* p) {
   if (!p || orc_dofs(p->problem) < 0) return -1;
   const long long m = orc_min_points(p->order);
   if (m < 0) return -2;
   if (p->nx < m) return -3;
   if (is_2d(p->problem) && p->ny < m) return -3;
+  if (p->problem == ORC_WAVE_3D && (p->ny < m || p->nz < m)) return -3;
   if ((p->problem == ORC_WAVE_VAR_2D || p->problem == ORC_WAVE_2BLOCK_2D) && (!p->rho || !p->K)) return -4;
   if (p->problem == ORC_WAVE_2BLOCK_2D && (p->ny % 2 || p->ny / 2 < m)) return -3;
   return 0;
@@ -133,6 +142,7 @@ int orc_apply(const orc_problem* p, double t, const double* src, double* dst) {
     case ORC_WAVE_MMS_2D: DISPATCH(wave_mms_apply, p, t, src, dst); break;
     case ORC_WAVE_VAR_2D: DISPATCH(wave_var_apply, p, src, dst); break;
     case ORC_WAVE_2BLOCK_2D: DISPATCH(wave_2block_apply, p, src, dst); break;
+    case ORC_WAVE_3D: DISPATCH(wave3d_apply, p, src, dst); break;
     case ORC_ADVECTION_1D: DISPATCH(adv1d_apply, p, src, dst); break;
     case ORC_ADVECTION_2D: DISPATCH(adv2d_apply, p, src, dst); break;
     case ORC_REFLECTION_1D: DISPATCH(refl_apply, p, src, dst); break;
@@ -148,6 +158,7 @@ int orc_bc(const orc_problem* p, const double* src, double* dst) {
     case ORC_WAVE_MMS_2D: DISPATCH(wave_free_surface_bc, p, src, dst); break;
     case ORC_WAVE_VAR_2D: DISPATCH(wave_var_bc, p, src, dst); break;
     case ORC_WAVE_2BLOCK_2D: DISPATCH(wave_2block_bc, p, src, dst); break;
+    case ORC_WAVE_3D: DISPATCH(wave3d_bc, p, src, dst); break;
     case ORC_ADVECTION_1D: DISPATCH(adv1d_bc, p, src, dst); break;
     case ORC_ADVECTION_2D: DISPATCH(adv2d_bc, p, src, dst); break;
     case ORC_REFLECTION_1D: /* proj_dirichlet_bc_{l,r} (reflection_rhs.h:108-120) */
@@ -211,7 +222,7 @@ int orc_rk45(const orc_problem* p, double t0, double t_end, double dt0, const or
   if (rc) return rc;
   orc_rk45_opts o;
   if (opts) o = *opts; else orc_rk45_default_opts(&o);
-  const long long n = p->nx * (is_2d(p->problem) ? p->ny : 1) * orc_dofs(p->problem);
+  const long long n = nscalars(p);
   double* k[6];
   double* w = (double*)malloc(sizeof(double) * n);
   double* u5 = (double*)malloc(sizeof(double) * n);
@@ -325,7 +336,7 @@ long long orc_rk4_nsteps(double t_end, double* dt_inout) {
 int orc_rk4(const orc_problem* p, double t0, double dt, long long nsteps, double* v) {
   int rc = check(p);
   if (rc) return rc;
-  const long long n = p->nx * (is_2d(p->problem) ? p->ny : 1) * orc_dofs(p->problem);
+  const long long n = nscalars(p);
   double* k1 = (double*)malloc(sizeof(double) * n);
   double* k2 = (double*)malloc(sizeof(double) * n);
   double* k3 = (double*)malloc(sizeof(double) * n);
@@ -380,6 +391,16 @@ double orc_hnorm(const double* v, long long nx, long long ny, long long dofs, do
     case 2: return hnorm_o2(v, nx, ny, dofs, hx, hy);
     case 4: return hnorm_o4(v, nx, ny, dofs, hx, hy);
     case 6: return hnorm_o6(v, nx, ny, dofs, hx, hy);
+    default: return -1;
+  }
+}
+
+double orc_hnorm3d(const double* v, long long nx, long long ny, long long nz, long long dofs, double hx, double hy,
+                   double hz, int order) {
+  switch (order) {
+    case 2: return hnorm3d_o2(v, nx, ny, nz, dofs, hx, hy, hz);
+    case 4: return hnorm3d_o4(v, nx, ny, nz, dofs, hx, hy, hz);
+    case 6: return hnorm3d_o6(v, nx, ny, nz, dofs, hx, hy, hz);
     default: return -1;
   }
 }
@@ -467,6 +488,27 @@ void orc_init_wave_pulse(double* v, long long nx, long long ny, double xl0, doub
       q[0] = 0.0;
       q[1] = 0.0;
       q[2] = amp * exp(-(x * x + y * y) / (w * w));
+    }
+  }
+}
+
+void orc_init_wave3d_mode(double* v, long long nx, long long ny, long long nz, double xl0, double xl1, double xl2,
+                          double hx, double hy, double hz, int a, int b, int c, double t) {
+  const double w = ORC_PI * sqrt((double)(a * a + b * b + c * c));
+  const double ka = a * ORC_PI, kb = b * ORC_PI, kc = c * ORC_PI;
+  for (long long k = 0; k < nz; k++) {
+    const double z = xl2 + k * hz;
+    for (long long j = 0; j < ny; j++) {
+      const double y = xl1 + j * hy;
+      for (long long i = 0; i < nx; i++) {
+        const double x = xl0 + i * hx;
+        double* q = v + 4 * (i + nx * (j + ny * k));
+        const double sx = sin(ka * x), sy = sin(kb * y), sz = sin(kc * z);
+        q[0] = -(ka / w) * sin(w * t) * cos(ka * x) * sy * sz;
+        q[1] = -(kb / w) * sin(w * t) * sx * cos(kb * y) * sz;
+        q[2] = -(kc / w) * sin(w * t) * sx * sy * cos(kc * z);
+        q[3] = cos(w * t) * sx * sy * sz;
+      }
     }
   }
 }

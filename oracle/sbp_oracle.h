@@ -27,8 +27,10 @@ enum orc_problem_kind {
   ORC_ADVECTION_2D = 4, /* code/demo/advection/advection_rhs.h:155-558 */
   ORC_REFLECTION_1D = 5,/* code/demo/reflection/reflection_rhs.h */
   ORC_WAVE_VAR_2D = 6,  /* rho(x,y), K(x,y) fields; no reference counterpart */
-  ORC_WAVE_2BLOCK_2D = 7 /* two ORC_WAVE_VAR_2D blocks (rows [0,ny/2) and [ny/2,ny)) sharing the
+  ORC_WAVE_2BLOCK_2D = 7,/* two ORC_WAVE_VAR_2D blocks (rows [0,ny/2) and [ny/2,ny)) sharing the
                             interface line y = (xl1+xr1)/2, coupled by an interface SAT */
+  ORC_WAVE_3D = 8        /* 3D acoustic wave (u, v, w, p), rho = K = 1; no reference counterpart
+                            (3D is a TODO at code/include/partitioned_rhs/rhs.h:400-402) */
 };
 
 enum orc_bc_kind {
@@ -46,6 +48,8 @@ typedef struct {
   double a, b;        /* advection velocities */
   const double* rho;  /* ORC_WAVE_VAR_2D: nx*ny density, row-major (j,i) */
   const double* K;    /* ORC_WAVE_VAR_2D: nx*ny bulk modulus */
+  long long nz;       /* ORC_WAVE_3D: points in z (element (k, j, i, comp) at dofs*(i + nx*(j + ny*k)) + comp) */
+  double hiz, xl2;    /* ORC_WAVE_3D: inverse z spacing, lower z bound */
 } orc_problem;
 
 /* ORC_WAVE_2BLOCK_2D: each block has ny/2 points in y over half the domain,
@@ -113,6 +117,10 @@ double orc_hnorm1d_reference(const double* v, long long n, long long dofs, doubl
 double orc_hnorm(const double* v, long long nx, long long ny, long long dofs,
                  double hx, double hy, int order);
 
+/* H-norm of a 3D state (tensor product of the three 1D quadratures). */
+double orc_hnorm3d(const double* v, long long nx, long long ny, long long nz, long long dofs, double hx, double hy,
+                   double hz, int order);
+
 /* H-norm of a two-block state (ny/2 rows per block, each block's quadrature). */
 double orc_hnorm_2block(const double* v, long long nx, long long ny, long long dofs, double hx, double hy,
                         int order);
@@ -134,6 +142,11 @@ void orc_init_wave_mms(double* v, long long nx, long long ny, double xl0, double
 /* Reflection pulses (reflection_sim.cpp:177-225): t = 0 gives the initial
  * condition, otherwise the exact solution with width W. */
 void orc_init_reflection(double* v, long long n, double xl, double h, double t, double W);
+/* Standing mode of ORC_WAVE_3D with p = 0 on the faces of [-1,1]^3 (a, b, c integers):
+ * p = cos(w t) sin(a pi x) sin(b pi y) sin(c pi z), u = -(a pi / w) sin(w t) cos(a pi x) sin(b pi y)
+ * sin(c pi z) (v, w alike), w = pi sqrt(a^2 + b^2 + c^2); components (u, v, w, p). */
+void orc_init_wave3d_mode(double* v, long long nx, long long ny, long long nz, double xl0, double xl1, double xl2,
+                          double hx, double hy, double hz, int a, int b, int c, double t);
 /* Gaussian pressure pulse p0 = amp*exp(-((x-x0)^2+(y-y0)^2)/w^2), u = v = 0. */
 void orc_init_wave_pulse(double* v, long long nx, long long ny, double xl0, double xl1,
                          double hx, double hy, double x0, double y0, double w, double amp);
