@@ -18,17 +18,23 @@ constexpr int kW3X = 64, kW3Y = 4, kW3Z = 16;
 // free surface (wave_eq_hom_rhs.h:389-441 per face): lower face F_ud -= bw_d p, upper F_ud += bw_d p;
 // characteristic (Z = c = 1): lower face g = bw_d (p + u_d): F_ud -= g/2, F_p -= g/2;
 // upper face g = bw_d (p - u_d): F_ud += g/2, F_p -= g/2.
+template <typename T> struct Rhs4 { T u, v, w, p; };
+
 template <typename T>
-__device__ __noinline__ void wave3d_sat(const Wave3Params<T>& prm, int i, int j, int k, const T (&cen)[4],
-                                        T (&kc)[4]) {
+__device__ __noinline__ Rhs4<T> wave3d_sat(const Wave3Params<T>& prm, int i, int j, int k, T uc, T vc, T wc, T pc,
+                                           Rhs4<T> kc) {
+  // values and results by value: a noinline function taking arrays by reference
+  // would keep the caller's arrays in local memory on every point
+  double f[4] = {(double)kc.u, (double)kc.v, (double)kc.w, (double)kc.p};
+  const double cen[3] = {(double)uc, (double)vc, (double)wc};
   const int idx[3] = {i, j, k};
   const int n[3] = {prm.nx, prm.ny, prm.nz};
-  double f[4] = {(double)kc[0], (double)kc[1], (double)kc[2], (double)kc[3]};
-  const double p = (double)cen[3];
+  const double p = (double)pc;
+#pragma unroll
   for (int d = 0; d < 3; d++) {
     const bool lo = idx[d] == 0, hi = idx[d] == n[d] - 1;
     if (!lo && !hi) continue;
-    const double ud = (double)cen[d];
+    const double ud = cen[d];
     if (prm.bc == BC_CHARACTERISTIC) {
       if (lo) {
         const double g = prm.bw[d] * (p + ud);
@@ -45,7 +51,7 @@ __device__ __noinline__ void wave3d_sat(const Wave3Params<T>& prm, int i, int j,
       if (hi) f[d] += prm.bw[d] * p;
     }
   }
-  for (int c = 0; c < 4; c++) kc[c] = (T)f[c];
+  return Rhs4<T>{(T)f[0], (T)f[1], (T)f[2], (T)f[3]};
 }
 
 template <typename T, int ORD, int STAGE>
@@ -67,8 +73,13 @@ __device__ __forceinline__ void wave3d_point(const Wave3Params<T>& prm, int i, i
   kc[3] = d1_line<T, ORD>(U + xo, 1, nx, i, prm.dx) + d1_line<T, ORD>(V + yo, pitch, ny, j, prm.dy) +
           d1_line<T, ORD>(W + zo, slab, nz, k, prm.dz);
   const T cen[4] = {__ldg(U + q), __ldg(V + q), __ldg(W + q), __ldg(P + q)};
-  if (prm.bc != BC_NONE && (i == 0 || j == 0 || k == 0 || i == nx - 1 || j == ny - 1 || k == nz - 1))
-    wave3d_sat<T>(prm, i, j, k, cen, kc);
+  if (prm.bc != BC_NONE && (i == 0 || j == 0 || k == 0 || i == nx - 1 || j == ny - 1 || k == nz - 1)) {
+    const Rhs4<T> r = wave3d_sat<T>(prm, i, j, k, cen[0], cen[1], cen[2], cen[3], Rhs4<T>{kc[0], kc[1], kc[2], kc[3]});
+    kc[0] = r.u;
+    kc[1] = r.v;
+    kc[2] = r.w;
+    kc[3] = r.p;
+  }
   // RK4 stage update (classical RK4, code/include/time_stepping/time_stepping.h:127-142)
 #pragma unroll
   for (int c = 0; c < 4; c++) {
@@ -96,14 +107,26 @@ __device__ __forceinline__ void wave3d_point(const Wave3Params<T>& prm, int i, i
   }
 }
 
+// Blocks per SM the register budget is sized for: the kernel is latency-bound, so
+// occupancy pays (measured at 256^3, order 4: FP64 1.02e10 / 1.14e10 / 1.17e10
+// point-stages/s at 2 / 3 / 4 blocks, flat beyond; FP32 1.48e10 / 2.10e10 /
+// 2.67e10 / 3.07e10 / 3.48e10 at 2 .. 6).
+#ifndef SBP_W3_BLOCKS_F64
+#define SBP_W3_BLOCKS_F64 4
+#endif
+#ifndef SBP_W3_BLOCKS_F32
+#define SBP_W3_BLOCKS_F32 6
+#endif
 template <typename T, int ORD, int STAGE>
-__global__ void __launch_bounds__(kW3X * kW3Y) wave3d_stage_kernel(const __grid_constant__ Wave3Params<T> prm) {
+__global__ void __launch_bounds__(kW3X * kW3Y, sizeof(T) == 8 ? SBP_W3_BLOCKS_F64 : SBP_W3_BLOCKS_F32)
+    wave3d_stage_kernel(const __grid_constant__ Wave3Params<T> prm) {
   if (prm.skip && *prm.skip) return;
   const int i = blockIdx.x * kW3X + threadIdx.x;
   const int j = blockIdx.y * kW3Y + threadIdx.y;
   if (i >= prm.nx || j >= prm.ny) return;
   const int k0 = blockIdx.z * kW3Z;
   const int k1 = k0 + kW3Z < prm.nz ? k0 + kW3Z : prm.nz;
+#pragma unroll 1
   for (int k = k0; k < k1; k++) wave3d_point<T, ORD, STAGE>(prm, i, j, k);
 }
 
