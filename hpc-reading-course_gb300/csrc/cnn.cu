@@ -12,8 +12,13 @@
 //                         K = 9 taps x input channels; also computes the input
 //                         gradient (dgrad) with the spatially flipped,
 //                         transposed weights.
-//   conv3x3_wgrad_kernel  GEMM, M = output channels, N = input channels per
-//                         tap, K = pixels (split over CTAs, FP32 atomics).
+//   conv3x3_wgrad_kernel  GEMM per tap, M = output channels, N = input channels,
+//                         K = pixels: a CTA stages a 8 x 16 pixel tile of dy and
+//                         the matching x tile with its one-pixel halo in shared
+//                         memory once for all nine taps, builds the fragments
+//                         with ldmatrix.trans (K runs over pixels, the rows of
+//                         both NHWC arrays), and folds its FP32 sums into dw
+//                         with atomics once at the end.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -127,71 +132,96 @@ __global__ void __launch_bounds__(128) conv3x3_fwd_kernel(const bf16* __restrict
   }
 }
 
-// dw[n][tap][c] += sum_p dy[p][n] * x[p + off(tap)][c]. Grid (pixel chunks, 9 taps); each warp
-// accumulates its pixel range in registers and adds its partial sums atomically.
+// Four 8x8 b16 matrices from shared memory, transposed: lanes 8q..8q+7 give the row
+// addresses of matrix q; a thread receives rows 2(lane%4), 2(lane%4)+1 of column lane/4.
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t (&r)[4], const bf16* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(a));
+}
+
+constexpr int kWgTH = 8, kWgTW = 16;  // pixel tile: 8 rows of 16 = 8 K steps of 16 pixels
+
+// dw[n][tap][c] += sum_p dy[p][n] * x[p + off(tap)][c], zero padding outside the image.
+// 4 warps: warp w owns output channels 16 (w % MT) .. +15 and input channels 16 (role / MT)
+// .. +15 for all nine taps; when there are fewer (m, n) blocks than warps, the warps of a
+// block split the tile's K steps.
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(128) conv3x3_wgrad_kernel(const bf16* __restrict__ x, const bf16* __restrict__ dy,
-                                                            float* __restrict__ dw, int B, int H, int W,
-                                                            int pix_per_warp) {
-  static_assert(CIN % 8 == 0 && COUT % 16 == 0, "channel padding");
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int g = lane >> 2, t = lane & 3;
-  const int tap = blockIdx.y, ddy = tap / 3 - 1, ddx = tap % 3 - 1;
-  const long long P = (long long)B * H * W;
-  const long long pbeg = ((long long)blockIdx.x * 4 + warp) * pix_per_warp;
-  if (pbeg >= P) return;
-  const long long pend = pbeg + pix_per_warp < P ? pbeg + pix_per_warp : P;
-  float acc[COUT / 16][CIN / 8][4];
+                                                            float* __restrict__ dw, int B, int H, int W) {
+  static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channel padding");
+  constexpr int RSX = CIN + 8, RSY = COUT + 8;  // shared row strides (16-byte padding: no bank conflicts)
+  constexpr int HR = kWgTH + 2, HC = kWgTW + 2;  // x tile with its halo
+  constexpr int MT = COUT / 16, NB = CIN / 16, ROLES = MT * NB, KG = 4 / ROLES;
+  static_assert(ROLES >= 1 && ROLES <= 4 && 4 % ROLES == 0, "warp roles");
+  __shared__ __align__(16) bf16 sX[HR * HC * RSX];
+  __shared__ __align__(16) bf16 sY[kWgTH * kWgTW * RSY];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int role = warp % ROLES, kg = warp / ROLES;
+  const int mt = role % MT, nb = role / MT;
+  float acc[9][2][4];
 #pragma unroll
-  for (int mb = 0; mb < COUT / 16; mb++)
+  for (int tp = 0; tp < 9; tp++)
 #pragma unroll
-    for (int cb = 0; cb < CIN / 8; cb++) acc[mb][cb][0] = acc[mb][cb][1] = acc[mb][cb][2] = acc[mb][cb][3] = 0.f;
-  const bf16 zero = __float2bfloat16(0.f);
-  for (long long p0 = pbeg; p0 < pend; p0 += 16) {
-    // the four pixels this thread reads: k = 2t, 2t+1, 2t+8, 2t+9
-    const bf16* dyp[4];
-    const bf16* xp[4];
-    bool vy[4], vx[4];
-#pragma unroll
-    for (int s = 0; s < 4; s++) {
-      const long long p = p0 + 2 * t + (s & 1) + 8 * (s >> 1);
-      vy[s] = p < pend;
-      const long long q = vy[s] ? p : 0;
-      const int pw_ = (int)(q % W), ph_ = (int)((q / W) % H), pb_ = (int)(q / ((long long)W * H));
-      const int hh = ph_ + ddy, ww = pw_ + ddx;
-      vx[s] = vy[s] && hh >= 0 && hh < H && ww >= 0 && ww < W;
-      dyp[s] = dy + q * COUT;
-      xp[s] = x + (((long long)pb_ * H + (vx[s] ? hh : 0)) * W + (vx[s] ? ww : 0)) * CIN;
+    for (int j = 0; j < 2; j++) acc[tp][j][0] = acc[tp][j][1] = acc[tp][j][2] = acc[tp][j][3] = 0.f;
+  const int tilesX = (W + kWgTW - 1) / kWgTW, tilesY = (H + kWgTH - 1) / kWgTH;
+  const long long ntiles = (long long)B * tilesY * tilesX;
+  const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+  const int q = lane >> 3, r = lane & 7;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int b = (int)(tile / ((long long)tilesY * tilesX));
+    const int rem = (int)(tile - (long long)b * tilesY * tilesX);
+    const int ty0 = (rem / tilesX) * kWgTH, tx0 = (rem % tilesX) * kWgTW;
+    // dy tile: pixel p = row * 16 + column, COUT channels in 16-byte chunks
+    for (int e = threadIdx.x; e < kWgTH * kWgTW * (COUT / 8); e += 128) {
+      const int p = e / (COUT / 8), ch = e % (COUT / 8);
+      const int yy = ty0 + p / kWgTW, xx = tx0 + p % kWgTW;
+      uint4 v = zero;
+      if (yy < H && xx < W) v = *reinterpret_cast<const uint4*>(dy + (((long long)b * H + yy) * W + xx) * COUT + ch * 8);
+      *reinterpret_cast<uint4*>(sY + p * RSY + ch * 8) = v;
     }
-#pragma unroll
-    for (int mb = 0; mb < COUT / 16; mb++) {
+    // x tile with a one-pixel halo
+    for (int e = threadIdx.x; e < HR * HC * (CIN / 8); e += 128) {
+      const int rr = e / (CIN / 8), ch = e % (CIN / 8);
+      const int yy = ty0 - 1 + rr / HC, xx = tx0 - 1 + rr % HC;
+      uint4 v = zero;
+      if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+        v = *reinterpret_cast<const uint4*>(x + (((long long)b * H + yy) * W + xx) * CIN + ch * 8);
+      *reinterpret_cast<uint4*>(sX + rr * RSX + ch * 8) = v;
+    }
+    __syncthreads();
+    for (int st = kg; st < kWgTH; st += KG) {  // K step: tile row st, 16 pixels
+      // A = dy^T (16 output channels x 16 pixels): matrices (pixels +8(q>>1), channels +8(q&1))
       uint32_t a[4];
-      const int m0 = mb * 16 + g, m1 = m0 + 8;
-      a[0] = pack_pair(vy[0] ? dyp[0][m0] : zero, vy[1] ? dyp[1][m0] : zero);
-      a[1] = pack_pair(vy[0] ? dyp[0][m1] : zero, vy[1] ? dyp[1][m1] : zero);
-      a[2] = pack_pair(vy[2] ? dyp[2][m0] : zero, vy[3] ? dyp[3][m0] : zero);
-      a[3] = pack_pair(vy[2] ? dyp[2][m1] : zero, vy[3] ? dyp[3][m1] : zero);
+      ldsm_x4_trans(a, sY + (st * kWgTW + r + 8 * (q >> 1)) * RSY + mt * 16 + 8 * (q & 1));
 #pragma unroll
-      for (int cb = 0; cb < CIN / 8; cb++) {
-        const int c = cb * 8 + g;
-        const uint32_t b[2] = {pack_pair(vx[0] ? xp[0][c] : zero, vx[1] ? xp[1][c] : zero),
-                               pack_pair(vx[2] ? xp[2][c] : zero, vx[3] ? xp[3][c] : zero)};
-        mma_16816(acc[mb][cb], a, b);
+      for (int tp = 0; tp < 9; tp++) {
+        // B = x shifted by the tap (16 pixels x 16 input channels): matrices
+        // (pixels +8(q&1), channels +8(q>>1)) -> b0, b1 of channels 0-7 and of 8-15
+        const int hy = st + tp / 3, hx = r + 8 * (q & 1) + tp % 3;
+        uint32_t bq[4];
+        ldsm_x4_trans(bq, sX + (hy * HC + hx) * RSX + nb * 16 + 8 * (q >> 1));
+        const uint32_t b0[2] = {bq[0], bq[1]}, b1[2] = {bq[2], bq[3]};
+        mma_16816(acc[tp][0], a, b0);
+        mma_16816(acc[tp][1], a, b1);
       }
     }
+    __syncthreads();
   }
+  // accumulator (m, n): c0, c1 at (g, 2t), (g, 2t+1); c2, c3 at (g+8, 2t), (g+8, 2t+1)
+  const int g = lane >> 2, t = lane & 3;
 #pragma unroll
-  for (int mb = 0; mb < COUT / 16; mb++)
+  for (int tp = 0; tp < 9; tp++)
 #pragma unroll
-    for (int cb = 0; cb < CIN / 8; cb++)
+    for (int j = 0; j < 2; j++)
 #pragma unroll
       for (int e = 0; e < 4; e++) {
-        const int n = mb * 16 + g + 8 * (e >> 1), c = cb * 8 + 2 * t + (e & 1);
-        atomicAdd(&dw[((long long)n * 9 + tap) * CIN + c], acc[mb][cb][e]);
+        const int m = mt * 16 + g + 8 * (e >> 1), n = nb * 16 + j * 8 + 2 * t + (e & 1);
+        atomicAdd(dw + ((long long)m * 9 + tp) * CIN + n, acc[tp][j][e]);
       }
 }
 
-// db[n] += sum_p dy[p][n]
 template <int COUT>
 __global__ void bias_grad_kernel(const bf16* __restrict__ dy, float* __restrict__ db, long long P) {
   __shared__ float sh[COUT];
@@ -451,14 +481,16 @@ cudaError_t conv_dgrad(int l, const bf16* dy, bf16* dx, const sbp_cnn* c, int ba
 }
 
 cudaError_t conv_wgrad(int l, const bf16* x, const bf16* dy, float* dw, const sbp_cnn* c, int batch, cudaStream_t s) {
-  const long long P = (long long)batch * c->H * c->W;
-  const int ppw = 1024;
-  const dim3 grid((unsigned)((P + 4LL * ppw - 1) / (4LL * ppw)), 9);
+  // at most one CTA per SM: each CTA adds its sums to dw once, so this bounds the atomics per entry
+  const long long ntiles = (long long)batch * ((c->H + kWgTH - 1) / kWgTH) * ((c->W + kWgTW - 1) / kWgTW);
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+  const unsigned grid = (unsigned)(ntiles < nsm ? ntiles : (nsm > 0 ? nsm : 1));
   switch (l) {
     case 0:
     case 1:
-    case 2: conv3x3_wgrad_kernel<32, 32><<<grid, 128, 0, s>>>(x, dy, dw, batch, c->H, c->W, ppw); break;
-    default: conv3x3_wgrad_kernel<32, 16><<<grid, 128, 0, s>>>(x, dy, dw, batch, c->H, c->W, ppw); break;
+    case 2: conv3x3_wgrad_kernel<32, 32><<<grid, 128, 0, s>>>(x, dy, dw, batch, c->H, c->W); break;
+    default: conv3x3_wgrad_kernel<32, 16><<<grid, 128, 0, s>>>(x, dy, dw, batch, c->H, c->W); break;
   }
   return cudaGetLastError();
 }
