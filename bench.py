@@ -476,7 +476,7 @@ def run_learned_study(args):
     network every 4 steps, trained on restricted fine (1025 x 2*513, FP64) trajectories with seeded
     pulse position U[-0.5,0.5]^2, width U[0.02,0.1], amplitude U[0.5,2] (seeds 1000..), two windows
     drawn from the 16-window horizon per trajectory, started on the restricted fine state; then
-    `--rollout-rounds` rounds that add windows started on the corrected solve's own states. Judged
+    `--rollout-rounds` rounds that add windows started on the corrected solve's own states. Measured
     against the fine solve on 100 held-out trajectories (seeds 5000..5099) after 16 windows."""
     import numpy as np
     import torch

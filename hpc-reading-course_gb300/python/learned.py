@@ -20,10 +20,10 @@ with targets that pull back to the fine solution). The network has no biases
 and ReLU activations, so it is positively homogeneous: scaling a sample's
 features and target by the same factor leaves the function to learn
 unchanged. Each sample is scaled to unit target RMS, so every trajectory
-counts equally in relative terms, as in the relative error it is judged by. A correction that raises
+counts equally in relative terms, as in the relative error it is measured by. A correction that raises
 the coarse state's H-norm by more than `guard` (relative) fails the energy
 check; then the run falls back to the fine solve: the answer is the fine
-solver's, restricted to the coarse grid. The fine solve is also the judge:
+solver's, restricted to the coarse grid. The fine solve is also the reference:
 errors are measured against the restricted fine solution.
 
 Device memory and small glue operations (restriction by slicing, target

@@ -40,7 +40,7 @@ def test_energy_guard_falls_back_to_fine_solve(sbp):
         solver = learned.LearnedSolver(sv, net, learned.Scales())
         res = learned.evaluate(sv, solver, [5000], windows=3)
     assert solver.fallbacks == 1
-    assert res["learned"][0] == 0.0  # the answer came from the fine solve, the judge itself
+    assert res["learned"][0] == 0.0  # the answer came from the fine solve, the reference itself
 
 
 def _features_np(q_aos, rho, K, nx, ny, nb):
