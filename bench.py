@@ -263,7 +263,40 @@ def run_precision_study(args):
                              "max_rel": float(np.abs(d).max() / np.abs(out["fp64"]).max())},
             "seconds": times, "speedup_fp32": times["fp64"] / times["fp32"],
             "fields": "1 + 0.5 tanh(sum of 8 Fourier modes, |k| <= 6, A ~ N(0,1)), seeds 0 (rho) and 1 (K)"}
+    # against an exact solution: the standing mode (n, m) = (3, 4) of the rho = K = 1 system with
+    # free-surface SAT, both precisions to t = 0.05 on grids from 512^2 to the study's grid, the L2
+    # error (sqrt(hx hy) ||v - v_exact||) and the wall time of each
+    t_exact = 0.05
+    rows = []
+    for ng in sorted({512, 1024, 2048, n}):
+        if ng > n:
+            continue
+        hg = 2.0 / (ng - 1)
+        ns, dts = sbpgpu.rk4_nsteps(t_exact, 0.2 * hg)
+        exact = fields.standing_mode(ng, ng, t_exact)
+        ex = {"grid": ng, "steps": ns}
+        for name, prec in (("fp64", sbpgpu.FP64), ("fp32", sbpgpu.FP32)):
+            with sbpgpu.Context(sbpgpu.WAVE_HOM_2D, order, ng, ng, precision=prec) as ctx:
+                ctx.set_state(fields.standing_mode(ng, ng, 0.0))
+                ctx.step_resident(0.0, dts, 3)  # warm-up (graph capture), then restart
+                ctx.synchronize()
+                ctx.set_state(fields.standing_mode(ng, ng, 0.0))
+                ctx.synchronize()
+                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                stream = torch.cuda.ExternalStream(ctx.stream)
+                ev0.record(stream)
+                ctx.step_resident(0.0, dts, ns)
+                ev1.record(stream)
+                ctx.synchronize()
+                l2, _ = ctx.error_norms(exact)
+                ex[name] = {"l2_error": l2, "seconds": ev0.elapsed_time(ev1) / 1e3}
+        ex["error_ratio_fp32_fp64"] = ex["fp32"]["l2_error"] / ex["fp64"]["l2_error"]
+        ex["speedup_fp32"] = ex["fp64"]["seconds"] / ex["fp32"]["seconds"]
+        rows.append(ex)
+    line2 = {"study": "precision_exact", "order": order, "problem": "wave_hom standing mode (3, 4)",
+             "bc": "free surface", "t_end": t_exact, "dt": "0.2 h", "grids": rows}
     print(json.dumps(line), flush=True)
+    print(json.dumps(line2), flush=True)
 
 
 def batched_instances(count: int, seed: int = 2):

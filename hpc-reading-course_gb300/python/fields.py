@@ -39,3 +39,18 @@ def gaussian_pulse(nx: int, ny: int, x0: float = 0.0, y0: float = 0.0, width: fl
     v = np.zeros((ny, nx, 3))
     v[:, :, 2] = amp * np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / width**2)
     return v.ravel()
+
+
+def standing_mode(nx: int, ny: int, t: float, n: int = 3, m: int = 4, xl=(-1.0, -1.0), xr=(1.0, 1.0)):
+    """Exact solution of the rho = K = 1 wave system with free-surface boundaries (p = 0 on x, y = +-1):
+    the standing mode of the reference's wave_hom demo (code/demo/wave_hom/wave_eq_hom_sim.cpp:211-233),
+    u = -n cos(n pi x) sin(m pi y) sin(pi w t) / w, v = -m sin(n pi x) cos(m pi y) sin(pi w t) / w,
+    p = sin(n pi x) sin(m pi y) cos(pi w t), w = sqrt(n^2 + m^2); AoS (j, i, comp)."""
+    x = np.linspace(xl[0], xr[0], nx)[None, :]
+    y = np.linspace(xl[1], xr[1], ny)[:, None]
+    w = np.sqrt(n * n + m * m)
+    out = np.empty((ny, nx, 3))
+    out[..., 0] = -n * np.cos(n * np.pi * x) * np.sin(m * np.pi * y) * np.sin(np.pi * w * t) / w
+    out[..., 1] = -m * np.sin(n * np.pi * x) * np.cos(m * np.pi * y) * np.sin(np.pi * w * t) / w
+    out[..., 2] = np.sin(np.pi * n * x) * np.sin(np.pi * m * y) * np.cos(np.pi * w * t)
+    return out.ravel()
