@@ -363,6 +363,42 @@ def run_batched_study(args):
             out[name] = {"value": units / sec, "unit": UNIT, "seconds": sec, "rk4_steps": 100 * chunks,
                          "points": b.points, "tile_heights": {o: b.tile_height(o) for o in (2, 4, 6)},
                          "gpu_launches": b.launches - launches0}
+    # the same instances one after another through single contexts (waves with c != 1 through the
+    # variable-coefficient context, rho = 1, K = c^2), the same number of RK4 steps; creation and
+    # graph capture outside the timed region
+    import numpy as np
+
+    steps = 100 * max(1, args.steps)
+    for name, prec in (("fp64", sbpgpu.FP64), ("fp32", sbpgpu.FP32)):
+        ctxs = []
+        for d, v in zip(insts, states):
+            if d["problem"] == sbpgpu.WAVE_HOM_2D:
+                ones = np.ones(d["nx"] * d["ny"])
+                c = sbpgpu.Context(sbpgpu.WAVE_VAR_2D, d["order"], d["nx"], d["ny"], rho=ones, K=ones * d["c"] ** 2,
+                                   bc=d["bc"], precision=prec)
+            else:
+                c = sbpgpu.Context(sbpgpu.ADVECTION_2D, d["order"], d["nx"], d["ny"], a=d["a"], b=d["b"],
+                                   precision=prec)
+            c.set_state(v)
+            c.step_resident(0.0, d["dt"], 50)  # warm-up: graph capture
+            c.synchronize()
+            ctxs.append(c)
+        device = 0.0
+        t0 = time.perf_counter()
+        for c, d in zip(ctxs, insts):
+            stream = torch.cuda.ExternalStream(c.stream)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            c.step_resident(0.0, d["dt"], steps)
+            ev1.record(stream)
+            c.synchronize()
+            device += ev0.elapsed_time(ev1) / 1e3
+        wall = time.perf_counter() - t0
+        for c in ctxs:
+            c.close()
+        out[name]["one_by_one"] = {"device_seconds": device, "wall_seconds": wall,
+                                   "speedup_batched_device": device / out[name]["seconds"],
+                                   "speedup_batched_wall": wall / out[name]["seconds"]}
     out["tune_cache"] = cache
     print(json.dumps(out), flush=True)
 
