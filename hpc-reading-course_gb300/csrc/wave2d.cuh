@@ -118,8 +118,13 @@ template <typename T, int KIND> constexpr int wave_ring() {
 #ifndef SBP_FP32_WARPS
 #define SBP_FP32_WARPS 16
 #endif
+// The variable-coefficient FP32 kernel (up to 124 registers) runs 12 warps on its
+// 24-row tiles: 2.20 s against 2.54 s with 8 for 1748 steps at 4096^2.
+#ifndef SBP_FP32_VAR_WARPS
+#define SBP_FP32_VAR_WARPS 12
+#endif
 template <typename T, int KIND> constexpr int wave_warps() {
-  return sizeof(T) == 4 ? (KIND != WK_VAR ? SBP_FP32_WARPS : kWaveConsumerWarps)
+  return sizeof(T) == 4 ? (KIND != WK_VAR ? SBP_FP32_WARPS : SBP_FP32_VAR_WARPS)
                         : (KIND == WK_HOM ? SBP_FP64_WARPS : kWaveConsumerWarps);
 }
 
