@@ -914,7 +914,7 @@ int sbp_rk45_resident(sbp_ctx* ctx, double t0, double t_end, double dt0, const s
   c.dt_max = o.dt_max;
   c.max_steps = o.max_steps;
   c.max_reject = o.max_reject;
-  c.n = (double)(ctx->dofs * ctx->nx * ctx->ny);
+  c.n = (double)ctx->nscalar;  // every scalar of the state (nz slabs included)
   c.last_accepted = 1;
   c.status = RK45_OK;
   rk45_first_step(t0, t_end, std::fmin(dt0, o.dt_max), &c.h, &c.final_step);

@@ -140,6 +140,22 @@ def test_gpu_wave3d_rk4_matches_oracle(sbp, port, order):
 
 
 @pytest.mark.gpu
+def test_gpu_wave3d_rk45_adaptive(sbp, port):
+    """Adaptive steps: the weighted error norm counts every scalar of the 3D state."""
+    n = (20, 17, 15)
+    ctx, pb = _pair(sbp, 4, n, True)
+    v0 = _pulse(n, 5)
+    with ctx:
+        ctx.set_state(v0)
+        st = ctx.rk45_resident(0.0, 0.3, 0.01, atol=1e-6, rtol=1e-6)
+        got = ctx.get_state()
+    ref, rst = port.rk45(pb, v0, 0.0, 0.3, 0.01, atol=1e-6, rtol=1e-6)
+    assert (st["accepted"], st["rejected"]) == (rst["accepted"], rst["rejected"]) and st["accepted"] > 5
+    assert abs(st["wlte"] - rst["wlte"]) <= 1e-6 * rst["wlte"]
+    assert relerr(got, ref) < 1e-9
+
+
+@pytest.mark.gpu
 def test_gpu_wave3d_rk45_norms(sbp, port):
     n = (21, 18, 16)
     ctx, pb = _pair(sbp, 4, n, True)
