@@ -96,6 +96,27 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     return LIB
 
 
+DRIVER = os.path.join(LIB_DIR, "sbp_demo")
+
+
+def build_driver(force: bool = False) -> str:
+    """The demo driver (drivers/sbp_demo.cpp): plain C++ against include/sbpgpu.h, linked to the
+    library beside it (rpath $ORIGIN). Returns its path."""
+    lib = build()
+    src = os.path.join(PKG, "drivers", "sbp_demo.cpp")
+    if not force and os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= max(os.path.getmtime(src),
+                                                                                  os.path.getmtime(lib)):
+        return DRIVER
+    cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), src, "-o", DRIVER + ".tmp",
+           "-L", LIB_DIR, "-lsbpgpu", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stdout + r.stderr)
+        raise RuntimeError("build of sbp_demo failed")
+    os.replace(DRIVER + ".tmp", DRIVER)
+    return DRIVER
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--force", action="store_true")

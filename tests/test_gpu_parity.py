@@ -171,7 +171,8 @@ def test_rk4_line_problems_match_oracle(sbp, port, prob):
 
 
 def test_kat_advection_config_on_gpu(sbp, port):
-    """BASELINE config 1 through ts_rk4's replacement: L2 = 3.930261e-04."""
+    """1D advection, a = 1, N = 201, order 4, CFL 0.1, T = 1.8, through ts_rk4's replacement:
+    L2 = 3.930261e-04, the reference operators' known answer."""
     n, a = 201, 1.0
     with sbp.Context(sbp.ADVECTION_1D, 4, n, a=a) as c:
         v = c.ts_rk4(port.init_adv1d(n, a, 0.0), 1.8, 0.1 * 2.0 / (n - 1))
