@@ -546,7 +546,8 @@ def run_learned_study(args):
     pulse position U[-0.5,0.5]^2, width U[0.02,0.1], amplitude U[0.5,2] (seeds 1000..), two windows
     drawn from the 16-window horizon per trajectory, started on the restricted fine state; then
     `--rollout-rounds` rounds that add windows started on the corrected solve's own states. Measured
-    against the fine solve on 100 held-out trajectories (seeds 5000..5099) after 16 windows."""
+    against the fine solve on 100 held-out trajectories (seeds 5000..5099) after 16 windows, and every
+    form, the fine one included, against a solve at twice the fine resolution ("vs_truth")."""
     import numpy as np
     import torch
 
@@ -556,7 +557,7 @@ def run_learned_study(args):
 
     gpu_build.build()
     s = learned.Setup()
-    sv = learned.Solvers(s, mid=True)
+    sv = learned.Solvers(s, mid=True, truth=True)
     t0 = time.perf_counter()
     seeds = range(1000, 1000 + args.trajectories)
     X, Y, scales = learned.normalize(*learned.collect(sv, seeds, 16, keep=2))
@@ -596,6 +597,12 @@ def run_learned_study(args):
            "rel_l2_mid_median": float(np.median(res["mid"])),
            "seconds_fine": res["t_fine"], "seconds_coarse": res["t_coarse"], "seconds_learned": res["t_learned"],
            "seconds_mid": res["t_mid"],
+           "vs_truth": {"truth_grid": [sv.truth_shape[0], 2 * sv.truth_shape[1]],
+                        **{k: float(np.mean(v)) for k, v in res["vs_truth"].items()},
+                        **{k + "_median": float(np.median(v)) for k, v in res["vs_truth"].items()},
+                        "learned_over_fine": float(np.mean(res["vs_truth"]["learned"]) /
+                                                   np.mean(res["vs_truth"]["fine"])),
+                        "fine_seconds_over_learned": res["t_fine"] / res["t_learned"]},
            "fallbacks": solver.fallbacks, "held_out": 100}
     print(json.dumps(out), flush=True)
 

@@ -107,9 +107,11 @@ def _ready():
 
 class Solvers:
     """The fine and coarse two-block contexts plus device buffers; with `mid`, also a plain solve
-    at twice the coarse resolution (for the time-against-error comparison)."""
+    at twice the coarse resolution (for the time-against-error comparison); with `truth`, a solve at
+    twice the fine resolution that stands in for the exact solution when the fine solve's own error
+    is measured."""
 
-    def __init__(self, s: Setup, device: int = 0, mid: bool = False):
+    def __init__(self, s: Setup, device: int = 0, mid: bool = False, truth: bool = False):
         self.s = s
         self.dev = torch.device(f"cuda:{device}")
         rf, kf = two_layer_fields(s.nxf, s.nbf, s.ratio)
@@ -126,6 +128,13 @@ class Solvers:
             self.mid = sbpgpu.Context(sbpgpu.WAVE_2BLOCK_2D, s.order, nxm, 2 * nbm, rho=rm, K=km, bc=bc,
                                       device=device)
             self.mid_shape = (nxm, nbm)
+        self.truth = None
+        if truth:
+            nxt, nbt = 2 * (s.nxf - 1) + 1, 2 * (s.nbf - 1) + 1
+            rt, kt = two_layer_fields(nxt, nbt, s.ratio)
+            self.truth = sbpgpu.Context(sbpgpu.WAVE_2BLOCK_2D, s.order, nxt, 2 * nbt, rho=rt, K=kt, bc=bc,
+                                        device=device)
+            self.truth_shape = (nxt, nbt)
         self.rho_c = torch.from_numpy(rc).to(self.dev)
         self.K_c = torch.from_numpy(kc).to(self.dev)
         self.npc = s.nxc * 2 * s.nbc
@@ -173,6 +182,21 @@ class Solvers:
         out = torch.empty(nxm * 2 * nbm * 3, dtype=torch.float64, device=self.dev)
         self.mid.get_state_ptr(out.data_ptr(), sbpgpu.DEVICE)
         return out.view(2, nbm, nxm, 3)[:, ::2, ::2, :].contiguous().view(-1)
+
+    def truth_solve(self, params, windows: int):
+        """The pulse of `params` (trajectory_params) sampled on the truth grid, solved over `windows`
+        coarse windows at a quarter of the fine step, restricted to the coarse grid (every 8th point)."""
+        s = self.s
+        nxt, nbt = self.truth_shape
+        x0, y0, w, a = params
+        st = torch.from_numpy(pulse_state(nxt, nbt, x0, y0, w, a)).to(self.dev)
+        _ready()
+        self.truth.set_state_ptr(st.data_ptr(), sbpgpu.DEVICE)
+        self.truth.step_resident(0.0, s.dtf / 2, 8 * s.window * windows)
+        self.truth.synchronize()
+        out = torch.empty(nxt * 2 * nbt * 3, dtype=torch.float64, device=self.dev)
+        self.truth.get_state_ptr(out.data_ptr(), sbpgpu.DEVICE)
+        return out.view(2, nbt, nxt, 3)[:, ::8, ::8, :].contiguous().view(-1)
 
     def features(self, coarse_aos, inv_scale: float = 1.0):
         s = self.s
@@ -325,9 +349,12 @@ class LearnedSolver:
 def evaluate(sv: Solvers, solver: LearnedSolver, seeds, windows: int):
     """Relative L2 errors against the restricted fine solution after `windows` windows, for
     the plain coarse solve and the corrected one (and the plain solve at twice the coarse
-    resolution, if `sv` has it), and the wall time of each form."""
+    resolution, if `sv` has it), and the wall time of each form. If `sv` has the truth solve, also
+    every form's error, the fine solve's included, against it on the coarse grid points
+    (out["vs_truth"])."""
     s = sv.s
-    out = {"coarse": [], "learned": [], "mid": [], "t_fine": 0.0, "t_coarse": 0.0, "t_learned": 0.0, "t_mid": 0.0}
+    out = {"coarse": [], "learned": [], "mid": [], "t_fine": 0.0, "t_coarse": 0.0, "t_learned": 0.0, "t_mid": 0.0,
+           "vs_truth": {"coarse": [], "learned": [], "mid": [], "fine": []}}
     forms = [("coarse", solver.run_plain), ("learned", solver.run)]
     if sv.mid is not None:
         forms.append(("mid", sv.mid_solve))
@@ -339,10 +366,15 @@ def evaluate(sv: Solvers, solver: LearnedSolver, seeds, windows: int):
         fine = sv.fine_steps_from(fine0, 4 * s.window * windows)
         out["t_fine"] += time.perf_counter() - t0
         ref = sv.restrict(fine)
+        truth = sv.truth_solve((x0, y0, w, a), windows) if sv.truth is not None else None
+        if truth is not None:
+            out["vs_truth"]["fine"].append(float(torch.linalg.norm(ref - truth) / torch.linalg.norm(truth)))
         for key, fn in forms:
             t0 = time.perf_counter()
             st = fn(fine0, windows)
             torch.cuda.synchronize()
             out["t_" + key] += time.perf_counter() - t0
             out[key].append(float(torch.linalg.norm(st - ref) / torch.linalg.norm(ref)))
+            if truth is not None:
+                out["vs_truth"][key].append(float(torch.linalg.norm(st - truth) / torch.linalg.norm(truth)))
     return out
