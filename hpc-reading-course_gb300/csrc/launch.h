@@ -68,6 +68,8 @@ cudaError_t launch_line(int order, int kind, int stage, const LineParams<T>& prm
 // The 3D wave stage kernel (wave3d.cu).
 template <typename T>
 cudaError_t launch_wave3d(int order, int stage, const Wave3Params<T>& prm, cudaStream_t s);
+// Shared-memory opt-in of the 3D stage kernels of one order (outside stream capture).
+template <typename T> cudaError_t configure_wave3d(int order);
 
 // Batched stage kernels (wave_batch_inst.cu, one unit per order). `ty` is the
 // tile height: 8 or 16 (FP64), 16 or 32 (FP32).

@@ -738,6 +738,10 @@ int sbp_create(const sbp_desc* desc, sbp_ctx** out) {
     e = ctx->fp32 ? configure_wave<float>(d.order, wave_kind(ctx)) : configure_wave<double>(d.order, wave_kind(ctx));
     if (e != cudaSuccess) return cuda_fail("configure stage kernels", e);
   }
+  if (ctx->three_d) {
+    e = ctx->fp32 ? configure_wave3d<float>(d.order) : configure_wave3d<double>(d.order);
+    if (e != cudaSuccess) return cuda_fail("configure 3D stage kernels", e);
+  }
   if ((e = cudaDeviceSynchronize()) != cudaSuccess) return cuda_fail("create", e);
   *out = ctx;
   return SBP_OK;

@@ -8,10 +8,12 @@ to the reference's headers) on states constant in z; its semi-discrete energy
 rate is zero to rounding with free-surface faces and negative with
 characteristic ones; it converges to a standing mode at the operators' order.
 
-GPU: the 3D stage kernel through the C ABI against the oracle on the same
-inputs: RHS and matrix-free apply (1e-12, norm-wise relative, the bar of the
-2D parity tests), RK4 (FP64 1e-12; compensated FP32 1e-5), RK45 at fixed
-steps (1e-12), the error norms and the 3D H-norm (1e-13).
+GPU: the 3D stage kernels (the plane-ring kernel; the column kernel where
+SBP_WAVE3D_COLUMN selects it) through the C ABI against the oracle on the same
+inputs: RHS and matrix-free apply (FP64 1e-12, norm-wise relative, the bar of
+the 2D parity tests; FP32 2e-6 on FP32-representable inputs), RK4 (FP64
+1e-12; compensated FP32 1e-5), RK45 at fixed steps (1e-12), the error norms and
+the 3D H-norm (1e-13).
 """
 import numpy as np
 import pytest
@@ -123,6 +125,22 @@ def test_gpu_wave3d_rhs_matches_oracle(sbp, port, order, bc_char, n):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("order", [2, 4, 6])
+@pytest.mark.parametrize("bc_char", [False, True], ids=["free_surface", "characteristic"])
+@pytest.mark.parametrize("n", SIZES + [(70, 30, 35)], ids=["x".join(map(str, s)) for s in SIZES + [(70, 30, 35)]])
+def test_gpu_wave3d_rhs_fp32_matches_oracle(sbp, port, order, bc_char, n):
+    """The FP32 state's RHS (shared-memory tiles with halos, register windows along z,
+    closure rows from global memory) against the FP64 oracle on FP32-representable inputs."""
+    ctx, pb = _pair(sbp, order, n, bc_char, precision=sbp.FP32)
+    v = np.random.default_rng(order + 3 * bc_char).standard_normal(pb.size).astype(np.float32).astype(np.float64)
+    with ctx:
+        got = ctx.rhs(v)
+        got_apply = ctx.apply(v)
+    assert relerr(got, port.rhs(pb, v)) < 2e-6
+    assert relerr(got_apply, port.apply(pb, v)) < 2e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [2, 4, 6])
 def test_gpu_wave3d_rk4_matches_oracle(sbp, port, order):
     n = (24, 20, 18)
     for bc_char in (False, True):
@@ -136,6 +154,31 @@ def test_gpu_wave3d_rk4_matches_oracle(sbp, port, order):
         ctx, pb = _pair(sbp, order, n, bc_char, precision=sbp.FP32)
         with ctx:
             got32 = ctx.rk4(v0, 0.0, dt, 12)
+        assert relerr(got32, ref) < 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [2, 4, 6])
+def test_gpu_wave3d_column_kernel_matches_oracle(sbp, port, order, monkeypatch):
+    """The column form (every tap a global load), which runs where the plane-ring
+    kernel's 32-bit offsets or 16-byte alignment do not hold, selected here by
+    SBP_WAVE3D_COLUMN: RHS and RK4 in FP64 and compensated FP32."""
+    monkeypatch.setenv("SBP_WAVE3D_COLUMN", "1")
+    n = (33, 20, 17)
+    for bc_char in (False, True):
+        ctx, pb = _pair(sbp, order, n, bc_char)
+        v = np.random.default_rng(order).standard_normal(pb.size)
+        v0 = _pulse(n)
+        dt = 0.2 * 2.0 / (max(n) - 1)
+        with ctx:
+            got = ctx.rhs(v)
+            got_rk = ctx.rk4(v0, 0.0, dt, 6)
+        assert relerr(got, port.rhs(pb, v)) < 1e-12
+        ref = port.rk4(pb, v0, 0.0, dt, 6)
+        assert relerr(got_rk, ref) < 1e-12
+        ctx, pb = _pair(sbp, order, n, bc_char, precision=sbp.FP32)
+        with ctx:
+            got32 = ctx.rk4(v0, 0.0, dt, 6)
         assert relerr(got32, ref) < 1e-5
 
 
