@@ -63,6 +63,9 @@ def parse():
                          "rk45: adaptive RKF45 (ts_rk45) on the bench's wave problem to --rk45-t-end. "
                          "wave3d: the 3D wave system on --grid3d^3 points, FP64 and FP32")
     ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--batched-forms", default="fp64,fp32", help="batched: comma-separated precisions to run")
+    ap.add_argument("--no-one-by-one", action="store_true",
+                    help="batched: skip the same instances run one after another through single contexts")
     ap.add_argument("--trajectories", type=int, default=2000, help="learned: training trajectories")
     ap.add_argument("--epochs", type=int, default=30, help="learned: training epochs per round")
     ap.add_argument("--rollout-rounds", type=int, default=2,
@@ -343,7 +346,8 @@ def run_batched_study(args):
     out = {"study": "batched", "instances": len(insts),
            "waves": sum(1 for d in insts if d["problem"] == sbpgpu.WAVE_HOM_2D),
            "orders": {o: sum(1 for d in insts if d["order"] == o) for o in (2, 4, 6)}}
-    for name, prec in (("fp64", sbpgpu.FP64), ("fp32", sbpgpu.FP32)):
+    forms = [f for f in (("fp64", sbpgpu.FP64), ("fp32", sbpgpu.FP32)) if f[0] in args.batched_forms.split(",")]
+    for name, prec in forms:
         with sbpgpu.Batch(insts, precision=prec) as b:
             for k, v in enumerate(states):
                 b.set_state(k, v)
@@ -369,7 +373,7 @@ def run_batched_study(args):
     import numpy as np
 
     steps = 100 * max(1, args.steps)
-    for name, prec in (("fp64", sbpgpu.FP64), ("fp32", sbpgpu.FP32)):
+    for name, prec in forms if not args.no_one_by_one else ():
         ctxs = []
         for d, v in zip(insts, states):
             if d["problem"] == sbpgpu.WAVE_HOM_2D:

@@ -199,11 +199,13 @@ int fill_params(sbp_batch* b) {
       p.bwx = hix * hi0;
       p.bwy = hiy * hi0;
       p.kconst = (T)(d.c * d.c);
+      p.kz = p.kc = std::sqrt((double)p.kconst);  // sqrt(rho K) = sqrt(K / rho) with rho = 1, rounded alike
       p.dt = d.dt;
       p.bc = d.bc == SBP_BC_CHARACTERISTIC ? BC_CHARACTERISTIC : BC_FREE_SURFACE;
       p.err = b->err;
       w.wa = (T*)at(b->wa, g.off);
       w.wb = (T*)at(b->wb, g.off);
+      batch_rk4_coefficients<T>(d.dt, w.c_acc, w.c_w);
       waves.push_back(w);
     } else {
       BatchLine<T> l;
@@ -228,6 +230,7 @@ int fill_params(sbp_batch* b) {
       l.wa = (T*)at(b->wa, g.off);
       l.wb = (T*)at(b->wb, g.off);
       l.dt = d.dt;
+      batch_rk4_coefficients<T>(d.dt, l.c_acc, l.c_w);
       lines.push_back(l);
     }
   }

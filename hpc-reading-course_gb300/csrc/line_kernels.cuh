@@ -69,7 +69,9 @@ __device__ __forceinline__ void line_point(const LineParams<T>& prm, const T* __
     const T* col = in + i;
     k[0] = d1_line<T, ORD>(row, 1, nx, i, prm.dx) + d1_line<T, ORD>(col, pitch, ny, j, prm.dy);
     cen[0] = in[q];
-    if (prm.bc) {  // SAT_bc_{west,south,east,north} (advection_rhs.h:460-528)
+    // SAT_bc_{west,south,east,north} (advection_rhs.h:460-528), FP64, at boundary
+    // points only (the FP64 round trip is exact elsewhere, and costly on the FP64 pipe)
+    if (prm.bc && (i == 0 || j == 0 || i == nx - 1 || j == ny - 1)) {
       double kk = (double)k[0];
       const double u = (double)cen[0];
       if (i == 0) kk += prm.sat[0] * u;

@@ -54,6 +54,7 @@ template <typename T> struct WaveParams {
   double bwx, bwy;    // hix * HI[0], hiy * HI[0]: SAT weights (FP64)
   T c_acc, c_w;       // acc (+)= c_acc * k ; w = u^n + c_w * k
   T kconst;           // WK_CONST: bulk modulus K (rho = 1)
+  double kz, kc;      // WK_CONST: sqrt(K) in FP64, the impedance and speed of the characteristic SAT
   double dt;          // batched: the instance's time step
   int bc;             // BcKind
   int ysplit;         // 0: one block; else rows [0,ysplit) and [ysplit,ny) are two blocks
@@ -221,8 +222,12 @@ __device__ __noinline__ Rhs3<T> apply_sat(const WaveParams<T>& prm, const T* in,
     if (i == nx - 1) ku64 = (KIND == WK_VAR) ? ku64 + ri * (prm.bwx * p64) : ku64 + prm.bwx * p64;
     if (j == ny - 1) kv64 = (KIND == WK_VAR) ? kv64 + ri * (prm.bwy * p64) : kv64 + prm.bwy * p64;
   } else {
-    // characteristic SAT on the incoming characteristic p + Z u_n
-    const double z = sqrt(rho * kk), c = sqrt(kk / rho), hr = 0.5 / rho, hc = 0.5 * c;
+    // characteristic SAT on the incoming characteristic p + Z u_n; WK_CONST reads
+    // Z = c = sqrt(K) from the parameters (computed once on the host: an FP64
+    // square root per boundary point is long on the FP64 pipe)
+    const double z = KIND == WK_CONST ? prm.kz : sqrt(rho * kk);
+    const double c = KIND == WK_CONST ? prm.kc : sqrt(kk / rho);
+    const double hr = 0.5 / rho, hc = 0.5 * c;
     const double u64 = (double)uc, v64 = (double)vc;
     if (i == 0) { const double g = prm.bwx * (p64 + z * u64); ku64 -= hr * g; kp64 -= hc * g; }
     if (j == 0) { const double g = prm.bwy * (p64 + z * v64); kv64 -= hr * g; kp64 -= hc * g; }

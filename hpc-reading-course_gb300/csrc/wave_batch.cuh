@@ -25,6 +25,7 @@ template <typename T> struct alignas(16) BatchWave {
   WaveParams<T> prm;  // geometry, taps, SAT weights, kconst, dt, un/acc/comp pointers
   T* wa;              // stage-input ping-pong buffers
   T* wb;
+  T c_acc[4], c_w[4];  // RK4 stage rk's coefficients at [rk - 1], computed on the host
 };
 
 // Tensor maps of one batched wave instance, in global memory (64-byte aligned):
@@ -40,15 +41,27 @@ __device__ __forceinline__ void bulk_copy_g2s(void* smem_dst, const void* gsrc, 
 }
 
 // Stage input and output buffers and RK4 coefficients of stage rk (1..4) of
-// the classical RK4 step sequence (see the single-instance runtime).
+// the classical RK4 step sequence (see the single-instance runtime). The
+// coefficients come from the instance block: computing dt / 6 here would put an
+// FP64 division per tile and thread on the FP64 pipe, which the FP32 kernels
+// otherwise barely use (measured: it held the pipe 58-64 % busy).
 template <typename T>
 __device__ __forceinline__ void batch_stage_buffers(const BatchWave<T>& I, int rk, const T*& in, T*& wout, T& c_acc,
                                                     T& c_w) {
-  const double dt = I.prm.dt;
   in = rk == 1 ? I.prm.un : (rk == 3 ? I.wb : I.wa);
   wout = (rk == 1 || rk == 3) ? I.wa : I.wb;
-  c_acc = (T)((rk == 1 || rk == 4) ? dt / 6 : dt / 3);
-  c_w = (T)(rk == 3 ? dt : 0.5 * dt);
+  c_acc = I.c_acc[rk - 1];
+  c_w = I.c_w[rk - 1];
+}
+
+// acc coefficients dt / 6, dt / 3, dt / 3, dt / 6 and stage-input coefficients
+// dt / 2, dt / 2, dt (the last stage has none) in the state type, rounded as the
+// single-instance runtime rounds them.
+template <typename T> inline void batch_rk4_coefficients(double dt, T (&c_acc)[4], T (&c_w)[4]) {
+  for (int rk = 1; rk <= 4; rk++) {
+    c_acc[rk - 1] = (T)((rk == 1 || rk == 4) ? dt / 6 : dt / 3);
+    c_w[rk - 1] = (T)(rk == 3 ? dt : 0.5 * dt);
+  }
 }
 
 // A tile-list entry: the instance's slot and the tile's origin, so the
@@ -57,11 +70,43 @@ struct BatchTile {
   int slot, i0, j0, pad;
 };
 
+// Consumer warps of the batched wave kernel per precision.
+#ifndef SBP_BATCH_WARPS_F32
+#define SBP_BATCH_WARPS_F32 16
+#endif
+#ifndef SBP_BATCH_WARPS_F64
+#define SBP_BATCH_WARPS_F64 8
+#endif
+template <typename T> constexpr int batch_warps() { return sizeof(T) == 4 ? SBP_BATCH_WARPS_F32 : SBP_BATCH_WARPS_F64; }
 template <typename T, int ORD, int STAGE, int TY>
-__global__ void __launch_bounds__(kWaveThreads, 1)
+using BatchWaveTile = WaveTile<T, ORD, STAGE, TY, (int)sizeof(BatchWave<T>), false, 2, batch_warps<T>()>;
+
+// Tile order of a CTA: with SBP_BATCH_BLOCKED a contiguous range of the tile
+// list (consecutive tiles mostly of one instance, so its tensor maps and
+// parameter block stay cached), else every gridDim.x-th tile.
+#ifndef SBP_BATCH_BLOCKED
+#define SBP_BATCH_BLOCKED 0
+#endif
+#ifndef SBP_BATCH_PREFETCH_MAPS
+#define SBP_BATCH_PREFETCH_MAPS 0
+#endif
+__device__ __forceinline__ void batch_tile_range(int ntiles, int& first, int& step, int& end) {
+  if (SBP_BATCH_BLOCKED) {
+    first = (int)((long long)ntiles * blockIdx.x / gridDim.x);
+    end = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
+    step = 1;
+  } else {
+    first = blockIdx.x;
+    end = ntiles;
+    step = gridDim.x;
+  }
+}
+
+template <typename T, int ORD, int STAGE, int TY>
+__global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, TY>::THREADS, 1)
     wave_batch_stage_kernel(const BatchWave<T>* __restrict__ insts, const CUtensorMap* __restrict__ maps,
                             const BatchTile* __restrict__ tiles, int ntiles, int rk, int* err) {
-  using Tile = WaveTile<T, ORD, STAGE, TY, (int)sizeof(BatchWave<T>)>;
+  using Tile = BatchWaveTile<T, ORD, STAGE, TY>;
   constexpr int HX = Tile::HX, HY = Tile::HY;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
@@ -71,20 +116,33 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
   if (threadIdx.x == 0) {
     mbar_init(&full[0], 1);
     mbar_init(&full[1], 1);
-    mbar_init(&empty[0], kWaveConsumerWarps);
-    mbar_init(&empty[1], kWaveConsumerWarps);
+    mbar_init(&empty[0], Tile::WARPS);
+    mbar_init(&empty[1], Tile::WARPS);
     fence_barrier_init();
   }
   __syncthreads();
   const int sel = rk == 1 ? 0 : (rk == 3 ? 2 : 1);  // which buffer is the stage input
+  int first, step, end;
+  batch_tile_range(ntiles, first, step, end);
 
-  if (warp == kWaveConsumerWarps) {
+  if (warp == Tile::WARPS) {
     if (lane == 0) {
       int k = 0;
-      BatchTile next = blockIdx.x < ntiles ? tiles[blockIdx.x] : BatchTile{0, 0, 0, 0};
-      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
+      BatchTile next = first < end ? tiles[first] : BatchTile{0, 0, 0, 0};
+      for (int tile = first; tile < end; tile += step, k++) {
         const BatchTile tt = next;
-        if (tile + (int)gridDim.x < ntiles) next = tiles[tile + gridDim.x];  // prefetch the next descriptor
+        if (tile + step < end) {
+          next = tiles[tile + step];  // the next descriptor, read ahead
+          if (SBP_BATCH_PREFETCH_MAPS && next.slot != tt.slot) {
+            const CUtensorMap* mn = maps + (long long)next.slot * kBatchMaps;
+            prefetch_tensormap(&mn[3 * sel + 0]);
+            prefetch_tensormap(&mn[3 * sel + 1]);
+            prefetch_tensormap(&mn[3 * sel + 2]);
+            if (Tile::LOAD_UN) prefetch_tensormap(&mn[9]);
+            if (Tile::LOAD_ACC) prefetch_tensormap(&mn[10]);
+            if (Tile::LOAD_COMP) prefetch_tensormap(&mn[11]);
+          }
+        }
         const int b = k & 1;
         if (k >= 2 && !mbar_wait_bounded(&empty[b], ((k >> 1) - 1) & 1)) {
           atomicOr(err, ERR_TMA_TIMEOUT);
@@ -108,7 +166,7 @@ __global__ void __launch_bounds__(kWaveThreads, 1)
   }
 
   int k = 0;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
+  for (int tile = first; tile < end; tile += step, k++) {
     const int b = k & 1;
     if (!mbar_wait_bounded(&full[b], (k >> 1) & 1)) {
       if (lane == 0) atomicOr(err, ERR_TMA_TIMEOUT);
@@ -135,6 +193,7 @@ template <typename T> struct alignas(16) BatchLine {
   T* wa;
   T* wb;
   double dt;
+  T c_acc[4], c_w[4];  // RK4 stage rk's coefficients at [rk - 1], computed on the host
 };
 
 constexpr int kLineTileX = 32, kLineTileY = 32, kLineThreadsY = 8;
@@ -153,11 +212,10 @@ __global__ void __launch_bounds__(kLineTileX * kLineThreadsY)
   }
   __syncthreads();
   const BatchLine<T>& I = *reinterpret_cast<const BatchLine<T>*>(blk);
-  const double dt = I.dt;
   const T* in = rk == 1 ? I.prm.un : (rk == 3 ? I.wb : I.wa);
   T* wout = (rk == 1 || rk == 3) ? I.wa : I.wb;
-  const T c_acc = (T)((rk == 1 || rk == 4) ? dt / 6 : dt / 3);
-  const T c_w = (T)(rk == 3 ? dt : 0.5 * dt);
+  const T c_acc = I.c_acc[rk - 1];
+  const T c_w = I.c_w[rk - 1];
   const int i = tt.i0 + threadIdx.x;
   if (i >= I.prm.nx) return;
 #pragma unroll

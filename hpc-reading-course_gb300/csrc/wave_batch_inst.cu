@@ -16,7 +16,7 @@ namespace {
 
 template <typename T, int STAGE, int TY>
 constexpr int batch_smem() {
-  return WaveTile<T, SBP_ORDER, STAGE, TY, (int)sizeof(BatchWave<T>)>::SMEM;
+  return BatchWaveTile<T, SBP_ORDER, STAGE, TY>::SMEM;
 }
 
 template <typename T, int TY>
@@ -40,15 +40,15 @@ cudaError_t launch_ty(int stage, const BatchWave<T>* insts, const CUtensorMap* m
   switch (stage) {
     case ST_FIRST:
       wave_batch_stage_kernel<T, SBP_ORDER, ST_FIRST, TY>
-          <<<grid, kWaveThreads, batch_smem<T, ST_FIRST, TY>(), s>>>(insts, maps, tiles, ntiles, rk, err);
+          <<<grid, BatchWaveTile<T, SBP_ORDER, ST_FIRST, TY>::THREADS, batch_smem<T, ST_FIRST, TY>(), s>>>(insts, maps, tiles, ntiles, rk, err);
       break;
     case ST_MID:
       wave_batch_stage_kernel<T, SBP_ORDER, ST_MID, TY>
-          <<<grid, kWaveThreads, batch_smem<T, ST_MID, TY>(), s>>>(insts, maps, tiles, ntiles, rk, err);
+          <<<grid, BatchWaveTile<T, SBP_ORDER, ST_MID, TY>::THREADS, batch_smem<T, ST_MID, TY>(), s>>>(insts, maps, tiles, ntiles, rk, err);
       break;
     case ST_LAST:
       wave_batch_stage_kernel<T, SBP_ORDER, ST_LAST, TY>
-          <<<grid, kWaveThreads, batch_smem<T, ST_LAST, TY>(), s>>>(insts, maps, tiles, ntiles, rk, err);
+          <<<grid, BatchWaveTile<T, SBP_ORDER, ST_LAST, TY>::THREADS, batch_smem<T, ST_LAST, TY>(), s>>>(insts, maps, tiles, ntiles, rk, err);
       break;
     default: return cudaErrorInvalidValue;
   }
