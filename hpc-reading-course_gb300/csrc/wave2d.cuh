@@ -159,10 +159,13 @@ struct WaveTile {
   static constexpr int BYTES_K = 2 * TY * kWaveTX * (int)sizeof(T);
   static constexpr int OFF_K = align128(OFF_C + (LOAD_COMP ? BYTES_PT : 0));
   static constexpr int OFF_PRM = align128(OFF_K + (LOAD_COEF ? BYTES_K : 0));  // batched: instance parameters
-  static constexpr int STAGE_BYTES = OFF_PRM + align128(PRM_BYTES);
+  // the RHS of the tile's x-face points, kept for the deferred SAT pass ([side][row][u, v, p])
+  static constexpr int OFF_DEF = OFF_PRM + align128(PRM_BYTES);
+  static constexpr int STAGE_BYTES = OFF_DEF + align128(2 * TY * 3 * (int)sizeof(T));
   static constexpr int NST = NST_;                            // ring depth
   static constexpr int OFF_BAR = NST * STAGE_BYTES;           // full[NST], empty[NST]
-  static constexpr int SMEM = OFF_BAR + 128;
+  static constexpr int OFF_DBAR = OFF_BAR + 128;              // deferred-pass barriers[NST]
+  static constexpr int SMEM = OFF_BAR + 256;
   static constexpr uint32_t TX_BYTES = BYTES_P + BYTES_U + BYTES_V + (LOAD_UN ? BYTES_PT : 0) +
                                        (LOAD_ACC ? BYTES_PT : 0) + (LOAD_COMP ? BYTES_PT : 0) +
                                        (LOAD_COEF ? BYTES_K : 0) + PRM_BYTES;
@@ -255,6 +258,37 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
+// RK4 stage update of component c of one point (o: its offset in the state,
+// sp: its place in a tile's 3-component point boxes).
+template <typename T, int STAGE, typename Tile>
+__device__ __forceinline__ void wave_point_store(const WaveParams<T>& prm, T* wout, const T c_acc, const T c_w,
+                                                 const T* sA, const T* sN, const T* sC, int sp, int c, long long o,
+                                                 T kc, T cen) {
+  constexpr int TPT = Tile::TY * kWaveTX;
+  if constexpr (STAGE == ST_RHS) {
+    prm.kout[o] = kc;
+  } else if constexpr (STAGE == ST_FIRST) {
+    // acc = u + dt/6 k1 (FP32 compensated: acc = dt/6 k1), w = u + dt/2 k1
+    st_stream(prm.acc + o, Tile::COMP ? c_acc * kc : fma(c_acc, kc, cen));
+    st_stream(wout + o, fma(c_w, kc, cen));
+  } else if constexpr (STAGE == ST_MID) {
+    st_stream(prm.acc + o, fma(c_acc, kc, sA[c * TPT + sp]));
+    st_stream(wout + o, fma(c_w, kc, sN[c * TPT + sp]));
+  } else if constexpr (STAGE == ST_LAST) {
+    const T d = fma(c_acc, kc, sA[c * TPT + sp]);
+    if constexpr (Tile::COMP) {
+      // Kahan summation of the step increment into the FP32 state
+      const T u0 = sN[c * TPT + sp], e = sC[c * TPT + sp];
+      const T yv = d - e;
+      const T tv = u0 + yv;
+      st_stream(prm.comp + o, (tv - u0) - yv);
+      st_stream(prm.un + o, tv);
+    } else {
+      st_stream(prm.un + o, d);
+    }
+  }
+}
+
 // One tile of the stage for the consumer warps: everything the tile needs is
 // in the shared-memory stage `st` (laid out as Tile), except closure-row taps
 // and coefficient fields. `in` is the stage input, `wout` the next stage input.
@@ -262,7 +296,8 @@ template <typename T, int ORD, int KIND, int STAGE, typename Tile>
 __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, const T* __restrict__ in, T* wout,
                                                   const T c_acc, const T c_w, const unsigned char* st, const int i0,
                                                   const int j0, const int warp, const int lane,
-                                                  double* errsq = nullptr) {
+                                                  double* errsq = nullptr, uint64_t* dbar = nullptr,
+                                                  uint32_t* dphase = nullptr, const int b = 0, const int k = 0) {
   constexpr bool COMP = Tile::COMP;
   constexpr int TY = Tile::TY, W = OpShape<ORD>::W, CS = OpShape<ORD>::CS, R = Tile::R;
   constexpr int HX = Tile::HX, HY = Tile::HY, PW = Tile::PW;
@@ -280,6 +315,16 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
   const T* sA = reinterpret_cast<const T*>(st + Tile::OFF_A);
   const T* sC = reinterpret_cast<const T*>(st + Tile::OFF_C);
   const T* sK = reinterpret_cast<const T*>(st + Tile::OFF_K);  // [1/rho | K] when Tile::LOAD_COEF
+  // Deferred SAT: a point on an x face only (not on a y face or the interface
+  // lines) leaves its RHS in the stage's deferred box and skips SAT and update;
+  // after every consumer warp has passed the tile's rows, one warp applies the
+  // SAT and the update to all of them, one point per lane. In a row warp a single
+  // x-face lane would hold the FP64 pipe for the whole SAT sequence.
+  constexpr bool DEFER_OK = !is_rkf_stage(STAGE);
+  const bool xfaces = DEFER_OK && dbar != nullptr && prm.bc != BC_NONE &&
+                      (i0 == 0 || (nx - 1 >= i0 && nx - 1 < i0 + kWaveTX));
+  T* sD = reinterpret_cast<T*>(const_cast<unsigned char*>(st) + Tile::OFF_DEF);
+  (void)sD;
   (void)sN;
   (void)sA;
   (void)sC;
@@ -385,6 +430,13 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
       const bool edge = (i == 0) || (j == 0) || (i == nx - 1) || (j == ny - 1) ||
                         (prm.ysplit > 0 && (j == prm.ysplit - 1 || j == prm.ysplit));
       if (prm.bc != BC_NONE && edge) {
+        if (xfaces && j != 0 && j != ny - 1 && !(prm.ysplit > 0 && (j == prm.ysplit - 1 || j == prm.ysplit))) {
+          T* d = sD + ((i == 0 ? 0 : TY) + y) * 3;  // an x-face point only: deferred
+          d[0] = ku;
+          d[1] = kv;
+          d[2] = kp;
+          continue;
+        }
         const Rhs3<T> r = apply_sat<T, KIND>(prm, in, i, j, pc, uc, vc, Rhs3<T>{ku, kv, kp});
         ku = r.u;
         kv = r.v;
@@ -419,26 +471,40 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
             st_stream(prm.rkunew + o, u5);
             *errsq += rkf_err_term(u5, u4, prm.rkatol, prm.rkrtol);
           }
-        } else if constexpr (STAGE == ST_FIRST) {
-          // acc = u + dt/6 k1 (FP32 compensated: acc = dt/6 k1), w = u + dt/2 k1
-          st_stream(prm.acc + o, COMP ? c_acc * kc[c] : fma(c_acc, kc[c], cen[c]));
-          st_stream(wout + o, fma(c_w, kc[c], cen[c]));
-        } else if constexpr (STAGE == ST_MID) {
-          st_stream(prm.acc + o, fma(c_acc, kc[c], sA[c * TPT + sp]));
-          st_stream(wout + o, fma(c_w, kc[c], sN[c * TPT + sp]));
-        } else {  // ST_LAST
-          const T d = fma(c_acc, kc[c], sA[c * TPT + sp]);
-          if constexpr (COMP) {
-            // Kahan summation of the step increment into the FP32 state
-            const T u0 = sN[c * TPT + sp], e = sC[c * TPT + sp];
-            const T yv = d - e;
-            const T tv = u0 + yv;
-            st_stream(prm.comp + o, (tv - u0) - yv);
-            st_stream(prm.un + o, tv);
-          } else {
-            st_stream(prm.un + o, d);
-          }
+        } else {
+          wave_point_store<T, STAGE, Tile>(prm, wout, c_acc, c_w, sA, sN, sC, sp, c, o, kc[c], cen[c]);
         }
+      }
+    }
+  }
+  if constexpr (DEFER_OK) {
+    if (xfaces) {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(dbar);  // this warp's deferred entries are in shared memory
+      const uint32_t par = (*dphase >> b) & 1u;
+      *dphase ^= 1u << b;
+      if (warp != k % Tile::WARPS) return;
+      if (!mbar_wait_bounded(dbar, par)) {
+        if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
+        return;
+      }
+      for (int e = lane; e < 2 * TY; e += 32) {
+        const int side = e / TY, y = e - side * TY, j = j0 + y;
+        const int i = side == 0 ? 0 : nx - 1;
+        if (i < i0 || i >= i0 + kWaveTX || j >= ny || j == 0 || j == ny - 1 ||
+            (prm.ysplit > 0 && (j == prm.ysplit - 1 || j == prm.ysplit)))
+          continue;
+        const int x = i - i0;
+        const T pc = sP[(y + HY) * PW + x + HX], uc = sU[y * PW + x + HX], vc = sV[(y + HY) * kWaveTX + x];
+        const T* d = sD + (side * TY + y) * 3;
+        const Rhs3<T> r = apply_sat<T, KIND>(prm, in, i, j, pc, uc, vc, Rhs3<T>{d[0], d[1], d[2]});
+        const T kc[3] = {r.u, r.v, r.p};
+        const T cen[3] = {uc, vc, pc};
+        const long long q = (long long)j * pitch + i;
+        const int sp = y * kWaveTX + x;
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+          wave_point_store<T, STAGE, Tile>(prm, wout, c_acc, c_w, sA, sN, sC, sp, c, c * plane + q, kc[c], cen[c]);
       }
     }
   }
@@ -467,10 +533,12 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
   const int ntiles = ntx * ((ny + TY - 1) / TY);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
+  uint64_t* dbar = reinterpret_cast<uint64_t*>(smem + Tile::OFF_DBAR);
   if (threadIdx.x == 0) {
     for (int s = 0; s < NST; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], WARPS);
+      mbar_init(&dbar[s], WARPS);
     }
     fence_barrier_init();
   }
@@ -506,6 +574,7 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
 
   // ---------------- consumers: warps 0-7
   double errsq = 0.0;  // ST_RKF6: this thread's share of the weighted error sum
+  uint32_t dphase = 0;  // parity of each stage's next deferred-pass barrier phase
   int k = 0;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
     const int b = k % NST;
@@ -515,7 +584,8 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
     }
     const int i0 = (tile % ntx) * kWaveTX, j0 = (tile / ntx) * TY;
     wave_tile_compute<T, ORD, KIND, STAGE, Tile>(prm, prm.in, prm.wout, prm.c_acc, prm.c_w,
-                                                 smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane, &errsq);
+                                                 smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane, &errsq, &dbar[b],
+                                                 &dphase, b, k);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[b]);
   }

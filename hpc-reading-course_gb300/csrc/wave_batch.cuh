@@ -113,11 +113,14 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, TY>::THREADS, 1)
   uint64_t* empty = full + 2;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
+  uint64_t* dbar = reinterpret_cast<uint64_t*>(smem + Tile::OFF_DBAR);
   if (threadIdx.x == 0) {
     mbar_init(&full[0], 1);
     mbar_init(&full[1], 1);
     mbar_init(&empty[0], Tile::WARPS);
     mbar_init(&empty[1], Tile::WARPS);
+    mbar_init(&dbar[0], Tile::WARPS);
+    mbar_init(&dbar[1], Tile::WARPS);
     fence_barrier_init();
   }
   __syncthreads();
@@ -165,6 +168,7 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, TY>::THREADS, 1)
     return;
   }
 
+  uint32_t dphase = 0;  // parity of each stage's next deferred-pass barrier phase
   int k = 0;
   for (int tile = first; tile < end; tile += step, k++) {
     const int b = k & 1;
@@ -180,7 +184,8 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, TY>::THREADS, 1)
     T* wout;
     T c_acc, c_w;
     batch_stage_buffers(I, rk, in, wout, c_acc, c_w);
-    wave_tile_compute<T, ORD, WK_CONST, STAGE, Tile>(I.prm, in, wout, c_acc, c_w, st, i0, j0, warp, lane);
+    wave_tile_compute<T, ORD, WK_CONST, STAGE, Tile>(I.prm, in, wout, c_acc, c_w, st, i0, j0, warp, lane, nullptr,
+                                                     &dbar[b], &dphase, b, k);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[b]);
   }
