@@ -276,6 +276,9 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 // warps issue most copies while the others compute. Measured at 256^3, order 4,
 // FP32: 6.3e10 point-stage updates/s, against 5.7e10 when a plane's chunks are
 // dealt evenly to all warps and 5.9e10 with one extra warp that issues every copy.
+// Deferring the x-face points' SAT to one warp after an extra barrier per plane (as
+// the 2D kernels do without a barrier of their own) measured slower here: FP32
+// 5.95e10, FP64 1.29e10 against 1.32e10.
 template <typename T, int NR, int NC, int V, int NT>
 __device__ __forceinline__ void copy_box(T* tile, int tp, const T* src, int gj0, int gi0, int nx, int ny, int pitch,
                                          int tid) {
