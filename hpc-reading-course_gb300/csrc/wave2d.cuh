@@ -289,6 +289,41 @@ __device__ __forceinline__ void wave_point_store(const WaveParams<T>& prm, T* wo
   }
 }
 
+// Fehlberg stage S = STAGE - ST_RKF1 + 1 of component c of one point: the same
+// sums, in the same order, as the unfused combination kernels (rk45.cu). kS is
+// this stage's derivative, pre[0..S-2] = k_1..k_{S-1} and pre[S-1] = u (S > 1).
+template <typename T, int STAGE, int NPRE>
+__device__ __forceinline__ void wave_point_rkf(const WaveParams<T>& prm, T* wout, long long o, double kS, double cen,
+                                               const double (&pre)[NPRE], double* errsq) {
+  constexpr int S = STAGE - ST_RKF1 + 1;
+  const double h = prm.tctl[1];
+  if constexpr (S < 6) {
+    prm.rkk[S - 1][o] = kS;
+    double s = kRkfA[S][0] * (S == 1 ? kS : pre[0]);
+#pragma unroll
+    for (int jj = 1; jj < S; jj++) s = fma(kRkfA[S][jj], jj == S - 1 ? kS : pre[jj], s);
+    const double u0 = S == 1 ? cen : pre[S - 1];
+    st_stream(wout + o, fma(h, s, u0));
+  } else {
+    double u5, u4;
+    rkf_candidate(pre[5], h, pre[0], pre[2], pre[3], pre[4], kS, u5, u4);
+    st_stream(prm.rkunew + o, u5);
+    *errsq += rkf_err_term(u5, u4, prm.rkatol, prm.rkrtol);
+  }
+}
+
+// k_1..k_{S-1} and u of one component of one point for Fehlberg stage S (stage 6
+// does not need k2: its weights are zero).
+template <typename T, int RKS>
+__device__ __forceinline__ void wave_rkf_preload(const WaveParams<T>& prm, long long o, double (&pre)[RKS]) {
+  if constexpr (RKS > 1) {
+#pragma unroll
+    for (int jj = 0; jj < RKS - 1; jj++)
+      if (RKS < 6 || jj != 1) pre[jj] = __ldg(prm.rkk[jj] + o);
+    pre[RKS - 1] = __ldg(prm.rku + o);
+  }
+}
+
 // One tile of the stage for the consumer warps: everything the tile needs is
 // in the shared-memory stage `st` (laid out as Tile), except closure-row taps
 // and coefficient fields. `in` is the stage input, `wout` the next stage input.
@@ -320,7 +355,7 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
   // after every consumer warp has passed the tile's rows, one warp applies the
   // SAT and the update to all of them, one point per lane. In a row warp a single
   // x-face lane would hold the FP64 pipe for the whole SAT sequence.
-  constexpr bool DEFER_OK = !is_rkf_stage(STAGE);
+  constexpr bool DEFER_OK = true;  // every stage kind, Fehlberg stages included
   const bool xfaces = DEFER_OK && dbar != nullptr && prm.bc != BC_NONE &&
                       (i0 == 0 || (nx - 1 >= i0 && nx - 1 < i0 + kWaveTX));
   T* sD = reinterpret_cast<T*>(const_cast<unsigned char*>(st) + Tile::OFF_DEF);
@@ -358,12 +393,7 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
       if constexpr (RKS > 1) {
         const long long q0 = (long long)j * pitch + i;
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-#pragma unroll
-          for (int jj = 0; jj < RKS - 1; jj++)
-            if (RKS < 6 || jj != 1) rkpre[c][jj] = __ldg(prm.rkk[jj] + c * plane + q0);
-          rkpre[c][RKS - 1] = __ldg(prm.rku + c * plane + q0);
-        }
+        for (int c = 0; c < 3; c++) wave_rkf_preload<T, RKS>(prm, c * plane + q0, rkpre[c]);
       }
       (void)rkpre;
 
@@ -453,24 +483,7 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
         if constexpr (STAGE == ST_RHS) {
           prm.kout[o] = kc[c];
         } else if constexpr (is_rkf_stage(STAGE)) {
-          // Fehlberg stage S: the same sums, in the same order, as the unfused
-          // combination kernels (rk45.cu); k_S is the register value.
-          constexpr int S = RKS;
-          const double h = prm.tctl[1];
-          const double kS = kc[c];
-          if constexpr (S < 6) {
-            prm.rkk[S - 1][o] = kS;
-            double s = kRkfA[S][0] * (S == 1 ? kS : rkpre[c][0]);
-#pragma unroll
-            for (int jj = 1; jj < S; jj++) s = fma(kRkfA[S][jj], jj == S - 1 ? kS : rkpre[c][jj], s);
-            const double u0 = S == 1 ? (double)cen[c] : rkpre[c][S - 1];
-            st_stream(wout + o, fma(h, s, u0));
-          } else {
-            double u5, u4;
-            rkf_candidate(rkpre[c][5], h, rkpre[c][0], rkpre[c][2], rkpre[c][3], rkpre[c][4], kS, u5, u4);
-            st_stream(prm.rkunew + o, u5);
-            *errsq += rkf_err_term(u5, u4, prm.rkatol, prm.rkrtol);
-          }
+          wave_point_rkf<T, STAGE, RKS>(prm, wout, o, (double)kc[c], (double)cen[c], rkpre[c], errsq);
         } else {
           wave_point_store<T, STAGE, Tile>(prm, wout, c_acc, c_w, sA, sN, sC, sp, c, o, kc[c], cen[c]);
         }
@@ -503,8 +516,16 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
         const long long q = (long long)j * pitch + i;
         const int sp = y * kWaveTX + x;
 #pragma unroll
-        for (int c = 0; c < 3; c++)
-          wave_point_store<T, STAGE, Tile>(prm, wout, c_acc, c_w, sA, sN, sC, sp, c, c * plane + q, kc[c], cen[c]);
+        for (int c = 0; c < 3; c++) {
+          if constexpr (is_rkf_stage(STAGE)) {
+            constexpr int RKS = STAGE - ST_RKF1 + 1;
+            double pre[RKS];
+            wave_rkf_preload<T, RKS>(prm, c * plane + q, pre);
+            wave_point_rkf<T, STAGE, RKS>(prm, wout, c * plane + q, (double)kc[c], (double)cen[c], pre, errsq);
+          } else {
+            wave_point_store<T, STAGE, Tile>(prm, wout, c_acc, c_w, sA, sN, sC, sp, c, c * plane + q, kc[c], cen[c]);
+          }
+        }
       }
     }
   }
