@@ -124,6 +124,12 @@ template <typename T, int KIND> constexpr int wave_ring() {
 #ifndef SBP_FP32_VAR_WARPS
 #define SBP_FP32_VAR_WARPS 12
 #endif
+// Where the variable-coefficient kernels read 1/rho and K: 1 from the tile's
+// TMA box in shared memory, 0 with read-only global loads (no box), 2 both
+// (the box loaded but unused; kept to measure what the box costs).
+#ifndef SBP_VAR_COEF
+#define SBP_VAR_COEF 1
+#endif
 template <typename T, int KIND> constexpr int wave_warps() {
   return sizeof(T) == 4 ? (KIND != WK_VAR ? SBP_FP32_WARPS : SBP_FP32_VAR_WARPS)
                         : (KIND == WK_HOM ? SBP_FP64_WARPS : kWaveConsumerWarps);
@@ -440,10 +446,17 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
         kv = dyp;
         kp = prm.kconst * kp;
       } else if constexpr (KIND == WK_VAR) {
-        const T ri = __ldg(prm.rinv + q);
+        T ri, km;
+        if constexpr (SBP_VAR_COEF == 1) {  // the tile's [1/rho | K] box
+          ri = sK[y * kWaveTX + x];
+          km = sK[TPT + y * kWaveTX + x];
+        } else {
+          ri = __ldg(prm.rinv + q);
+          km = __ldg(prm.kmod + q);
+        }
         ku = ri * dxp;
         kv = ri * dyp;
-        kp = __ldg(prm.kmod + q) * kp;
+        kp = km * kp;
       } else {  // WK_MMS (FP64): code/demo/wave/wave_eq_rhs.h:42-64
         const double PI = 3.14159265358979323846264;
         const double xx = mms_x(prm.xl0, i, prm.hix), yy = mms_x(prm.xl1, j, prm.hiy);
@@ -533,8 +546,8 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
 
 // The Tile type of the single-instance kernel for (T, order, kind, stage).
 template <typename T, int ORD, int KIND, int STAGE>
-using WaveStageTile = WaveTile<T, ORD, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR, wave_ring<T, KIND>(),
-                               wave_warps<T, KIND>()>;
+using WaveStageTile = WaveTile<T, ORD, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR && SBP_VAR_COEF != 0,
+                               wave_ring<T, KIND>(), wave_warps<T, KIND>()>;
 
 template <typename T, int ORD, int KIND, int STAGE>
 __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
