@@ -30,34 +30,40 @@ template <typename T>
 __device__ __noinline__ Rhs4<T> wave3d_sat(const Wave3Params<T>& prm, int i, int j, int k, T uc, T vc, T wc, T pc,
                                            Rhs4<T> kc) {
   // values and results by value: a noinline function taking arrays by reference
-  // would keep the caller's arrays in local memory on every point
-  double f[4] = {(double)kc.u, (double)kc.v, (double)kc.w, (double)kc.p};
-  const double cen[3] = {(double)uc, (double)vc, (double)wc};
+  // would keep the caller's arrays in local memory on every point. Only the
+  // components a face changes go through FP64 (the others would round-trip
+  // exactly), in the order of the faces, so that a point on one face costs about
+  // ten FP64-pipe instructions.
+  const T cen[3] = {uc, vc, wc};
+  T f[3] = {kc.u, kc.v, kc.w};
   const int idx[3] = {i, j, k};
   const int n[3] = {prm.nx, prm.ny, prm.nz};
   const double p = (double)pc;
+  double fp = (double)kc.p;
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     const bool lo = idx[d] == 0, hi = idx[d] == n[d] - 1;
     if (!lo && !hi) continue;
-    const double ud = cen[d];
+    const double ud = (double)cen[d];
+    double fd = (double)f[d];
     if (prm.bc == BC_CHARACTERISTIC) {
       if (lo) {
         const double g = prm.bw[d] * (p + ud);
-        f[d] -= 0.5 * g;
-        f[3] -= 0.5 * g;
+        fd -= 0.5 * g;
+        fp -= 0.5 * g;
       }
       if (hi) {
         const double g = prm.bw[d] * (p - ud);
-        f[d] += 0.5 * g;
-        f[3] -= 0.5 * g;
+        fd += 0.5 * g;
+        fp -= 0.5 * g;
       }
     } else {
-      if (lo) f[d] -= prm.bw[d] * p;
-      if (hi) f[d] += prm.bw[d] * p;
+      if (lo) fd -= prm.bw[d] * p;
+      if (hi) fd += prm.bw[d] * p;
     }
+    f[d] = (T)fd;
   }
-  return Rhs4<T>{(T)f[0], (T)f[1], (T)f[2], (T)f[3]};
+  return Rhs4<T>{f[0], f[1], f[2], (T)fp};
 }
 
 // FP64: the z neighbours of p and w come from a per-thread register window (one new
