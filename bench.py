@@ -568,7 +568,7 @@ def run_learned_study(args):
     t_data = time.perf_counter() - t0
     t_train = 0.0
     rounds = []
-    with sbpgpu.Cnn(2 * s.nbc, s.nxc, 8) as net:
+    with sbpgpu.Cnn(2 * s.nbc, s.nxc, 8, stream=sv.stream.cuda_stream) as net:
         for r in range(1 + args.rollout_rounds):
             if r > 0:  # windows started on the corrected solve's own states
                 t0 = time.perf_counter()

@@ -119,8 +119,12 @@ class Solvers:
         bc = sbpgpu.BC_CHARACTERISTIC
         self.fine = sbpgpu.Context(sbpgpu.WAVE_2BLOCK_2D, s.order, s.nxf, 2 * s.nbf, rho=rf, K=kf, bc=bc,
                                    device=device)
+        # the coarse context runs on this stream; a network created on it (Cnn(stream=
+        # stream.cuda_stream)) lets the corrected solve run without host syncs between
+        # its steps, features, network and correction
+        self.stream = torch.cuda.Stream(device=self.dev)
         self.coarse = sbpgpu.Context(sbpgpu.WAVE_2BLOCK_2D, s.order, s.nxc, 2 * s.nbc, rho=rc, K=kc, bc=bc,
-                                     device=device)
+                                     stream=self.stream.cuda_stream, device=device)
         self.mid = None
         if mid:
             nxm, nbm = 2 * (s.nxc - 1) + 1, 2 * (s.nbc - 1) + 1
@@ -301,6 +305,9 @@ class LearnedSolver:
     def __init__(self, sv: Solvers, net: sbpgpu.Cnn, scales: Scales, guard: float = 0.01):
         self.sv, self.net, self.scales, self.guard = sv, net, scales, guard
         self.delta = torch.empty(sv.npc * 3, dtype=torch.float32, device=sv.dev)
+        self.pred = torch.empty(sv.npc * 3, dtype=torch.float64, device=sv.dev)
+        self.x = torch.empty(sv.npc * 24, dtype=torch.float32, device=sv.dev)
+        self.shared = getattr(net, "stream", None) == sv.stream.cuda_stream
         self.fallbacks = 0
 
     def hnorm(self, state):
@@ -330,15 +337,40 @@ class LearnedSolver:
 
     def run(self, fine0, windows: int):
         """`windows` corrected windows from the fine initial state `fine0` (restricted); if a
-        correction fails the energy check, the fine solve from `fine0` gives the answer."""
+        correction fails the energy check, the fine solve from `fine0` gives the answer.
+        The state stays in the coarse context between windows and all work is ordered on
+        its stream: the host waits only for the two H-norms of the energy check (and around
+        the network when that runs on another stream). The same operations as
+        corrected_window, so the same results."""
         sv, s = self.sv, self.sv.s
-        state = sv.restrict(fine0)
-        for _ in range(windows):
-            state = self.corrected_window(state)
-            if state is None:
-                self.fallbacks += 1
-                return sv.restrict(sv.fine_steps_from(fine0, 4 * s.window * windows))
-        return state
+        ctx, S = sv.coarse, sv.stream
+        _ready()
+        with torch.cuda.stream(S):
+            start = sv.restrict(fine0)
+            ctx.set_state_ptr(start.data_ptr(), sbpgpu.DEVICE)
+            for _ in range(windows):
+                ctx.step_resident(0.0, s.dtc, s.window)
+                e0 = ctx.hnorm()
+                ctx.get_state_ptr(self.pred.data_ptr(), sbpgpu.DEVICE)
+                sbpgpu.cnn_features(self.pred.data_ptr(), sv.rho_c.data_ptr(), sv.K_c.data_ptr(), s.nxc, 2 * s.nbc,
+                                    s.nbc, 1.0 / self.scales.inp, self.x.data_ptr(), S.cuda_stream)
+                if not self.shared:
+                    S.synchronize()
+                self.net.forward(self.x.data_ptr(), 1, self.delta.data_ptr())
+                if not self.shared:
+                    _ready()
+                sbpgpu.cnn_correct(self.pred.data_ptr(), self.delta.data_ptr(), sv.rho_c.data_ptr(), sv.K_c.data_ptr(),
+                                   sv.npc, self.scales.out, S.cuda_stream)
+                ctx.set_state_ptr(self.pred.data_ptr(), sbpgpu.DEVICE)
+                e1 = ctx.hnorm()
+                if not np.isfinite(e1) or e1 > e0 * (1.0 + self.guard):
+                    break
+            else:
+                out = self.pred.clone()
+                S.synchronize()
+                return out
+        self.fallbacks += 1
+        return sv.restrict(sv.fine_steps_from(fine0, 4 * s.window * windows))
 
     def run_plain(self, fine0, windows: int):
         """The coarse solve without corrections."""

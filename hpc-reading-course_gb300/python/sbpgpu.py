@@ -470,6 +470,7 @@ class Cnn:
         if rc:
             raise SbpError(rc, L.sbp_cnn_last_error(None).decode())
         self._h = h
+        self.stream = stream  # the cudaStream_t it was created on (None: its own)
         if seed != 1234:
             self._check(L.sbp_cnn_init(h, seed))
 

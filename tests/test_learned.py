@@ -86,3 +86,31 @@ def test_features_and_zero_state_gives_zero_correction(sbp):
         net.forward(zero.data_ptr(), 1, out.data_ptr())
         torch.cuda.synchronize()
     assert float(out.abs().max()) == 0.0
+
+
+@pytest.mark.parametrize("shared", [True, False], ids=["net_on_coarse_stream", "net_on_own_stream"])
+def test_run_matches_window_by_window_solve(sbp, shared):
+    """LearnedSolver.run (state resident in the coarse context, one stream, two host
+    waits per window) gives bit for bit the state of the window-by-window path
+    (corrected_window), with the network on the coarse context's stream or its own."""
+    import learned
+    import torch
+
+    s = _small()
+    sv = learned.Solvers(s)
+    kw = {"stream": sv.stream.cuda_stream} if shared else {}
+    with sbp.Cnn(2 * s.nbc, s.nxc, 1, **kw) as net:
+        p = net.get_params()
+        net.set_params((p + 0.02 * np.random.default_rng(1).standard_normal(p.size)).astype(np.float32))
+        solver = learned.LearnedSolver(sv, net, learned.Scales(inp=2.0, out=1e-3), guard=1e9)
+        assert solver.shared == shared
+        x0, y0, w, a = learned.trajectory_params(5001)
+        fine0 = torch.from_numpy(learned.pulse_state(s.nxf, s.nbf, x0, y0, w, a)).to(sv.dev)
+        fast = solver.run(fine0, 5)
+        state = sv.restrict(fine0)
+        for _ in range(5):
+            state = solver.corrected_window(state)
+        torch.cuda.synchronize()
+    assert solver.fallbacks == 0
+    assert float((state - sv.restrict(fine0)).abs().max()) > 0.0
+    assert torch.equal(fast, state)
