@@ -6,16 +6,20 @@
 // the first/last cls_sz lines of each direction, the central stencil between.
 //
 // Persistent, warp-specialised pipeline. One CTA per SM walks the tiles of
-// the grid (TX x TY points each) in a fixed stride. Warp 8 is the producer:
-// its lane 0 issues the TMA loads of tile k+1 into one of two shared-memory
-// stages while warps 0-7 compute tile k from the other:
+// the grid (TX x TY points each) in a fixed stride. The last warp is the
+// producer: its lane 0 issues the TMA loads of tile k+1 into a ring of
+// shared-memory stages while the consumer warps (8 to 16 per kind and
+// precision) compute tile k from another:
 //   * the stage input with halos: p with an x and y halo, u with an x halo,
 //     v with a y halo (the star stencil needs no corners of u, v);
 //   * the per-point RK4 operands the stage needs, each as one 3-component
 //     box: u^n and acc for stages 2-3, acc for stage 4, plus u^n and the
 //     Kahan term for the FP32 stage 4.
+//   * variable coefficients: [1/rho | K] as one 2-component box.
 // Consumers touch global memory only for their outputs (coalesced streaming
-// stores), for closure-row taps (boundary strips) and for coefficient fields.
+// stores), for closure-row taps (boundary strips) and for the FP64 copies of
+// the coefficients at boundary points. The SAT of x-face points runs in a
+// separate pass per tile (see wave_tile_compute).
 // Every mbarrier wait is bounded by %globaltimer; a timeout sets an error bit
 // that the host reads and the CTA stops after letting its copies land.
 //
@@ -72,7 +76,7 @@ template <typename T> struct WaveParams {
 };
 
 constexpr int kWaveTX = 64;            // tile width (x, contiguous)
-constexpr int kWaveConsumerWarps = 8;  // compute warps (FP64, variable-coefficient FP32, batched)
+constexpr int kWaveConsumerWarps = 8;  // compute warps where no kind- or form-specific count is set
 constexpr int kWaveThreads = 32 * (kWaveConsumerWarps + 1);
 
 // FP32 keeps the state with a Kahan-compensated final update.
@@ -606,7 +610,7 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
     return;
   }
 
-  // ---------------- consumers: warps 0-7
+  // ---------------- consumers: warps 0 .. WARPS-1
   double errsq = 0.0;  // ST_RKF6: this thread's share of the weighted error sum
   uint32_t dphase = 0;  // parity of each stage's next deferred-pass barrier phase
   int k = 0;
@@ -624,7 +628,7 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
     if (lane == 0) mbar_arrive(&empty[b]);
   }
   if constexpr (STAGE == ST_RKF6) {
-    // fixed-order sum over the 256 consumer threads -> one partial per CTA
+    // fixed-order sum over the consumer threads -> one partial per CTA
     __shared__ double warp_sum[WARPS];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) errsq += __shfl_down_sync(0xffffffffu, errsq, off);

@@ -81,27 +81,11 @@ template <typename T> constexpr int batch_warps() { return sizeof(T) == 4 ? SBP_
 template <typename T, int ORD, int STAGE, int TY>
 using BatchWaveTile = WaveTile<T, ORD, STAGE, TY, (int)sizeof(BatchWave<T>), false, 2, batch_warps<T>()>;
 
-// Tile order of a CTA: with SBP_BATCH_BLOCKED a contiguous range of the tile
-// list (consecutive tiles mostly of one instance, so its tensor maps and
-// parameter block stay cached), else every gridDim.x-th tile.
-#ifndef SBP_BATCH_BLOCKED
-#define SBP_BATCH_BLOCKED 0
-#endif
-#ifndef SBP_BATCH_PREFETCH_MAPS
-#define SBP_BATCH_PREFETCH_MAPS 0
-#endif
-__device__ __forceinline__ void batch_tile_range(int ntiles, int& first, int& step, int& end) {
-  if (SBP_BATCH_BLOCKED) {
-    first = (int)((long long)ntiles * blockIdx.x / gridDim.x);
-    end = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
-    step = 1;
-  } else {
-    first = blockIdx.x;
-    end = ntiles;
-    step = gridDim.x;
-  }
-}
-
+// A CTA takes every gridDim.x-th tile of the list, so neighbouring tiles of an
+// instance run at the same time on neighbouring CTAs and share their halo rows in
+// L2. Measured at 512 instances: contiguous ranges of the list per CTA ran at
+// 1.39e10 (FP64) / 2.36e10 (FP32) point-stage updates/s against 1.72e10 / 3.22e10,
+// and prefetching the next instance's tensor maps changed nothing.
 template <typename T, int ORD, int STAGE, int TY>
 __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, TY>::THREADS, 1)
     wave_batch_stage_kernel(const BatchWave<T>* __restrict__ insts, const CUtensorMap* __restrict__ maps,
@@ -125,8 +109,7 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, TY>::THREADS, 1)
   }
   __syncthreads();
   const int sel = rk == 1 ? 0 : (rk == 3 ? 2 : 1);  // which buffer is the stage input
-  int first, step, end;
-  batch_tile_range(ntiles, first, step, end);
+  const int first = blockIdx.x, step = gridDim.x, end = ntiles;
 
   if (warp == Tile::WARPS) {
     if (lane == 0) {
@@ -134,18 +117,7 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, TY>::THREADS, 1)
       BatchTile next = first < end ? tiles[first] : BatchTile{0, 0, 0, 0};
       for (int tile = first; tile < end; tile += step, k++) {
         const BatchTile tt = next;
-        if (tile + step < end) {
-          next = tiles[tile + step];  // the next descriptor, read ahead
-          if (SBP_BATCH_PREFETCH_MAPS && next.slot != tt.slot) {
-            const CUtensorMap* mn = maps + (long long)next.slot * kBatchMaps;
-            prefetch_tensormap(&mn[3 * sel + 0]);
-            prefetch_tensormap(&mn[3 * sel + 1]);
-            prefetch_tensormap(&mn[3 * sel + 2]);
-            if (Tile::LOAD_UN) prefetch_tensormap(&mn[9]);
-            if (Tile::LOAD_ACC) prefetch_tensormap(&mn[10]);
-            if (Tile::LOAD_COMP) prefetch_tensormap(&mn[11]);
-          }
-        }
+        if (tile + step < end) next = tiles[tile + step];  // the next descriptor, read ahead
         const int b = k & 1;
         if (k >= 2 && !mbar_wait_bounded(&empty[b], ((k >> 1) - 1) & 1)) {
           atomicOr(err, ERR_TMA_TIMEOUT);
