@@ -47,6 +47,50 @@ __device__ __forceinline__ T d1_line(const T* __restrict__ line, long long st, i
   return closure_line<T, ORD>(line, st, n, i, d.cls);
 }
 
+// RK4 stage update of one component of one point at offset o.
+template <typename T, int STAGE>
+__device__ __forceinline__ void line_store(const LineParams<T>& prm, T* wout, const T c_acc, const T c_w, long long o,
+                                           T k, T cen) {
+  if constexpr (STAGE == ST_RHS) {
+    prm.kout[o] = k;
+  } else if constexpr (STAGE == ST_FIRST) {
+    prm.acc[o] = prm.compensated ? c_acc * k : fma(c_acc, k, cen);
+    wout[o] = fma(c_w, k, cen);
+  } else if constexpr (STAGE == ST_MID) {
+    const T u0 = prm.un[o];
+    prm.acc[o] = fma(c_acc, k, prm.acc[o]);
+    wout[o] = fma(c_w, k, u0);
+  } else {
+    const T d = fma(c_acc, k, prm.acc[o]);
+    if (prm.compensated) {
+      const T u0 = prm.un[o], e = prm.comp[o];
+      const T yv = d - e;
+      const T tv = u0 + yv;
+      prm.comp[o] = (tv - u0) - yv;
+      prm.un[o] = tv;
+    } else {
+      prm.un[o] = d;
+    }
+  }
+}
+
+// SAT_bc_{west,south,east,north} of 2D advection (advection_rhs.h:460-528), FP64,
+// at boundary points only (the FP64 round trip is exact elsewhere, and costly on
+// the FP64 pipe).
+template <typename T>
+__device__ __forceinline__ T adv2d_sat(const LineParams<T>& prm, int i, int j, T k, T cen) {
+  if (prm.bc && (i == 0 || j == 0 || i == prm.nx - 1 || j == prm.ny - 1)) {
+    double kk = (double)k;
+    const double u = (double)cen;
+    if (i == 0) kk += prm.sat[0] * u;
+    if (j == 0) kk += prm.sat[1] * u;
+    if (i == prm.nx - 1) kk += prm.sat[2] * u;
+    if (j == prm.ny - 1) kk += prm.sat[3] * u;
+    return (T)kk;
+  }
+  return k;
+}
+
 // One grid point of a stage: RHS, boundary terms and the RK4 stage update.
 template <typename T, int ORD, int KIND, int STAGE>
 __device__ __forceinline__ void line_point(const LineParams<T>& prm, const T* __restrict__ in, T* wout, const T c_acc,
@@ -69,17 +113,7 @@ __device__ __forceinline__ void line_point(const LineParams<T>& prm, const T* __
     const T* col = in + i;
     k[0] = d1_line<T, ORD>(row, 1, nx, i, prm.dx) + d1_line<T, ORD>(col, pitch, ny, j, prm.dy);
     cen[0] = in[q];
-    // SAT_bc_{west,south,east,north} (advection_rhs.h:460-528), FP64, at boundary
-    // points only (the FP64 round trip is exact elsewhere, and costly on the FP64 pipe)
-    if (prm.bc && (i == 0 || j == 0 || i == nx - 1 || j == ny - 1)) {
-      double kk = (double)k[0];
-      const double u = (double)cen[0];
-      if (i == 0) kk += prm.sat[0] * u;
-      if (j == 0) kk += prm.sat[1] * u;
-      if (i == nx - 1) kk += prm.sat[2] * u;
-      if (j == ny - 1) kk += prm.sat[3] * u;
-      k[0] = (T)kk;
-    }
+    k[0] = adv2d_sat<T>(prm, i, j, k[0], cen[0]);
   } else {  // LK_REFL1D: dst(i,1) = D1 u, dst(i,0) = D1 v
     k[1] = d1_line<T, ORD>(in, 1, nx, i, prm.dx);
     k[0] = d1_line<T, ORD>(in + plane, 1, nx, i, prm.dx);
@@ -88,30 +122,7 @@ __device__ __forceinline__ void line_point(const LineParams<T>& prm, const T* __
     if (prm.bc && (i == 0 || i == nx - 1)) k[0] = T(0);  // proj_dirichlet_bc_{l,r}
   }
 #pragma unroll
-  for (int c = 0; c < NC; c++) {
-    const long long o = c * plane + q;
-    if constexpr (STAGE == ST_RHS) {
-      prm.kout[o] = k[c];
-    } else if constexpr (STAGE == ST_FIRST) {
-      prm.acc[o] = prm.compensated ? c_acc * k[c] : fma(c_acc, k[c], cen[c]);
-      wout[o] = fma(c_w, k[c], cen[c]);
-    } else if constexpr (STAGE == ST_MID) {
-      const T u0 = prm.un[o];
-      prm.acc[o] = fma(c_acc, k[c], prm.acc[o]);
-      wout[o] = fma(c_w, k[c], u0);
-    } else {
-      const T d = fma(c_acc, k[c], prm.acc[o]);
-      if (prm.compensated) {
-        const T u0 = prm.un[o], e = prm.comp[o];
-        const T yv = d - e;
-        const T tv = u0 + yv;
-        prm.comp[o] = (tv - u0) - yv;
-        prm.un[o] = tv;
-      } else {
-        prm.un[o] = d;
-      }
-    }
-  }
+  for (int c = 0; c < NC; c++) line_store<T, STAGE>(prm, wout, c_acc, c_w, c * plane + q, k[c], cen[c]);
 }
 
 template <typename T, int ORD, int KIND, int STAGE>
