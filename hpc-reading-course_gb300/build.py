@@ -49,6 +49,7 @@ def units():
     out.append(("cnn.o", "cnn.cu", []))
     out.append(("rk45.o", "rk45.cu", []))
     out.append(("wave3d.o", "wave3d.cu", []))
+    out.append(("decomp.o", "decomp.cu", []))
     return out
 
 

@@ -42,7 +42,9 @@ EXPORTS = ("sbp_create", "sbp_destroy", "sbp_last_error", "sbp_dofs", "sbp_rhs",
            "sbp_cnn_create", "sbp_cnn_destroy", "sbp_cnn_last_error", "sbp_cnn_param_count", "sbp_cnn_init",
            "sbp_cnn_get_params", "sbp_cnn_set_params", "sbp_cnn_forward", "sbp_cnn_gradients", "sbp_cnn_train_step",
            "sbp_cnn_features", "sbp_cnn_correct", "sbp_cnn_launch_count",
-           "sbp_rk45_default_opts", "sbp_rk45_resident", "sbp_ts_rk45")
+           "sbp_rk45_default_opts", "sbp_rk45_resident", "sbp_ts_rk45",
+           "sbp_decomp_create", "sbp_decomp_destroy", "sbp_decomp_last_error", "sbp_decomp_set_state",
+           "sbp_decomp_get_state", "sbp_decomp_rhs", "sbp_decomp_rk4_resident")
 
 _dp = C.POINTER(C.c_double)
 ERR_DIVERGED = -6
@@ -156,6 +158,14 @@ def load(path: str = LIB_PATH) -> C.CDLL:
                                   C.c_void_p]
     L.sbp_cnn_launch_count.argtypes = [P]
     L.sbp_cnn_launch_count.restype = C.c_longlong
+    L.sbp_decomp_create.argtypes = [C.POINTER(Desc), C.c_int, C.c_int, C.POINTER(P)]
+    L.sbp_decomp_destroy.argtypes = [P]
+    L.sbp_decomp_last_error.argtypes = [P]
+    L.sbp_decomp_last_error.restype = C.c_char_p
+    L.sbp_decomp_set_state.argtypes = [P, C.c_void_p, C.c_int]
+    L.sbp_decomp_get_state.argtypes = [P, C.c_void_p, C.c_int]
+    L.sbp_decomp_rhs.argtypes = [P, C.c_void_p, C.c_void_p, C.c_int]
+    L.sbp_decomp_rk4_resident.argtypes = [P, C.c_double, C.c_longlong]
     L.sbp_write_petsc_vec.argtypes = [C.c_char_p, C.c_void_p, C.c_longlong]
     L.sbp_read_petsc_vec.argtypes = [C.c_char_p, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]
     _lib = L
@@ -374,6 +384,68 @@ class Context:
     @property
     def launches(self) -> int:
         return self._L.sbp_launch_count(self._h)
+
+
+class Decomp:
+    """One SBP_WAVE_HOM_2D grid (FP64) as px x py subdomains with ghost lines and a device halo
+    exchange before every stage (sbp_decomp_*); states are the full grid's AoS arrays."""
+
+    def __init__(self, order: int, nx: int, ny: int, px: int, py: int, *, bc: int = BC_REFERENCE,
+                 xl=(-1.0, -1.0), xr=(1.0, 1.0), stream: int | None = None, device: int = 0):
+        L = load()
+        self._L = L
+        self.nx, self.ny, self.px, self.py = nx, ny, px, py
+        self.size = 3 * nx * ny
+        d = Desc(WAVE_HOM_2D, order, bc, FP64, nx, ny, (C.c_double * 2)(*xl[:2]), (C.c_double * 2)(*xr[:2]),
+                 0.0, 0.0, None, None, stream, device, 1, -1.0, 1.0)
+        h = C.c_void_p()
+        rc = L.sbp_decomp_create(C.byref(d), px, py, C.byref(h))
+        if rc:
+            raise SbpError(rc, "sbp_decomp_create failed")
+        self._h = h
+
+    def _check(self, rc):
+        if rc:
+            raise SbpError(rc, self._L.sbp_decomp_last_error(self._h).decode())
+
+    def close(self):
+        if self._h:
+            self._L.sbp_decomp_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, v: np.ndarray):
+        self._check(self._L.sbp_decomp_set_state(self._h, _host(v).ctypes.data, HOST))
+
+    def get_state(self) -> np.ndarray:
+        out = np.empty(self.size)
+        self._check(self._L.sbp_decomp_get_state(self._h, out.ctypes.data, HOST))
+        return out
+
+    def rhs(self, src: np.ndarray) -> np.ndarray:
+        src = _host(src)
+        dst = np.empty_like(src)
+        self._check(self._L.sbp_decomp_rhs(self._h, src.ctypes.data, dst.ctypes.data, HOST))
+        return dst
+
+    def step_resident(self, dt: float, nsteps: int):
+        self._check(self._L.sbp_decomp_rk4_resident(self._h, dt, nsteps))
+
+    def rk4(self, v0: np.ndarray, dt: float, nsteps: int) -> np.ndarray:
+        self.set_state(v0)
+        self.step_resident(dt, nsteps)
+        return self.get_state()
 
 
 class Batch:

@@ -232,6 +232,28 @@ int sbp_batch_get_stream(const sbp_batch* batch, void** stream);
 long long sbp_batch_points(const sbp_batch* batch);       /* grid points over all instances */
 long long sbp_batch_launch_count(const sbp_batch* batch); /* kernels launched so far */
 
+/* ---------------------------------------------------------------- decomposed grid
+ * One SBP_WAVE_HOM_2D grid (FP64) split into px x py subdomains, each with its
+ * own state and R ghost lines per side, on one device. Replaces the reference's
+ * decomposed path: rhs_local / rhs_all per DMDA block
+ * (code/include/partitioned_rhs/rhs.h:97-181, 183-360) with the VecScatter ghost
+ * update before each RHS (code/src/scatter/scatter_ctx.cpp:149-211), here a
+ * device halo-exchange kernel before each RK4 stage. Subdomain widths are
+ * floor(N*(b+1)/p) - floor(N*b/p) >= the closure width (2 / 6 / 9 points for
+ * orders 2 / 4 / 6), else SBP_ERR_INVALID; other problems or FP32:
+ * SBP_ERR_UNSUPPORTED. Results equal sbp_create's single grid to rounding.
+ * States are the full grid's AoS arrays (as sbp_set_state). Synchronous. */
+typedef struct sbp_decomp sbp_decomp;
+int sbp_decomp_create(const sbp_desc* desc, int px, int py, sbp_decomp** dec);
+int sbp_decomp_destroy(sbp_decomp* dec);
+const char* sbp_decomp_last_error(const sbp_decomp* dec);
+int sbp_decomp_set_state(sbp_decomp* dec, const double* state, int where);
+int sbp_decomp_get_state(sbp_decomp* dec, double* state, int where);
+/* dst = F(src) (the system is autonomous): halo exchange, then the RHS of every subdomain. */
+int sbp_decomp_rhs(sbp_decomp* dec, const double* src, double* dst, int where);
+/* nsteps classical RK4 steps of the resident state, a halo exchange before each stage. */
+int sbp_decomp_rk4_resident(sbp_decomp* dec, double dt, long long nsteps);
+
 /* ---------------------------------------------------------------- learned correction
  * A 4-layer 3x3 convolutional network (24 -> 32 -> 32 -> 32 -> 3 channels,
  * ReLU) that corrects a coarse solve; no counterpart in the reference.
