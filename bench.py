@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--bc", default="characteristic", choices=["characteristic", "free_surface"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--study", default=None, choices=["precision", "batched", "learned", "rk45", "wave3d"],
+    ap.add_argument("--study", default=None, choices=["precision", "batched", "learned", "rk45", "wave3d", "decomp"],
                     help="precision: variable rho, K (seeded Fourier fields) to --t-end in FP64 and in "
                          "compensated FP32; prints errors of FP32 against FP64 and both wall times. "
                          "batched: 512 uneven wave/advection instances in one batch, FP64 and FP32. "
@@ -477,6 +477,49 @@ def run_rk45_study(args):
     print(json.dumps(line), flush=True)
 
 
+def run_decomp_study(args):
+    """The decomposed path (sbp_decomp_*): the --grid^2 wave (rho = K = 1, order --order, FP64,
+    characteristic SAT, Gaussian pulse) as px x py subdomains with ghost lines and a halo exchange
+    before every stage, against the single-grid context; 50 RK4 steps each after 3 warm-up steps,
+    wall time around the synchronous calls, and the two results compared."""
+    import numpy as np
+
+    import build as gpu_build
+    import sbpgpu
+
+    gpu_build.build()
+    n, order, steps = args.grid, args.order, 50
+    h = 2.0 / (n - 1)
+    dt = 0.2 * h
+    v0 = initial_state(n)
+    out = {"study": "decomp", "grid": [n, n], "order": order, "rk4_steps": steps, "bc": "characteristic"}
+    with sbpgpu.Context(sbpgpu.WAVE_HOM_2D, order, n, n, bc=sbpgpu.BC_CHARACTERISTIC) as c:
+        c.set_state(v0)
+        c.step_resident(0.0, dt, 3)
+        c.synchronize()
+        t0 = time.perf_counter()
+        c.step_resident(0.0, dt, steps)
+        c.synchronize()
+        sec = time.perf_counter() - t0
+        c.set_state(v0)
+        c.step_resident(0.0, dt, 3 + steps)
+        single = c.get_state()
+    out["single_grid"] = {"point_stage_per_s": 4.0 * n * n * steps / sec, "seconds": sec}
+    rows = []
+    for px, py in ((1, 1), (2, 2), (4, 4), (8, 8)):
+        with sbpgpu.Decomp(order, n, n, px, py, bc=sbpgpu.BC_CHARACTERISTIC) as d:
+            d.set_state(v0)
+            d.step_resident(dt, 3)
+            t0 = time.perf_counter()
+            d.step_resident(dt, steps)
+            sec = time.perf_counter() - t0
+            got = d.get_state()
+        rows.append({"px": px, "py": py, "point_stage_per_s": 4.0 * n * n * steps / sec, "seconds": sec,
+                     "rel_max_diff_vs_single": float(np.max(np.abs(got - single)) / np.max(np.abs(single)))})
+    out["decomposed"] = rows
+    print(json.dumps(out), flush=True)
+
+
 def run_wave3d_study(args):
     """3D wave (u, v, w, p), rho = K = 1, characteristic SAT on the six faces, Gaussian pulse
     w = 0.2 at the origin, --grid3d^3 points, order --order, dt = 0.2 h, 100 RK4 steps per timed run,
@@ -627,6 +670,9 @@ def main():
         return
     if args.study == "wave3d":
         run_wave3d_study(args)
+        return
+    if args.study == "decomp":
+        run_decomp_study(args)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
