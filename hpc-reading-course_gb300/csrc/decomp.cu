@@ -235,6 +235,8 @@ struct sbp_decomp {
 
 namespace {
 
+std::string g_decomp_create_error;  // the message of the last failed sbp_decomp_create
+
 int dfail(sbp_decomp* c, int code, const std::string& m) {
   if (c) c->msg = m;
   return code;
@@ -294,27 +296,33 @@ cudaError_t scatter(sbp_decomp* c, const double* aos_in, double* aos_out, double
 extern "C" {
 
 int sbp_decomp_create(const sbp_desc* desc, int px, int py, sbp_decomp** out) {
-  if (!desc || !out) return SBP_ERR_INVALID;
+  auto reject = [](int code, const char* why) {
+    g_decomp_create_error = why;
+    return code;
+  };
+  if (!desc || !out) return reject(SBP_ERR_INVALID, "null description or output");
   *out = nullptr;
-  if (desc->problem != SBP_WAVE_HOM_2D) return SBP_ERR_UNSUPPORTED;
-  if (desc->precision != SBP_FP64) return SBP_ERR_UNSUPPORTED;
-  if (desc->order != 2 && desc->order != 4 && desc->order != 6) return SBP_ERR_INVALID;
+  if (desc->problem != SBP_WAVE_HOM_2D) return reject(SBP_ERR_UNSUPPORTED, "only SBP_WAVE_HOM_2D is decomposed");
+  if (desc->precision != SBP_FP64) return reject(SBP_ERR_UNSUPPORTED, "the decomposed path is FP64");
+  if (desc->order != 2 && desc->order != 4 && desc->order != 6) return reject(SBP_ERR_INVALID, "order must be 2, 4 or 6");
   const ops::Operator& op = ops::get(desc->order);
   const long long NX = desc->nx, NY = desc->ny;
-  if (px < 1 || py < 1 || px > 64 || py > 64) return SBP_ERR_INVALID;
+  if (px < 1 || py < 1 || px > 64 || py > 64) return reject(SBP_ERR_INVALID, "px, py must be in [1, 64]");
   // every subdomain at least one closure block wide (it then holds the closure
   // lines of a physical boundary and the ghost lines its neighbour needs)
-  if (NX / px < op.cls_width || NY / py < op.cls_width || NX > (1 << 20) || NY > (1 << 20)) return SBP_ERR_INVALID;
-  if (!(desc->xr[0] > desc->xl[0]) || !(desc->xr[1] > desc->xl[1])) return SBP_ERR_INVALID;
+  if (NX / px < op.cls_width || NY / py < op.cls_width || NX > (1 << 20) || NY > (1 << 20))
+    return reject(SBP_ERR_INVALID, "subdomains narrower than the closure width, or grid above 2^20 per direction");
+  if (!(desc->xr[0] > desc->xl[0]) || !(desc->xr[1] > desc->xl[1])) return reject(SBP_ERR_INVALID, "empty domain");
   sbp_decomp* c = new (std::nothrow) sbp_decomp;
-  if (!c) return SBP_ERR_CUDA;
+  if (!c) return reject(SBP_ERR_CUDA, "host allocation");
   c->d = *desc;
   c->px = px;
   c->py = py;
   c->sw = (op.width - 1) / 2;
-  auto cfail = [&](int code, const char*) {
+  auto cfail = [&](int code, const char* why) {
     release(c);
     delete c;
+    g_decomp_create_error = why;
     return code;
   };
   if (cudaSetDevice(desc->device) != cudaSuccess) return cfail(SBP_ERR_CUDA, "cudaSetDevice");
@@ -394,7 +402,7 @@ int sbp_decomp_destroy(sbp_decomp* c) {
   return SBP_OK;
 }
 
-const char* sbp_decomp_last_error(const sbp_decomp* c) { return c ? c->msg.c_str() : "null decomposition"; }
+const char* sbp_decomp_last_error(const sbp_decomp* c) { return c ? c->msg.c_str() : g_decomp_create_error.c_str(); }
 
 int sbp_decomp_set_state(sbp_decomp* c, const double* aos, int where) {
   if (!c || !aos) return SBP_ERR_INVALID;

@@ -401,7 +401,7 @@ class Decomp:
         h = C.c_void_p()
         rc = L.sbp_decomp_create(C.byref(d), px, py, C.byref(h))
         if rc:
-            raise SbpError(rc, "sbp_decomp_create failed")
+            raise SbpError(rc, L.sbp_decomp_last_error(None).decode())
         self._h = h
 
     def _check(self, rc):

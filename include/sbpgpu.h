@@ -246,7 +246,7 @@ long long sbp_batch_launch_count(const sbp_batch* batch); /* kernels launched so
 typedef struct sbp_decomp sbp_decomp;
 int sbp_decomp_create(const sbp_desc* desc, int px, int py, sbp_decomp** dec);
 int sbp_decomp_destroy(sbp_decomp* dec);
-const char* sbp_decomp_last_error(const sbp_decomp* dec);
+const char* sbp_decomp_last_error(const sbp_decomp* dec); /* NULL: the last failed sbp_decomp_create */
 int sbp_decomp_set_state(sbp_decomp* dec, const double* state, int where);
 int sbp_decomp_get_state(sbp_decomp* dec, double* state, int where);
 /* dst = F(src) (the system is autonomous): halo exchange, then the RHS of every subdomain. */

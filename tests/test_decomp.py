@@ -40,6 +40,7 @@ def test_decomp_rejects_unsupported_descriptions(sbp, case):
     h = C.c_void_p()
     assert L.sbp_decomp_create(C.byref(_desc(sbp, order, nx, ny, **kw)), px, py, C.byref(h)) == code
     assert not h.value
+    assert L.sbp_decomp_last_error(None)  # says why
 
 
 CASES = [(2, 37, 29, 2, 3), (4, 40, 40, 4, 4), (4, 65, 33, 3, 2), (6, 27, 60, 1, 5), (6, 50, 41, 2, 2), (4, 33, 33, 1, 1)]
