@@ -157,12 +157,14 @@ def profiled_traffic(order: int, precision: str):
 
 
 def cpu_baseline(n: int, order: int, precision: str, bc: str, budget_s: float, repeats: int = 1):
-    """The reference path on the host cores: oracle/_ref when built here and
-    loadable, else the oracle restatement (OpenMP over all cores). Returns
-    (point-stage updates/s, description)."""
+    """The path on the host cores: the oracle restatement of the reference's
+    operators (oracle/sbp_oracle.c, pinned bit for bit to the reference's own
+    headers by tests/test_oracle.py), built with the reference's -O3
+    -ffast-math and run with OpenMP over all cores, on the same problem as the
+    GPU arm (rho = K = 1, the same SAT). oracle/_ref, the reference's headers
+    compiled in this checkout, is built only where the reference checkout
+    exists and is not timed here. Returns (rates, kind, threads, sample)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import numpy as np
-
     import oracle as O
 
     O.build()
@@ -171,11 +173,8 @@ def cpu_baseline(n: int, order: int, precision: str, bc: str, budget_s: float, r
     port.set_threads(threads)
     v = initial_state(n)
     h = 2.0 / (n - 1)
-    ones = np.ones(n * n)
-    if bc == "characteristic":
-        pb = O.Problem(O.WAVE_VAR_2D, order, n, n, rho=ones, K=ones, bc=O.BC_CHARACTERISTIC)
-    else:
-        pb = O.Problem(O.WAVE_HOM_2D, order, n, n)
+    pb = O.Problem(O.WAVE_HOM_2D, order, n, n,
+                   bc=O.BC_CHARACTERISTIC if bc == "characteristic" else O.BC_REFERENCE)
     t0 = time.perf_counter()
     v = port.rk4(pb, v, 0.0, 0.2 * h, 1)
     t1 = time.perf_counter() - t0

@@ -310,6 +310,10 @@ int sbp_decomp_create(const sbp_desc* desc, int px, int py, sbp_decomp** out) {
   if (px < 1 || py < 1 || px > 64 || py > 64) return reject(SBP_ERR_INVALID, "px, py must be in [1, 64]");
   // every subdomain at least one closure block wide (it then holds the closure
   // lines of a physical boundary and the ghost lines its neighbour needs)
+  // the whole grid at least the operator's minimum size, as sbp_create demands: below
+  // it the left and right closure blocks would overlap
+  const long long m = ops::min_points(desc->order);
+  if (NX < m || NY < m) return reject(SBP_ERR_INVALID, "grid smaller than the operator's minimum size");
   if (NX / px < op.cls_width || NY / py < op.cls_width || NX > (1 << 20) || NY > (1 << 20))
     return reject(SBP_ERR_INVALID, "subdomains narrower than the closure width, or grid above 2^20 per direction");
   if (!(desc->xr[0] > desc->xl[0]) || !(desc->xr[1] > desc->xl[1])) return reject(SBP_ERR_INVALID, "empty domain");

@@ -20,7 +20,12 @@
 //     array and give wrong results -- serialise them;
 //   * the first call on a device does a one-time set-up on that device (the
 //     array's device address and the stage kernels' shared-memory opt-in);
-//     make that first call before any stream capture.
+//     make that first call before any stream capture. Later calls look the
+//     address up again (no allocation) and redo the set-up if it moved, as it
+//     can after cudaDeviceReset reloads the module;
+//   * every call is synchronous: it waits on its stream for its own work and
+//     reads the kernel's error word back before it returns;
+//   * the calling thread's current device is the same on return as on entry.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -50,23 +55,35 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-// One-time set-up per device, with that device current: the device address of
-// the static array (host code may not use the symbol itself as a pointer) and
-// the shared-memory opt-in of the FP64 stage kernels.
+// Set-up per device, with that device current: the device address of the
+// static array (host code may not use the symbol itself as a pointer) and the
+// shared-memory opt-in of the FP64 stage kernels. The opt-in runs once per
+// device; the address is looked up on every call (cheap, allocates nothing)
+// so that a module reloaded after cudaDeviceReset never gets a stale address,
+// and a changed address repeats the opt-in on the reloaded module.
 int setup_device(int device, double** scratch) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (g_scratch_addr[device]) {
-    *scratch = g_scratch_addr[device];
-    return SBP_OK;
-  }
   double* ptr = nullptr;
   if (cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return SBP_ERR_CUDA;
-  for (int order : {2, 4, 6})
-    if (configure_wave<double>(order, WK_HOM) != cudaSuccess) return SBP_ERR_CUDA;
-  g_scratch_addr[device] = ptr;
+  if (g_scratch_addr[device] != ptr) {
+    for (int order : {2, 4, 6})
+      if (configure_wave<double>(order, WK_HOM) != cudaSuccess) return SBP_ERR_CUDA;
+    g_scratch_addr[device] = ptr;
+  }
   *scratch = ptr;
   return SBP_OK;
 }
+
+// Puts the caller's current device back on every return path.
+struct DeviceRestore {
+  int dev = -1;
+  DeviceRestore() {
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+  }
+  ~DeviceRestore() {
+    if (dev >= 0) cudaSetDevice(dev);
+  }
+};
 
 EncodeTiledFn encode_fn() {
   static EncodeTiledFn fn = nullptr;
@@ -109,6 +126,7 @@ extern "C" int sbp_wave_rhs_noalloc(const sbp_desc* d, double t, const double* s
     return reject(SBP_ERR_TOO_LARGE,
                   "grid exceeds the static scratch: roundup(nx, 64) * ny must be <= SBP_NOALLOC_MAX_PLANE");
   if (d->device < 0 || d->device >= kMaxDevices) return reject(SBP_ERR_INVALID, "device ordinal out of range");
+  const DeviceRestore restore;
   if (cudaSetDevice(d->device) != cudaSuccess) return reject(SBP_ERR_CUDA, "cudaSetDevice failed");
   double* scratch = nullptr;
   if (setup_device(d->device, &scratch)) return reject(SBP_ERR_CUDA, "set-up of the static scratch failed");

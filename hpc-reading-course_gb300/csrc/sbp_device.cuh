@@ -71,14 +71,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Waits for phase `parity` of the barrier with a time limit. Returns false on
-// timeout. Every thread of the CTA calls it.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+// Waits for phase `parity` of the barrier with a time limit (nanoseconds of
+// %globaltimer; 0 means kWaitLimitNs). Returns false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns = 0) {
   if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t lim = limit_ns ? limit_ns : kWaitLimitNs;
   const uint64_t t0 = globaltimer_ns();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
+    if (globaltimer_ns() - t0 > lim) return false;
   }
 }
 

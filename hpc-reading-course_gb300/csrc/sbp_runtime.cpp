@@ -79,6 +79,8 @@ struct sbp_ctx {
   std::map<long long, cudaGraphExec_t> graphs;
   double graph_dt = 0.0;
   long long launches = 0;
+  unsigned long long wait_ns = 0;  // limit of the wave stage kernels' bounded waits (0: the kernel default)
+  int drop_tile = 0;               // test aid: tile + 1 whose load the next RHS evaluation skips
   std::string msg;
 };
 
@@ -247,6 +249,11 @@ int launch_stage(sbp_ctx* ctx, int stage, int rk, double t, double dt, void* in,
     p.c_acc = c_acc;
     p.c_w = c_w;
     p.t = t;
+    p.wait_ns = ctx->wait_ns;
+    if (stage == ST_RHS) {  // a direct launch (RHS evaluation), never a captured one
+      p.test_drop_tile = ctx->drop_tile;
+      ctx->drop_tile = 0;
+    }
     if (ctl) {  // adaptive integrator: stage time and stop flag from device memory
       p.tctl = &ctl->t;
       p.tc = tc;
@@ -488,6 +495,7 @@ int launch_rkf_wave_stage(sbp_ctx* ctx, int s, void* in, const WaveMaps* in_maps
   p.rkpart = ctx->partial;
   p.rkatol = ctx->rk_atol;
   p.rkrtol = ctx->rk_rtol;
+  p.wait_ns = ctx->wait_ns;
   CK(launch_wave<double>(ctx->d.order, wave_kind(ctx), ST_RKF1 + s - 1, *in_maps, p, ctx->stream));
   ctx->launches++;
   return SBP_OK;
@@ -955,6 +963,30 @@ int sbp_ts_rk45(sbp_ctx* ctx, double t_end, double dt, double* v, int where) {
   if ((rc = sbp_set_state(ctx, v, where))) return rc;
   if ((rc = sbp_rk45_resident(ctx, 0.0, t_end, dt, nullptr, nullptr))) return rc;
   return sbp_get_state(ctx, v, where);
+}
+
+int sbp_set_wait_limit(sbp_ctx* ctx, long long ns) {
+  if (!ctx) return SBP_ERR_INVALID;
+  if (ns < 0 || ns > 60LL * 1000 * 1000 * 1000) return fail(ctx, SBP_ERR_INVALID, "wait limit must be in [0, 60 s]");
+  CK(cudaSetDevice(ctx->d.device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->wait_ns = (unsigned long long)ns;
+  drop_graphs(ctx);  // captured launches carry the old limit
+  if (ctx->rk_graph) {
+    cudaGraphExecDestroy(ctx->rk_graph);
+    ctx->rk_graph = nullptr;
+  }
+  return SBP_OK;
+}
+
+int sbp_test_drop_tile(sbp_ctx* ctx, long long tile) {
+  if (!ctx) return SBP_ERR_INVALID;
+  if (!ctx->wave) return fail(ctx, SBP_ERR_UNSUPPORTED, "the tile-drop test aid exists for the 2D wave kernels");
+  const int ty = wave_tile_height((int)ctx->es, wave_kind(ctx));
+  const long long ntiles = ((ctx->nx + kWaveTX - 1) / kWaveTX) * ((ctx->ny + ty - 1) / ty);
+  if (tile < 0 || tile >= ntiles) return fail(ctx, SBP_ERR_INVALID, "tile index out of range");
+  ctx->drop_tile = (int)(tile + 1);
+  return SBP_OK;
 }
 
 int sbp_get_stream(const sbp_ctx* ctx, void** stream) {

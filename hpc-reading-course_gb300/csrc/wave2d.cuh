@@ -73,6 +73,11 @@ template <typename T> struct WaveParams {
   double* rkpart;      // ST_RKF6: one error partial sum per CTA
   double rkatol, rkrtol;
   int* err;
+  // Bounded waits: limit of every mbarrier wait in ns (0: kWaitLimitNs). Test
+  // aid for that path: test_drop_tile = k + 1 makes the producer issue no load
+  // for tile k, so the consumers' wait for it runs out (0: none).
+  unsigned long long wait_ns;
+  int test_drop_tile;
 };
 
 constexpr int kWaveTX = 64;            // tile width (x, contiguous)
@@ -514,7 +519,7 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
       const uint32_t par = (*dphase >> b) & 1u;
       *dphase ^= 1u << b;
       if (warp != k % Tile::WARPS) return;
-      if (!mbar_wait_bounded(dbar, par)) {
+      if (!mbar_wait_bounded(dbar, par, prm.wait_ns)) {
         if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
         return;
       }
@@ -589,10 +594,11 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
       int k = 0;
       for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
         const int b = k % NST;
-        if (k >= NST && !mbar_wait_bounded(&empty[b], ((k / NST) - 1) & 1)) {
+        if (k >= NST && !mbar_wait_bounded(&empty[b], ((k / NST) - 1) & 1, prm.wait_ns)) {
           atomicOr(prm.err, ERR_TMA_TIMEOUT);
           break;
         }
+        if (tile + 1 == prm.test_drop_tile) continue;  // no load: the consumers' wait runs out
         unsigned char* st = smem + b * Tile::STAGE_BYTES;
         const int i0 = (tile % ntx) * kWaveTX, j0 = (tile / ntx) * TY;
         mbar_arrive_expect_tx(&full[b], Tile::TX_BYTES);
@@ -605,7 +611,8 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
         if (Tile::LOAD_COEF) tma_load_3d(st + Tile::OFF_K, &mapK, i0, j0, 0, &full[b]);
       }
       // the CTA must not exit with copies in flight: wait for the last NST stages
-      for (int kk = (k >= NST ? k - NST : 0); kk < k; kk++) mbar_wait_bounded(&full[kk % NST], (kk / NST) & 1);
+      for (int kk = (k >= NST ? k - NST : 0); kk < k; kk++)
+        mbar_wait_bounded(&full[kk % NST], (kk / NST) & 1, prm.wait_ns);
     }
     return;
   }
@@ -616,7 +623,7 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
   int k = 0;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
     const int b = k % NST;
-    if (!mbar_wait_bounded(&full[b], (k / NST) & 1)) {
+    if (!mbar_wait_bounded(&full[b], (k / NST) & 1, prm.wait_ns)) {
       if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
       break;
     }

@@ -35,6 +35,7 @@ DOFS = {WAVE_HOM_2D: 3, WAVE_MMS_2D: 3, WAVE_VAR_2D: 3, ADVECTION_1D: 1, ADVECTI
 EXPORTS = ("sbp_create", "sbp_destroy", "sbp_last_error", "sbp_dofs", "sbp_rhs", "sbp_apply", "sbp_rk4_nsteps",
            "sbp_ts_rk4", "sbp_rk4", "sbp_set_state", "sbp_get_state", "sbp_rk4_resident", "sbp_synchronize",
            "sbp_error_norms", "sbp_hnorm", "sbp_get_stream", "sbp_launch_count", "sbp_probe_dfma_rate",
+           "sbp_set_wait_limit", "sbp_test_drop_tile",
            "sbp_wave_rhs_noalloc", "sbp_write_petsc_vec", "sbp_read_petsc_vec",
            "sbp_batch_create", "sbp_batch_destroy", "sbp_batch_last_error", "sbp_batch_set_state",
            "sbp_batch_get_state", "sbp_batch_rk4_resident", "sbp_batch_synchronize", "sbp_batch_autotune",
@@ -124,6 +125,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.sbp_launch_count.argtypes = [P]
     L.sbp_launch_count.restype = C.c_longlong
     L.sbp_probe_dfma_rate.argtypes = [C.c_int, _dp]
+    L.sbp_set_wait_limit.argtypes = [P, C.c_longlong]
+    L.sbp_test_drop_tile.argtypes = [P, C.c_longlong]
     L.sbp_wave_rhs_noalloc.argtypes = [C.POINTER(Desc), C.c_double, C.c_void_p, C.c_void_p]
     L.sbp_batch_create.argtypes = [C.POINTER(Instance), C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(P)]
     L.sbp_batch_destroy.argtypes = [P]
@@ -307,6 +310,15 @@ class Context:
         dst = np.empty_like(src)
         self._check(self._L.sbp_apply(self._h, t, src.ctypes.data, dst.ctypes.data, HOST))
         return dst
+
+    def set_wait_limit(self, ns: int):
+        """Limit of the stage kernels' bounded device waits (0: the default, 200 ms)."""
+        self._check(self._L.sbp_set_wait_limit(self._h, ns))
+
+    def test_drop_tile(self, tile: int):
+        """Test aid: the next rhs()/apply() issues no load for this tile, so its
+        bounded wait runs out and the call raises SbpError(ERR_DEVICE)."""
+        self._check(self._L.sbp_test_drop_tile(self._h, tile))
 
     def rhs_ptr(self, t: float, src_ptr: int, dst_ptr: int, where: int):
         self._check(self._L.sbp_rhs(self._h, t, src_ptr, dst_ptr, where))

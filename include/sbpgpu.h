@@ -187,6 +187,21 @@ int sbp_ts_rk45(sbp_ctx* ctx, double t_end, double dt, double* v, int where);
 int sbp_get_stream(const sbp_ctx* ctx, void** stream);
 long long sbp_launch_count(const sbp_ctx* ctx);
 
+/* Failure detection (no counterpart in the reference, whose MPI ranks have
+ * no device waits). Every mbarrier wait in the 2D wave stage kernels is
+ * bounded by %globaltimer; a wait that runs out sets the context's error word,
+ * the kernel lets its copies in flight land and returns, and the next
+ * sbp_synchronize (or the synchronous entry point that launched it) returns
+ * SBP_ERR_DEVICE and clears the word: the context stays usable.
+ * sbp_set_wait_limit: the limit in ns (default 200 ms; 0 restores it); drops
+ *   the context's captured step graphs, which carry the old limit.
+ * sbp_test_drop_tile: test aid for that path. The next sbp_rhs / sbp_apply of
+ *   a 2D wave context issues no load for tile `tile` (row-major index of the
+ *   stage kernel's tiles), so the wait for it runs out and the call returns
+ *   SBP_ERR_DEVICE. Nothing faults or hangs; never applies to RK4 steps. */
+int sbp_set_wait_limit(sbp_ctx* ctx, long long ns);
+int sbp_test_drop_tile(sbp_ctx* ctx, long long tile);
+
 /* Measured FP64 FMA throughput of the current device in DFMA/s (a
  * 1-second-scale probe). No counterpart in the reference; used to state the
  * FP64 ALU roof beside the HBM roof. */
@@ -327,7 +342,11 @@ int sbp_read_petsc_vec(const char* path, double* v, long long capacity, long lon
  *       overlaps (other streams or threads) race on the array: serialise them.
  * First call on a device: does a one-time set-up on that device (the array's
  *       device address, the kernels' shared-memory opt-in); make it before
- *       any stream capture. */
+ *       any stream capture. Later calls look the address up again and redo
+ *       the set-up if it moved (after cudaDeviceReset).
+ * Every call is synchronous: it waits on desc->stream for its own work and
+ *       reads the kernel's error word back to the host before returning.
+ *       The calling thread's current device is restored on return. */
 #define SBP_NOALLOC_MAX_PLANE 65536
 int sbp_wave_rhs_noalloc(const sbp_desc* desc, double t, const double* src, double* dst);
 

@@ -50,6 +50,17 @@ class _Problem(C.Structure):
                 ("nz", C.c_longlong), ("hiz", C.c_double), ("xl2", C.c_double)]
 
 
+def reference_dir() -> str | None:
+    """Where the reference checkout is, if anywhere: $REF_DIR, else baseline/_ref/
+    beside the repository, else the container's checkout. None when none holds the
+    reference's hot-path headers (the GPU machine has none)."""
+    root = os.path.dirname(HERE)
+    for cand in (os.environ.get("REF_DIR"), os.path.join(root, "baseline", "_ref"), "/root/reference"):
+        if cand and os.path.isdir(os.path.join(cand, "code", "include", "sbpops")):
+            return cand
+    return None
+
+
 def build(ref_dir: str | None = None, quiet: bool = True) -> None:
     """Build the port (always) and oracle/_ref (when the reference checkout exists)."""
     args = ["make", "-s", "-C", HERE, "-j8", "all"]

@@ -155,6 +155,12 @@ int orc_bc(const orc_problem* p, const double* src, double* dst) {
   if (rc) return rc;
   switch (p->problem) {
     case ORC_WAVE_HOM_2D:
+      if (p->bc == ORC_BC_CHARACTERISTIC) {
+        DISPATCH(wave_hom_char_bc, p, src, dst);
+      } else {
+        DISPATCH(wave_free_surface_bc, p, src, dst);
+      }
+      break;
     case ORC_WAVE_MMS_2D: DISPATCH(wave_free_surface_bc, p, src, dst); break;
     case ORC_WAVE_VAR_2D: DISPATCH(wave_var_bc, p, src, dst); break;
     case ORC_WAVE_2BLOCK_2D: DISPATCH(wave_2block_bc, p, src, dst); break;

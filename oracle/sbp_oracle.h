@@ -35,7 +35,7 @@ enum orc_problem_kind {
 
 enum orc_bc_kind {
   ORC_BC_REFERENCE = 0,      /* the problem's own BC in the reference */
-  ORC_BC_CHARACTERISTIC = 1  /* ORC_WAVE_VAR_2D only: non-reflecting SAT */
+  ORC_BC_CHARACTERISTIC = 1  /* ORC_WAVE_VAR_2D, ORC_WAVE_2BLOCK_2D, ORC_WAVE_3D and ORC_WAVE_HOM_2D (rho = K = 1): non-reflecting SAT */
 };
 
 typedef struct {

@@ -45,9 +45,12 @@ def cases():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-dir", default="/root/reference")
+    ap.add_argument("--ref-dir", default=O.reference_dir(),
+                    help="the reference checkout (default: $REF_DIR, baseline/_ref/, the container's checkout)")
     ap.add_argument("--out", default=os.path.join(HERE, "ref_rhs.npz"))
     args = ap.parse_args()
+    if not args.ref_dir:
+        sys.exit("no reference checkout found: set REF_DIR or pass --ref-dir")
     O.build(ref_dir=args.ref_dir)
     if not O.Reference.available():
         sys.exit("oracle/_ref was not built: the reference checkout is needed")

@@ -35,7 +35,7 @@ def test_reference_arm_two_ranks_prints_one_line():
     assert d["e2e"]["h2d_bytes_per_step"] == 0
 
 
-def test_max_over_ranks_reduction_gloo():
+def test_max_over_ranks_reduction_gloo(tmp_path):
     """The timing reduction bench.py uses (all_reduce MAX of elapsed times)."""
     code = r'''
 import os, torch, torch.distributed as dist
@@ -48,14 +48,10 @@ if r == 0:
     print("OK")
 dist.destroy_process_group()
 '''
-    path = os.path.join(ROOT, "tests", "_maxreduce_child.py")
-    with open(path, "w") as f:
-        f.write(code)
-    try:
-        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
-               "--master-addr=127.0.0.1", f"--master-port={_free_port()}", path]
-        r = subprocess.run(cmd, capture_output=True, text=True, timeout=120)
-        assert r.returncode == 0, r.stderr[-2000:]
-        assert "OK" in r.stdout
-    finally:
-        os.remove(path)
+    path = tmp_path / "maxreduce_child.py"
+    path.write_text(code)
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
+           "--master-addr=127.0.0.1", f"--master-port={_free_port()}", str(path)]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "OK" in r.stdout

@@ -27,8 +27,9 @@ def _desc(sbp, order, nx, ny, precision=None, problem=None):
 
 
 @pytest.mark.parametrize("case", [(4, 20, 20, 4, 1, -1), (6, 40, 17, 2, 2, -1), (4, 30, 30, 2, 2, -4, "fp32"),
-                                  (4, 30, 30, 2, 2, -4, "adv")],
-                         ids=["too_narrow_x", "too_narrow_y", "fp32", "other_problem"])
+                                  (4, 30, 30, 2, 2, -4, "adv"), (4, 7, 30, 1, 1, -1), (6, 40, 11, 1, 1, -1)],
+                         ids=["too_narrow_x", "too_narrow_y", "fp32", "other_problem", "below_min_points_x",
+                              "below_min_points_y"])
 def test_decomp_rejects_unsupported_descriptions(sbp, case):
     order, nx, ny, px, py, code = case[:6]
     kw = {}

@@ -149,6 +149,26 @@ def test_var_coefficients_reduce_to_homogeneous(port):
         assert np.array_equal(hom, var)
 
 
+def test_constant_coefficient_characteristic_sat_equals_unit_fields(port):
+    """The rho = K = 1 characteristic SAT of the constant-coefficient problem (the
+    bench workload's CPU form) is the variable-coefficient SAT on unit fields, bit
+    for bit, on square and non-square grids."""
+    rng = np.random.default_rng(4)
+    for order in (2, 4, 6):
+        for nx, ny in ((23, 23), (31, 17)):
+            ones = np.ones(nx * ny)
+            src = rng.standard_normal(3 * nx * ny)
+            hom = port.rhs(O.Problem(O.WAVE_HOM_2D, order, nx, ny, bc=O.BC_CHARACTERISTIC), src)
+            var = port.rhs(O.Problem(O.WAVE_VAR_2D, order, nx, ny, rho=ones, K=ones, bc=O.BC_CHARACTERISTIC), src)
+            assert np.array_equal(hom, var)
+            h = 2.0 / (nx - 1)
+            v = port.init_wave_pulse(nx, ny, 0.1, -0.2, 0.2)
+            a = port.rk4(O.Problem(O.WAVE_HOM_2D, order, nx, ny, bc=O.BC_CHARACTERISTIC), v, 0.0, 0.2 * h, 5)
+            b = port.rk4(O.Problem(O.WAVE_VAR_2D, order, nx, ny, rho=ones, K=ones, bc=O.BC_CHARACTERISTIC), v, 0.0,
+                         0.2 * h, 5)
+            assert np.array_equal(a, b)
+
+
 def _energy(port, v, n, order, rho, K):
     h = 2.0 / (n - 1)
     w = np.empty_like(v)

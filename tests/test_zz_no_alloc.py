@@ -4,8 +4,9 @@ Such callers -- a host framework that owns all device memory through its own
 pool, or a latency-bound loop that cannot take cudaMalloc's device
 synchronisation -- cannot create a context (sbp_create allocates). The entry
 point keeps its scratch in a static device array instead, and must give what
-sbp_rhs gives. Two calls in a row on different grids check that the contents
-the first call leaves in the shared array do not leak into the second.
+sbp_rhs and the oracle give. Two calls in a row on different grids check that
+the contents the first call leaves in the shared array do not leak into the
+second.
 
 This file is collected last so a run that stops at the first failure has run
 every other test before it.
@@ -29,8 +30,10 @@ def test_noalloc_rejects_grids_beyond_the_static_scratch(sbp):
 
 
 @pytest.mark.gpu
-def test_noalloc_matches_sbp_rhs_on_two_calls_in_a_row(sbp):
+def test_noalloc_matches_sbp_rhs_on_two_calls_in_a_row(sbp, port):
     import torch
+
+    import oracle as O
 
     rng = np.random.default_rng(2026)
     cases = [  # (order, nx, ny, bc): a larger grid first, then a smaller one
@@ -49,3 +52,5 @@ def test_noalloc_matches_sbp_rhs_on_two_calls_in_a_row(sbp):
         got = d_dst.cpu().numpy()
         assert np.isfinite(got).all()
         assert relerr(got, expected) <= TOL64
+        obc = O.BC_CHARACTERISTIC if bc == sbp.BC_CHARACTERISTIC else O.BC_REFERENCE
+        assert relerr(got, port.rhs(O.Problem(O.WAVE_HOM_2D, order, nx, ny, bc=obc), src, 0.25)) <= TOL64
