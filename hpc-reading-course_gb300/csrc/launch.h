@@ -25,6 +25,25 @@ inline int wave_tile_height(int elem_bytes, int kind = WK_HOM) {
   return kind == WK_VAR ? wave_ty<float, WK_VAR>() : wave_ty<float, WK_HOM>();
 }
 
+// Scales of the fixed-point FP64 stages (wave2d_fixed.cuh) for one launch: the
+// RHS in units of sigma = -hi/den per direction, and the stage's RK4
+// coefficients times sigma of each component (u and p: x, v: y). Every launch of
+// a constant-coefficient FP64 stage sets them; the kernel refuses to run without.
+inline void set_fixed_scales(WaveParams<double>& p, int order, double hix, double hiy) {
+  const double den = order == 2 ? 2.0 : (order == 4 ? 12.0 : 60.0);
+  p.fx_sig[0] = -hix / den;
+  p.fx_sig[1] = -hiy / den;
+  p.fx_isig[0] = -den / hix;
+  p.fx_isig[1] = -den / hiy;
+  p.fx_rho = hiy / hix;
+  p.fx_square = hix == hiy ? 1 : 0;
+  const double sg[3] = {p.fx_sig[0], p.fx_sig[1], p.fx_sig[0]};
+  for (int c = 0; c < 3; c++) {
+    p.fx_ca[c] = p.c_acc * sg[c];
+    p.fx_cw[c] = p.c_w * sg[c];
+  }
+}
+
 // Streaming multiprocessors of the current device (cached per device).
 int device_sm_count();
 

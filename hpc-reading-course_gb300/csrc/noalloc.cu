@@ -175,6 +175,7 @@ extern "C" int sbp_wave_rhs_noalloc(const sbp_desc* d, double t, const double* s
   p.kout = out;
   p.t = t;
   p.err = err;
+  set_fixed_scales(p, d->order, hix, hiy);
 
   // The error word must start at zero; everything else is overwritten.
   if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return reject(SBP_ERR_CUDA, "cudaMemsetAsync failed");

@@ -250,6 +250,7 @@ int launch_stage(sbp_ctx* ctx, int stage, int rk, double t, double dt, void* in,
     p.c_w = c_w;
     p.t = t;
     p.wait_ns = ctx->wait_ns;
+    if constexpr (sizeof(T) == 8) set_fixed_scales(p, ctx->d.order, ctx->hix, ctx->hiy);
     if (stage == ST_RHS) {  // a direct launch (RHS evaluation), never a captured one
       p.test_drop_tile = ctx->drop_tile;
       ctx->drop_tile = 0;

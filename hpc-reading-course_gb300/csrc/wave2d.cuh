@@ -40,6 +40,17 @@ enum Stage : int { ST_RHS = 0, ST_FIRST = 1, ST_MID = 2, ST_LAST = 4, ST_RKF1 = 
 // error partial sum (s = 6).
 constexpr bool is_rkf_stage(int stage) { return stage >= ST_RKF1 && stage <= ST_RKF6; }
 
+// The constant-coefficient FP64 stages (RHS and RK4; rho = K = 1) evaluate their
+// interior stencils in exact integer arithmetic (wave2d_fixed.cuh) instead of
+// FP64 FMAs, which GB300 issues at about 1/64 of its FP32 rate. The build may set
+// SBP_FP64_FIXED=0 to compare with the FP64 tap chains.
+#ifndef SBP_FP64_FIXED
+#define SBP_FP64_FIXED 1
+#endif
+template <typename T, int KIND, int STAGE> constexpr bool wave_fixed() {
+  return SBP_FP64_FIXED != 0 && sizeof(T) == 8 && KIND == WK_HOM && !is_rkf_stage(STAGE);
+}
+
 template <typename T> struct WaveParams {
   int nx, ny;
   long long pitch;    // elements per row
@@ -78,6 +89,13 @@ template <typename T> struct WaveParams {
   // for tile k, so the consumers' wait for it runs out (0: none).
   unsigned long long wait_ns;
   int test_drop_tile;
+  // Fixed-point FP64 stages (wave_fixed): the RHS is formed in units of
+  // sigma = -hi/den per direction (den: the interior stencil's common denominator),
+  // fx_isig = 1/sigma, fx_rho = sigma_y/sigma_x, fx_square = (sigma_x == sigma_y),
+  // and fx_ca/fx_cw are c_acc/c_w times sigma of each component (u: x, v: y, p: x).
+  double fx_sig[2], fx_isig[2], fx_rho;
+  double fx_ca[3], fx_cw[3];
+  int fx_square;
 };
 
 constexpr int kWaveTX = 64;            // tile width (x, contiguous)
@@ -103,12 +121,14 @@ template <typename T> constexpr int default_wave_ty() { return sizeof(T) == 8 ? 
 #endif
 
 // Pipeline shape of the constant-coefficient FP64 kernel (tile rows, consumer
-// warps); the build may override them to compare shapes.
+// warps); the build may override them to compare shapes. Measured with the
+// fixed-point stencils at 4096^2, order 4 (point-stage updates/s): (8, 8) 2.78e10,
+// (12, 12) 3.36e10, (16, 8) 3.06e10, (16, 16) 3.45e10, (20, 10) 3.59e10.
 #ifndef SBP_FP64_TILE_ROWS
-#define SBP_FP64_TILE_ROWS 12
+#define SBP_FP64_TILE_ROWS 20
 #endif
 #ifndef SBP_FP64_WARPS
-#define SBP_FP64_WARPS 12
+#define SBP_FP64_WARPS 10
 #endif
 
 // Tile height of the single-instance kernel: the variable-coefficient FP32
@@ -145,7 +165,7 @@ template <typename T, int KIND> constexpr int wave_warps() {
 }
 
 template <typename T, int ORD, int STAGE, int TY_ = default_wave_ty<T>(), int PRM_BYTES = 0, bool COEF = false,
-          int NST_ = 2, int WARPS_ = kWaveConsumerWarps>
+          int NST_ = 2, int WARPS_ = kWaveConsumerWarps, bool FIX_ = false>
 struct WaveTile {
   static constexpr int WARPS = WARPS_;                        // consumer warps
   static constexpr int THREADS = 32 * (WARPS_ + 1);           // + the producer warp
@@ -157,7 +177,10 @@ struct WaveTile {
   static constexpr int HY = R;                                // y halo loaded
   static constexpr int PW = kWaveTX + 2 * HX;                 // p/u tile row length
   static constexpr int PH = TY + 2 * HY;                      // p/v tile rows
-  static constexpr bool LOAD_UN = (STAGE == ST_MID) || (STAGE == ST_LAST && COMP);
+  static constexpr bool FIX = FIX_;  // fixed-point FP64 stage: the p/u/v boxes become int64 in place
+  // u^n as a point box: the stages that read it, and the fixed-point first stage, whose
+  // stencil boxes no longer hold the doubles of u^n once converted
+  static constexpr bool LOAD_UN = (STAGE == ST_MID) || (STAGE == ST_LAST && COMP) || (FIX_ && STAGE == ST_FIRST);
   static constexpr bool LOAD_ACC = (STAGE == ST_MID) || (STAGE == ST_LAST);
   static constexpr bool LOAD_COMP = (STAGE == ST_LAST && COMP);
   static constexpr bool LOAD_COEF = COEF;  // 1/rho and K planes as one 2-component point box
@@ -180,7 +203,10 @@ struct WaveTile {
   static constexpr int NST = NST_;                            // ring depth
   static constexpr int OFF_BAR = NST * STAGE_BYTES;           // full[NST], empty[NST]
   static constexpr int OFF_DBAR = OFF_BAR + 128;              // deferred-pass barriers[NST]
-  static constexpr int SMEM = OFF_BAR + 256;
+  // fixed-point stages: exponent-maximum and conversion barriers[NST] each, then
+  // the maxima of the p and u/v boxes per stage (int[NST][2])
+  static constexpr int OFF_FX = OFF_BAR + 256;
+  static constexpr int SMEM = OFF_BAR + 256 + (FIX_ ? 192 : 0);
   static constexpr uint32_t TX_BYTES = BYTES_P + BYTES_U + BYTES_V + (LOAD_UN ? BYTES_PT : 0) +
                                        (LOAD_ACC ? BYTES_PT : 0) + (LOAD_COMP ? BYTES_PT : 0) +
                                        (LOAD_COEF ? BYTES_K : 0) + PRM_BYTES;
@@ -556,7 +582,13 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
 // The Tile type of the single-instance kernel for (T, order, kind, stage).
 template <typename T, int ORD, int KIND, int STAGE>
 using WaveStageTile = WaveTile<T, ORD, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR && SBP_VAR_COEF != 0,
-                               wave_ring<T, KIND>(), wave_warps<T, KIND>()>;
+                               wave_ring<T, KIND>(), wave_warps<T, KIND>(), wave_fixed<T, KIND, STAGE>()>;
+
+}  // namespace sbp
+
+#include "wave2d_fixed.cuh"
+
+namespace sbp {
 
 template <typename T, int ORD, int KIND, int STAGE>
 __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
@@ -577,11 +609,25 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   uint64_t* dbar = reinterpret_cast<uint64_t*>(smem + Tile::OFF_DBAR);
+  uint64_t* fxa = reinterpret_cast<uint64_t*>(smem + Tile::OFF_FX);       // fixed: exponent maxima known
+  uint64_t* fxb = fxa + 8;                                                 // fixed: boxes converted
+  int* fxmax = reinterpret_cast<int*>(smem + Tile::OFF_FX + 128);          // fixed: [NST][2] maxima
+  if constexpr (Tile::FIX) {
+    if (prm.fx_sig[0] == 0.0 || prm.fx_sig[1] == 0.0) {  // the host did not set the fixed-point scales
+      if (threadIdx.x == 0) atomicOr(prm.err, ERR_BAD_LAUNCH);
+      return;
+    }
+  }
   if (threadIdx.x == 0) {
     for (int s = 0; s < NST; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], WARPS);
       mbar_init(&dbar[s], WARPS);
+      if constexpr (Tile::FIX) {
+        mbar_init(&fxa[s], WARPS);
+        mbar_init(&fxb[s], WARPS);
+        fxmax[2 * s] = fxmax[2 * s + 1] = 0;
+      }
     }
     fence_barrier_init();
   }
@@ -628,9 +674,24 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
       break;
     }
     const int i0 = (tile % ntx) * kWaveTX, j0 = (tile / ntx) * TY;
-    wave_tile_compute<T, ORD, KIND, STAGE, Tile>(prm, prm.in, prm.wout, prm.c_acc, prm.c_w,
-                                                 smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane, &errsq, &dbar[b],
-                                                 &dphase, b, k);
+    if constexpr (Tile::FIX) {
+      int emax[2];
+      bool bad;
+      if (!fx_convert_tile<Tile>(smem + b * Tile::STAGE_BYTES, &fxa[b], &fxb[b], fxmax + 2 * b, (k / NST) & 1,
+                                 prm.wait_ns, threadIdx.x, emax, bad)) {
+        if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
+        break;
+      }
+      wave_tile_fixed<ORD, STAGE, Tile>(prm, prm.in, prm.wout, smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane,
+                                        emax[0], emax[1], bad, &dbar[b], &dphase, b, k);
+      // the converted boxes were written through the generic proxy; order those writes
+      // before the TMA (async proxy) refills the stage
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    } else {
+      wave_tile_compute<T, ORD, KIND, STAGE, Tile>(prm, prm.in, prm.wout, prm.c_acc, prm.c_w,
+                                                   smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane, &errsq, &dbar[b],
+                                                   &dphase, b, k);
+    }
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[b]);
   }

@@ -1,0 +1,295 @@
+// wave2d_fixed.cuh -- the FP64 constant-coefficient wave stage (rho = K = 1)
+// with its interior stencils in exact integer arithmetic.
+//
+// GB300 issues FP64 FMAs at about 1/64 of its FP32 rate, and the FP64 tap
+// chains of wave_tile_compute (4 derivatives x 4 taps at order 4, plus the
+// stage update) keep that pipe busy long before HBM is. The interior stencils
+// of the central SBP operators have rational weights with a small common
+// denominator (code/include/sbpops/D1_central.h:245,254,266):
+//     order 2: (1/2)  (v1 - v-1)
+//     order 4: (1/12) (8 (v1 - v-1) - (v2 - v-2))
+//     order 6: (1/60) (45 (v1 - v-1) - 9 (v2 - v-2) + (v3 - v-3))
+// so den * sum is an integer combination of the point values. Each tile's
+// stencil boxes are converted once, in place, to 64-bit integers in units of
+// 2^(Emax - 1075), where Emax is the largest biased exponent among the box
+// values of the group (p; u and v together): a double +-M 2^(E-1075) with its
+// 53-bit mantissa M becomes +-round(M / 2^(Emax - E)), |V| < 2^53. The sums
+// are then exact in int64 (|S| < 110 * 2^54 < 2^61 at order 6, and the sum of
+// the u and v terms as well), and one conversion back to a double, rounded to
+// nearest, carries the only rounding of the stencil: the result is as accurate
+// as the reference's FP64 evaluation (the conversion to fixed point rounds each
+// value to 2^-53 of the box's largest magnitude, the FP64 sum rounds each
+// partial sum to 2^-53 of its own). The integer work runs on the INT pipe; the
+// FP64 pipe is left with the RK4 stage update, 1-2 FMAs per component, into
+// which the scale sigma = -hi/den is folded (fx_ca, fx_cw).
+//
+// Closure rows (boundary strips) keep the FP64 taps read from global memory
+// and are brought to the same units by 1/sigma; SAT terms are applied in FP64
+// in true units as in wave_tile_compute. A box holding a non-finite value gives
+// NaN for every point of its tile.
+#pragma once
+
+#include "sbp_device.cuh"
+
+namespace sbp {
+
+template <int ORD> struct FixDen;
+template <> struct FixDen<2> { static constexpr int value = 2; };
+template <> struct FixDen<4> { static constexpr int value = 12; };
+template <> struct FixDen<6> { static constexpr int value = 60; };
+
+// v (given as its two 32-bit words) as a signed integer in units of
+// 2^(emax - 1075), truncated towards zero; emax >= the exponent of v. Zero and
+// subnormal values give 0, as does any shift of 64 or more.
+__device__ __forceinline__ long long fx_from(unsigned lo, unsigned hi, int emax) {
+  const unsigned e = (hi >> 20) & 0x7FFu;
+  const unsigned mh = (hi & 0x000FFFFFu) | 0x00100000u;  // the 53-bit mantissa is mh:lo
+  const unsigned sh = e == 0 ? 64u : (unsigned)emax - e;
+  const unsigned rlo = sh < 32 ? __funnelshift_rc(lo, mh, sh) : __funnelshift_rc(mh, 0u, sh - 32u);
+  const unsigned rhi = __funnelshift_rc(mh, 0u, sh);
+  const long long r = (long long)(((unsigned long long)rhi << 32) | rlo);
+  const long long sg = (long long)((int)hi >> 31);  // 0 or -1
+  return (r ^ sg) - sg;
+}
+
+// s * 2^(eb - 11 - 1075) as a double, truncated towards zero (eb = emax + 11 of
+// the box; the tile guard keeps emax in [64, 2030], so the exponent stays normal).
+__device__ __forceinline__ double fx_to(long long s, int eb) {
+  const long long sg = s >> 63;
+  const unsigned long long a = (unsigned long long)((s ^ sg) - sg);
+  const int lz = __clzll((long long)a);                        // >= 2: |s| < 2^62
+  const unsigned long long n = a << (lz & 63);                  // leading one at bit 63
+  const unsigned mh = (unsigned)(n >> 43);                      // leading one + 20 fraction bits
+  const unsigned ml = (unsigned)(n >> 11);                      // the other 32 fraction bits
+  const unsigned hw = (((unsigned)(eb - lz - 1)) << 20) + mh;   // the leading one adds the last 1 to the exponent
+  const double r = __hiloint2double((int)(hw | ((unsigned)sg & 0x80000000u)), (int)ml);
+  return a == 0 ? 0.0 : r;
+}
+
+// den * (interior stencil sum) at the point c of an int64 line with stride st.
+template <int ORD>
+__device__ __forceinline__ long long fx_stencil(const long long* c, int st) {
+  if constexpr (ORD == 2) {
+    return c[st] - c[-st];
+  } else if constexpr (ORD == 4) {
+    return 8 * (c[st] - c[-st]) - (c[2 * st] - c[-2 * st]);
+  } else {
+    return 45 * (c[st] - c[-st]) - 9 * (c[2 * st] - c[-2 * st]) + (c[3 * st] - c[-3 * st]);
+  }
+}
+
+// Converts the p, u and v boxes of one ring stage to int64 in place (all
+// consumer threads). Each thread keeps its elements in registers between the
+// two barriers, both with bounded waits: the exponent maxima are known (fxa),
+// the boxes are converted (fxb). Returns false if a wait ran out. emax[0..1]
+// are the p and u/v maxima; a box whose maximum is below 64 (values under
+// 2^-959) converts to zeros, and one at 2031 or more (values from 2^1008, Inf,
+// NaN) marks the tile bad: its points get NaN.
+template <typename Tile>
+__device__ __forceinline__ bool fx_convert_tile(unsigned char* st, uint64_t* fxa, uint64_t* fxb, int* fxmax,
+                                                uint32_t parity, unsigned long long wait_ns, int tid, int (&emax)[2],
+                                                bool& bad) {
+  constexpr int NT = 32 * Tile::WARPS;
+  constexpr int NP = Tile::PH * Tile::PW, NU = Tile::TY * Tile::PW, NV = Tile::PH * kWaveTX;
+  constexpr int CP = (NP + NT - 1) / NT, CU = (NU + NT - 1) / NT, CV = (NV + NT - 1) / NT;
+  uint2* wP = reinterpret_cast<uint2*>(st);
+  uint2* wU = reinterpret_cast<uint2*>(st + Tile::OFF_U);
+  uint2* wV = reinterpret_cast<uint2*>(st + Tile::OFF_V);
+  const int lane = tid & 31;
+  uint2 rp[CP], ru[CU], rv[CV];
+  unsigned mp = 0, muv = 0;
+#pragma unroll
+  for (int c = 0; c < CP; c++) {
+    const int e = tid + c * NT;
+    rp[c] = (c < NP / NT || e < NP) ? wP[e] : make_uint2(0u, 0u);
+    mp = max(mp, rp[c].y & 0x7FF00000u);
+  }
+#pragma unroll
+  for (int c = 0; c < CU; c++) {
+    const int e = tid + c * NT;
+    ru[c] = (c < NU / NT || e < NU) ? wU[e] : make_uint2(0u, 0u);
+    muv = max(muv, ru[c].y & 0x7FF00000u);
+  }
+#pragma unroll
+  for (int c = 0; c < CV; c++) {
+    const int e = tid + c * NT;
+    rv[c] = (c < NV / NT || e < NV) ? wV[e] : make_uint2(0u, 0u);
+    muv = max(muv, rv[c].y & 0x7FF00000u);
+  }
+  mp = __reduce_max_sync(0xffffffffu, mp);
+  muv = __reduce_max_sync(0xffffffffu, muv);
+  if (lane == 0) {
+    atomicMax(&fxmax[0], (int)(mp >> 20));
+    atomicMax(&fxmax[1], (int)(muv >> 20));
+  }
+  __syncwarp();
+  if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(fxa)) : "memory");
+  if (!mbar_wait_bounded(fxa, parity, wait_ns)) return false;
+  int ep = fxmax[0], euv = fxmax[1];
+  bad = ep >= 2031 || euv >= 2031;
+  if (ep < 64) ep = 2111;  // every value converts to 0
+  if (euv < 64) euv = 2111;
+  long long* iP = reinterpret_cast<long long*>(wP);
+  long long* iU = reinterpret_cast<long long*>(wU);
+  long long* iV = reinterpret_cast<long long*>(wV);
+#pragma unroll
+  for (int c = 0; c < CP; c++) {
+    const int e = tid + c * NT;
+    if (c < NP / NT || e < NP) iP[e] = fx_from(rp[c].x, rp[c].y, ep);
+  }
+#pragma unroll
+  for (int c = 0; c < CU; c++) {
+    const int e = tid + c * NT;
+    if (c < NU / NT || e < NU) iU[e] = fx_from(ru[c].x, ru[c].y, euv);
+  }
+#pragma unroll
+  for (int c = 0; c < CV; c++) {
+    const int e = tid + c * NT;
+    if (c < NV / NT || e < NV) iV[e] = fx_from(rv[c].x, rv[c].y, euv);
+  }
+  __syncwarp();
+  if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(fxb)) : "memory");
+  if (!mbar_wait_bounded(fxb, parity, wait_ns)) return false;
+  // every consumer has read the maxima: clear them for the stage's next tile (its
+  // atomics come after this warp's arrivals on the next tile's barriers)
+  if (tid == 0) fxmax[0] = fxmax[1] = 0;
+  emax[0] = ep;
+  emax[1] = euv;
+  return true;
+}
+
+// One tile of a fixed-point FP64 stage for the consumer warps. The stage's p,
+// u, v boxes hold int64 (fx_convert_tile); u^n, acc are FP64 point boxes.
+template <int ORD, int STAGE, typename Tile>
+__device__ __forceinline__ void wave_tile_fixed(const WaveParams<double>& prm, const double* __restrict__ in,
+                                                double* wout, const unsigned char* st, const int i0, const int j0,
+                                                const int warp, const int lane, const int ep, const int euv,
+                                                const bool bad, uint64_t* dbar, uint32_t* dphase, const int b,
+                                                const int k) {
+  constexpr int TY = Tile::TY, CS = OpShape<ORD>::CS;
+  constexpr int HX = Tile::HX, HY = Tile::HY, PW = Tile::PW;
+  constexpr int ROWS = TY / Tile::WARPS;
+  constexpr int TPT = TY * kWaveTX;
+  const int nx = prm.nx, ny = prm.ny;
+  const long long pitch = prm.pitch, plane = prm.plane;
+  const long long* iP = reinterpret_cast<const long long*>(st);
+  const long long* iU = reinterpret_cast<const long long*>(st + Tile::OFF_U);
+  const long long* iV = reinterpret_cast<const long long*>(st + Tile::OFF_V);
+  const double* sN = reinterpret_cast<const double*>(st + Tile::OFF_N);
+  const double* sA = reinterpret_cast<const double*>(st + Tile::OFF_A);
+  double* sD = reinterpret_cast<double*>(const_cast<unsigned char*>(st) + Tile::OFF_DEF);
+  const bool xfaces = dbar != nullptr && prm.bc != BC_NONE && (i0 == 0 || (nx - 1 >= i0 && nx - 1 < i0 + kWaveTX));
+  const double sg[3] = {prm.fx_sig[0], prm.fx_sig[1], prm.fx_sig[0]};
+  const int ebp = ep + 11, ebuv = euv + 11;  // fx_to's exponent bases
+  (void)sN;
+  (void)sA;
+#pragma unroll
+  for (int rr = 0; rr < ROWS; rr++) {
+    const int y = warp * ROWS + rr;
+    const int j = j0 + y;
+    if (j >= ny) continue;
+    const bool yint = (j >= CS) && (j < ny - CS);
+#pragma unroll
+    for (int cc = 0; cc < kWaveTX / 32; cc++) {
+      const int x = lane + 32 * cc;
+      const int i = i0 + x;
+      if (i >= nx) continue;
+      const bool xint = (i >= CS) && (i < nx - CS);
+      const long long* cP = iP + (y + HY) * PW + (x + HX);
+      const long long* cU = iU + y * PW + (x + HX);
+      const long long* cV = iV + (y + HY) * kWaveTX + x;
+      // RHS in units of sigma per component: F_u = sx ku, F_v = sy kv, F_p = sx kp
+      double ku, kv, kp;
+      if (xint) {
+        ku = fx_to(fx_stencil<ORD>(cP, 1), ebp);
+      } else {
+        ku = closure_line<double, ORD>(in + 2 * plane + (long long)j * pitch, 1, nx, i, prm.dx.cls) * prm.fx_isig[0];
+      }
+      if (yint) {
+        kv = fx_to(fx_stencil<ORD>(cP, PW), ebp);
+      } else {
+        kv = closure_line<double, ORD>(in + 2 * plane + i, pitch, ny, j, prm.dy.cls) * prm.fx_isig[1];
+      }
+      if (xint && yint && prm.fx_square) {
+        kp = fx_to(fx_stencil<ORD>(cU, 1) + fx_stencil<ORD>(cV, kWaveTX), ebuv);
+      } else {
+        const double ax = xint ? fx_to(fx_stencil<ORD>(cU, 1), ebuv)
+                               : closure_line<double, ORD>(in + (long long)j * pitch, 1, nx, i, prm.dx.cls) *
+                                     prm.fx_isig[0];
+        const double ay = yint ? fx_to(fx_stencil<ORD>(cV, kWaveTX), ebuv)
+                               : closure_line<double, ORD>(in + plane + i, pitch, ny, j, prm.dy.cls) * prm.fx_isig[1];
+        kp = fma(prm.fx_rho, ay, ax);
+      }
+      if (bad) ku = kv = kp = __longlong_as_double(0x7FF8000000000000ll);
+
+      const long long q = (long long)j * pitch + i;
+      const int sp = y * kWaveTX + x;  // point within a 3-component smem box
+      const bool edge = (i == 0) || (j == 0) || (i == nx - 1) || (j == ny - 1);
+      if (prm.bc != BC_NONE && edge) {
+        if (xfaces && j != 0 && j != ny - 1) {
+          double* d = sD + ((i == 0 ? 0 : TY) + y) * 3;  // an x-face point only: deferred
+          d[0] = ku;
+          d[1] = kv;
+          d[2] = kp;
+          continue;
+        }
+        // SAT and the stage update in true units
+        const double pc = in[2 * plane + q], uc = in[q], vc = in[plane + q];
+        const Rhs3<double> r =
+            apply_sat<double, WK_HOM>(prm, in, i, j, pc, uc, vc, Rhs3<double>{sg[0] * ku, sg[1] * kv, sg[2] * kp});
+        const double kt[3] = {r.u, r.v, r.p};
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const double cen = (STAGE == ST_FIRST) ? sN[c * TPT + sp] : 0.0;
+          wave_point_store<double, STAGE, Tile>(prm, wout, prm.c_acc, prm.c_w, sA, sN, nullptr, sp, c,
+                                                c * plane + q, kt[c], cen);
+        }
+        continue;
+      }
+      const double kf[3] = {ku, kv, kp};
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const long long o = c * plane + q;
+        if constexpr (STAGE == ST_RHS) {
+          prm.kout[o] = sg[c] * kf[c];
+        } else {
+          const double cen = (STAGE == ST_FIRST) ? sN[c * TPT + sp] : 0.0;
+          wave_point_store<double, STAGE, Tile>(prm, wout, prm.fx_ca[c], prm.fx_cw[c], sA, sN, nullptr, sp, c, o,
+                                                kf[c], cen);
+        }
+      }
+    }
+  }
+  if (xfaces) {
+    __syncwarp();
+    if (lane == 0) mbar_arrive(dbar);  // this warp's deferred entries are in shared memory
+    const uint32_t par = (*dphase >> b) & 1u;
+    *dphase ^= 1u << b;
+    if (warp != k % Tile::WARPS) return;
+    if (!mbar_wait_bounded(dbar, par, prm.wait_ns)) {
+      if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
+      return;
+    }
+    for (int e = lane; e < 2 * TY; e += 32) {
+      const int side = e / TY, y = e - side * TY, j = j0 + y;
+      const int i = side == 0 ? 0 : nx - 1;
+      if (i < i0 || i >= i0 + kWaveTX || j >= ny || j == 0 || j == ny - 1) continue;
+      const int x = i - i0;
+      const long long q = (long long)j * pitch + i;
+      const double pc = in[2 * plane + q], uc = in[q], vc = in[plane + q];
+      const double* d = sD + (side * TY + y) * 3;
+      const Rhs3<double> r =
+          apply_sat<double, WK_HOM>(prm, in, i, j, pc, uc, vc, Rhs3<double>{sg[0] * d[0], sg[1] * d[1], sg[2] * d[2]});
+      const double kt[3] = {r.u, r.v, r.p};
+      const int sp = y * kWaveTX + x;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const double cen = (STAGE == ST_FIRST) ? sN[c * TPT + sp] : 0.0;
+        wave_point_store<double, STAGE, Tile>(prm, wout, prm.c_acc, prm.c_w, sA, sN, nullptr, sp, c, c * plane + q,
+                                              kt[c], cen);
+      }
+    }
+  }
+}
+
+}  // namespace sbp
