@@ -69,6 +69,7 @@ struct sbp_ctx {
   void *rinv = nullptr, *kmod = nullptr;     // WAVE_VAR: T planes
   double *rho64 = nullptr, *k64 = nullptr;   // WAVE_VAR: nx*ny FP64
   int* err = nullptr;
+  int* sched = nullptr;  // the wave stage kernels' dynamic tile queue (2 ints, zero between launches)
   WaveMaps maps_un{}, maps_wa{}, maps_wb{};
   // adaptive RK45 (FP64; allocated on first use)
   double* rk_k[6] = {};
@@ -250,6 +251,7 @@ int launch_stage(sbp_ctx* ctx, int stage, int rk, double t, double dt, void* in,
     p.c_w = c_w;
     p.t = t;
     p.wait_ns = ctx->wait_ns;
+    p.sched = ctx->sched;
     if constexpr (sizeof(T) == 8) set_fixed_scales(p, ctx->d.order, ctx->hix, ctx->hiy);
     if (stage == ST_RHS) {  // a direct launch (RHS evaluation), never a captured one
       p.test_drop_tile = ctx->drop_tile;
@@ -595,7 +597,7 @@ void release(sbp_ctx* ctx) {
   if (ctx->rk_unew) cudaFree(ctx->rk_unew);
   if (ctx->rk_ctrl) cudaFree(ctx->rk_ctrl);
   void* bufs[] = {ctx->un, ctx->acc, ctx->wa, ctx->wb, ctx->comp, ctx->io, ctx->partial, ctx->red,
-                  ctx->rinv, ctx->rho64, ctx->k64, ctx->err};  // kmod lives inside the rinv allocation
+                  ctx->rinv, ctx->rho64, ctx->k64, ctx->err, ctx->sched};  // kmod lives inside the rinv allocation
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -700,6 +702,8 @@ int sbp_create(const sbp_desc* desc, sbp_ctx** out) {
   if ((e = cudaMalloc((void**)&ctx->red, 4 * sizeof(double))) != cudaSuccess) return cuda_fail("cudaMalloc(red)", e);
   if ((e = cudaMalloc((void**)&ctx->err, sizeof(int))) != cudaSuccess) return cuda_fail("cudaMalloc(err)", e);
   cudaMemset(ctx->err, 0, sizeof(int));
+  if ((e = cudaMalloc((void**)&ctx->sched, 2 * sizeof(int))) != cudaSuccess) return cuda_fail("cudaMalloc(sched)", e);
+  cudaMemset(ctx->sched, 0, 2 * sizeof(int));
 
   if (has_fields(d.problem)) {
     const size_t np = (size_t)ctx->npts;

@@ -96,6 +96,11 @@ template <typename T> struct WaveParams {
   double fx_sig[2], fx_isig[2], fx_rho;
   double fx_ca[3], fx_cw[3];
   int fx_square;
+  // Dynamic tile queue: sched[0] hands out tile indices, sched[1] counts the CTAs
+  // done; the last CTA resets both to zero for the next launch. Null: each CTA
+  // walks the tiles with a fixed stride (the Fehlberg stages always do, so their
+  // per-CTA error partials keep a fixed summation order).
+  int* sched;
 };
 
 constexpr int kWaveTX = 64;            // tile width (x, contiguous)
@@ -122,13 +127,15 @@ template <typename T> constexpr int default_wave_ty() { return sizeof(T) == 8 ? 
 
 // Pipeline shape of the constant-coefficient FP64 kernel (tile rows, consumer
 // warps); the build may override them to compare shapes. Measured with the
-// fixed-point stencils at 4096^2, order 4 (point-stage updates/s): (8, 8) 2.78e10,
-// (12, 12) 3.36e10, (16, 8) 3.06e10, (16, 16) 3.45e10, (20, 10) 3.59e10.
+// fixed-point stencils at 4096^2, order 4 (point-stage updates/s), with the dynamic
+// tile queue: (12, 12) 3.76e10, (16, 16) 4.20e10, (20, 10) 4.05e10, (18, 18) 4.37e10,
+// (20, 20) 4.43e10, (22, 22) 4.56e10; a third ring stage: (12, 12) 3.74e10, (8, 8)
+// 3.09e10. More warps hide more of the integer pipeline's latency.
 #ifndef SBP_FP64_TILE_ROWS
-#define SBP_FP64_TILE_ROWS 20
+#define SBP_FP64_TILE_ROWS 22
 #endif
 #ifndef SBP_FP64_WARPS
-#define SBP_FP64_WARPS 10
+#define SBP_FP64_WARPS 22
 #endif
 
 // Tile height of the single-instance kernel: the variable-coefficient FP32
@@ -137,8 +144,11 @@ template <typename T, int KIND> constexpr int wave_ty() {
   return sizeof(T) == 8 ? (KIND == WK_HOM ? SBP_FP64_TILE_ROWS : 16) : (KIND == WK_VAR ? 24 : SBP_FP32_TILE_ROWS);
 }
 // Shared-memory ring depth (tiles in flight + the one being computed).
+#ifndef SBP_FP64_RING
+#define SBP_FP64_RING 2
+#endif
 template <typename T, int KIND> constexpr int wave_ring() {
-  return (sizeof(T) == 4 && KIND != WK_VAR) ? SBP_FP32_RING : 2;
+  return (sizeof(T) == 4 && KIND != WK_VAR) ? SBP_FP32_RING : (sizeof(T) == 8 && KIND == WK_HOM ? SBP_FP64_RING : 2);
 }
 // Consumer warps of the single-instance kernel. The variable-coefficient and
 // manufactured-solution FP64 kernels need up to 166 registers a thread, which
@@ -180,6 +190,9 @@ struct WaveTile {
   static constexpr bool FIX = FIX_;  // fixed-point FP64 stage: the p/u/v boxes become int64 in place
   // u^n as a point box: the stages that read it, and the fixed-point first stage, whose
   // stencil boxes no longer hold the doubles of u^n once converted
+  // (Reading u^n and acc with streaming loads instead of point boxes, to free shared
+  // memory for taller tiles, measured slower: 22 rows 4.23e10 against 4.56e10 point-stage
+  // updates/s at 4096^2, 31 rows with 31 warps 4.55e10.)
   static constexpr bool LOAD_UN = (STAGE == ST_MID) || (STAGE == ST_LAST && COMP) || (FIX_ && STAGE == ST_FIRST);
   static constexpr bool LOAD_ACC = (STAGE == ST_MID) || (STAGE == ST_LAST);
   static constexpr bool LOAD_COMP = (STAGE == ST_LAST && COMP);
@@ -203,6 +216,7 @@ struct WaveTile {
   static constexpr int NST = NST_;                            // ring depth
   static constexpr int OFF_BAR = NST * STAGE_BYTES;           // full[NST], empty[NST]
   static constexpr int OFF_DBAR = OFF_BAR + 128;              // deferred-pass barriers[NST]
+  // + 192: the tile index of each stage (int[NST]; -1 marks the end)
   // fixed-point stages: exponent-maximum and conversion barriers[NST] each, then
   // the maxima of the p and u/v boxes per stage (int[NST][2])
   static constexpr int OFF_FX = OFF_BAR + 256;
@@ -633,20 +647,34 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
   }
   __syncthreads();
 
+  int* tslot = reinterpret_cast<int*>(smem + Tile::OFF_BAR + 192);
+  const bool dyn = prm.sched != nullptr && !is_rkf_stage(STAGE);
+
   if (warp == WARPS) {
-    // ---------------- producer: TMA loads of tile k into stage k % NST
+    // ---------------- producer: TMA loads of the CTA's k-th tile into stage k % NST
     if (lane == 0) {
       prefetch_tensormap(&mapP);
       int k = 0;
-      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
+      int tile = dyn ? atomicAdd(prm.sched, 1) : (int)blockIdx.x;
+      for (;; k++) {
         const int b = k % NST;
         if (k >= NST && !mbar_wait_bounded(&empty[b], ((k / NST) - 1) & 1, prm.wait_ns)) {
           atomicOr(prm.err, ERR_TMA_TIMEOUT);
           break;
         }
-        if (tile + 1 == prm.test_drop_tile) continue;  // no load: the consumers' wait runs out
+        if (tile >= ntiles) {  // the end marker: a phase completed without bytes
+          tslot[b] = -1;
+          mbar_arrive(&full[b]);
+          k++;
+          break;
+        }
+        tslot[b] = tile;
+        const int cur = tile;
+        // the next index is fetched now: the atomic's latency overlaps this tile's loads
+        tile = dyn ? atomicAdd(prm.sched, 1) : tile + (int)gridDim.x;
+        if (cur + 1 == prm.test_drop_tile) continue;  // no load: the consumers' wait runs out
         unsigned char* st = smem + b * Tile::STAGE_BYTES;
-        const int i0 = (tile % ntx) * kWaveTX, j0 = (tile / ntx) * TY;
+        const int i0 = (cur % ntx) * kWaveTX, j0 = (cur / ntx) * TY;
         mbar_arrive_expect_tx(&full[b], Tile::TX_BYTES);
         tma_load_3d(st, &mapP, i0 - HX, j0 - HY, 2, &full[b]);
         tma_load_3d(st + Tile::OFF_U, &mapU, i0 - HX, j0, 0, &full[b]);
@@ -659,6 +687,13 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
       // the CTA must not exit with copies in flight: wait for the last NST stages
       for (int kk = (k >= NST ? k - NST : 0); kk < k; kk++)
         mbar_wait_bounded(&full[kk % NST], (kk / NST) & 1, prm.wait_ns);
+      if (dyn) {  // every CTA has stopped taking tiles when the last one gets here
+        __threadfence();
+        if (atomicAdd(prm.sched + 1, 1) == (int)gridDim.x - 1) {
+          atomicExch(prm.sched, 0);
+          atomicExch(prm.sched + 1, 0);
+        }
+      }
     }
     return;
   }
@@ -666,13 +701,14 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
   // ---------------- consumers: warps 0 .. WARPS-1
   double errsq = 0.0;  // ST_RKF6: this thread's share of the weighted error sum
   uint32_t dphase = 0;  // parity of each stage's next deferred-pass barrier phase
-  int k = 0;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
+  for (int k = 0;; k++) {
     const int b = k % NST;
     if (!mbar_wait_bounded(&full[b], (k / NST) & 1, prm.wait_ns)) {
       if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
       break;
     }
+    const int tile = tslot[b];
+    if (tile < 0) break;
     const int i0 = (tile % ntx) * kWaveTX, j0 = (tile / ntx) * TY;
     if constexpr (Tile::FIX) {
       int emax[2];
