@@ -128,14 +128,16 @@ template <typename T> constexpr int default_wave_ty() { return sizeof(T) == 8 ? 
 // Pipeline shape of the constant-coefficient FP64 kernel (tile rows, consumer
 // warps); the build may override them to compare shapes. Measured with the
 // fixed-point stencils at 4096^2, order 4 (point-stage updates/s), with the dynamic
-// tile queue: (12, 12) 3.76e10, (16, 16) 4.20e10, (20, 10) 4.05e10, (18, 18) 4.37e10,
-// (20, 20) 4.43e10, (22, 22) 4.56e10; a third ring stage: (12, 12) 3.74e10, (8, 8)
-// 3.09e10. More warps hide more of the integer pipeline's latency.
+// tile queue: compute warps converting their own tiles (12, 12) 3.76e10, (16, 16)
+// 4.20e10, (20, 20) 4.43e10, (22, 22) 4.56e10; a third ring stage (12, 12) 3.74e10;
+// with converter warps (SBP_FP64_CONV) overlapping the conversion of the next tile:
+// (22, 22) 5.11e10 (4 converters) / 5.18e10 (6), and, with the shared memory of a
+// third ring stage, (12, 12) 5.39e10 (4), (14, 14) 5.63e10 (4) / 5.67e10 (6).
 #ifndef SBP_FP64_TILE_ROWS
-#define SBP_FP64_TILE_ROWS 22
+#define SBP_FP64_TILE_ROWS 14
 #endif
 #ifndef SBP_FP64_WARPS
-#define SBP_FP64_WARPS 22
+#define SBP_FP64_WARPS 14
 #endif
 
 // Tile height of the single-instance kernel: the variable-coefficient FP32
@@ -145,7 +147,13 @@ template <typename T, int KIND> constexpr int wave_ty() {
 }
 // Shared-memory ring depth (tiles in flight + the one being computed).
 #ifndef SBP_FP64_RING
-#define SBP_FP64_RING 2
+#define SBP_FP64_RING 3
+#endif
+// Converter warps of the fixed-point FP64 stages: they convert tile k+1 to int64
+// while the compute warps work on tile k (0: the compute warps convert each tile
+// themselves, between two barriers).
+#ifndef SBP_FP64_CONV
+#define SBP_FP64_CONV 6
 #endif
 template <typename T, int KIND> constexpr int wave_ring() {
   return (sizeof(T) == 4 && KIND != WK_VAR) ? SBP_FP32_RING : (sizeof(T) == 8 && KIND == WK_HOM ? SBP_FP64_RING : 2);
@@ -175,10 +183,11 @@ template <typename T, int KIND> constexpr int wave_warps() {
 }
 
 template <typename T, int ORD, int STAGE, int TY_ = default_wave_ty<T>(), int PRM_BYTES = 0, bool COEF = false,
-          int NST_ = 2, int WARPS_ = kWaveConsumerWarps, bool FIX_ = false>
+          int NST_ = 2, int WARPS_ = kWaveConsumerWarps, bool FIX_ = false, int CONV_ = 0>
 struct WaveTile {
-  static constexpr int WARPS = WARPS_;                        // consumer warps
-  static constexpr int THREADS = 32 * (WARPS_ + 1);           // + the producer warp
+  static constexpr int WARPS = WARPS_;                        // consumer (compute) warps
+  static constexpr int CONV = CONV_;                          // fixed-point stages: converter warps
+  static constexpr int THREADS = 32 * (WARPS_ + CONV_ + 1);   // + the producer warp
   static constexpr bool COMP = IsCompensated<T>::value;
   static constexpr int TY = TY_;                              // tile height
   static constexpr int R = (OpShape<ORD>::W - 1) / 2;
@@ -217,14 +226,17 @@ struct WaveTile {
   static constexpr int OFF_BAR = NST * STAGE_BYTES;           // full[NST], empty[NST]
   static constexpr int OFF_DBAR = OFF_BAR + 128;              // deferred-pass barriers[NST]
   // + 192: the tile index of each stage (int[NST]; -1 marks the end)
-  // fixed-point stages: exponent-maximum and conversion barriers[NST] each, then
-  // the maxima of the p and u/v boxes per stage (int[NST][2])
+  // Fixed-point stages, at OFF_FX: barriers[8] "exponent maxima known" (+0) and
+  // "boxes converted" (+64), then per stage the p and u/v exponent maxima: one pair
+  // per converter warp (int[8][8][2], +128) when converter warps convert, or one
+  // shared pair (int[8][2]) when the compute warps do.
   static constexpr int OFF_FX = OFF_BAR + 256;
-  static constexpr int SMEM = OFF_BAR + 256 + (FIX_ ? 192 : 0);
+  static constexpr int SMEM = OFF_BAR + 256 + (FIX_ ? 640 : 0);
   static constexpr uint32_t TX_BYTES = BYTES_P + BYTES_U + BYTES_V + (LOAD_UN ? BYTES_PT : 0) +
                                        (LOAD_ACC ? BYTES_PT : 0) + (LOAD_COMP ? BYTES_PT : 0) +
                                        (LOAD_COEF ? BYTES_K : 0) + PRM_BYTES;
   static_assert(TY % WARPS == 0, "tile rows must split evenly over the consumer warps");
+  static_assert(CONV <= 8, "converter warps");
   static_assert(NST >= 2 && NST <= 8, "ring depth");
   static_assert(SMEM <= 227 * 1024, "wave tile pipeline exceeds shared memory");
 };
@@ -596,7 +608,63 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
 // The Tile type of the single-instance kernel for (T, order, kind, stage).
 template <typename T, int ORD, int KIND, int STAGE>
 using WaveStageTile = WaveTile<T, ORD, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR && SBP_VAR_COEF != 0,
-                               wave_ring<T, KIND>(), wave_warps<T, KIND>(), wave_fixed<T, KIND, STAGE>()>;
+                               wave_ring<T, KIND>(), wave_warps<T, KIND>(), wave_fixed<T, KIND, STAGE>(),
+                               wave_fixed<T, KIND, STAGE>() ? SBP_FP64_CONV : 0>;
+
+// The producer (one lane): takes the CTA's tiles, from the dynamic queue or with a
+// fixed stride, writes each tile's index into its ring stage and issues the stage's
+// TMA loads; a stage holding -1, completed without bytes, marks the end. Waits for
+// every copy it issued before it returns, then counts the CTA done in the queue.
+template <typename Tile, typename T>
+__device__ __forceinline__ void wave_produce(const CUtensorMap& mapP, const CUtensorMap& mapU, const CUtensorMap& mapV,
+                                             const CUtensorMap& mapN, const CUtensorMap& mapA, const CUtensorMap& mapC,
+                                             const CUtensorMap& mapK, const WaveParams<T>& prm, unsigned char* smem,
+                                             uint64_t* full, uint64_t* empty, int* tslot, bool dyn) {
+  constexpr int TY = Tile::TY, HX = Tile::HX, HY = Tile::HY, NST = Tile::NST;
+  const int ntx = (prm.nx + kWaveTX - 1) / kWaveTX;
+  const int ntiles = ntx * ((prm.ny + TY - 1) / TY);
+  prefetch_tensormap(&mapP);
+  int k = 0;
+  int tile = dyn ? atomicAdd(prm.sched, 1) : (int)blockIdx.x;
+  for (;; k++) {
+    const int b = k % NST;
+    if (k >= NST && !mbar_wait_bounded(&empty[b], ((k / NST) - 1) & 1, prm.wait_ns)) {
+      atomicOr(prm.err, ERR_TMA_TIMEOUT);
+      break;
+    }
+    if (tile >= ntiles) {  // the end marker: a phase completed without bytes
+      tslot[b] = -1;
+      mbar_arrive(&full[b]);
+      k++;
+      break;
+    }
+    tslot[b] = tile;
+    const int cur = tile;
+    // the next index is fetched now: the atomic's latency overlaps this tile's loads
+    tile = dyn ? atomicAdd(prm.sched, 1) : tile + (int)gridDim.x;
+    if (cur + 1 == prm.test_drop_tile) continue;  // no load: the consumers' wait runs out
+    unsigned char* st = smem + b * Tile::STAGE_BYTES;
+    const int i0 = (cur % ntx) * kWaveTX, j0 = (cur / ntx) * TY;
+    mbar_arrive_expect_tx(&full[b], Tile::TX_BYTES);
+    tma_load_3d(st, &mapP, i0 - HX, j0 - HY, 2, &full[b]);
+    tma_load_3d(st + Tile::OFF_U, &mapU, i0 - HX, j0, 0, &full[b]);
+    tma_load_3d(st + Tile::OFF_V, &mapV, i0, j0 - HY, 1, &full[b]);
+    if (Tile::LOAD_UN) tma_load_3d(st + Tile::OFF_N, &mapN, i0, j0, 0, &full[b]);
+    if (Tile::LOAD_ACC) tma_load_3d(st + Tile::OFF_A, &mapA, i0, j0, 0, &full[b]);
+    if (Tile::LOAD_COMP) tma_load_3d(st + Tile::OFF_C, &mapC, i0, j0, 0, &full[b]);
+    if (Tile::LOAD_COEF) tma_load_3d(st + Tile::OFF_K, &mapK, i0, j0, 0, &full[b]);
+  }
+  // the CTA must not exit with copies in flight: wait for the last NST stages
+  for (int kk = (k >= NST ? k - NST : 0); kk < k; kk++)
+    mbar_wait_bounded(&full[kk % NST], (kk / NST) & 1, prm.wait_ns);
+  if (dyn) {  // every CTA has stopped taking tiles when the last one gets here
+    __threadfence();
+    if (atomicAdd(prm.sched + 1, 1) == (int)gridDim.x - 1) {
+      atomicExch(prm.sched, 0);
+      atomicExch(prm.sched + 1, 0);
+    }
+  }
+}
 
 }  // namespace sbp
 
@@ -651,50 +719,7 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
   const bool dyn = prm.sched != nullptr && !is_rkf_stage(STAGE);
 
   if (warp == WARPS) {
-    // ---------------- producer: TMA loads of the CTA's k-th tile into stage k % NST
-    if (lane == 0) {
-      prefetch_tensormap(&mapP);
-      int k = 0;
-      int tile = dyn ? atomicAdd(prm.sched, 1) : (int)blockIdx.x;
-      for (;; k++) {
-        const int b = k % NST;
-        if (k >= NST && !mbar_wait_bounded(&empty[b], ((k / NST) - 1) & 1, prm.wait_ns)) {
-          atomicOr(prm.err, ERR_TMA_TIMEOUT);
-          break;
-        }
-        if (tile >= ntiles) {  // the end marker: a phase completed without bytes
-          tslot[b] = -1;
-          mbar_arrive(&full[b]);
-          k++;
-          break;
-        }
-        tslot[b] = tile;
-        const int cur = tile;
-        // the next index is fetched now: the atomic's latency overlaps this tile's loads
-        tile = dyn ? atomicAdd(prm.sched, 1) : tile + (int)gridDim.x;
-        if (cur + 1 == prm.test_drop_tile) continue;  // no load: the consumers' wait runs out
-        unsigned char* st = smem + b * Tile::STAGE_BYTES;
-        const int i0 = (cur % ntx) * kWaveTX, j0 = (cur / ntx) * TY;
-        mbar_arrive_expect_tx(&full[b], Tile::TX_BYTES);
-        tma_load_3d(st, &mapP, i0 - HX, j0 - HY, 2, &full[b]);
-        tma_load_3d(st + Tile::OFF_U, &mapU, i0 - HX, j0, 0, &full[b]);
-        tma_load_3d(st + Tile::OFF_V, &mapV, i0, j0 - HY, 1, &full[b]);
-        if (Tile::LOAD_UN) tma_load_3d(st + Tile::OFF_N, &mapN, i0, j0, 0, &full[b]);
-        if (Tile::LOAD_ACC) tma_load_3d(st + Tile::OFF_A, &mapA, i0, j0, 0, &full[b]);
-        if (Tile::LOAD_COMP) tma_load_3d(st + Tile::OFF_C, &mapC, i0, j0, 0, &full[b]);
-        if (Tile::LOAD_COEF) tma_load_3d(st + Tile::OFF_K, &mapK, i0, j0, 0, &full[b]);
-      }
-      // the CTA must not exit with copies in flight: wait for the last NST stages
-      for (int kk = (k >= NST ? k - NST : 0); kk < k; kk++)
-        mbar_wait_bounded(&full[kk % NST], (kk / NST) & 1, prm.wait_ns);
-      if (dyn) {  // every CTA has stopped taking tiles when the last one gets here
-        __threadfence();
-        if (atomicAdd(prm.sched + 1, 1) == (int)gridDim.x - 1) {
-          atomicExch(prm.sched, 0);
-          atomicExch(prm.sched + 1, 0);
-        }
-      }
-    }
+    if (lane == 0) wave_produce<Tile>(mapP, mapU, mapV, mapN, mapA, mapC, mapK, prm, smem, full, empty, tslot, dyn);
     return;
   }
 

@@ -292,4 +292,174 @@ __device__ __forceinline__ void wave_tile_fixed(const WaveParams<double>& prm, c
   }
 }
 
+// Converter warps: the p, u and v boxes of one ring stage to int64 in place.
+// t is the thread's index among the converter threads. The exponent maxima go
+// through one barrier among the converters (fxa, bounded wait): each converter
+// warp writes its own p and u/v maxima to wmax[warp][0..1], every converter then
+// takes the maximum over them, and so does every compute warp later (fx_tile_emax),
+// so nothing has to be reset between tiles. Returns false if the wait ran out.
+template <typename Tile>
+__device__ __forceinline__ bool fx_convert_stage(unsigned char* st, uint64_t* fxa, int* wmax, uint32_t parity,
+                                                 unsigned long long wait_ns, int t);
+
+// The p and u/v exponent maxima of a converted stage from its converter warps'
+// pairs, with the tile guard applied: a box whose maximum is below 64 (values
+// under 2^-959) converts to zeros, and one at 2031 or more (values from 2^1008,
+// Inf, NaN) marks the tile bad.
+template <int CONV>
+__device__ __forceinline__ void fx_tile_emax(const int* wmax, int& ep, int& euv, bool& bad) {
+  ep = 0;
+  euv = 0;
+#pragma unroll
+  for (int c = 0; c < CONV; c++) {
+    ep = max(ep, wmax[2 * c]);
+    euv = max(euv, wmax[2 * c + 1]);
+  }
+  bad = ep >= 2031 || euv >= 2031;
+  if (ep < 64) ep = 2111;  // every value converts to 0
+  if (euv < 64) euv = 2111;
+}
+
+template <typename Tile>
+__device__ __forceinline__ bool fx_convert_stage(unsigned char* st, uint64_t* fxa, int* wmax, uint32_t parity,
+                                                 unsigned long long wait_ns, int t) {
+  constexpr int NT = 32 * Tile::CONV;
+  constexpr int NP = Tile::PH * Tile::PW, NU = Tile::TY * Tile::PW, NV = Tile::PH * kWaveTX;
+  uint2* wP = reinterpret_cast<uint2*>(st);
+  uint2* wU = reinterpret_cast<uint2*>(st + Tile::OFF_U);
+  uint2* wV = reinterpret_cast<uint2*>(st + Tile::OFF_V);
+  const int lane = t & 31, cw = t >> 5;
+  unsigned mp = 0, muv = 0;
+  for (int e = t; e < NP; e += NT) mp = max(mp, wP[e].y & 0x7FF00000u);
+  for (int e = t; e < NU; e += NT) muv = max(muv, wU[e].y & 0x7FF00000u);
+  for (int e = t; e < NV; e += NT) muv = max(muv, wV[e].y & 0x7FF00000u);
+  mp = __reduce_max_sync(0xffffffffu, mp);
+  muv = __reduce_max_sync(0xffffffffu, muv);
+  if (lane == 0) {
+    wmax[2 * cw] = (int)(mp >> 20);
+    wmax[2 * cw + 1] = (int)(muv >> 20);
+  }
+  __syncwarp();
+  if (lane == 0) mbar_arrive(fxa);
+  if (!mbar_wait_bounded(fxa, parity, wait_ns)) return false;
+  int ep, euv;
+  bool bad;
+  fx_tile_emax<Tile::CONV>(wmax, ep, euv, bad);
+  (void)bad;
+  long long* iP = reinterpret_cast<long long*>(wP);
+  long long* iU = reinterpret_cast<long long*>(wU);
+  long long* iV = reinterpret_cast<long long*>(wV);
+#pragma unroll 4
+  for (int e = t; e < NP; e += NT) {
+    const uint2 w = wP[e];
+    iP[e] = fx_from(w.x, w.y, ep);
+  }
+#pragma unroll 4
+  for (int e = t; e < NU; e += NT) {
+    const uint2 w = wU[e];
+    iU[e] = fx_from(w.x, w.y, euv);
+  }
+#pragma unroll 4
+  for (int e = t; e < NV; e += NT) {
+    const uint2 w = wV[e];
+    iV[e] = fx_from(w.x, w.y, euv);
+  }
+  // the converted boxes were written through the generic proxy; order those writes
+  // before the TMA (async proxy) refills the stage
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  return true;
+}
+
+// A fixed-point FP64 stage with warp roles: WARPS compute warps, CONV converter
+// warps and one producer warp. Per ring stage: the producer's TMA loads complete
+// `full` (1 arrival + bytes), the converters convert the stage's boxes and arrive on
+// `conv` (CONV arrivals), the compute warps evaluate the tile and arrive on
+// `empty` (WARPS arrivals), which lets the producer refill the stage. Conversion
+// of the next tile thus overlaps the computation of the current one, and the
+// compute warps meet no barrier but the deferred x-face pass. Every wait is
+// bounded (prm.wait_ns); a wait that runs out sets the error word and the warp
+// stops, so the others' waits run out in turn.
+template <int ORD, int STAGE>
+__global__ void __launch_bounds__(WaveStageTile<double, ORD, WK_HOM, STAGE>::THREADS, 1)
+    wave_fixed_kernel(const __grid_constant__ CUtensorMap mapP, const __grid_constant__ CUtensorMap mapU,
+                      const __grid_constant__ CUtensorMap mapV, const __grid_constant__ CUtensorMap mapN,
+                      const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapC,
+                      const __grid_constant__ CUtensorMap mapK, const __grid_constant__ WaveParams<double> prm) {
+  using Tile = WaveStageTile<double, ORD, WK_HOM, STAGE>;
+  constexpr int TY = Tile::TY, NST = Tile::NST, WARPS = Tile::WARPS, CONV = Tile::CONV;
+  static_assert(CONV >= 1, "the converter-warp kernel needs converter warps");
+  extern __shared__ __align__(128) unsigned char smem[];
+  if (prm.fx_sig[0] == 0.0 || prm.fx_sig[1] == 0.0) {  // the host did not set the fixed-point scales
+    if (threadIdx.x == 0) atomicOr(prm.err, ERR_BAD_LAUNCH);
+    return;
+  }
+  if (prm.skip && *prm.skip) return;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
+  uint64_t* empty = full + NST;
+  uint64_t* dbar = reinterpret_cast<uint64_t*>(smem + Tile::OFF_DBAR);
+  int* tslot = reinterpret_cast<int*>(smem + Tile::OFF_BAR + 192);
+  uint64_t* fxa = reinterpret_cast<uint64_t*>(smem + Tile::OFF_FX);  // [8]: exponent maxima known
+  uint64_t* conv = fxa + 8;                                          // [8]: stage converted
+  int* wmax = reinterpret_cast<int*>(smem + Tile::OFF_FX + 128);     // [8][8][2]
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NST; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], WARPS);
+      mbar_init(&dbar[s], WARPS);
+      mbar_init(&fxa[s], CONV);
+      mbar_init(&conv[s], CONV);
+    }
+    fence_barrier_init();
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntx = (prm.nx + kWaveTX - 1) / kWaveTX;
+
+  if (warp == WARPS + CONV) {
+    if (lane == 0)
+      wave_produce<Tile>(mapP, mapU, mapV, mapN, mapA, mapC, mapK, prm, smem, full, empty, tslot, prm.sched != nullptr);
+    return;
+  }
+  if (warp >= WARPS) {
+    // ---------------- converters
+    const int t = threadIdx.x - 32 * WARPS;
+    for (int k = 0;; k++) {
+      const int b = k % NST;
+      if (!mbar_wait_bounded(&full[b], (k / NST) & 1, prm.wait_ns)) {
+        if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
+        break;
+      }
+      const int tile = tslot[b];
+      if (tile >= 0 && !fx_convert_stage<Tile>(smem + b * Tile::STAGE_BYTES, &fxa[b], wmax + 16 * b, (k / NST) & 1,
+                                                prm.wait_ns, t)) {
+        if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
+        break;
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&conv[b]);  // converted, or the end marker passed on
+      if (tile < 0) break;
+    }
+    return;
+  }
+  // ---------------- compute warps
+  uint32_t dphase = 0;  // parity of each stage's next deferred-pass barrier phase
+  for (int k = 0;; k++) {
+    const int b = k % NST;
+    if (!mbar_wait_bounded(&conv[b], (k / NST) & 1, prm.wait_ns)) {
+      if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
+      break;
+    }
+    const int tile = tslot[b];
+    if (tile < 0) break;
+    const int i0 = (tile % ntx) * kWaveTX, j0 = (tile / ntx) * TY;
+    int ep, euv;
+    bool bad;
+    fx_tile_emax<CONV>(wmax + 16 * b, ep, euv, bad);
+    wave_tile_fixed<ORD, STAGE, Tile>(prm, prm.in, prm.wout, smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane, ep,
+                                      euv, bad, &dbar[b], &dphase, b, k);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[b]);
+  }
+}
+
 }  // namespace sbp

@@ -16,10 +16,22 @@ namespace sbp {
 
 namespace {
 
+// The fixed-point FP64 stages with converter warps run their own kernel
+// (wave_fixed_kernel); every other stage runs wave_stage_kernel.
+template <typename T, int KIND, int STAGE>
+constexpr bool uses_fixed_kernel() {
+  return WaveStageTile<T, SBP_ORDER, KIND, STAGE>::FIX && WaveStageTile<T, SBP_ORDER, KIND, STAGE>::CONV > 0;
+}
+
 template <typename T, int KIND, int STAGE>
 cudaError_t configure_one() {
-  return cudaFuncSetAttribute(wave_stage_kernel<T, SBP_ORDER, KIND, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              WaveStageTile<T, SBP_ORDER, KIND, STAGE>::SMEM);
+  if constexpr (uses_fixed_kernel<T, KIND, STAGE>())
+    return cudaFuncSetAttribute(wave_fixed_kernel<SBP_ORDER, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                WaveStageTile<T, SBP_ORDER, KIND, STAGE>::SMEM);
+  else
+    return cudaFuncSetAttribute(wave_stage_kernel<T, SBP_ORDER, KIND, STAGE>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                WaveStageTile<T, SBP_ORDER, KIND, STAGE>::SMEM);
 }
 
 template <typename T, int KIND>
@@ -43,8 +55,11 @@ cudaError_t configure_kind() {
 template <typename T, int KIND, int STAGE>
 cudaError_t launch_one(const WaveMaps& m, const WaveParams<T>& prm, dim3 grid, cudaStream_t s) {
   using Tile = WaveStageTile<T, SBP_ORDER, KIND, STAGE>;
-  wave_stage_kernel<T, SBP_ORDER, KIND, STAGE>
-      <<<grid, Tile::THREADS, Tile::SMEM, s>>>(m.p, m.u, m.v, m.n, m.a, m.c, m.k, prm);
+  if constexpr (uses_fixed_kernel<T, KIND, STAGE>())
+    wave_fixed_kernel<SBP_ORDER, STAGE><<<grid, Tile::THREADS, Tile::SMEM, s>>>(m.p, m.u, m.v, m.n, m.a, m.c, m.k, prm);
+  else
+    wave_stage_kernel<T, SBP_ORDER, KIND, STAGE>
+        <<<grid, Tile::THREADS, Tile::SMEM, s>>>(m.p, m.u, m.v, m.n, m.a, m.c, m.k, prm);
   return cudaGetLastError();
 }
 
