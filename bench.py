@@ -143,9 +143,15 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def profile_summary(order: int, precision: str) -> str:
+    """The committed ncu summary of the stage kernel this precision runs."""
+    kernel = "wave_fixed" if precision == "fp64" else "wave_stage"
+    return os.path.join("profiles", f"{kernel}_{precision}_o{order}_4096.md")
+
+
 def profiled_traffic(order: int, precision: str):
     """DRAM bytes per point of one middle-stage launch, from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", f"wave_stage_{precision}_o{order}_4096.md")
+    path = os.path.join(ROOT, profile_summary(order, precision))
     try:
         with open(path) as f:
             for line in f:
@@ -759,15 +765,22 @@ def main():
     mid_alg = (5 * 3 * es) * n * n  # algorithmic bytes of one middle-stage launch
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": (traffic_pp * n * n if traffic_pp else None),
-                "traffic_note": "DRAM bytes of one middle-stage (stage 2/3) launch from the committed ncu capture "
-                                "(2560^2, scaled by points); its algorithmic bytes: %d" % mid_alg,
+                "traffic_note": ("imported, not measured by this run: DRAM bytes of one middle-stage (stage 2/3) "
+                                 "launch from the ncu capture summarised in %s (2560^2, scaled by points); "
+                                 "that launch's algorithmic bytes: %d" % (profile_summary(order, args.precision),
+                                                                          mid_alg)),
                 "peak_source": peak_src,
                 "algorithmic_bytes_per_launch": bytes_per_launch,
-                "kernel": "wave_stage_kernel (fused RHS + SAT + RK4 stage)", "avg_launch_ms": kernel_ms}
+                "kernel": ("wave_fixed_kernel (fused RHS + SAT + RK4 stage, fixed-point stencils)"
+                           if args.precision == "fp64" else "wave_stage_kernel (fused RHS + SAT + RK4 stage)"),
+                "avg_launch_ms": kernel_ms}
     if args.precision == "fp64":
         try:
             rate = sbpgpu.probe_dfma_rate(local)
-            dp_ops = {2: 13.25, 4: 21.25, 6: 29.25}[order]
+            # The fixed-point stages leave only the RK4 update on the FP64 pipe: 2 FMAs per
+            # component in stages 1-3, 1 in stage 4 (5.25 per point-stage); the stencils run as
+            # int64 on the INT pipe. (The FP64 tap form needed 13.25 / 21.25 / 29.25.)
+            dp_ops = 5.25
             roofline["fp64_alu"] = {"dfma_per_s": rate, "dp_instr_per_point_stage": dp_ops,
                                     "bound_point_stage_per_s": rate / dp_ops,
                                     "frac_of_dp_bound": (units_per_step / (ms_per_step * 1e-3)) / (rate / dp_ops)}
