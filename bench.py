@@ -40,6 +40,10 @@ sys.path.insert(0, PKG)
 import fields  # noqa: E402  (seeded inputs: initial data and coefficient fields)
 
 METRIC = "RK4 point-updates/s"
+# The port's speed against the reference's own wave_hom RHS headers, both built with the
+# reference's -O3 -ffast-math, one thread, 1024^2, orders 2/4/6 (oracle/time_reference.py,
+# on the x86 host where the reference checkout exists; the GPU machine has none).
+REF_CODE_RATIO = "port / reference code = 1.01 / 0.94 / 0.91 (orders 2 / 4 / 6)"
 UNIT = "grid-point stage updates/s"
 
 
@@ -211,7 +215,8 @@ def run_reference(args, rank: int):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_of(args),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample,
+                         "port_vs_reference_code": REF_CODE_RATIO},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -811,7 +816,8 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         rates, kind, threads, sample = cpu_baseline(n, order, args.precision, args.bc, 10.0)
-        cpu = {"value": rates[0], "unit": UNIT, "cores": threads, "kind": kind, "sample": sample}
+        cpu = {"value": rates[0], "unit": UNIT, "cores": threads, "kind": kind, "sample": sample,
+               "port_vs_reference_code": REF_CODE_RATIO}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
