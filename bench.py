@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--bc", default="characteristic", choices=["characteristic", "free_surface"])
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the forms record (other orders and sizes, FP32, the batched form)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--study", default=None, choices=["precision", "batched", "learned", "rk45", "wave3d", "decomp"],
                     help="precision: variable rho, K (seeded Fourier fields) to --t-end in FP64 and in "
@@ -341,6 +343,115 @@ def batched_instances(count: int, seed: int = 2):
             y = np.linspace(-1, 1, ny) - y0
             states.append(np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / 0.1**2).ravel())
     return insts, states
+
+
+def _timed_steps(ctx, dt: float, steps: int) -> float:
+    """Seconds of `steps` resident RK4 steps, CUDA events on the context's stream."""
+    import torch
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    ctx.step_resident(0.0, dt, steps)
+    ev1.record(stream)
+    ctx.synchronize()
+    return ev0.elapsed_time(ev1) / 1e3
+
+
+def _relerr(a, b) -> float:
+    import numpy as np
+
+    return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+
+
+def measure_forms(peak: float, device: int = 0) -> dict:
+    """The bench's other forms, each bounded to seconds, for the JSON line's `forms` record:
+    FP64 at orders 2 and 6 (4096^2) and at 1024^2 (order 4); FP32 at 4096^2 with its error
+    against FP64 after the same steps; the 512-instance batch in FP64 and FP32 with the largest
+    relative error of 16 sampled instances against the plain FP64 path (single contexts).
+    Roofline fractions use the same algorithmic bytes as the headline: 16*c*s per point per
+    RK4 step (19*c*4 for compensated FP32)."""
+    import numpy as np
+    import torch
+
+    import sbpgpu
+
+    out = {}
+    bc = sbpgpu.BC_CHARACTERISTIC
+    for name, n, order, steps in (("fp64_4096_o2", 4096, 2, 200), ("fp64_4096_o6", 4096, 6, 200),
+                                  ("fp64_1024_o4", 1024, 4, 1000)):
+        dt = 0.2 * 2.0 / (n - 1)
+        with sbpgpu.Context(sbpgpu.WAVE_HOM_2D, order, n, n, bc=bc, device=device) as c:
+            c.set_state(initial_state(n))
+            c.step_resident(0.0, dt, 50)
+            c.synchronize()
+            sec = _timed_steps(c, dt, steps)
+        rate = n * n * 4 * steps / sec
+        out[name] = {"value": rate, "unit": UNIT, "rk4_steps": steps, "roofline_frac": rate * 96 / 1e9 / peak}
+    # FP32 against FP64 from the same state after the same steps
+    n, order, steps = 4096, 4, 500
+    dt = 0.2 * 2.0 / (n - 1)
+    v0 = initial_state(n)
+    res = {}
+    for prec in (sbpgpu.FP64, sbpgpu.FP32):
+        with sbpgpu.Context(sbpgpu.WAVE_HOM_2D, order, n, n, bc=bc, precision=prec, device=device) as c:
+            c.set_state(v0)
+            c.step_resident(0.0, dt, 3)  # graph capture, then restart from v0
+            c.synchronize()
+            c.set_state(v0)
+            sec = _timed_steps(c, dt, steps)
+            res[prec] = (sec, c.get_state())
+    rate = n * n * 4 * steps / res[sbpgpu.FP32][0]
+    d = res[sbpgpu.FP32][1] - res[sbpgpu.FP64][1]
+    out["fp32_4096_o4"] = {"value": rate, "unit": UNIT, "rk4_steps": steps,
+                           "roofline_frac": rate * 57 / 1e9 / peak,
+                           "fp64_seconds_same_steps": res[sbpgpu.FP64][0], "fp32_seconds": res[sbpgpu.FP32][0],
+                           "rel_max_err_vs_fp64": _relerr(res[sbpgpu.FP32][1], res[sbpgpu.FP64][1]),
+                           "rel_l2_err_vs_fp64": float(np.linalg.norm(d) / np.linalg.norm(res[sbpgpu.FP64][1]))}
+    # the batched form
+    insts, states = batched_instances(512)
+    rng = np.random.default_rng(7)
+    sizes = [d["nx"] * d["ny"] for d in insts]
+    sample = sorted(set([int(np.argmin(sizes)), int(np.argmax(sizes))] +
+                        [next(k for k, d in enumerate(insts) if d["order"] == o and d["problem"] == p)
+                         for o in (2, 4, 6) for p in (sbpgpu.WAVE_HOM_2D, sbpgpu.ADVECTION_2D)] +
+                        [int(k) for k in rng.choice(len(insts), 16, replace=False)]))[:16]
+    acc_steps = 100
+    plain = {}
+    for k in sample:
+        d = insts[k]
+        if d["problem"] == sbpgpu.WAVE_HOM_2D:
+            ones = np.ones(d["nx"] * d["ny"])
+            c = sbpgpu.Context(sbpgpu.WAVE_VAR_2D, d["order"], d["nx"], d["ny"], rho=ones, K=ones * d["c"] ** 2,
+                               bc=d["bc"], device=device)
+        else:
+            c = sbpgpu.Context(sbpgpu.ADVECTION_2D, d["order"], d["nx"], d["ny"], a=d["a"], b=d["b"], device=device)
+        with c:
+            plain[k] = c.rk4(states[k], 0.0, d["dt"], acc_steps)
+    for pname, prec, es, comp in (("batched_fp64", sbpgpu.FP64, 8, 16), ("batched_fp32", sbpgpu.FP32, 4, 19)):
+        with sbpgpu.Batch(insts, precision=prec, device=device) as b:
+            for k, v in enumerate(states):
+                b.set_state(k, v)
+            b.step_resident(acc_steps)
+            b.synchronize()
+            err = max(_relerr(b.get_state(k), plain[k]) for k in sample)
+            b.step_resident(100)  # warm
+            b.synchronize()
+            stream = torch.cuda.ExternalStream(b.stream)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            b.step_resident(200)
+            ev1.record(stream)
+            b.synchronize()
+            sec = ev0.elapsed_time(ev1) / 1e3
+            pts = b.points
+        comps = sum((3 if d["problem"] == sbpgpu.WAVE_HOM_2D else 1) * d["nx"] * d["ny"] for d in insts)
+        bytes_per_step = comp * es * comps  # per RK4 step, all instances
+        out[pname] = {"value": pts * 4 * 200 / sec, "unit": UNIT, "instances": len(insts), "points": pts,
+                      "rk4_steps": 200, "roofline_frac": bytes_per_step * 200 / sec / 1e9 / peak,
+                      "max_rel_err_vs_plain_fp64": err, "sampled_instances": len(sample),
+                      "error_after_rk4_steps": acc_steps}
+    return out
 
 
 def run_batched_study(args):
@@ -813,6 +924,10 @@ def main():
                "d2h_bytes_per_step": host.nbytes, "ms_per_step": el * 1e3,
                "call": "sbp_rk4(ctx, 0, dt, steps, host_aos, SBP_HOST)"}
 
+    forms = None
+    if rank == 0 and not args.no_forms and args.precision == "fp64":
+        forms = measure_forms(peak, local)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         rates, kind, threads, sample = cpu_baseline(n, order, args.precision, args.bc, 10.0)
@@ -825,7 +940,7 @@ def main():
                 "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
                 "data": "synthetic (Gaussian pressure pulse)", "config": config_of(args),
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clock_info,
-                "gpu_launches": launches}
+                "gpu_launches": launches, "forms": forms}
         print(json.dumps(line), flush=True)
     ctx.close()
     if dist:
