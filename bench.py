@@ -314,37 +314,6 @@ def run_precision_study(args):
     print(json.dumps(line2), flush=True)
 
 
-def batched_instances(count: int, seed: int = 2):
-    """N = round(exp(U[ln 64, ln 512])) per side, order from {2, 4, 6}, speed c ~ U[0.5, 2];
-    even members are waves (rho = 1, K = c^2, characteristic SAT), odd members advection
-    with |(a, b)| = c in a random direction; dt = 0.2 h / c; pulses centred in [-0.5, 0.5]^2."""
-    import numpy as np
-
-    import sbpgpu
-
-    rng = np.random.default_rng(seed)
-    insts, states = [], []
-    for k in range(count):
-        nx = int(round(np.exp(rng.uniform(np.log(64), np.log(512)))))
-        ny = int(round(np.exp(rng.uniform(np.log(64), np.log(512)))))
-        order = int(rng.choice([2, 4, 6]))
-        c = float(rng.uniform(0.5, 2.0))
-        x0, y0 = rng.uniform(-0.5, 0.5, 2)
-        h = min(2.0 / (nx - 1), 2.0 / (ny - 1))
-        if k % 2 == 0:
-            insts.append(dict(problem=sbpgpu.WAVE_HOM_2D, order=order, nx=nx, ny=ny, c=c, dt=0.2 * h / c,
-                              bc=sbpgpu.BC_CHARACTERISTIC))
-            states.append(fields.gaussian_pulse(nx, ny, x0, y0, 0.1, 1.0))
-        else:
-            ang = rng.uniform(0.0, 2 * np.pi)
-            insts.append(dict(problem=sbpgpu.ADVECTION_2D, order=order, nx=nx, ny=ny, a=c * np.cos(ang),
-                              b=c * np.sin(ang), dt=0.2 * h / c))
-            x = np.linspace(-1, 1, nx) - x0
-            y = np.linspace(-1, 1, ny) - y0
-            states.append(np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / 0.1**2).ravel())
-    return insts, states
-
-
 def _timed_steps(ctx, dt: float, steps: int) -> float:
     """Seconds of `steps` resident RK4 steps, CUDA events on the context's stream."""
     import torch
@@ -409,13 +378,8 @@ def measure_forms(peak: float, device: int = 0) -> dict:
                            "rel_max_err_vs_fp64": _relerr(res[sbpgpu.FP32][1], res[sbpgpu.FP64][1]),
                            "rel_l2_err_vs_fp64": float(np.linalg.norm(d) / np.linalg.norm(res[sbpgpu.FP64][1]))}
     # the batched form
-    insts, states = batched_instances(512)
-    rng = np.random.default_rng(7)
-    sizes = [d["nx"] * d["ny"] for d in insts]
-    sample = sorted(set([int(np.argmin(sizes)), int(np.argmax(sizes))] +
-                        [next(k for k, d in enumerate(insts) if d["order"] == o and d["problem"] == p)
-                         for o in (2, 4, 6) for p in (sbpgpu.WAVE_HOM_2D, sbpgpu.ADVECTION_2D)] +
-                        [int(k) for k in rng.choice(len(insts), 16, replace=False)]))[:16]
+    insts, states = fields.batched_instances(512)
+    sample = fields.batched_sample(insts, 16)
     acc_steps = 100
     plain = {}
     for k in sample:
@@ -462,7 +426,7 @@ def run_batched_study(args):
     import sbpgpu
 
     gpu_build.build()
-    insts, states = batched_instances(args.instances)
+    insts, states = fields.batched_instances(args.instances)
     cache = os.environ.get("SBP_TUNE_CACHE", os.path.join(PKG, "_build", "batch_tiles.json"))
     out = {"study": "batched", "instances": len(insts),
            "waves": sum(1 for d in insts if d["problem"] == sbpgpu.WAVE_HOM_2D),

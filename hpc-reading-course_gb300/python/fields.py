@@ -54,3 +54,53 @@ def standing_mode(nx: int, ny: int, t: float, n: int = 3, m: int = 4, xl=(-1.0, 
     out[..., 1] = -m * np.sin(n * np.pi * x) * np.cos(m * np.pi * y) * np.sin(np.pi * w * t) / w
     out[..., 2] = np.sin(np.pi * n * x) * np.sin(np.pi * m * y) * np.cos(np.pi * w * t)
     return out.ravel()
+
+
+def batched_instances(count: int, seed: int = 2):
+    """The batched workload: `count` independent instances (512 in the benchmark configuration).
+    N = round(exp(U[ln 64, ln 512])) per side, order from {2, 4, 6}, speed c ~ U[0.5, 2];
+    even members are waves (rho = 1, K = c^2, characteristic SAT), odd members advection
+    with |(a, b)| = c in a random direction; dt = 0.2 h / c; pulses centred in [-0.5, 0.5]^2."""
+    import sbpgpu
+
+    rng = np.random.default_rng(seed)
+    insts, states = [], []
+    for k in range(count):
+        nx = int(round(np.exp(rng.uniform(np.log(64), np.log(512)))))
+        ny = int(round(np.exp(rng.uniform(np.log(64), np.log(512)))))
+        order = int(rng.choice([2, 4, 6]))
+        c = float(rng.uniform(0.5, 2.0))
+        x0, y0 = rng.uniform(-0.5, 0.5, 2)
+        h = min(2.0 / (nx - 1), 2.0 / (ny - 1))
+        if k % 2 == 0:
+            insts.append(dict(problem=sbpgpu.WAVE_HOM_2D, order=order, nx=nx, ny=ny, c=c, dt=0.2 * h / c,
+                              bc=sbpgpu.BC_CHARACTERISTIC))
+            states.append(gaussian_pulse(nx, ny, x0, y0, 0.1, 1.0))
+        else:
+            ang = rng.uniform(0.0, 2 * np.pi)
+            insts.append(dict(problem=sbpgpu.ADVECTION_2D, order=order, nx=nx, ny=ny, a=c * np.cos(ang),
+                              b=c * np.sin(ang), dt=0.2 * h / c))
+            x = np.linspace(-1, 1, nx) - x0
+            y = np.linspace(-1, 1, ny) - y0
+            states.append(np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / 0.1**2).ravel())
+    return insts, states
+
+
+def batched_sample(insts, count: int = 16, seed: int = 7):
+    """Indices of `count` instances of a batch to check one by one: the smallest and the largest,
+    the first wave and the first advection instance of each order, the rest drawn from `seed`."""
+    import sbpgpu
+
+    sizes = [d["nx"] * d["ny"] for d in insts]
+    pick = [int(np.argmin(sizes)), int(np.argmax(sizes))]
+    for o in (2, 4, 6):
+        for p in (sbpgpu.WAVE_HOM_2D, sbpgpu.ADVECTION_2D):
+            k = next((k for k, d in enumerate(insts) if d["order"] == o and d["problem"] == p), None)
+            if k is not None:
+                pick.append(k)
+    rng = np.random.default_rng(seed)
+    for k in rng.permutation(len(insts)):
+        if len(set(pick)) >= count:
+            break
+        pick.append(int(k))
+    return sorted(set(pick))[:count]

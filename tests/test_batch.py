@@ -95,3 +95,40 @@ def test_batch_autotune_keeps_states_and_caches(sbp, tmp_path):
     for k, d in enumerate(insts):
         ref = _single(sbp, d, v0[k], 20, 0)
         assert np.max(np.abs(got[k] - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batched_configuration_sample_against_oracle(sbp, port, precision):
+    """The benchmark's batched configuration -- 512 uneven wave and advection instances
+    (fields.batched_instances) -- advanced 20 RK4 steps in one batch; 16 of its instances (the
+    smallest, the largest, a wave and an advection instance of each order, the rest drawn) against
+    the oracle: waves as the variable-coefficient problem with rho = 1, K = c^2 and the
+    characteristic SAT, advection with its (a, b). FP64 1e-12, FP32 1e-5 norm-wise relative."""
+    import oracle as O
+
+    insts, states = fields.batched_instances(512)
+    sample = fields.batched_sample(insts, 16)
+    assert len(sample) == 16
+    steps = 20
+    prec, tol = (sbp.FP64, 1e-12) if precision == "fp64" else (sbp.FP32, 1e-5)
+    with sbp.Batch(insts, precision=prec) as b:
+        for k, v in enumerate(states):
+            b.set_state(k, v)
+        b.step_resident(steps)
+        b.synchronize()
+        got = {k: b.get_state(k) for k in sample}
+    orders = set()
+    for k in sample:
+        d = insts[k]
+        orders.add(d["order"])
+        if d["problem"] == sbp.WAVE_HOM_2D:
+            ones = np.ones(d["nx"] * d["ny"])
+            pb = O.Problem(O.WAVE_VAR_2D, d["order"], d["nx"], d["ny"], rho=ones, K=ones * d["c"] ** 2,
+                           bc=O.BC_CHARACTERISTIC)
+        else:
+            pb = O.Problem(O.ADVECTION_2D, d["order"], d["nx"], d["ny"], a=d["a"], b=d["b"])
+        ref = port.rk4(pb, states[k], 0.0, d["dt"], steps)
+        err = np.max(np.abs(got[k] - ref)) / np.max(np.abs(ref))
+        assert err <= tol, (k, d, err)
+    assert orders == {2, 4, 6}
