@@ -23,8 +23,16 @@ template <typename T> struct LineParams {
   T* wout;
   T* kout;
   T* comp;
-  DirTaps<T> dx, dy;  // advection: -a*hix, -b*hiy scaled; reflection: +hix scaled
-  double sat[4];      // advection SAT factors 0.5*tau*hi*HI[0] for W, S, E, N
+  DirTaps<T> dx, dy;  // advection: -a*hix, -b*hiy scaled (+hix, +hiy with velocity fields); reflection: +hix
+  double sat[4];      // advection SAT factors 0.5*tau*hi*HI[0] for W, S, E, N (constant velocities)
+  // Advection with a velocity at every point (null: the constants folded into the taps):
+  // the velocity planes in T (pitched like the state) for the interior, FP64 copies
+  // (nx*ny, row-major) for the SAT, and hi*HI[0] per direction
+  const T* va;
+  const T* vb;
+  const double* va64;
+  const double* vb64;
+  double bw[2];
   int bc;             // 0: none, 1: the reference's boundary treatment
   int compensated;
   T c_acc, c_w;
@@ -82,6 +90,15 @@ __device__ __forceinline__ T adv2d_sat(const LineParams<T>& prm, int i, int j, T
   if (prm.bc && (i == 0 || j == 0 || i == prm.nx - 1 || j == prm.ny - 1)) {
     double kk = (double)k;
     const double u = (double)cen;
+    if (prm.va64) {  // tau from the velocity at the boundary point
+      const long long g = (long long)j * prm.nx + i;
+      const double a = prm.va64[g], b = prm.vb64[g];
+      if (i == 0) kk += 0.5 * (-0.5 * (a + fabs(a))) * prm.bw[0] * u;
+      if (j == 0) kk += 0.5 * (-0.5 * (b + fabs(b))) * prm.bw[1] * u;
+      if (i == prm.nx - 1) kk += 0.5 * (0.5 * (a - fabs(a))) * prm.bw[0] * u;
+      if (j == prm.ny - 1) kk += 0.5 * (0.5 * (b - fabs(b))) * prm.bw[1] * u;
+      return (T)kk;
+    }
     if (i == 0) kk += prm.sat[0] * u;
     if (j == 0) kk += prm.sat[1] * u;
     if (i == prm.nx - 1) kk += prm.sat[2] * u;
@@ -103,15 +120,28 @@ __device__ __forceinline__ void line_point(const LineParams<T>& prm, const T* __
   T cen[NC];
   if constexpr (KIND == LK_ADV1D) {
     k[0] = d1_line<T, ORD>(in, 1, nx, i, prm.dx);
+    if (prm.va) k[0] = -prm.va[q] * k[0];  // -a(i) D1 u
     cen[0] = in[q];
     if (prm.bc) {  // SAT_bc_l / SAT_bc_r (advection_rhs.h:94-119)
-      if (i == 0) k[0] = (T)((double)k[0] + prm.sat[0] * (double)cen[0]);
-      if (i == nx - 1) k[0] = (T)((double)k[0] + prm.sat[2] * (double)cen[0]);
+      if (prm.va64) {
+        if (i == 0 || i == nx - 1) {
+          const double a = prm.va64[i];
+          const double tau = i == 0 ? -0.5 * (a + fabs(a)) : 0.5 * (a - fabs(a));
+          k[0] = (T)((double)k[0] + 0.5 * tau * prm.bw[0] * (double)cen[0]);
+        }
+      } else {
+        if (i == 0) k[0] = (T)((double)k[0] + prm.sat[0] * (double)cen[0]);
+        if (i == nx - 1) k[0] = (T)((double)k[0] + prm.sat[2] * (double)cen[0]);
+      }
     }
   } else if constexpr (KIND == LK_ADV2D) {
     const T* row = in + (long long)j * pitch;
     const T* col = in + i;
-    k[0] = d1_line<T, ORD>(row, 1, nx, i, prm.dx) + d1_line<T, ORD>(col, pitch, ny, j, prm.dy);
+    if (prm.va) {  // -(a(i,j) D1x u + b(i,j) D1y u)
+      k[0] = -(prm.va[q] * d1_line<T, ORD>(row, 1, nx, i, prm.dx) + prm.vb[q] * d1_line<T, ORD>(col, pitch, ny, j, prm.dy));
+    } else {
+      k[0] = d1_line<T, ORD>(row, 1, nx, i, prm.dx) + d1_line<T, ORD>(col, pitch, ny, j, prm.dy);
+    }
     cen[0] = in[q];
     k[0] = adv2d_sat<T>(prm, i, j, k[0], cen[0]);
   } else {  // LK_REFL1D: dst(i,1) = D1 u, dst(i,0) = D1 v

@@ -67,6 +67,8 @@ struct sbp_ctx {
   double* partial = nullptr;  // reduction scratch, 2 * kReduceBlocks
   double* red = nullptr;      // reduction result, 4
   void *rinv = nullptr, *kmod = nullptr;     // WAVE_VAR: T planes
+  void *va = nullptr, *vb = nullptr;         // advection with velocity fields: T planes (pitched)
+  double *va64 = nullptr, *vb64 = nullptr;   // the same in FP64, nx*ny row-major (SAT)
   double *rho64 = nullptr, *k64 = nullptr;   // WAVE_VAR: nx*ny FP64
   int* err = nullptr;
   int* sched = nullptr;  // the wave stage kernels' dynamic tile queue (2 ints, zero between launches)
@@ -204,6 +206,15 @@ LineParams<T> line_params(sbp_ctx* ctx) {
   const double a = ctx->d.a, b = ctx->d.b;
   if (ctx->d.problem == SBP_REFLECTION_1D) {
     fill_taps<T>(p.dx, ctx->d.order, ctx->hix);
+  } else if (ctx->va) {  // velocity fields: the kernel forms -(a(x) D1x + b(x) D1y)
+    fill_taps<T>(p.dx, ctx->d.order, ctx->hix);
+    fill_taps<T>(p.dy, ctx->d.order, ctx->hiy);
+    p.va = (const T*)ctx->va;
+    p.vb = (const T*)ctx->vb;
+    p.va64 = ctx->va64;
+    p.vb64 = ctx->vb64;
+    p.bw[0] = ctx->hix * hi0;
+    p.bw[1] = ctx->hiy * hi0;
   } else {
     fill_taps<T>(p.dx, ctx->d.order, -a * ctx->hix);
     fill_taps<T>(p.dy, ctx->d.order, -b * ctx->hiy);
@@ -597,7 +608,8 @@ void release(sbp_ctx* ctx) {
   if (ctx->rk_unew) cudaFree(ctx->rk_unew);
   if (ctx->rk_ctrl) cudaFree(ctx->rk_ctrl);
   void* bufs[] = {ctx->un, ctx->acc, ctx->wa, ctx->wb, ctx->comp, ctx->io, ctx->partial, ctx->red,
-                  ctx->rinv, ctx->rho64, ctx->k64, ctx->err, ctx->sched};  // kmod lives inside the rinv allocation
+                  ctx->rinv, ctx->rho64, ctx->k64, ctx->err, ctx->sched, ctx->va, ctx->va64};
+  // kmod lives inside the rinv allocation, vb and vb64 inside those of va and va64
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -738,6 +750,45 @@ int sbp_create(const sbp_desc* desc, sbp_ctx** out) {
     e = cudaDeviceSynchronize();
     cudaFree(tmp);
     if (e != cudaSuccess) return cuda_fail("coefficient upload", e);
+  }
+  const bool adv = d.problem == SBP_ADVECTION_1D || d.problem == SBP_ADVECTION_2D;
+  if (!adv && (d.a_field || d.b_field)) {
+    g_create_error = "velocity fields are for the advection problems";
+    release(ctx);
+    delete ctx;
+    return SBP_ERR_INVALID;
+  }
+  if (adv && (d.a_field || (ctx->two_d && d.b_field))) {
+    // velocities at every point: FP64 copies for the SAT, planes of T for the interior
+    const size_t np = (size_t)ctx->npts;
+    double* host = new (std::nothrow) double[2 * np];
+    if (!host) return cuda_fail("host allocation", cudaErrorMemoryAllocation);
+    for (size_t q = 0; q < np; q++) {
+      host[q] = d.a_field ? d.a_field[q] : d.a;
+      host[np + q] = (ctx->two_d && d.b_field) ? d.b_field[q] : d.b;
+    }
+    const int nf = ctx->two_d ? 2 : 1;
+    if ((e = cudaMalloc((void**)&ctx->va64, nf * np * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&ctx->va, nf * ctx->plane * ctx->es)) != cudaSuccess) {
+      delete[] host;
+      return cuda_fail("cudaMalloc(velocity fields)", e);
+    }
+    cudaMemset(ctx->va, 0, nf * ctx->plane * ctx->es);
+    ctx->vb64 = ctx->va64 + (nf - 1) * np;  // 1D: vb is never read
+    ctx->vb = static_cast<unsigned char*>(ctx->va) + (nf - 1) * ctx->plane * ctx->es;
+    e = cudaMemcpy(ctx->va64, host, np * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && nf == 2)
+      e = cudaMemcpy(ctx->vb64, host + np, np * sizeof(double), cudaMemcpyHostToDevice);
+    delete[] host;
+    if (e != cudaSuccess) return cuda_fail("velocity upload", e);
+    for (int f = 0; f < nf; f++) {
+      const double* src = f == 0 ? ctx->va64 : ctx->vb64;
+      void* dst = f == 0 ? ctx->va : ctx->vb;
+      e = ctx->fp32 ? launch_pack<float>(src, (float*)dst, (int)ctx->nx, (int)ctx->ny, 1, ctx->pitch, ctx->plane, 0)
+                    : launch_pack<double>(src, (double*)dst, (int)ctx->nx, (int)ctx->ny, 1, ctx->pitch, ctx->plane, 0);
+      if (e != cudaSuccess) return cuda_fail("velocity packing", e);
+    }
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return cuda_fail("velocity packing", e);
   }
   if (ctx->wave) {
     if (make_maps(ctx, ctx->un, ctx->maps_un) || make_maps(ctx, ctx->wa, ctx->maps_wa) ||

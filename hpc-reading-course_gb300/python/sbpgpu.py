@@ -69,7 +69,8 @@ class Desc(C.Structure):
                 ("a", C.c_double), ("b", C.c_double),
                 ("rho", _dp), ("K", _dp),
                 ("stream", C.c_void_p), ("device", C.c_int),
-                ("nz", C.c_longlong), ("xl2", C.c_double), ("xr2", C.c_double)]
+                ("nz", C.c_longlong), ("xl2", C.c_double), ("xr2", C.c_double),
+                ("a_field", _dp), ("b_field", _dp)]
 
 
 class Instance(C.Structure):
@@ -232,7 +233,7 @@ class Context:
 
     def __init__(self, problem: int, order: int, nx: int, ny: int = 1, nz: int = 1, *, bc: int = BC_REFERENCE,
                  precision: int = FP64, xl=(-1.0, -1.0, -1.0), xr=(1.0, 1.0, 1.0), a: float = 1.0, b: float = 0.0,
-                 rho=None, K=None, stream: int | None = None, device: int = 0):
+                 rho=None, K=None, stream: int | None = None, device: int = 0, a_field=None, b_field=None):
         L = load()
         self._L = L
         self.problem, self.order, self.nx = problem, order, nx
@@ -250,6 +251,13 @@ class Context:
         if self._rho is not None:
             d.rho = self._rho.ctypes.data_as(_dp)
             d.K = self._K.ctypes.data_as(_dp)
+        # advection: velocities at every point (copied by sbp_create)
+        self._va = None if a_field is None else np.ascontiguousarray(a_field, dtype=np.float64).ravel()
+        self._vb = None if b_field is None else np.ascontiguousarray(b_field, dtype=np.float64).ravel()
+        if self._va is not None:
+            d.a_field = self._va.ctypes.data_as(_dp)
+        if self._vb is not None:
+            d.b_field = self._vb.ctypes.data_as(_dp)
         h = C.c_void_p()
         rc = L.sbp_create(C.byref(d), C.byref(h))
         if rc:

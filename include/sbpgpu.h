@@ -84,6 +84,15 @@ typedef struct {
   int device;         /* CUDA device ordinal */
   long long nz;       /* SBP_WAVE_3D: grid points in z (ignored otherwise) */
   double xl2, xr2;    /* SBP_WAVE_3D: z extent of the domain */
+  /* Advection with a velocity at every point, the reference's velocity
+   * callables a(i) (code/demo/advection/advection_rhs.h:12-51) and a(i,j),
+   * b(i,j) (:155-393), whose inflow SAT takes tau from the velocity at the
+   * boundary point (:94-119, :460-528): host arrays of nx (1D) or nx*ny (2D,
+   * (j,i) row-major) velocities, copied at sbp_create. NULL: the constants a, b
+   * (in 2D, a field given for one direction and not the other takes the
+   * constant for the other everywhere). Single contexts only. */
+  const double* a_field;
+  const double* b_field;
 } sbp_desc;
 
 /* Creates a context: validates the description (N >= max(closure width,

@@ -47,7 +47,8 @@ class _Problem(C.Structure):
                 ("xl0", C.c_double), ("xl1", C.c_double),
                 ("a", C.c_double), ("b", C.c_double),
                 ("rho", _dp), ("K", _dp),
-                ("nz", C.c_longlong), ("hiz", C.c_double), ("xl2", C.c_double)]
+                ("nz", C.c_longlong), ("hiz", C.c_double), ("xl2", C.c_double),
+                ("va", _dp), ("vb", _dp)]
 
 
 def reference_dir() -> str | None:
@@ -73,7 +74,8 @@ class Problem:
     """A grid problem on [xl, xr]^d with N points per direction, h = (xr-xl)/(N-1)."""
 
     def __init__(self, problem: int, order: int, nx: int, ny: int = 1, nz: int = 1, *, xl=(-1.0, -1.0, -1.0),
-                 xr=(1.0, 1.0, 1.0), a: float = 1.0, b: float = 0.0, bc: int = BC_REFERENCE, rho=None, K=None):
+                 xr=(1.0, 1.0, 1.0), a: float = 1.0, b: float = 0.0, bc: int = BC_REFERENCE, rho=None, K=None,
+                 a_field=None, b_field=None):
         self.problem, self.order, self.bc = problem, order, bc
         self.nx, self.ny = nx, (ny if problem in TWO_D or problem == WAVE_3D else 1)
         self.nz = nz if problem == WAVE_3D else 1
@@ -87,6 +89,9 @@ class Problem:
         self.a, self.b = a, b
         self.rho = None if rho is None else np.ascontiguousarray(rho, dtype=np.float64).ravel()
         self.K = None if K is None else np.ascontiguousarray(K, dtype=np.float64).ravel()
+        # advection: the velocity at every point (the reference's a(i) / a(i,j), b(i,j))
+        self.a_field = None if a_field is None else np.ascontiguousarray(a_field, dtype=np.float64).ravel()
+        self.b_field = None if b_field is None else np.ascontiguousarray(b_field, dtype=np.float64).ravel()
         self.dofs = DOFS[problem]
 
     @property
@@ -99,6 +104,10 @@ class Problem:
         if self.rho is not None:
             s.rho = _ptr(self.rho)
             s.K = _ptr(self.K)
+        if self.a_field is not None:
+            s.va = _ptr(self.a_field)
+        if self.b_field is not None:
+            s.vb = _ptr(self.b_field)
         return s
 
 
@@ -287,6 +296,11 @@ class Reference:
                 getattr(L, f"{n}_o{o}").argtypes = [C.c_longlong, C.c_double, C.c_double, _dp, _dp]
             for n in ("ref_adv2d_apply", "ref_adv2d_bc"):
                 getattr(L, f"{n}_o{o}").argtypes = [C.c_longlong, C.c_longlong] + [C.c_double] * 4 + [_dp, _dp]
+            for n in ("ref_adv1d_apply_var", "ref_adv1d_bc_var"):
+                getattr(L, f"{n}_o{o}").argtypes = [C.c_longlong, C.c_double, _dp, _dp, _dp]
+            for n in ("ref_adv2d_apply_var", "ref_adv2d_bc_var"):
+                getattr(L, f"{n}_o{o}").argtypes = [C.c_longlong, C.c_longlong, C.c_double, C.c_double, _dp, _dp,
+                                                     _dp, _dp]
             getattr(L, f"ref_refl_apply_o{o}").argtypes = [C.c_longlong, C.c_double, _dp, _dp]
             getattr(L, f"ref_refl_bc_o{o}").argtypes = [C.c_longlong, _dp, _dp]
             getattr(L, f"ref_hnorm1d_o{o}").argtypes = [C.c_longlong, C.c_longlong, C.c_double, _dp]
@@ -306,6 +320,15 @@ class Reference:
             getattr(L, f"{base}_apply_o{o}")(pb.nx, pb.ny, pb.hix, pb.hiy, pb.xl[0], pb.xl[1], t, _ptr(src), _ptr(dst))
             if with_bc:
                 getattr(L, f"{base}_bc_o{o}")(pb.nx, pb.ny, pb.hix, pb.hiy, _ptr(src), _ptr(dst))
+        elif pb.problem == ADVECTION_1D and pb.a_field is not None:
+            getattr(L, f"ref_adv1d_apply_var_o{o}")(pb.nx, pb.hix, _ptr(pb.a_field), _ptr(src), _ptr(dst))
+            if with_bc:
+                getattr(L, f"ref_adv1d_bc_var_o{o}")(pb.nx, pb.hix, _ptr(pb.a_field), _ptr(src), _ptr(dst))
+        elif pb.problem == ADVECTION_2D and pb.a_field is not None:
+            args = (pb.nx, pb.ny, pb.hix, pb.hiy, _ptr(pb.a_field), _ptr(pb.b_field), _ptr(src), _ptr(dst))
+            getattr(L, f"ref_adv2d_apply_var_o{o}")(*args)
+            if with_bc:
+                getattr(L, f"ref_adv2d_bc_var_o{o}")(*args)
         elif pb.problem == ADVECTION_1D:
             getattr(L, f"ref_adv1d_apply_o{o}")(pb.nx, pb.hix, pb.a, _ptr(src), _ptr(dst))
             if with_bc:

@@ -108,6 +108,44 @@ extern "C" void SYM(ref_adv2d_bc)(long long nx, long long ny, double hix, double
   grid::grid_function_2d<PetscScalar> s(const_cast<double*>(src), L), d(dst, L);
   advection_bc_serial(d, s, HI, std::array<double, 2>{hix, hiy}, va, vb);
 }
+/* The same with a velocity at every point, the reference's callable a(i)
+ * (advection_1D_sim.cpp:19): a[i]. */
+extern "C" void SYM(ref_adv1d_apply_var)(long long n, double hi, const double* a, const double* src, double* dst) {
+  const FirstDerivativeOp D1;
+  auto vel = [a](const PetscInt i) { return a[i]; };
+  grid::partitioned_layout_1d L(grid::extents_1d(n, 1), 0, n);
+  grid::grid_function_1d<PetscScalar> s(const_cast<double*>(src), L), d(dst, L);
+  advection_serial(d, s, D1, hi, vel);
+}
+
+extern "C" void SYM(ref_adv1d_bc_var)(long long n, double hi, const double* a, const double* src, double* dst) {
+  const InverseNormOp HI;
+  auto vel = [a](const PetscInt i) { return a[i]; };
+  grid::partitioned_layout_1d L(grid::extents_1d(n, 1), 0, n);
+  grid::grid_function_1d<PetscScalar> s(const_cast<double*>(src), L), d(dst, L);
+  advection_bc_serial(d, s, HI, hi, vel);
+}
+
+/* 2D with velocity fields a(i,j) = a[i + nx*j], b(i,j) = b[i + nx*j]. */
+extern "C" void SYM(ref_adv2d_apply_var)(long long nx, long long ny, double hix, double hiy, const double* a,
+                                         const double* b, const double* src, double* dst) {
+  const FirstDerivativeOp D1;
+  std::function<double(PetscInt, PetscInt)> va = [a, nx](PetscInt i, PetscInt j) { return a[i + nx * j]; };
+  std::function<double(PetscInt, PetscInt)> vb = [b, nx](PetscInt i, PetscInt j) { return b[i + nx * j]; };
+  grid::partitioned_layout_2d L(grid::extents_2d(nx, ny, 1), 0, nx, ny);
+  grid::grid_function_2d<PetscScalar> s(const_cast<double*>(src), L), d(dst, L);
+  advection_serial(d, s, D1, std::array<double, 2>{hix, hiy}, va, vb);
+}
+
+extern "C" void SYM(ref_adv2d_bc_var)(long long nx, long long ny, double hix, double hiy, const double* a,
+                                      const double* b, const double* src, double* dst) {
+  const InverseNormOp HI;
+  std::function<double(PetscInt, PetscInt)> va = [a, nx](PetscInt i, PetscInt j) { return a[i + nx * j]; };
+  std::function<double(PetscInt, PetscInt)> vb = [b, nx](PetscInt i, PetscInt j) { return b[i + nx * j]; };
+  grid::partitioned_layout_2d L(grid::extents_2d(nx, ny, 1), 0, nx, ny);
+  grid::grid_function_2d<PetscScalar> s(const_cast<double*>(src), L), d(dst, L);
+  advection_bc_serial(d, s, HI, std::array<double, 2>{hix, hiy}, va, vb);
+}
 #elif REF_PROBLEM == 4
 #include "reflection/reflection_rhs.h"
 

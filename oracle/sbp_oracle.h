@@ -50,6 +50,8 @@ typedef struct {
   const double* K;    /* ORC_WAVE_VAR_2D: nx*ny bulk modulus */
   long long nz;       /* ORC_WAVE_3D: points in z (element (k, j, i, comp) at dofs*(i + nx*(j + ny*k)) + comp) */
   double hiz, xl2;    /* ORC_WAVE_3D: inverse z spacing, lower z bound */
+  const double* va;   /* advection: velocity a at every point (1D: nx; 2D: nx*ny, row-major (j,i)), or NULL for a */
+  const double* vb;   /* 2D advection: velocity b at every point, or NULL for b */
 } orc_problem;
 
 /* ORC_WAVE_2BLOCK_2D: each block has ny/2 points in y over half the domain,

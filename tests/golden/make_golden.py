@@ -80,8 +80,34 @@ def main():
             hn.append([order, n, dofs, h, ref.hnorm1d(v, n, dofs, h, order)])
     blobs["meta"] = np.array(meta, dtype=np.float64)
     blobs["hnorm"] = np.array(hn, dtype=np.float64)
+    # advection with a velocity at every point (the reference's callables a(i), a(i,j), b(i,j)),
+    # from a generator of their own so the cases above keep their inputs
+    vrng = np.random.default_rng(20261204)
+    vmeta = []
+    for order in (2, 4, 6):
+        for n in sorted({MIN_N[order], 33, 201}):
+            x = np.linspace(-1.0, 1.0, n)
+            a = 0.8 + np.sin(2 * np.pi * x + vrng.uniform(-0.3, 0.3))  # changes sign inside the domain
+            k = len(vmeta)
+            blobs[f"va{k}"], blobs[f"vb{k}"] = a, np.zeros(1)
+            blobs[f"vsrc{k}"] = vrng.standard_normal(n)
+            pb = O.Problem(O.ADVECTION_1D, order, n, a_field=a)
+            blobs[f"vdst{k}"] = ref.rhs(pb, blobs[f"vsrc{k}"])
+            vmeta.append([O.ADVECTION_1D, order, n])
+        for n in sorted({max(MIN_N[order], 12), 33}):
+            x = np.linspace(-1.0, 1.0, n)
+            X, Y = np.meshgrid(x, x)
+            a = 1.2 + 0.4 * np.sin(2 * X + Y + vrng.uniform(-0.3, 0.3))
+            b = -0.8 + 0.3 * np.cos(X - 2 * Y + vrng.uniform(-0.3, 0.3))
+            k = len(vmeta)
+            blobs[f"va{k}"], blobs[f"vb{k}"] = a.ravel(), b.ravel()
+            blobs[f"vsrc{k}"] = vrng.standard_normal(n * n)
+            pb = O.Problem(O.ADVECTION_2D, order, n, n, a_field=a, b_field=b)
+            blobs[f"vdst{k}"] = ref.rhs(pb, blobs[f"vsrc{k}"])
+            vmeta.append([O.ADVECTION_2D, order, n])
+    blobs["vmeta"] = np.array(vmeta, dtype=np.float64)
     np.savez_compressed(args.out, **blobs)
-    print(f"wrote {len(meta)} RHS cases and {len(hn)} H-norm cases to {args.out}")
+    print(f"wrote {len(meta)} RHS cases, {len(vmeta)} velocity-field cases and {len(hn)} H-norm cases to {args.out}")
 
 
 if __name__ == "__main__":

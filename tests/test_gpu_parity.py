@@ -308,3 +308,67 @@ def test_two_block_reflection_coefficient_on_gpu(sbp):
     col = out[:, nx // 2, 2]
     assert col[:nb].max() == pytest.approx(0.6, abs=0.01)
     assert col[nb:].max() == pytest.approx(1.6, abs=0.01)
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+def test_advection_velocity_fields_against_reference_fixtures(sbp, golden, order):
+    """Velocities at every point (the reference's callables a(i), a(i,j), b(i,j)): the CUDA
+    path against the reference's own RHS in tests/golden (its out-of-bounds boundary reads
+    masked), 1e-12 norm-wise."""
+    vmeta = golden["vmeta"]
+    seen = 0
+    for k, (prob, o, n) in enumerate(vmeta):
+        prob, o, n = int(prob), int(o), int(n)
+        if o != order:
+            continue
+        src, ref = golden[f"vsrc{k}"], golden[f"vdst{k}"]
+        if prob == O.ADVECTION_1D:
+            ctx = sbp.Context(sbp.ADVECTION_1D, order, n, a_field=golden[f"va{k}"])
+            mask = np.zeros(n, dtype=bool)
+            mask[n - 1] = True
+        else:
+            ctx = sbp.Context(sbp.ADVECTION_2D, order, n, n, a_field=golden[f"va{k}"], b_field=golden[f"vb{k}"])
+            mask = np.zeros(n * n, dtype=bool)
+            mask[:n] = True
+        with ctx as c:
+            got = c.rhs(src)
+        assert relerr(got[~mask], ref[~mask]) <= TOL64
+        seen += 1
+    assert seen >= 4
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_advection_velocity_fields_rhs_and_rk4(sbp, port, order, precision):
+    """Fields whose sign changes along every boundary (inflow and outflow on each side), a
+    non-square 2D grid and a 1D field changing sign inside: RHS and 20 RK4 steps against
+    the oracle."""
+    prec, tol = (sbp.FP64, TOL64) if precision == "fp64" else (sbp.FP32, TOL32)
+    nx, ny = 83, 57
+    x, y = np.linspace(-1, 1, nx), np.linspace(-1, 1, ny)
+    X, Y = np.meshgrid(x, y)
+    a = np.sin(2 * X + Y) + 0.2
+    b = np.cos(X - 2 * Y) - 0.3
+    rng = np.random.default_rng(order)
+    src = rng.standard_normal(nx * ny)
+    v0 = np.exp(-((X - 0.1) ** 2 + (Y + 0.2) ** 2) / 0.2 ** 2).ravel()
+    pb = O.Problem(O.ADVECTION_2D, order, nx, ny, a_field=a, b_field=b)
+    dt = 0.1 * 2.0 / (nx - 1)
+    with sbp.Context(sbp.ADVECTION_2D, order, nx, ny, a_field=a, b_field=b, precision=prec) as c:
+        assert relerr(c.rhs(src), port.rhs(pb, src)) <= tol
+        assert relerr(c.rk4(v0, 0.0, dt, 20), port.rk4(pb, v0, 0.0, dt, 20)) <= tol
+    n = 101
+    x = np.linspace(-1, 1, n)
+    a1 = 0.1 - np.sin(3 * x)  # > 0 at the left end and < 0 at the right: inflow through both ends
+    src1 = rng.standard_normal(n)
+    pb1 = O.Problem(O.ADVECTION_1D, order, n, a_field=a1)
+    w0 = np.exp(-(x / 0.2) ** 2)
+    with sbp.Context(sbp.ADVECTION_1D, order, n, a_field=a1, precision=prec) as c:
+        assert relerr(c.rhs(src1), port.rhs(pb1, src1)) <= tol
+        assert relerr(c.rk4(w0, 0.0, 0.1 * 2.0 / (n - 1), 20), port.rk4(pb1, w0, 0.0, 0.1 * 2.0 / (n - 1), 20)) <= tol
+
+
+def test_velocity_fields_rejected_for_other_problems(sbp):
+    with pytest.raises(sbp.SbpError) as e:
+        sbp.Context(sbp.WAVE_HOM_2D, 4, 20, 20, a_field=np.ones(400))
+    assert e.value.code == sbp.ERR_INVALID

@@ -49,6 +49,26 @@ def test_golden_rhs_bit_exact(port, golden):
         assert np.isfinite(out).all()
 
 
+def test_golden_velocity_fields_bit_exact(port, golden):
+    """Advection with a velocity at every point -- the reference's callables a(i) (1D) and
+    a(i,j), b(i,j) (2D), one 1D field changing sign inside the domain -- against the
+    reference's own headers, bit for bit except at its out-of-bounds boundary reads."""
+    vmeta = golden["vmeta"]
+    assert len(vmeta) >= 15
+    for k, (prob, order, n) in enumerate(vmeta):
+        prob, order, n = int(prob), int(order), int(n)
+        src, ref = golden[f"vsrc{k}"], golden[f"vdst{k}"]
+        if prob == O.ADVECTION_1D:
+            pb = O.Problem(prob, order, n, a_field=golden[f"va{k}"])
+        else:
+            pb = O.Problem(prob, order, n, n, a_field=golden[f"va{k}"], b_field=golden[f"vb{k}"])
+        out = port.rhs(pb, src)
+        mask = _defect_mask(pb, ref)
+        assert not (~np.isfinite(ref) & ~mask).any()
+        assert np.array_equal(out[~mask], ref[~mask]), f"velocity case {k}: not bit-identical"
+        assert np.isfinite(out).all()
+
+
 def test_golden_hnorm_reference_form(port, golden):
     for k, (order, n, dofs, h, val) in enumerate(golden["hnorm"]):
         v = golden[f"hn_v{k}"]
