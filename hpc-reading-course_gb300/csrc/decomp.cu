@@ -1,19 +1,28 @@
 // decomp.cu -- the 2D wave system (rho = K = 1, FP64) on a P x Q decomposition of
-// one grid, on one GPU: each subdomain holds its own SoA state with sw = R ghost
-// lines on each side, and every RK4 stage first copies the neighbours' edge lines
-// into the ghosts (a halo-exchange kernel), then evaluates the RHS and the stage
-// update of all subdomains in one launch. It is the reference's non-overlapped
-// decomposed path -- rhs_local / rhs_all over a DMDA block grid
+// one grid, on one GPU: each subdomain holds its own SoA state with R ghost lines
+// on each side, and every RK4 stage first copies the neighbours' edge lines into
+// the ghosts (a halo-exchange kernel), then evaluates the RHS and the stage update
+// of all subdomains in one launch. It is the reference's non-overlapped decomposed
+// path -- rhs_local / rhs_all over a DMDA block grid
 // (code/include/partitioned_rhs/rhs.h:97-181, 183-360) with the VecScatter ghost
-// update of code/src/scatter/scatter_ctx.cpp:149-211 -- with the halo exchange
-// on the device, the step towards one subdomain per GPU.
+// update of code/src/scatter/scatter_ctx.cpp:149-211 -- with the halo exchange on
+// the device, the step towards one subdomain per GPU.
 //
-// Interior points of a subdomain evaluate the central stencil across internal
-// edges from the ghosts; closure rows and SAT terms apply only at the physical
-// boundary, so a subdomain at least one closure block wide holds every closure
-// line it needs. The arithmetic per point is that of the single-grid path
-// (d1_line / closure_line tap order, the wave_hom SAT in FP64), so a decomposed
-// run matches the single grid to rounding.
+// The stage kernel is the single grid's fixed-point FP64 kernel with converter
+// warps (wave2d_fixed.cuh, wave_fixed_kernel<ORD, STAGE, true>) over the
+// subdomains' tile list: its producer loads each tile's p/u/v boxes, ghosts
+// included, with TMA maps of the tile's subdomain, and the compute warps take the
+// central stencil across internal edges from the ghosts and closure rows and SAT
+// terms only at the physical boundary (global indices), so a decomposed run
+// matches the single grid to rounding. A subdomain's arrays keep ghost_x(order)
+// ghost columns (R rounded up to an even count: TMA x coordinates must be 16-byte
+// aligned) and R ghost rows. In the RK4 loop the exchange is fused into the
+// stages: a point within R of an internal edge also stores the value it gives the
+// next stage input into the neighbour's ghost line, so the exchange overlaps the
+// stage's computation and costs no launch (the reference overlaps its VecScatter
+// with rhs_local, code/demo/wave_hom/wave_eq_hom_sim.cpp:258-261). The halo
+// kernel remains for states set from outside (before an RHS, at the start of a
+// run of steps).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -30,57 +39,14 @@
 namespace sbp {
 namespace {
 
-struct DecompSub {
-  int nx, ny;        // interior points
-  int xoff, yoff;    // global index of the interior's first column / row
-  long long pitch;   // elements per row, ghosts included
-  long long plane;   // elements per component plane (ny + 2 sw rows)
-  long long base;    // element offset of the subdomain's planes in a pool
-};
-
-struct DecompTile {
-  int sub, i0, j0, pad;
-};
+// x ghost width of the pools: R rounded up to an even count, so that every TMA
+// box of a subdomain starts on a 16-byte boundary (the fixed-point tile's HX).
+constexpr int ghost_x(int order) { return ((order / 2 + 1) / 2) * 2; }
 
 struct DecompParams {
-  int NX, NY, sw, bc, px, py;
-  DirTaps<double> dx, dy;  // -hi * stencils
-  double bwx, bwy;         // hi * HI[0]: SAT weights
-  const DecompSub* subs;
+  int NX, NY, sw, col0, px, py;
+  const FxSub* subs;
 };
-
-constexpr int kDTX = 32, kDTY = 32, kDRows = 8;  // a CTA: 32 x 8 threads over a 32 x 32 tile
-
-// D1 of a line held by one subdomain: the element of global index g is at
-// base[(g - off) * st] (ghost cells included). Interior points use the central
-// stencil; the closure rows (d1_line / closure_line order) need the line's first
-// or last closure block inside the subdomain, which the width check guarantees.
-template <int ORD>
-__device__ __forceinline__ double d1_sub(const DirTaps<double>& d, const double* base, long long st, int off, int n,
-                                         int I) {
-  constexpr int W = OpShape<ORD>::W, CS = OpShape<ORD>::CS, CW = OpShape<ORD>::CW, R = (W - 1) / 2;
-  if (I >= CS && I < n - CS) {
-    const double* c = base + (long long)(I - R - off) * st;
-    double s = d.taps[0] * c[0];
-#pragma unroll
-    for (int k = 1; k < W; k++)
-      if (k != R) s = fma(d.taps[k], c[k * st], s);
-    return s;
-  }
-  if (I < CS) {
-    const double* c = base - (long long)off * st;  // off == 0: the first subdomain
-    double s = d.cls[I][0] * c[0];
-#pragma unroll
-    for (int k = 1; k < CW; k++) s = fma(d.cls[I][k], c[k * st], s);
-    return s;
-  }
-  const int r = n - 1 - I;
-  const double* c = base + (long long)(n - CW - off) * st;
-  double s = -d.cls[r][CW - 1] * c[0];
-#pragma unroll
-  for (int k = 1; k < CW; k++) s = fma(-d.cls[r][CW - 1 - k], c[k * st], s);
-  return s;
-}
 
 // Ghost update of the stage input: blockIdx.y = subdomain, blockIdx.z = side
 // (0 west, 1 east, 2 south, 3 north); each thread copies scalars of the sw lines
@@ -91,7 +57,7 @@ __global__ void decomp_halo_kernel(const __grid_constant__ DecompParams P, doubl
   const int nbx = side == 0 ? bx - 1 : (side == 1 ? bx + 1 : bx);
   const int nby = side == 2 ? by - 1 : (side == 3 ? by + 1 : by);
   if (nbx < 0 || nbx >= P.px || nby < 0 || nby >= P.py) return;
-  const DecompSub S = P.subs[b], N = P.subs[nby * P.px + nbx];
+  const FxSub S = P.subs[b], N = P.subs[nby * P.px + nbx];
   const int len = side < 2 ? S.ny : S.nx;
   const long long total = 3LL * sw * len;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
@@ -104,67 +70,8 @@ __global__ void decomp_halo_kernel(const __grid_constant__ DecompParams P, doubl
     else if (side == 1) { di = S.nx + g; dj = p; si = g; sj = p; }
     else if (side == 2) { di = p; dj = -sw + g; si = p; sj = N.ny - sw + g; }
     else { di = p; dj = S.ny + g; si = p; sj = g; }
-    pool[S.base + c * S.plane + (dj + sw) * S.pitch + (di + sw)] =
-        pool[N.base + c * N.plane + (sj + sw) * N.pitch + (si + sw)];
-  }
-}
-
-template <int ORD, int STAGE>
-__global__ void __launch_bounds__(kDTX * kDRows)
-    decomp_stage_kernel(const __grid_constant__ DecompParams P, const DecompTile* __restrict__ tiles,
-                        const double* __restrict__ in, double* un, double* acc, double* wout, double* kout,
-                        const double c_acc, const double c_w) {
-  const DecompTile t = tiles[blockIdx.x];
-  const DecompSub S = P.subs[t.sub];
-  const int sw = P.sw;
-  const int i = t.i0 + threadIdx.x;
-  if (i >= S.nx) return;
-  const int I = S.xoff + i;
-  const double* U = in + S.base;
-  const double* V = U + S.plane;
-  const double* Pp = V + S.plane;
-#pragma unroll 1
-  for (int r = 0; r < kDTY / kDRows; r++) {
-    const int j = t.j0 + threadIdx.y + kDRows * r;
-    if (j >= S.ny) continue;
-    const int J = S.yoff + j;
-    const long long row = (long long)(j + sw) * S.pitch + sw;  // local i = 0 of row j
-    const long long col = (long long)sw * S.pitch + (i + sw);  // local j = 0 of column i
-    const long long q = row + i;
-    double ku = d1_sub<ORD>(P.dx, Pp + row, 1, S.xoff, P.NX, I);
-    double kv = d1_sub<ORD>(P.dy, Pp + col, S.pitch, S.yoff, P.NY, J);
-    double kp = d1_sub<ORD>(P.dx, U + row, 1, S.xoff, P.NX, I) + d1_sub<ORD>(P.dy, V + col, S.pitch, S.yoff, P.NY, J);
-    const double uc = U[q], vc = V[q], pc = Pp[q];
-    // SAT at the physical boundary (the wave_hom terms of the single-grid path, rho = K = 1)
-    if (P.bc != BC_NONE && (I == 0 || J == 0 || I == P.NX - 1 || J == P.NY - 1)) {
-      if (P.bc == BC_FREE_SURFACE) {
-        if (I == 0) ku = ku - P.bwx * pc;
-        if (J == 0) kv = kv - P.bwy * pc;
-        if (I == P.NX - 1) ku = ku + P.bwx * pc;
-        if (J == P.NY - 1) kv = kv + P.bwy * pc;
-      } else {
-        if (I == 0) { const double g = P.bwx * (pc + 1.0 * uc); ku -= 0.5 * g; kp -= 0.5 * g; }
-        if (J == 0) { const double g = P.bwy * (pc + 1.0 * vc); kv -= 0.5 * g; kp -= 0.5 * g; }
-        if (I == P.NX - 1) { const double g = P.bwx * (pc - 1.0 * uc); ku += 0.5 * g; kp -= 0.5 * g; }
-        if (J == P.NY - 1) { const double g = P.bwy * (pc - 1.0 * vc); kv += 0.5 * g; kp -= 0.5 * g; }
-      }
-    }
-    const double kc[3] = {ku, kv, kp}, cen[3] = {uc, vc, pc};
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const long long o = S.base + c * S.plane + q;
-      if constexpr (STAGE == ST_RHS) {
-        kout[o] = kc[c];
-      } else if constexpr (STAGE == ST_FIRST) {
-        acc[o] = fma(c_acc, kc[c], cen[c]);
-        wout[o] = fma(c_w, kc[c], cen[c]);
-      } else if constexpr (STAGE == ST_MID) {
-        acc[o] = fma(c_acc, kc[c], acc[o]);
-        wout[o] = fma(c_w, kc[c], un[o]);
-      } else {
-        un[o] = fma(c_acc, kc[c], acc[o]);
-      }
-    }
+    pool[S.base + c * S.plane + (dj + sw) * S.pitch + (di + P.col0)] =
+        pool[N.base + c * N.plane + (sj + sw) * N.pitch + (si + P.col0)];
   }
 }
 
@@ -176,8 +83,8 @@ __global__ void decomp_scatter_kernel(const __grid_constant__ DecompParams P, co
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
     const int J = (int)(g / P.NX), I = (int)(g - (long long)J * P.NX);
     const int bx = xsub[I], by = ysub[J];
-    const DecompSub S = P.subs[by * P.px + bx];
-    const long long q = S.base + (long long)(J - S.yoff + P.sw) * S.pitch + (I - S.xoff + P.sw);
+    const FxSub S = P.subs[by * P.px + bx];
+    const long long q = S.base + (long long)(J - S.yoff + P.sw) * S.pitch + (I - S.xoff + P.col0);
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       if (aos_in)
@@ -188,28 +95,47 @@ __global__ void decomp_scatter_kernel(const __grid_constant__ DecompParams P, co
   }
 }
 
-template <int ORD>
-cudaError_t launch_stage_o(int stage, const DecompParams& P, const DecompTile* tiles, int ntiles, const double* in,
-                           double* un, double* acc, double* wout, double* kout, double c_acc, double c_w,
-                           cudaStream_t s) {
-  const dim3 block(kDTX, kDRows);
-  switch (stage) {
-    case ST_RHS:
-      decomp_stage_kernel<ORD, ST_RHS><<<ntiles, block, 0, s>>>(P, tiles, in, un, acc, wout, kout, c_acc, c_w);
-      break;
-    case ST_FIRST:
-      decomp_stage_kernel<ORD, ST_FIRST><<<ntiles, block, 0, s>>>(P, tiles, in, un, acc, wout, kout, c_acc, c_w);
-      break;
-    case ST_MID:
-      decomp_stage_kernel<ORD, ST_MID><<<ntiles, block, 0, s>>>(P, tiles, in, un, acc, wout, kout, c_acc, c_w);
-      break;
-    case ST_LAST:
-      decomp_stage_kernel<ORD, ST_LAST><<<ntiles, block, 0, s>>>(P, tiles, in, un, acc, wout, kout, c_acc, c_w);
-      break;
-    default: return cudaErrorInvalidValue;
-  }
+// The stage kernels of a decomposed grid: the fixed-point FP64 stage kernel over
+// the subdomains' tile list (wave_fixed_kernel<ORD, STAGE, true>).
+template <int ORD, int STAGE>
+cudaError_t launch_dec_one(const WaveParams<double>& prm, unsigned grid, cudaStream_t s) {
+  using Tile = WaveStageTile<double, ORD, WK_HOM, STAGE>;
+  static_assert(Tile::FIX && Tile::CONV > 0, "the decomposed path runs the converter-warp kernel");
+  static_assert(Tile::HX == ghost_x(ORD), "pool x ghost width and tile halo must agree");
+  CUtensorMap none;
+  std::memset(&none, 0, sizeof(none));
+  wave_fixed_kernel<ORD, STAGE, true><<<grid, fx_kernel_threads<Tile, true>(), Tile::SMEM, s>>>(
+      none, none, none, none, none, none, none, prm);
   return cudaGetLastError();
 }
+
+template <int ORD>
+cudaError_t launch_dec(int stage, const WaveParams<double>& prm, unsigned grid, cudaStream_t s) {
+  switch (stage) {
+    case ST_RHS: return launch_dec_one<ORD, ST_RHS>(prm, grid, s);
+    case ST_FIRST: return launch_dec_one<ORD, ST_FIRST>(prm, grid, s);
+    case ST_MID: return launch_dec_one<ORD, ST_MID>(prm, grid, s);
+    case ST_LAST: return launch_dec_one<ORD, ST_LAST>(prm, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int ORD, int STAGE>
+cudaError_t configure_dec_one() {
+  return cudaFuncSetAttribute(wave_fixed_kernel<ORD, STAGE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              WaveStageTile<double, ORD, WK_HOM, STAGE>::SMEM);
+}
+
+template <int ORD>
+cudaError_t configure_dec() {
+  cudaError_t e;
+  if ((e = configure_dec_one<ORD, ST_RHS>()) != cudaSuccess) return e;
+  if ((e = configure_dec_one<ORD, ST_FIRST>()) != cudaSuccess) return e;
+  if ((e = configure_dec_one<ORD, ST_MID>()) != cudaSuccess) return e;
+  return configure_dec_one<ORD, ST_LAST>();
+}
+
+template <int ORD> constexpr int dec_tile_rows() { return WaveStageTile<double, ORD, WK_HOM, ST_MID>::TY; }
 
 }  // namespace
 }  // namespace sbp
@@ -218,18 +144,26 @@ using namespace sbp;
 
 struct sbp_decomp {
   sbp_desc d{};
-  int px = 1, py = 1, sw = 1;
+  int px = 1, py = 1, sw = 1, col0 = 2, ty = 14;
   DecompParams prm{};
-  std::vector<DecompSub> subs;
-  DecompSub* d_subs = nullptr;
-  DecompTile* d_tiles = nullptr;
+  WaveParams<double> wprm{};  // the stage-independent fields of the stage kernels' parameters
+  std::vector<FxSub> subs;
+  FxSub* d_subs = nullptr;
+  FxTile* d_tiles = nullptr;
+  unsigned char* d_tinfo = nullptr;  // per tile its geometry block (kFxTileInfoBytes each)
+  CUtensorMap* d_maps = nullptr;  // [3 input buffers: un, wa, wb][sub][p, u, v], then [sub][u^n, acc]
   int ntiles = 0, maxlen = 0;
   int* d_xsub = nullptr;
   int* d_ysub = nullptr;
+  int* d_err = nullptr;    // the stage kernels' error word
+  int* d_sched = nullptr;  // their dynamic tile queue
   long long pool = 0;  // elements per state pool
   double *un = nullptr, *acc = nullptr, *wa = nullptr, *wb = nullptr, *io = nullptr;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  cudaGraphExec_t graph = nullptr;  // a chunk of RK4 steps
+  long long graph_steps = 0;
+  double graph_dt = 0.0;
   std::string msg;
 };
 
@@ -243,10 +177,15 @@ int dfail(sbp_decomp* c, int code, const std::string& m) {
 }
 
 void release(sbp_decomp* c) {
+  if (c->graph) cudaGraphExecDestroy(c->graph);
   cudaFree(c->d_subs);
   cudaFree(c->d_tiles);
+  cudaFree(c->d_tinfo);
+  cudaFree(c->d_maps);
   cudaFree(c->d_xsub);
   cudaFree(c->d_ysub);
+  cudaFree(c->d_err);
+  cudaFree(c->d_sched);
   cudaFree(c->un);
   cudaFree(c->acc);
   cudaFree(c->wa);
@@ -263,6 +202,33 @@ void decomp_taps(DirTaps<double>& t, int order, double scale) {
     for (int s = 0; s < op.cls_width; s++) t.cls[r][s] = scale * op.closure[r][s];
 }
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// One 3-component tensor map over subdomain S's arrays (ghosts included) in buffer buf.
+bool encode_sub(EncodeTiledFn enc, double* buf, const FxSub& S, int col0, int sw, const cuuint32_t box[3],
+                CUtensorMap* out) {
+  const cuuint64_t dims[3] = {(cuuint64_t)(S.nx + 2 * col0), (cuuint64_t)(S.ny + 2 * sw), 3};
+  const cuuint64_t strides[2] = {(cuuint64_t)(S.pitch * 8), (cuuint64_t)(S.plane * 8)};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, buf + S.base, dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 cudaError_t halo(sbp_decomp* c, double* pool) {
   const int threads = 256;
   const long long total = 3LL * c->sw * c->maxlen;
@@ -271,10 +237,24 @@ cudaError_t halo(sbp_decomp* c, double* pool) {
   return cudaGetLastError();
 }
 
+// One stage over every subdomain; in is one of un, wa, wb (its maps are chosen by it).
 cudaError_t stage(sbp_decomp* c, int st, const double* in, double* wout, double* kout, double c_acc, double c_w) {
+  WaveParams<double> p = c->wprm;
+  p.in = in;
+  p.wout = wout;
+  p.kout = kout;
+  p.c_acc = c_acc;
+  p.c_w = c_w;
+  set_fixed_scales(p, c->d.order, p.hix, p.hiy);
+  const int nsub = c->px * c->py;
+  const int which = in == c->un ? 0 : (in == c->wa ? 1 : 2);
+  p.dmaps_in = c->d_maps + (long long)which * 3 * nsub;
+  p.dmaps_na = c->d_maps + 9LL * nsub;
+  const int nsm = device_sm_count();
+  const unsigned grid = (unsigned)(c->ntiles < nsm ? c->ntiles : nsm);
   const int o = c->d.order;
-  const auto f = o == 2 ? launch_stage_o<2> : (o == 4 ? launch_stage_o<4> : launch_stage_o<6>);
-  return f(st, c->prm, c->d_tiles, c->ntiles, in, c->un, c->acc, wout, kout, c_acc, c_w, c->stream);
+  return o == 2 ? launch_dec<2>(st, p, grid, c->stream)
+                : (o == 4 ? launch_dec<4>(st, p, grid, c->stream) : launch_dec<6>(st, p, grid, c->stream));
 }
 
 // AoS -> the subdomains' interiors (aos_in) or back (aos_out); one of them is null.
@@ -285,11 +265,35 @@ cudaError_t scatter(sbp_decomp* c, const double* aos_in, double* aos_out, double
   return cudaGetLastError();
 }
 
+// One classical RK4 step (code/include/time_stepping/time_stepping.h:127-142). Each
+// stage writes the ghost lines of the next stage's input as it produces the values
+// (the fused exchange of wave_tile_fixed); u^n's ghosts must be current on entry.
+cudaError_t enqueue_step(sbp_decomp* c, double dt) {
+  cudaError_t e;
+  if ((e = stage(c, ST_FIRST, c->un, c->wa, nullptr, dt / 6, 0.5 * dt)) != cudaSuccess) return e;
+  if ((e = stage(c, ST_MID, c->wa, c->wb, nullptr, dt / 3, 0.5 * dt)) != cudaSuccess) return e;
+  if ((e = stage(c, ST_MID, c->wb, c->wa, nullptr, dt / 3, dt)) != cudaSuccess) return e;
+  return stage(c, ST_LAST, c->wa, nullptr, nullptr, dt / 6, 0.0);
+}
+
 #define DCK(call)                                                              \
   do {                                                                         \
     cudaError_t e_ = (call);                                                   \
     if (e_ != cudaSuccess) return dfail(c, SBP_ERR_CUDA, cudaGetErrorString(e_)); \
   } while (0)
+
+// Synchronises the stream and reads (and clears) the stage kernels' error word.
+int finish(sbp_decomp* c) {
+  int h = 0;
+  DCK(cudaMemcpyAsync(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  DCK(cudaStreamSynchronize(c->stream));
+  if (h) {
+    DCK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+    DCK(cudaStreamSynchronize(c->stream));
+    return dfail(c, SBP_ERR_DEVICE, "a bounded wait ran out in a stage kernel");
+  }
+  return SBP_OK;
+}
 
 }  // namespace
 
@@ -308,21 +312,25 @@ int sbp_decomp_create(const sbp_desc* desc, int px, int py, sbp_decomp** out) {
   const ops::Operator& op = ops::get(desc->order);
   const long long NX = desc->nx, NY = desc->ny;
   if (px < 1 || py < 1 || px > 64 || py > 64) return reject(SBP_ERR_INVALID, "px, py must be in [1, 64]");
-  // every subdomain at least one closure block wide (it then holds the closure
-  // lines of a physical boundary and the ghost lines its neighbour needs)
   // the whole grid at least the operator's minimum size, as sbp_create demands: below
   // it the left and right closure blocks would overlap
   const long long m = ops::min_points(desc->order);
   if (NX < m || NY < m) return reject(SBP_ERR_INVALID, "grid smaller than the operator's minimum size");
+  // every subdomain at least one closure block wide (it then holds the closure
+  // lines of a physical boundary and the ghost lines its neighbour needs)
   if (NX / px < op.cls_width || NY / py < op.cls_width || NX > (1 << 20) || NY > (1 << 20))
     return reject(SBP_ERR_INVALID, "subdomains narrower than the closure width, or grid above 2^20 per direction");
   if (!(desc->xr[0] > desc->xl[0]) || !(desc->xr[1] > desc->xl[1])) return reject(SBP_ERR_INVALID, "empty domain");
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return reject(SBP_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
   sbp_decomp* c = new (std::nothrow) sbp_decomp;
   if (!c) return reject(SBP_ERR_CUDA, "host allocation");
   c->d = *desc;
   c->px = px;
   c->py = py;
   c->sw = (op.width - 1) / 2;
+  c->col0 = ghost_x(desc->order);
+  c->ty = desc->order == 2 ? dec_tile_rows<2>() : (desc->order == 4 ? dec_tile_rows<4>() : dec_tile_rows<6>());
   auto cfail = [&](int code, const char* why) {
     release(c);
     delete c;
@@ -337,19 +345,26 @@ int sbp_decomp_create(const sbp_desc* desc, int px, int py, sbp_decomp** out) {
       return cfail(SBP_ERR_CUDA, "cudaStreamCreate");
     c->own_stream = true;
   }
-  // splits: subdomain b along x covers [b NX / px, (b + 1) NX / px)
+  // splits: subdomain b along x covers [b NX / px, (b + 1) NX / px). Each subdomain's
+  // arrays: R ghost rows, col0 ghost columns (R rounded up to even), a row pitch of a
+  // multiple of 32 doubles, planes starting at multiples of the pitch (TMA wants
+  // 16-byte aligned bases, strides and x coordinates).
   std::vector<int> xsub(NX), ysub(NY);
   long long off = 0;
   for (int by = 0; by < py; by++)
     for (int bx = 0; bx < px; bx++) {
-      DecompSub s{};
+      FxSub s{};
       s.xoff = (int)(bx * NX / px);
       s.yoff = (int)(by * NY / py);
       s.nx = (int)((bx + 1) * NX / px) - s.xoff;
       s.ny = (int)((by + 1) * NY / py) - s.yoff;
-      s.pitch = (s.nx + 2 * c->sw + 31) / 32 * 32;
+      s.pitch = (s.nx + 2 * c->col0 + 31) / 32 * 32;
       s.plane = (long long)(s.ny + 2 * c->sw) * s.pitch;
       s.base = off;
+      s.nbr[0] = bx > 0 ? by * px + bx - 1 : -1;
+      s.nbr[1] = bx < px - 1 ? by * px + bx + 1 : -1;
+      s.nbr[2] = by > 0 ? (by - 1) * px + bx : -1;
+      s.nbr[3] = by < py - 1 ? (by + 1) * px + bx : -1;
       off += 3 * s.plane;
       c->subs.push_back(s);
       c->maxlen = std::max(c->maxlen, std::max(s.nx, s.ny));
@@ -359,40 +374,106 @@ int sbp_decomp_create(const sbp_desc* desc, int px, int py, sbp_decomp** out) {
     for (long long i = bx * NX / px; i < (bx + 1) * NX / px; i++) xsub[i] = bx;
   for (int by = 0; by < py; by++)
     for (long long j = by * NY / py; j < (by + 1) * NY / py; j++) ysub[j] = by;
-  std::vector<DecompTile> tiles;
+  std::vector<FxTile> tiles;
   for (int b = 0; b < px * py; b++)
-    for (int j0 = 0; j0 < c->subs[b].ny; j0 += kDTY)
-      for (int i0 = 0; i0 < c->subs[b].nx; i0 += kDTX) tiles.push_back(DecompTile{b, i0, j0, 0});
+    for (int j0 = 0; j0 < c->subs[b].ny; j0 += c->ty)
+      for (int i0 = 0; i0 < c->subs[b].nx; i0 += kWaveTX) tiles.push_back(FxTile{b, i0, j0, 0});
   c->ntiles = (int)tiles.size();
+  const int nsub = px * py;
+  // each tile's geometry block: the compute warps' FxGeom, the tile origin and the
+  // neighbours' arrays the fused exchange writes into
+  std::vector<unsigned char> tinfo(tiles.size() * kFxTileInfoBytes, 0);
+  for (size_t t = 0; t < tiles.size(); t++) {
+    const FxSub& S = c->subs[tiles[t].sub];
+    FxTileInfo info{};
+    info.g = FxGeom{S.nx, S.ny, S.xoff, S.yoff, c->col0, c->sw, S.pitch, S.plane, S.base};
+    info.i0 = tiles[t].i0;
+    info.j0 = tiles[t].j0;
+    for (int side = 0; side < 4; side++) {
+      info.nb[side] = FxNbr{0, 0, 0, -1, 0};
+      if (S.nbr[side] >= 0) {
+        const FxSub& N = c->subs[S.nbr[side]];
+        info.nb[side] = FxNbr{N.base, N.pitch, N.plane, side < 2 ? N.nx : N.ny, 0};
+      }
+    }
+    std::memcpy(&tinfo[t * kFxTileInfoBytes], &info, sizeof(info));
+  }
   const size_t bytes = (size_t)c->pool * sizeof(double);
-  if (cudaMalloc(&c->d_subs, c->subs.size() * sizeof(DecompSub)) != cudaSuccess ||
-      cudaMalloc(&c->d_tiles, tiles.size() * sizeof(DecompTile)) != cudaSuccess ||
+  if (cudaMalloc(&c->d_subs, c->subs.size() * sizeof(FxSub)) != cudaSuccess ||
+      cudaMalloc(&c->d_tiles, tiles.size() * sizeof(FxTile)) != cudaSuccess ||
+      cudaMalloc(&c->d_tinfo, tinfo.size()) != cudaSuccess ||
+      cudaMalloc(&c->d_maps, 11 * (size_t)nsub * sizeof(CUtensorMap)) != cudaSuccess ||
       cudaMalloc(&c->d_xsub, NX * sizeof(int)) != cudaSuccess || cudaMalloc(&c->d_ysub, NY * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&c->d_err, sizeof(int)) != cudaSuccess || cudaMalloc(&c->d_sched, 2 * sizeof(int)) != cudaSuccess ||
       cudaMalloc(&c->un, bytes) != cudaSuccess || cudaMalloc(&c->acc, bytes) != cudaSuccess ||
       cudaMalloc(&c->wa, bytes) != cudaSuccess || cudaMalloc(&c->wb, bytes) != cudaSuccess ||
       cudaMalloc(&c->io, (size_t)NX * NY * 3 * sizeof(double)) != cudaSuccess)
     return cfail(SBP_ERR_CUDA, "cudaMalloc");
-  // zeroed pools: ghost cells outside the grid are never read, but stay defined
+  // TMA maps per subdomain: the p/u/v boxes of each possible stage input, then u^n and acc
+  const int HX = c->col0, HY = c->sw, TY = c->ty;
+  const cuuint32_t boxP[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)(TY + 2 * HY), 1};
+  const cuuint32_t boxU[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)TY, 1};
+  const cuuint32_t boxV[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)(TY + 2 * HY), 1};
+  const cuuint32_t boxPt[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)TY, 3};
+  std::vector<CUtensorMap> maps(11 * (size_t)nsub);
+  double* inbufs[3] = {c->un, c->wa, c->wb};
+  bool ok = true;
+  for (int w = 0; w < 3; w++)
+    for (int b = 0; b < nsub; b++) {
+      CUtensorMap* mm = &maps[((size_t)w * nsub + b) * 3];
+      ok = ok && encode_sub(enc, inbufs[w], c->subs[b], c->col0, c->sw, boxP, &mm[0]) &&
+           encode_sub(enc, inbufs[w], c->subs[b], c->col0, c->sw, boxU, &mm[1]) &&
+           encode_sub(enc, inbufs[w], c->subs[b], c->col0, c->sw, boxV, &mm[2]);
+    }
+  for (int b = 0; b < nsub; b++) {
+    CUtensorMap* mm = &maps[9 * (size_t)nsub + 2 * (size_t)b];
+    ok = ok && encode_sub(enc, c->un, c->subs[b], c->col0, c->sw, boxPt, &mm[0]) &&
+         encode_sub(enc, c->acc, c->subs[b], c->col0, c->sw, boxPt, &mm[1]);
+  }
+  if (!ok) return cfail(SBP_ERR_CUDA, "cuTensorMapEncodeTiled failed for a subdomain");
+  // zeroed pools: ghost cells outside the grid are never used, but stay defined
   if (cudaMemset(c->un, 0, bytes) != cudaSuccess || cudaMemset(c->acc, 0, bytes) != cudaSuccess ||
       cudaMemset(c->wa, 0, bytes) != cudaSuccess || cudaMemset(c->wb, 0, bytes) != cudaSuccess ||
-      cudaMemcpy(c->d_subs, c->subs.data(), c->subs.size() * sizeof(DecompSub), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(c->d_tiles, tiles.data(), tiles.size() * sizeof(DecompTile), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess || cudaMemset(c->d_sched, 0, 2 * sizeof(int)) != cudaSuccess ||
+      cudaMemcpy(c->d_subs, c->subs.data(), c->subs.size() * sizeof(FxSub), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(c->d_tiles, tiles.data(), tiles.size() * sizeof(FxTile), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(c->d_tinfo, tinfo.data(), tinfo.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(c->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(c->d_xsub, xsub.data(), NX * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(c->d_ysub, ysub.data(), NY * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
     return cfail(SBP_ERR_CUDA, "set-up copies");
+  const cudaError_t ce =
+      desc->order == 2 ? configure_dec<2>() : (desc->order == 4 ? configure_dec<4>() : configure_dec<6>());
+  if (ce != cudaSuccess) return cfail(SBP_ERR_CUDA, "shared-memory opt-in of the stage kernels");
+  if (cudaDeviceSynchronize() != cudaSuccess) return cfail(SBP_ERR_CUDA, "set-up");
   const double hix = (NX - 1) / (desc->xr[0] - desc->xl[0]), hiy = (NY - 1) / (desc->xr[1] - desc->xl[1]);
   DecompParams& P = c->prm;
   P.NX = (int)NX;
   P.NY = (int)NY;
   P.sw = c->sw;
+  P.col0 = c->col0;
   P.px = px;
   P.py = py;
-  P.bc = desc->bc == SBP_BC_CHARACTERISTIC ? BC_CHARACTERISTIC : BC_FREE_SURFACE;
-  decomp_taps(P.dx, desc->order, -hix);
-  decomp_taps(P.dy, desc->order, -hiy);
-  P.bwx = hix * op.hinv0;
-  P.bwy = hiy * op.hinv0;
   P.subs = c->d_subs;
+  WaveParams<double>& W = c->wprm;
+  std::memset(&W, 0, sizeof(W));
+  W.nx = (int)NX;  // the global grid: closure regions and SAT faces
+  W.ny = (int)NY;
+  W.un = c->un;
+  W.acc = c->acc;
+  decomp_taps(W.dx, desc->order, -hix);
+  decomp_taps(W.dy, desc->order, -hiy);
+  W.bwx = hix * op.hinv0;
+  W.bwy = hiy * op.hinv0;
+  W.bc = desc->bc == SBP_BC_CHARACTERISTIC ? BC_CHARACTERISTIC : BC_FREE_SURFACE;
+  W.hix = hix;
+  W.hiy = hiy;
+  W.err = c->d_err;
+  W.sched = c->d_sched;
+  W.dtiles = c->d_tiles;
+  W.dtinfo = c->d_tinfo;
+  W.dsubs = c->d_subs;
+  W.dntiles = c->ntiles;
   *out = c;
   return SBP_OK;
 }
@@ -451,27 +532,42 @@ int sbp_decomp_rhs(sbp_decomp* c, const double* src, double* dst, int where) {
   } else {
     DCK(scatter(c, nullptr, dst, c->wb));
   }
-  DCK(cudaStreamSynchronize(c->stream));
-  return SBP_OK;
+  return finish(c);
 }
 
 int sbp_decomp_rk4_resident(sbp_decomp* c, double dt, long long nsteps) {
   if (!c || nsteps < 0 || !(dt > 0)) return SBP_ERR_INVALID;
   cudaSetDevice(c->d.device);
-  // classical RK4 (code/include/time_stepping/time_stepping.h:127-142), a ghost
-  // update of each stage input before its stage
-  for (long long n = 0; n < nsteps; n++) {
-    DCK(halo(c, c->un));
-    DCK(stage(c, ST_FIRST, c->un, c->wa, nullptr, dt / 6, 0.5 * dt));
-    DCK(halo(c, c->wa));
-    DCK(stage(c, ST_MID, c->wa, c->wb, nullptr, dt / 3, 0.5 * dt));
-    DCK(halo(c, c->wb));
-    DCK(stage(c, ST_MID, c->wb, c->wa, nullptr, dt / 3, dt));
-    DCK(halo(c, c->wa));
-    DCK(stage(c, ST_LAST, c->wa, nullptr, nullptr, dt / 6, 0.0));
+  // u^n's ghost lines from its neighbours once (after sbp_decomp_set_state they are
+  // stale); from there each stage keeps the next stage input's ghosts current
+  DCK(halo(c, c->un));
+  // chunks of up to 50 steps captured once as a CUDA graph (4 launches a step)
+  const long long chunk = 50;
+  long long left = nsteps;
+  while (left > 0) {
+    const long long n = left < chunk ? left : chunk;
+    if (!c->graph || c->graph_steps != n || c->graph_dt != dt) {
+      if (c->graph) cudaGraphExecDestroy(c->graph);
+      c->graph = nullptr;
+      cudaGraph_t g = nullptr;
+      DCK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = cudaSuccess;
+      for (long long k = 0; k < n && e == cudaSuccess; k++) e = enqueue_step(c, dt);
+      const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+      if (e != cudaSuccess || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return dfail(c, SBP_ERR_CUDA, cudaGetErrorString(e != cudaSuccess ? e : ce));
+      }
+      const cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
+      cudaGraphDestroy(g);
+      DCK(ie);
+      c->graph_steps = n;
+      c->graph_dt = dt;
+    }
+    DCK(cudaGraphLaunch(c->graph, c->stream));
+    left -= n;
   }
-  DCK(cudaStreamSynchronize(c->stream));
-  return SBP_OK;
+  return finish(c);
 }
 
 }  // extern "C"

@@ -51,6 +51,9 @@ template <typename T, int KIND, int STAGE> constexpr bool wave_fixed() {
   return SBP_FP64_FIXED != 0 && sizeof(T) == 8 && KIND == WK_HOM && !is_rkf_stage(STAGE);
 }
 
+struct FxSub;   // a subdomain of a decomposed grid (wave2d_fixed.cuh)
+struct FxTile;  // a tile of a decomposed grid (wave2d_fixed.cuh)
+
 template <typename T> struct WaveParams {
   int nx, ny;
   long long pitch;    // elements per row
@@ -101,6 +104,15 @@ template <typename T> struct WaveParams {
   // walks the tiles with a fixed stride (the Fehlberg stages always do, so their
   // per-CTA error partials keep a fixed summation order).
   int* sched;
+  // Decomposed grid (wave_fixed_kernel<.., true>): the tile list, the subdomains,
+  // and per subdomain the TMA maps of the stage input's p, u, v boxes ([sub][3])
+  // and the point maps of u^n and acc ([sub][2]), all in device memory.
+  const FxTile* dtiles;
+  const FxSub* dsubs;
+  const unsigned char* dtinfo;  // per tile its FxTileInfo block (kFxTileInfoBytes each)
+  const CUtensorMap* dmaps_in;
+  const CUtensorMap* dmaps_na;
+  int dntiles;
 };
 
 constexpr int kWaveTX = 64;            // tile width (x, contiguous)
@@ -231,7 +243,12 @@ struct WaveTile {
   // per converter warp (int[8][8][2], +128) when converter warps convert, or one
   // shared pair (int[8][2]) when the compute warps do.
   static constexpr int OFF_FX = OFF_BAR + 256;
-  static constexpr int SMEM = OFF_BAR + 256 + (FIX_ ? 640 : 0);
+  // Decomposed grids: eight 192-byte slots of tile geometry (that of its subdomain's
+  // neighbours included): one per ring stage, the rest the exchange queue; then the
+  // exchange queue's barriers (full[8] at +0, empty[8] at +64)
+  static constexpr int OFF_TINFO = OFF_FX + 640;
+  static constexpr int OFF_XBAR = OFF_TINFO + 8 * 192;
+  static constexpr int SMEM = OFF_BAR + 256 + (FIX_ ? 640 + 8 * 192 + 128 : 0);
   static constexpr uint32_t TX_BYTES = BYTES_P + BYTES_U + BYTES_V + (LOAD_UN ? BYTES_PT : 0) +
                                        (LOAD_ACC ? BYTES_PT : 0) + (LOAD_COMP ? BYTES_PT : 0) +
                                        (LOAD_COEF ? BYTES_K : 0) + PRM_BYTES;
@@ -656,7 +673,7 @@ __device__ __forceinline__ void wave_produce(const CUtensorMap& mapP, const CUte
   }
   // the CTA must not exit with copies in flight: wait for the last NST stages
   for (int kk = (k >= NST ? k - NST : 0); kk < k; kk++)
-    mbar_wait_bounded(&full[kk % NST], (kk / NST) & 1, prm.wait_ns);
+    if (!mbar_wait_bounded(&full[kk % NST], (kk / NST) & 1, prm.wait_ns)) atomicOr(prm.err, ERR_TMA_TIMEOUT);
   if (dyn) {  // every CTA has stopped taking tiles when the last one gets here
     __threadfence();
     if (atomicAdd(prm.sched + 1, 1) == (int)gridDim.x - 1) {
@@ -743,8 +760,9 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
         if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
         break;
       }
-      wave_tile_fixed<ORD, STAGE, Tile>(prm, prm.in, prm.wout, smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane,
-                                        emax[0], emax[1], bad, &dbar[b], &dphase, b, k);
+      const FxGeom g{prm.nx, prm.ny, 0, 0, 0, 0, prm.pitch, prm.plane, 0};
+      wave_tile_fixed<ORD, STAGE, Tile>(prm, g, prm.wout, smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane, emax[0],
+                                        emax[1], bad, &dbar[b], &dphase, b, k);
       // the converted boxes were written through the generic proxy; order those writes
       // before the TMA (async proxy) refills the stage
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

@@ -158,27 +158,301 @@ __device__ __forceinline__ bool fx_convert_tile(unsigned char* st, uint64_t* fxa
   return true;
 }
 
-// One tile of a fixed-point FP64 stage for the consumer warps. The stage's p,
-// u, v boxes hold int64 (fx_convert_tile); u^n, acc are FP64 point boxes.
+// Where a tile's points live: the interior extent of the arrays holding them
+// (the grid, or one subdomain of a decomposed grid), the global index of their
+// first interior point, that point's array column and row (ghost lines before
+// it), the row pitch, the component plane and the arrays' offset in the stage's
+// buffers. The single grid: offsets zero, the arrays the whole buffers.
+struct FxGeom {
+  int nx, ny;
+  int xoff, yoff;
+  int col0, row0;
+  long long pitch, plane, base;
+};
+
+// A subdomain of a decomposed grid: its interior points, the global index of its
+// first interior point, and its arrays (row pitch, component plane, offset in the
+// stage's buffers). Its first interior point sits at array column Tile::HX (the x
+// ghost width, rounded up so every TMA x coordinate is 16-byte aligned) and row
+// Tile::HY; the R ghost lines next to the interior hold the neighbours' values.
+struct FxSub {
+  int nx, ny, xoff, yoff;
+  long long pitch, plane, base;
+  int nbr[4];  // the neighbouring subdomain to the west, east, south, north, or -1
+};
+struct FxTile {
+  int sub, i0, j0, pad;  // subdomain and tile origin in its interior indices
+};
+
+// A decomposed grid's tile as the producer hands it to the compute warps through
+// shared memory (its geometry and origin), so they need no global loads per tile.
+// A neighbour's arrays as a stage writes into its ghost lines: offset, row pitch,
+// component plane and its interior extent across the shared edge (nx for a
+// west/east neighbour, ny for a south/north one); n < 0 for none.
+struct FxNbr {
+  long long base, pitch, plane;
+  int n, pad;
+};
+struct FxTileInfo {
+  FxGeom g;
+  int i0, j0;
+  FxNbr nb[4];  // west, east, south, north
+};
+// Each tile's block in device memory (built by the host) and in a ring stage's slot:
+// 192 bytes, a multiple of 16 for the bulk copy.
+constexpr int kFxTileInfoBytes = 192;
+static_assert(sizeof(FxTileInfo) <= kFxTileInfoBytes, "tile information slot");
+
+// Decomposed grids: the halo exchange fused into the stages that produce the next
+// stage input (the reference's VecScatter ghost update,
+// code/src/scatter/scatter_ctx.cpp:149-211). Once a tile is done, each of its points
+// within R of an edge shared with a neighbour copies its new value (w, or u^n in the
+// last stage) into the neighbour's ghost line that mirrors it, so the next stage finds
+// every ghost it reads without a separate exchange. Run by the 32 lanes of the
+// exchange warp after the compute warps released the tile. The copies are enumerated
+// side by side (each side's strip of the tile, component-major), and each lane issues
+// U loads before its U stores, so one batch costs about two memory latencies.
+template <typename Tile, int STAGE>
+__device__ __forceinline__ void fx_exchange_tile(const WaveParams<double>& prm, const FxTileInfo& T, int lane) {
+  constexpr int R = Tile::R, TY = Tile::TY, COL0 = Tile::HX, U = 4;
+  const FxGeom& g = T.g;
+  const int ie = min(T.i0 + kWaveTX, g.nx), je = min(T.j0 + TY, g.ny);
+  // each side's strip of the tile, in the subdomain's interior indices: columns
+  // [T.i0, iw) west, [ia, ie) east, rows [T.j0, js) south, [ja, je) north; the
+  // strips of the sides without a neighbour are empty
+  const int iw = min(ie, R), ia = max(T.i0, g.nx - R), js = min(je, R), ja = max(T.j0, g.ny - R);
+  const int rows = je - T.j0, cols = ie - T.i0;
+  const int c0 = T.nb[0].n >= 0 && iw > T.i0 ? 3 * (iw - T.i0) * rows : 0;
+  const int c1 = T.nb[1].n >= 0 && ie > ia ? 3 * (ie - ia) * rows : 0;
+  const int c2 = T.nb[2].n >= 0 && js > T.j0 ? 3 * cols * (js - T.j0) : 0;
+  const int c3 = T.nb[3].n >= 0 && je > ja ? 3 * cols * (je - ja) : 0;
+  const int total = c0 + c1 + c2 + c3;
+  if (total == 0) return;
+  double* obuf = STAGE == ST_LAST ? prm.un : prm.wout;
+  for (int e0 = 0; e0 < total; e0 += 32 * U) {
+    double v[U];
+    long long dst[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      int e = e0 + lane + 32 * u;
+      dst[u] = -1;
+      if (e >= total) continue;
+      int s, x0, w, y0, h;  // the side and its strip
+      if (e < c0) {
+        s = 0, x0 = T.i0, w = iw - T.i0, y0 = T.j0, h = rows;
+      } else if ((e -= c0) < c1) {
+        s = 1, x0 = ia, w = ie - ia, y0 = T.j0, h = rows;
+      } else if ((e -= c1) < c2) {
+        s = 2, x0 = T.i0, w = cols, y0 = T.j0, h = js - T.j0;
+      } else {
+        e -= c2;
+        s = 3, x0 = T.i0, w = cols, y0 = ja, h = je - ja;
+      }
+      const int wh = w * h, c = e / wh, r = e - c * wh, j = y0 + r / w, i = x0 + r % w;
+      v[u] = obuf[g.base + c * g.plane + (long long)(j + g.row0) * g.pitch + (i + g.col0)];
+      const FxNbr& N = T.nb[s];
+      const long long row = s == 0 || s == 1 ? j + g.row0 : (s == 2 ? N.n + j + g.row0 : j - g.ny + g.row0);
+      const int col = s == 0 ? N.n + i + COL0 : (s == 1 ? i - g.nx + COL0 : i + COL0);
+      dst[u] = N.base + c * N.plane + row * N.pitch + col;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      if (dst[u] >= 0) obuf[dst[u]] = v[u];
+  }
+}
+
+// The threads of a fixed-point stage kernel: compute, converter and producer warps,
+// and on a decomposed grid the exchange warp.
+template <typename Tile, bool DEC>
+constexpr int fx_kernel_threads() {
+  return Tile::THREADS + (DEC ? 32 : 0);
+}
+
+// The exchange queue of a decomposed grid: the producer hands each released tile's
+// geometry block to the exchange warp through the shared-memory slots after the NST
+// ring stages' ones (Tile::OFF_TINFO), with a full/empty barrier pair per slot.
+template <typename Tile>
+struct FxExchangeQueue {
+  static constexpr int SLOTS = 8 - Tile::NST;
+  static_assert(SLOTS >= 2, "the tile geometry area leaves the exchange queue too few slots");
+  unsigned char* slot0;
+  uint64_t* full;
+  uint64_t* empty;
+  __device__ FxExchangeQueue(unsigned char* smem)
+      : slot0(smem + Tile::OFF_TINFO + kFxTileInfoBytes * Tile::NST),
+        full(reinterpret_cast<uint64_t*>(smem + Tile::OFF_XBAR)),
+        empty(reinterpret_cast<uint64_t*>(smem + Tile::OFF_XBAR + 64)) {}
+  __device__ FxTileInfo* slot(int s) const { return reinterpret_cast<FxTileInfo*>(slot0 + kFxTileInfoBytes * s); }
+  // Push number q (all 32 lanes of the producer warp): the geometry block `from`, or
+  // the end marker (i0 = -1) for nullptr. False if the wait for a free slot ran out.
+  __device__ bool push(int q, const unsigned char* from, int lane, const WaveParams<double>& prm) const {
+    const int s = q % SLOTS;
+    if (q >= SLOTS && !mbar_wait_bounded(&empty[s], ((q / SLOTS) - 1) & 1, prm.wait_ns)) {
+      if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
+      return false;
+    }
+    int4* to = reinterpret_cast<int4*>(slot(s));
+    if (from) {
+      if (lane < kFxTileInfoBytes / 16) to[lane] = reinterpret_cast<const int4*>(from)[lane];
+    } else if (lane == 0) {
+      slot(s)->i0 = -1;
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&full[s]);
+    return true;
+  }
+};
+
+// The exchange warp of a decomposed grid: takes the released tiles' geometry blocks
+// from the exchange queue and runs their fused exchange, until the end marker. The
+// compute warps' stores reach it through the ring stage's `empty` barrier and the
+// queue's `full` barrier. Every wait is bounded.
+template <typename Tile, int STAGE>
+__device__ __forceinline__ void decomp_exchange(const WaveParams<double>& prm, const FxExchangeQueue<Tile>& xq,
+                                                int lane) {
+  constexpr int SLOTS = FxExchangeQueue<Tile>::SLOTS;
+  for (int q = 0;; q++) {
+    const int s = q % SLOTS;
+    if (!mbar_wait_bounded(&xq.full[s], (q / SLOTS) & 1, prm.wait_ns)) {
+      if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
+      return;
+    }
+    const FxTileInfo& T = *xq.slot(s);
+    if (T.i0 < 0) return;
+    fx_exchange_tile<Tile, STAGE>(prm, T, lane);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&xq.empty[s]);
+  }
+}
+
+// The producer warp of a decomposed grid: lane 0 takes the tiles (dynamic queue or
+// fixed stride) and issues each stage's loads -- TMA boxes with the maps of the tile's
+// subdomain, and the tile's geometry block by a bulk copy on the stage's barrier --
+// reading the next tile's descriptor one tile ahead. In the stages that produce the
+// next stage input, each tile the compute warps release goes to the exchange queue
+// (its geometry block copied by the 32 lanes) before its ring stage is refilled; the
+// tiles still held at the end follow after their release, then the end marker.
+// Every wait is bounded.
+template <typename Tile, int STAGE>
+__device__ __forceinline__ void decomp_produce(const WaveParams<double>& prm, unsigned char* smem, uint64_t* full,
+                                               uint64_t* empty, int* tslot, const FxExchangeQueue<Tile>& xq,
+                                               int lane) {
+  constexpr int HY = Tile::HY, HX = Tile::HX, NST = Tile::NST;
+  constexpr bool EXCH = STAGE == ST_FIRST || STAGE == ST_MID || STAGE == ST_LAST;
+  const int ntiles = prm.dntiles;
+  const bool dyn = prm.sched != nullptr;
+  const unsigned char* tinfo = smem + Tile::OFF_TINFO;
+  int k = 0, issued = 0, pushed = 0, sent = 0;  // sent: stage phases begun, the end marker's included
+  int tile = 0;
+  FxTile next{0, 0, 0, 0};
+  if (lane == 0) {
+    tile = dyn ? atomicAdd(prm.sched, 1) : (int)blockIdx.x;
+    if (tile < ntiles) next = prm.dtiles[tile];
+  }
+  tile = __shfl_sync(0xffffffffu, tile, 0);
+  bool ok = true;
+  for (;; k++) {
+    const int b = k % NST;
+    if (k >= NST) {
+      if (!mbar_wait_bounded(&empty[b], ((k / NST) - 1) & 1, prm.wait_ns)) {
+        if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
+        ok = false;
+        break;
+      }
+      if constexpr (EXCH) {  // the tile this stage held is done: to the exchange warp
+        if (!xq.push(pushed, tinfo + kFxTileInfoBytes * b, lane, prm)) {
+          ok = false;
+          break;
+        }
+        pushed++;
+      }
+    }
+    if (tile >= ntiles) {
+      if (lane == 0) {
+        tslot[b] = -1;
+        mbar_arrive(&full[b]);
+      }
+      sent = k + 1;
+      break;
+    }
+    if (lane == 0) {
+      tslot[b] = tile;
+      const int cur = tile;
+      const FxTile t = next;
+      tile = dyn ? atomicAdd(prm.sched, 1) : tile + (int)gridDim.x;
+      if (tile < ntiles) next = prm.dtiles[tile];  // in flight while this tile's loads are issued
+      const CUtensorMap* in = prm.dmaps_in + 3 * t.sub;
+      const CUtensorMap* na = prm.dmaps_na + 2 * t.sub;
+      unsigned char* st = smem + b * Tile::STAGE_BYTES;
+      // array coordinates: the interior starts at column HX, row HY
+      const int x = t.i0, y = t.j0;
+      mbar_arrive_expect_tx(&full[b], Tile::TX_BYTES + kFxTileInfoBytes);
+      bulk_copy_g2s(smem + Tile::OFF_TINFO + kFxTileInfoBytes * b, prm.dtinfo + (long long)kFxTileInfoBytes * cur,
+                    kFxTileInfoBytes, &full[b]);
+      tma_load_3d(st, &in[0], x, y, 2, &full[b]);                     // p: origin (HX + i0 - HX, HY + j0 - HY)
+      tma_load_3d(st + Tile::OFF_U, &in[1], x, y + HY, 0, &full[b]);  // u: x halo only
+      tma_load_3d(st + Tile::OFF_V, &in[2], x + HX, y, 1, &full[b]);  // v: y halo only
+      if (Tile::LOAD_UN) tma_load_3d(st + Tile::OFF_N, &na[0], x + HX, y + HY, 0, &full[b]);
+      if (Tile::LOAD_ACC) tma_load_3d(st + Tile::OFF_A, &na[1], x + HX, y + HY, 0, &full[b]);
+    }
+    tile = __shfl_sync(0xffffffffu, tile, 0);
+    issued = sent = k + 1;
+  }
+  if constexpr (EXCH) {
+    // the tiles still held: to the exchange warp after their release; then the end marker
+    for (int kk = pushed; ok && kk < issued; kk++) {
+      if (!mbar_wait_bounded(&empty[kk % NST], (kk / NST) & 1, prm.wait_ns)) {
+        if (lane == 0) atomicOr(prm.err, ERR_TMA_TIMEOUT);
+        ok = false;
+        break;
+      }
+      ok = xq.push(pushed, tinfo + kFxTileInfoBytes * (kk % NST), lane, prm);
+      pushed += ok;
+    }
+    if (ok) xq.push(pushed, nullptr, lane, prm);  // else the exchange warp's own wait runs out
+  }
+  if (lane == 0) {
+    // the CTA must not exit with copies in flight
+    for (int kk = (sent >= NST ? sent - NST : 0); kk < sent; kk++)
+      if (!mbar_wait_bounded(&full[kk % NST], (kk / NST) & 1, prm.wait_ns)) atomicOr(prm.err, ERR_TMA_TIMEOUT);
+    if (dyn) {
+      __threadfence();
+      if (atomicAdd(prm.sched + 1, 1) == (int)gridDim.x - 1) {
+        atomicExch(prm.sched, 0);
+        atomicExch(prm.sched + 1, 0);
+      }
+    }
+  }
+}
+
+// One tile of a fixed-point FP64 stage for the compute warps: tile origin (i0, j0)
+// in the arrays' interior indices. The stage's p, u, v boxes hold int64
+// (converted by the converter warps); u^n, acc are FP64 point boxes. Closure rows
+// and SAT faces follow the global indices I = xoff + i, J = yoff + j (prm.nx,
+// prm.ny: the global grid); interior stencils read across subdomain edges from
+// the ghost lines the boxes include.
 template <int ORD, int STAGE, typename Tile>
-__device__ __forceinline__ void wave_tile_fixed(const WaveParams<double>& prm, const double* __restrict__ in,
-                                                double* wout, const unsigned char* st, const int i0, const int j0,
-                                                const int warp, const int lane, const int ep, const int euv,
-                                                const bool bad, uint64_t* dbar, uint32_t* dphase, const int b,
-                                                const int k) {
+__device__ __forceinline__ void wave_tile_fixed(const WaveParams<double>& prm, const FxGeom& g, double* wout,
+                                                const unsigned char* st, const int i0, const int j0, const int warp,
+                                                const int lane, const int ep, const int euv, const bool bad,
+                                                uint64_t* dbar, uint32_t* dphase, const int b, const int k) {
   constexpr int TY = Tile::TY, CS = OpShape<ORD>::CS;
   constexpr int HX = Tile::HX, HY = Tile::HY, PW = Tile::PW;
   constexpr int ROWS = TY / Tile::WARPS;
   constexpr int TPT = TY * kWaveTX;
-  const int nx = prm.nx, ny = prm.ny;
-  const long long pitch = prm.pitch, plane = prm.plane;
+  const int NX = prm.nx, NY = prm.ny;
+  const long long pitch = g.pitch, plane = g.plane;
+  const double* in = prm.in + g.base;
   const long long* iP = reinterpret_cast<const long long*>(st);
   const long long* iU = reinterpret_cast<const long long*>(st + Tile::OFF_U);
   const long long* iV = reinterpret_cast<const long long*>(st + Tile::OFF_V);
   const double* sN = reinterpret_cast<const double*>(st + Tile::OFF_N);
   const double* sA = reinterpret_cast<const double*>(st + Tile::OFF_A);
   double* sD = reinterpret_cast<double*>(const_cast<unsigned char*>(st) + Tile::OFF_DEF);
-  const bool xfaces = dbar != nullptr && prm.bc != BC_NONE && (i0 == 0 || (nx - 1 >= i0 && nx - 1 < i0 + kWaveTX));
+  // x faces of the global grid inside this tile (their SAT goes to the deferred pass)
+  const int iw = -g.xoff, ie = NX - 1 - g.xoff;  // local indices of global columns 0 and NX - 1
+  const bool xfaces = dbar != nullptr && prm.bc != BC_NONE &&
+                      ((iw >= i0 && iw < i0 + kWaveTX) || (ie >= i0 && ie < i0 + kWaveTX && ie < g.nx));
   const double sg[3] = {prm.fx_sig[0], prm.fx_sig[1], prm.fx_sig[0]};
   const int ebp = ep + 11, ebuv = euv + 11;  // fx_to's exponent bases
   (void)sN;
@@ -187,47 +461,53 @@ __device__ __forceinline__ void wave_tile_fixed(const WaveParams<double>& prm, c
   for (int rr = 0; rr < ROWS; rr++) {
     const int y = warp * ROWS + rr;
     const int j = j0 + y;
-    if (j >= ny) continue;
-    const bool yint = (j >= CS) && (j < ny - CS);
+    if (j >= g.ny) continue;
+    const int J = g.yoff + j;
+    const bool yint = (J >= CS) && (J < NY - CS);
+    const long long rowq = (long long)(j + g.row0) * pitch;
 #pragma unroll
     for (int cc = 0; cc < kWaveTX / 32; cc++) {
       const int x = lane + 32 * cc;
       const int i = i0 + x;
-      if (i >= nx) continue;
-      const bool xint = (i >= CS) && (i < nx - CS);
+      if (i >= g.nx) continue;
+      const int I = g.xoff + i;
+      const bool xint = (I >= CS) && (I < NX - CS);
       const long long* cP = iP + (y + HY) * PW + (x + HX);
       const long long* cU = iU + y * PW + (x + HX);
       const long long* cV = iV + (y + HY) * kWaveTX + x;
+      // closure lines start at the global first point of the line (inside the arrays
+      // for a subdomain at the physical boundary, which holds a whole closure block)
+      const double* xline = in + rowq + g.col0 - g.xoff;
+      const double* yline = in + (long long)(g.row0 - g.yoff) * pitch + (i + g.col0);
       // RHS in units of sigma per component: F_u = sx ku, F_v = sy kv, F_p = sx kp
       double ku, kv, kp;
       if (xint) {
         ku = fx_to(fx_stencil<ORD>(cP, 1), ebp);
       } else {
-        ku = closure_line<double, ORD>(in + 2 * plane + (long long)j * pitch, 1, nx, i, prm.dx.cls) * prm.fx_isig[0];
+        ku = closure_line<double, ORD>(xline + 2 * plane, 1, NX, I, prm.dx.cls) * prm.fx_isig[0];
       }
       if (yint) {
         kv = fx_to(fx_stencil<ORD>(cP, PW), ebp);
       } else {
-        kv = closure_line<double, ORD>(in + 2 * plane + i, pitch, ny, j, prm.dy.cls) * prm.fx_isig[1];
+        kv = closure_line<double, ORD>(yline + 2 * plane, pitch, NY, J, prm.dy.cls) * prm.fx_isig[1];
       }
       if (xint && yint && prm.fx_square) {
         kp = fx_to(fx_stencil<ORD>(cU, 1) + fx_stencil<ORD>(cV, kWaveTX), ebuv);
       } else {
         const double ax = xint ? fx_to(fx_stencil<ORD>(cU, 1), ebuv)
-                               : closure_line<double, ORD>(in + (long long)j * pitch, 1, nx, i, prm.dx.cls) *
-                                     prm.fx_isig[0];
+                               : closure_line<double, ORD>(xline, 1, NX, I, prm.dx.cls) * prm.fx_isig[0];
         const double ay = yint ? fx_to(fx_stencil<ORD>(cV, kWaveTX), ebuv)
-                               : closure_line<double, ORD>(in + plane + i, pitch, ny, j, prm.dy.cls) * prm.fx_isig[1];
+                               : closure_line<double, ORD>(yline + plane, pitch, NY, J, prm.dy.cls) * prm.fx_isig[1];
         kp = fma(prm.fx_rho, ay, ax);
       }
       if (bad) ku = kv = kp = __longlong_as_double(0x7FF8000000000000ll);
 
-      const long long q = (long long)j * pitch + i;
+      const long long q = rowq + i + g.col0;
       const int sp = y * kWaveTX + x;  // point within a 3-component smem box
-      const bool edge = (i == 0) || (j == 0) || (i == nx - 1) || (j == ny - 1);
+      const bool edge = (I == 0) || (J == 0) || (I == NX - 1) || (J == NY - 1);
       if (prm.bc != BC_NONE && edge) {
-        if (xfaces && j != 0 && j != ny - 1) {
-          double* d = sD + ((i == 0 ? 0 : TY) + y) * 3;  // an x-face point only: deferred
+        if (xfaces && J != 0 && J != NY - 1) {
+          double* d = sD + ((I == 0 ? 0 : TY) + y) * 3;  // an x-face point only: deferred
           d[0] = ku;
           d[1] = kv;
           d[2] = kp;
@@ -236,20 +516,20 @@ __device__ __forceinline__ void wave_tile_fixed(const WaveParams<double>& prm, c
         // SAT and the stage update in true units
         const double pc = in[2 * plane + q], uc = in[q], vc = in[plane + q];
         const Rhs3<double> r =
-            apply_sat<double, WK_HOM>(prm, in, i, j, pc, uc, vc, Rhs3<double>{sg[0] * ku, sg[1] * kv, sg[2] * kp});
+            apply_sat<double, WK_HOM>(prm, in, I, J, pc, uc, vc, Rhs3<double>{sg[0] * ku, sg[1] * kv, sg[2] * kp});
         const double kt[3] = {r.u, r.v, r.p};
 #pragma unroll
         for (int c = 0; c < 3; c++) {
           const double cen = (STAGE == ST_FIRST) ? sN[c * TPT + sp] : 0.0;
           wave_point_store<double, STAGE, Tile>(prm, wout, prm.c_acc, prm.c_w, sA, sN, nullptr, sp, c,
-                                                c * plane + q, kt[c], cen);
+                                                g.base + c * plane + q, kt[c], cen);
         }
         continue;
       }
       const double kf[3] = {ku, kv, kp};
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-        const long long o = c * plane + q;
+        const long long o = g.base + c * plane + q;
         if constexpr (STAGE == ST_RHS) {
           prm.kout[o] = sg[c] * kf[c];
         } else {
@@ -272,21 +552,21 @@ __device__ __forceinline__ void wave_tile_fixed(const WaveParams<double>& prm, c
     }
     for (int e = lane; e < 2 * TY; e += 32) {
       const int side = e / TY, y = e - side * TY, j = j0 + y;
-      const int i = side == 0 ? 0 : nx - 1;
-      if (i < i0 || i >= i0 + kWaveTX || j >= ny || j == 0 || j == ny - 1) continue;
+      const int I = side == 0 ? 0 : NX - 1, i = I - g.xoff, J = g.yoff + j;
+      if (i < i0 || i >= i0 + kWaveTX || i >= g.nx || j >= g.ny || J == 0 || J == NY - 1) continue;
       const int x = i - i0;
-      const long long q = (long long)j * pitch + i;
+      const long long q = (long long)(j + g.row0) * pitch + i + g.col0;
       const double pc = in[2 * plane + q], uc = in[q], vc = in[plane + q];
       const double* d = sD + (side * TY + y) * 3;
       const Rhs3<double> r =
-          apply_sat<double, WK_HOM>(prm, in, i, j, pc, uc, vc, Rhs3<double>{sg[0] * d[0], sg[1] * d[1], sg[2] * d[2]});
+          apply_sat<double, WK_HOM>(prm, in, I, J, pc, uc, vc, Rhs3<double>{sg[0] * d[0], sg[1] * d[1], sg[2] * d[2]});
       const double kt[3] = {r.u, r.v, r.p};
       const int sp = y * kWaveTX + x;
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         const double cen = (STAGE == ST_FIRST) ? sN[c * TPT + sp] : 0.0;
-        wave_point_store<double, STAGE, Tile>(prm, wout, prm.c_acc, prm.c_w, sA, sN, nullptr, sp, c, c * plane + q,
-                                              kt[c], cen);
+        wave_point_store<double, STAGE, Tile>(prm, wout, prm.c_acc, prm.c_w, sA, sN, nullptr, sp, c,
+                                              g.base + c * plane + q, kt[c], cen);
       }
     }
   }
@@ -379,8 +659,8 @@ __device__ __forceinline__ bool fx_convert_stage(unsigned char* st, uint64_t* fx
 // compute warps meet no barrier but the deferred x-face pass. Every wait is
 // bounded (prm.wait_ns); a wait that runs out sets the error word and the warp
 // stops, so the others' waits run out in turn.
-template <int ORD, int STAGE>
-__global__ void __launch_bounds__(WaveStageTile<double, ORD, WK_HOM, STAGE>::THREADS, 1)
+template <int ORD, int STAGE, bool DEC = false>
+__global__ void __launch_bounds__(fx_kernel_threads<WaveStageTile<double, ORD, WK_HOM, STAGE>, DEC>(), 1)
     wave_fixed_kernel(const __grid_constant__ CUtensorMap mapP, const __grid_constant__ CUtensorMap mapU,
                       const __grid_constant__ CUtensorMap mapV, const __grid_constant__ CUtensorMap mapN,
                       const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapC,
@@ -409,6 +689,13 @@ __global__ void __launch_bounds__(WaveStageTile<double, ORD, WK_HOM, STAGE>::THR
       mbar_init(&fxa[s], CONV);
       mbar_init(&conv[s], CONV);
     }
+    if constexpr (DEC) {
+      const FxExchangeQueue<Tile> xq(smem);
+      for (int s = 0; s < FxExchangeQueue<Tile>::SLOTS; s++) {
+        mbar_init(&xq.full[s], 1);
+        mbar_init(&xq.empty[s], 1);
+      }
+    }
     fence_barrier_init();
   }
   __syncthreads();
@@ -416,9 +703,19 @@ __global__ void __launch_bounds__(WaveStageTile<double, ORD, WK_HOM, STAGE>::THR
   const int ntx = (prm.nx + kWaveTX - 1) / kWaveTX;
 
   if (warp == WARPS + CONV) {
-    if (lane == 0)
-      wave_produce<Tile>(mapP, mapU, mapV, mapN, mapA, mapC, mapK, prm, smem, full, empty, tslot, prm.sched != nullptr);
+    if constexpr (DEC)
+      decomp_produce<Tile, STAGE>(prm, smem, full, empty, tslot, FxExchangeQueue<Tile>(smem), lane);
+    else if (lane == 0)
+      wave_produce<Tile>(mapP, mapU, mapV, mapN, mapA, mapC, mapK, prm, smem, full, empty, tslot,
+                         prm.sched != nullptr);
     return;
+  }
+  if constexpr (DEC) {
+    if (warp == WARPS + CONV + 1) {  // the exchange warp
+      if constexpr (STAGE == ST_FIRST || STAGE == ST_MID || STAGE == ST_LAST)
+        decomp_exchange<Tile, STAGE>(prm, FxExchangeQueue<Tile>(smem), lane);
+      return;
+    }
   }
   if (warp >= WARPS) {
     // ---------------- converters
@@ -451,12 +748,23 @@ __global__ void __launch_bounds__(WaveStageTile<double, ORD, WK_HOM, STAGE>::THR
     }
     const int tile = tslot[b];
     if (tile < 0) break;
-    const int i0 = (tile % ntx) * kWaveTX, j0 = (tile / ntx) * TY;
+    int i0, j0;
+    FxGeom g;
+    if constexpr (DEC) {
+      const FxTileInfo* info = reinterpret_cast<const FxTileInfo*>(smem + Tile::OFF_TINFO + kFxTileInfoBytes * b);
+      g = info->g;
+      i0 = info->i0;
+      j0 = info->j0;
+    } else {
+      i0 = (tile % ntx) * kWaveTX;
+      j0 = (tile / ntx) * TY;
+      g = FxGeom{prm.nx, prm.ny, 0, 0, 0, 0, prm.pitch, prm.plane, 0};
+    }
     int ep, euv;
     bool bad;
     fx_tile_emax<CONV>(wmax + 16 * b, ep, euv, bad);
-    wave_tile_fixed<ORD, STAGE, Tile>(prm, prm.in, prm.wout, smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane, ep,
-                                      euv, bad, &dbar[b], &dphase, b, k);
+    wave_tile_fixed<ORD, STAGE, Tile>(prm, g, prm.wout, smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane, ep, euv, bad,
+                                      &dbar[b], &dphase, b, k);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[b]);
   }

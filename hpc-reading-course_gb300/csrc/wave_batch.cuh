@@ -33,13 +33,6 @@ template <typename T> struct alignas(16) BatchWave {
 // tile boxes; [9], [10], [11] = u^n, acc, comp point boxes.
 constexpr int kBatchMaps = 12;
 
-__device__ __forceinline__ void bulk_copy_g2s(void* smem_dst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_addr(smem_dst)),
-               "l"(reinterpret_cast<uint64_t>(gsrc)), "r"(bytes), "r"(smem_addr(bar))
-               : "memory");
-}
-
 // Stage input and output buffers and RK4 coefficients of stage rk (1..4) of
 // the classical RK4 step sequence (see the single-instance runtime). The
 // coefficients come from the instance block: computing dt / 6 here would put an
@@ -135,7 +128,8 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, TY>::THREADS, 1)
         if (Tile::LOAD_COMP) tma_load_3d(st + Tile::OFF_C, &m[11], i0, j0, 0, &full[b]);
         bulk_copy_g2s(st + Tile::OFF_PRM, &insts[tt.slot], (uint32_t)sizeof(BatchWave<T>), &full[b]);
       }
-      for (int kk = (k >= 2 ? k - 2 : 0); kk < k; kk++) mbar_wait_bounded(&full[kk & 1], (kk >> 1) & 1);
+      for (int kk = (k >= 2 ? k - 2 : 0); kk < k; kk++)
+        if (!mbar_wait_bounded(&full[kk & 1], (kk >> 1) & 1)) atomicOr(err, ERR_TMA_TIMEOUT);
     }
     return;
   }
