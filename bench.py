@@ -79,6 +79,7 @@ def parse():
     ap.add_argument("--t-end", type=float, default=1.0)
     ap.add_argument("--rk45-t-end", type=float, default=0.25, help="rk45: final time")
     ap.add_argument("--grid3d", type=int, default=256, help="wave3d: points per direction")
+    ap.add_argument("--decomps", default="1x1,2x2,4x4,8x8", help="decomp: the px x py decompositions to run")
     return ap.parse_args()
 
 
@@ -564,9 +565,9 @@ def run_rk45_study(args):
 
 def run_decomp_study(args):
     """The decomposed path (sbp_decomp_*): the --grid^2 wave (rho = K = 1, order --order, FP64,
-    characteristic SAT, Gaussian pulse) as px x py subdomains with ghost lines and a halo exchange
-    before every stage, against the single-grid context; 50 RK4 steps each after 3 warm-up steps,
-    wall time around the synchronous calls, and the two results compared."""
+    characteristic SAT, Gaussian pulse) as px x py subdomains (--decomps) with ghost lines, the halo
+    exchange fused into the stage kernels, against the single-grid context; 50 RK4 steps each after
+    3 warm-up steps, wall time around the synchronous calls, and the two results compared."""
     import numpy as np
 
     import build as gpu_build
@@ -591,7 +592,7 @@ def run_decomp_study(args):
         single = c.get_state()
     out["single_grid"] = {"point_stage_per_s": 4.0 * n * n * steps / sec, "seconds": sec}
     rows = []
-    for px, py in ((1, 1), (2, 2), (4, 4), (8, 8)):
+    for px, py in (tuple(int(v) for v in d.split("x")) for d in args.decomps.split(",")):
         with sbpgpu.Decomp(order, n, n, px, py, bc=sbpgpu.BC_CHARACTERISTIC) as d:
             d.set_state(v0)
             d.step_resident(dt, steps)  # warm-up: captures the step graph

@@ -261,8 +261,10 @@ long long sbp_batch_launch_count(const sbp_batch* batch); /* kernels launched so
  * own state and R ghost lines per side, on one device. Replaces the reference's
  * decomposed path: rhs_local / rhs_all per DMDA block
  * (code/include/partitioned_rhs/rhs.h:97-181, 183-360) with the VecScatter ghost
- * update before each RHS (code/src/scatter/scatter_ctx.cpp:149-211), here a
- * device halo-exchange kernel before each RK4 stage. Subdomain widths are
+ * update before each RHS (code/src/scatter/scatter_ctx.cpp:149-211), here fused
+ * into the RK4 stage kernels: each stage writes its edge values into the
+ * neighbours' ghost lines as well (a halo kernel runs once per call, for the
+ * state it starts from). Subdomain widths are
  * floor(N*(b+1)/p) - floor(N*b/p) >= the closure width (2 / 6 / 9 points for
  * orders 2 / 4 / 6), else SBP_ERR_INVALID; other problems or FP32:
  * SBP_ERR_UNSUPPORTED. Results equal sbp_create's single grid to rounding.
@@ -275,7 +277,8 @@ int sbp_decomp_set_state(sbp_decomp* dec, const double* state, int where);
 int sbp_decomp_get_state(sbp_decomp* dec, double* state, int where);
 /* dst = F(src) (the system is autonomous): halo exchange, then the RHS of every subdomain. */
 int sbp_decomp_rhs(sbp_decomp* dec, const double* src, double* dst, int where);
-/* nsteps classical RK4 steps of the resident state, a halo exchange before each stage. */
+/* nsteps classical RK4 steps of the resident state; every stage also fills the ghost lines its
+ * successor reads. */
 int sbp_decomp_rk4_resident(sbp_decomp* dec, double dt, long long nsteps);
 
 /* ---------------------------------------------------------------- learned correction

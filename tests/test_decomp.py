@@ -1,5 +1,5 @@
 """The decomposed path (sbp_decomp_*): one 2D wave grid as px x py subdomains
-with ghost lines and a device halo exchange before every stage, the reference's
+with ghost lines and the halo exchange fused into the stage kernels, the reference's
 DMDA block decomposition with its VecScatter ghost update on one GPU.
 
 CPU: descriptions the path does not take are rejected before any device work.
