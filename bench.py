@@ -70,6 +70,8 @@ def parse():
                          "wave3d: the 3D wave system on --grid3d^3 points, FP64 and FP32")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--batched-forms", default="fp64,fp32", help="batched: comma-separated precisions to run")
+    ap.add_argument("--no-entry-sweep", action="store_true",
+                    help="batched: skip timing every group on each configuration-table entry")
     ap.add_argument("--no-one-by-one", action="store_true",
                     help="batched: skip the same instances run one after another through single contexts")
     ap.add_argument("--trajectories", type=int, default=2000, help="learned: training trajectories")
@@ -393,10 +395,13 @@ def measure_forms(peak: float, device: int = 0) -> dict:
             c = sbpgpu.Context(sbpgpu.ADVECTION_2D, d["order"], d["nx"], d["ny"], a=d["a"], b=d["b"], device=device)
         with c:
             plain[k] = c.rk4(states[k], 0.0, d["dt"], acc_steps)
+    cache = os.environ.get("SBP_TUNE_CACHE", os.path.join(PKG, "_build", "batch_tiles.json"))
     for pname, prec, es, comp in (("batched_fp64", sbpgpu.FP64, 8, 16), ("batched_fp32", sbpgpu.FP32, 4, 19)):
         with sbpgpu.Batch(insts, precision=prec, device=device) as b:
             for k, v in enumerate(states):
                 b.set_state(k, v)
+            b.autotune(cache)
+            cfgs = batch_kernel_configs(b, sbpgpu)
             b.step_resident(acc_steps)
             b.synchronize()
             err = max(_relerr(b.get_state(k), plain[k]) for k in sample)
@@ -415,12 +420,25 @@ def measure_forms(peak: float, device: int = 0) -> dict:
         out[pname] = {"value": pts * 4 * 200 / sec, "unit": UNIT, "instances": len(insts), "points": pts,
                       "rk4_steps": 200, "roofline_frac": bytes_per_step * 200 / sec / 1e9 / peak,
                       "max_rel_err_vs_plain_fp64": err, "sampled_instances": len(sample),
-                      "error_after_rk4_steps": acc_steps}
+                      "error_after_rk4_steps": acc_steps, "kernel_configs": cfgs}
+    return out
+
+
+def batch_kernel_configs(b, sbpgpu):
+    """The kernel configuration each (problem, order) group of a batch runs: tile rows, compute
+    warps, ring depth, CTAs per SM."""
+    out = {}
+    for name, problem in (("wave", sbpgpu.WAVE_HOM_2D), ("advection", sbpgpu.ADVECTION_2D)):
+        for order in (2, 4, 6):
+            cfg = b.kernel_config(order, problem)
+            if cfg["rows"]:
+                out[f"{name}_o{order}"] = [cfg["rows"], cfg["warps"], cfg["ring"], cfg["ctas_per_sm"]]
     return out
 
 
 def run_batched_study(args):
-    """One batch of --instances uneven instances; 100-step graph chunks; autotuned tile heights."""
+    """One batch of --instances uneven instances; 100-step graph chunks; autotuned kernel
+    configurations ([tile rows, compute warps, ring depth, CTAs per SM] per group)."""
     import torch
 
     import build as gpu_build
@@ -451,8 +469,25 @@ def run_batched_study(args):
             sec = ev0.elapsed_time(ev1) / 1e3
             units = b.points * 4 * 100 * chunks
             out[name] = {"value": units / sec, "unit": UNIT, "seconds": sec, "rk4_steps": 100 * chunks,
-                         "points": b.points, "tile_heights": {o: b.tile_height(o) for o in (2, 4, 6)},
+                         "points": b.points, "kernel_configs": batch_kernel_configs(b, sbpgpu),
                          "gpu_launches": b.launches - launches0}
+            # every group on the same table entry, entry by entry (the autotuner's choices per
+            # group above; this shows what each axis gives on the whole batch)
+            per_entry = []
+            for index in range(0 if args.no_entry_sweep else 4):
+                for order in (2, 4, 6):
+                    for problem in (sbpgpu.WAVE_HOM_2D, sbpgpu.ADVECTION_2D):
+                        b.select_config(order, problem, index)
+                b.step_resident(100)  # graph capture
+                b.synchronize()
+                ev0.record(stream)
+                b.step_resident(100 * chunks)
+                ev1.record(stream)
+                b.synchronize()
+                per_entry.append({"entry": index, "value": units / (ev0.elapsed_time(ev1) / 1e3),
+                                  "kernel_configs": batch_kernel_configs(b, sbpgpu)})
+            if per_entry:
+                out[name]["every_group_on_entry"] = per_entry
     # the same instances one after another through single contexts (waves with c != 1 through the
     # variable-coefficient context, rho = 1, K = c^2), the same number of RK4 steps; creation and
     # graph capture outside the timed region

@@ -7,12 +7,15 @@
 // (wave) tensor maps; per operator order, a tile list of (instance, tile)
 // pairs. Each RK4 stage launches, per order group, one persistent wave kernel
 // over its tile list and one advection kernel over its tiles. The step loop is
-// captured into CUDA graphs of 100 steps.
+// captured into CUDA graphs of 100 steps, in which the six groups (order x
+// problem kind), which share no data, are independent chains of launches: the
+// device runs them side by side, so one group's tail and its memory-latency gaps
+// are filled with another group's tiles.
 //
-// Autotuner: the tile height of each order group's wave kernel (FP64 8 or
-// 16 rows, FP32 16 or 32) is chosen by timing the stage kernel on the batch
-// itself; choices are cached in a flat JSON file keyed by device, precision,
-// order and the group's size.
+// Autotuner: each group's kernel configuration (tile rows, compute warps, ring
+// depth, CTAs per SM: the tables of wave_batch.cuh) is chosen by timing the
+// group's middle stage on the batch itself; choices are cached in a flat JSON
+// file keyed by device, precision, problem kind, order and the group's size.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -73,14 +76,17 @@ struct sbp_batch {
   void* d_wave = nullptr;        // BatchWave<T>[n_wave]
   CUtensorMap* d_maps = nullptr; // kBatchMaps per wave instance
   void* d_line = nullptr;        // BatchLine<T>[n_line]
+  CUtensorMap* d_maps_adv = nullptr;  // kAdvMaps per advection instance
   std::vector<int> wave_slot, line_slot;  // instance -> slot in d_wave / d_line (-1 if other kind)
   BatchTile* d_tiles_wave[3] = {nullptr, nullptr, nullptr};
   int n_tiles_wave[3] = {0, 0, 0};
   BatchTile* d_tiles_line[3] = {nullptr, nullptr, nullptr};
   int n_tiles_line[3] = {0, 0, 0};
-  int ty[3] = {0, 0, 0};
+  int cfg[6] = {0, 0, 0, 0, 0, 0};  // per group (2 * order index + kind): its configuration
   double* io = nullptr;
   int* err = nullptr;
+  cudaStream_t gstream[6] = {};  // capture streams of the six groups' chains
+  cudaEvent_t fork = nullptr, join[6] = {};
   std::map<long long, cudaGraphExec_t> graphs;
   long long launches = 0, points = 0;
   std::string msg;
@@ -113,29 +119,37 @@ void fill_taps(DirTaps<T>& t, int order, double scale) {
 
 void* at(void* pool, size_t off) { return pool ? static_cast<unsigned char*>(pool) + off : nullptr; }
 
-int default_ty(bool fp32) { return fp32 ? 32 : 16; }
-
-// Encodes the 12 tensor maps of one wave instance for tile height ty.
+// Encodes the tensor maps of instance i for tile height ty: the 12 of a wave
+// instance (kBatchMaps) or the 6 of an advection instance (kAdvMaps).
 int encode_instance_maps(sbp_batch* b, int i, int ty, CUtensorMap* out) {
   EncodeTiledFn enc = encode_fn();
   if (!enc) return bfail(b, SBP_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
   const Geo& g = b->geo[i];
   const int R = g.order / 2, hxa = 16 / (int)b->es;
   const int HX = (R + hxa - 1) / hxa * hxa, HY = R;
-  const cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, 3};
+  const cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.dofs};
   const cuuint64_t strides[2] = {(cuuint64_t)(g.pitch * b->es), (cuuint64_t)(g.plane * b->es)};
   const cuuint32_t estr[3] = {1, 1, 1};
   const cuuint32_t boxP[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)(ty + 2 * HY), 1};
   const cuuint32_t boxU[3] = {(cuuint32_t)(kWaveTX + 2 * HX), (cuuint32_t)ty, 1};
   const cuuint32_t boxV[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)(ty + 2 * HY), 1};
-  const cuuint32_t boxPt[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)ty, 3};
+  const cuuint32_t boxPt[3] = {(cuuint32_t)kWaveTX, (cuuint32_t)ty, (cuuint32_t)g.dofs};
   const CUtensorMapDataType dt = b->fp32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
   void* inputs[3] = {at(b->un, g.off), at(b->wa, g.off), at(b->wb, g.off)};
-  struct Req { void* base; const cuuint32_t* box; } reqs[kBatchMaps] = {
-      {inputs[0], boxP}, {inputs[0], boxU}, {inputs[0], boxV}, {inputs[1], boxP}, {inputs[1], boxU},
-      {inputs[1], boxV}, {inputs[2], boxP}, {inputs[2], boxU}, {inputs[2], boxV}, {at(b->un, g.off), boxPt},
-      {at(b->acc, g.off), boxPt}, {b->comp ? at(b->comp, g.off) : at(b->acc, g.off), boxPt}};
-  for (int k = 0; k < kBatchMaps; k++)
+  void* comp = b->comp ? at(b->comp, g.off) : at(b->acc, g.off);
+  struct Req {
+    void* base;
+    const cuuint32_t* box;
+  };
+  const Req wave[kBatchMaps] = {{inputs[0], boxP}, {inputs[0], boxU}, {inputs[0], boxV}, {inputs[1], boxP},
+                                {inputs[1], boxU}, {inputs[1], boxV}, {inputs[2], boxP}, {inputs[2], boxU},
+                                {inputs[2], boxV}, {at(b->un, g.off), boxPt}, {at(b->acc, g.off), boxPt},
+                                {comp, boxPt}};
+  const Req adv[kAdvMaps] = {{inputs[0], boxP},          {inputs[1], boxP},           {inputs[2], boxP},
+                             {at(b->un, g.off), boxPt}, {at(b->acc, g.off), boxPt}, {comp, boxPt}};
+  const Req* reqs = g.wave ? wave : adv;
+  const int n = g.wave ? kBatchMaps : kAdvMaps;
+  for (int k = 0; k < n; k++)
     if (enc(&out[k], dt, 3, reqs[k].base, dims, strides, reqs[k].box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
         CUDA_SUCCESS)
@@ -143,31 +157,47 @@ int encode_instance_maps(sbp_batch* b, int i, int ty, CUtensorMap* out) {
   return SBP_OK;
 }
 
-// (Re)builds the tensor maps and tile list of one order group for tile height ty.
-int build_wave_group(sbp_batch* b, int oi, int ty) {
-  const int order = 2 * (oi + 1);
+// Group g = 2 * (order / 2 - 1) + kind (0 wave, 1 advection).
+bool group_is_wave(int g) { return (g & 1) == 0; }
+int group_order(int g) { return 2 * ((g >> 1) + 1); }
+BatchTile*& group_tiles(sbp_batch* b, int g) { return (g & 1) ? b->d_tiles_line[g >> 1] : b->d_tiles_wave[g >> 1]; }
+int& group_ntiles(sbp_batch* b, int g) { return (g & 1) ? b->n_tiles_line[g >> 1] : b->n_tiles_wave[g >> 1]; }
+bool group_used(const sbp_batch* b, int g) {
+  return (g & 1) ? b->n_tiles_line[g >> 1] > 0 : b->n_tiles_wave[g >> 1] > 0;
+}
+BatchCfg group_cfg(const sbp_batch* b, int g, int cfg) {
+  return b->fp32 ? batch_cfg<float>(group_is_wave(g), cfg) : batch_cfg<double>(group_is_wave(g), cfg);
+}
+
+// (Re)builds the tensor maps and tile list of group g for configuration cfg.
+int build_group(sbp_batch* b, int g, int cfg) {
+  const int order = group_order(g);
+  const bool wave = group_is_wave(g);
+  const int ty = group_cfg(b, g, cfg).ty;
   std::vector<BatchTile> tiles;
   for (size_t i = 0; i < b->inst.size(); i++) {
-    const Geo& g = b->geo[i];
-    if (!g.wave || g.order != order) continue;
-    const int s = b->wave_slot[i];
-    for (long long j0 = 0; j0 < g.ny; j0 += ty)
-      for (long long i0 = 0; i0 < g.nx; i0 += kWaveTX) tiles.push_back(BatchTile{s, (int)i0, (int)j0, 0});
+    const Geo& geo = b->geo[i];
+    if (geo.wave != wave || geo.order != order) continue;
+    const int s = wave ? b->wave_slot[i] : b->line_slot[i];
+    for (long long j0 = 0; j0 < geo.ny; j0 += ty)
+      for (long long i0 = 0; i0 < geo.nx; i0 += kWaveTX) tiles.push_back(BatchTile{s, (int)i0, (int)j0, 0});
     CUtensorMap m[kBatchMaps];
     int rc = encode_instance_maps(b, (int)i, ty, m);
     if (rc) return rc;
-    BCK(cudaMemcpyAsync(b->d_maps + (size_t)s * kBatchMaps, m, sizeof(m), cudaMemcpyHostToDevice, b->stream));
-  }
-  if (b->d_tiles_wave[oi]) cudaFree(b->d_tiles_wave[oi]);
-  b->d_tiles_wave[oi] = nullptr;
-  b->n_tiles_wave[oi] = (int)tiles.size();
-  if (!tiles.empty()) {
-    BCK(cudaMalloc((void**)&b->d_tiles_wave[oi], tiles.size() * sizeof(BatchTile)));
-    BCK(cudaMemcpyAsync(b->d_tiles_wave[oi], tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice,
+    CUtensorMap* dst = wave ? b->d_maps + (size_t)s * kBatchMaps : b->d_maps_adv + (size_t)s * kAdvMaps;
+    BCK(cudaMemcpyAsync(dst, m, (wave ? kBatchMaps : kAdvMaps) * sizeof(CUtensorMap), cudaMemcpyHostToDevice,
                         b->stream));
-    BCK(b->fp32 ? configure_wave_batch<float>(order, ty) : configure_wave_batch<double>(order, ty));
   }
-  b->ty[oi] = ty;
+  BatchTile*& d = group_tiles(b, g);
+  if (d) cudaFree(d);
+  d = nullptr;
+  group_ntiles(b, g) = (int)tiles.size();
+  if (!tiles.empty()) {
+    BCK(cudaMalloc((void**)&d, tiles.size() * sizeof(BatchTile)));
+    BCK(cudaMemcpyAsync(d, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, b->stream));
+    BCK(b->fp32 ? configure_batch<float>(order, wave, cfg) : configure_batch<double>(order, wave, cfg));
+  }
+  b->cfg[g] = cfg;
   BCK(cudaStreamSynchronize(b->stream));
   for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
   b->graphs.clear();
@@ -242,55 +272,51 @@ int fill_params(sbp_batch* b) {
   if (!lines.empty()) {
     BCK(cudaMalloc(&b->d_line, lines.size() * sizeof(BatchLine<T>)));
     BCK(cudaMemcpy(b->d_line, lines.data(), lines.size() * sizeof(BatchLine<T>), cudaMemcpyHostToDevice));
+    BCK(cudaMalloc((void**)&b->d_maps_adv, lines.size() * kAdvMaps * sizeof(CUtensorMap)));
   }
-  // advection tile lists (32 x 8 points per CTA)
-  for (int oi = 0; oi < 3; oi++) {
-    std::vector<BatchTile> tiles;
-    for (size_t i = 0; i < b->inst.size(); i++) {
-      const Geo& g = b->geo[i];
-      if (g.wave || order_index(g.order) != oi) continue;
-      for (long long j0 = 0; j0 < g.ny; j0 += kLineTileY)
-        for (long long i0 = 0; i0 < g.nx; i0 += kLineTileX)
-          tiles.push_back(BatchTile{b->line_slot[i], (int)i0, (int)j0, 0});
-    }
-    b->n_tiles_line[oi] = (int)tiles.size();
-    if (!tiles.empty()) {
-      BCK(cudaMalloc((void**)&b->d_tiles_line[oi], tiles.size() * sizeof(BatchTile)));
-      BCK(cudaMemcpy(b->d_tiles_line[oi], tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice));
-    }
-  }
-  for (int oi = 0; oi < 3; oi++) {
-    int rc = build_wave_group(b, oi, default_ty(b->fp32));
-    if (rc) return rc;
-  }
+  for (int g = 0; g < 6; g++)
+    if (int rc = build_group(b, g, 0)) return rc;
   return SBP_OK;
 }
 
+// One stage of group g with configuration cfg on stream s.
 template <typename T>
-int launch_stage_all(sbp_batch* b, int stage, int rk) {
-  for (int oi = 0; oi < 3; oi++) {
-    const int order = 2 * (oi + 1);
-    if (b->n_tiles_wave[oi]) {
-      BCK(launch_wave_batch<T>(order, stage, b->ty[oi], (const BatchWave<T>*)b->d_wave, b->d_maps,
-                               b->d_tiles_wave[oi], b->n_tiles_wave[oi], rk, b->err, b->stream));
-      b->launches++;
-    }
-    if (b->n_tiles_line[oi]) {
-      BCK(launch_adv_batch<T>(order, stage, (const BatchLine<T>*)b->d_line, b->d_tiles_line[oi],
-                              b->n_tiles_line[oi], rk, b->stream));
-      b->launches++;
-    }
-  }
-  return SBP_OK;
+cudaError_t launch_group_stage_cfg(sbp_batch* b, int g, int cfg, int stage, int rk, cudaStream_t s) {
+  const bool wave = group_is_wave(g);
+  return launch_batch<T>(group_order(g), wave, stage, cfg, wave ? b->d_wave : b->d_line,
+                         wave ? b->d_maps : b->d_maps_adv, group_tiles(b, g), group_ntiles(b, g), rk, b->err, s);
 }
 
 template <typename T>
-int enqueue_step(sbp_batch* b) {
-  int rc;
-  if ((rc = launch_stage_all<T>(b, ST_FIRST, 1))) return rc;
-  if ((rc = launch_stage_all<T>(b, ST_MID, 2))) return rc;
-  if ((rc = launch_stage_all<T>(b, ST_MID, 3))) return rc;
-  return launch_stage_all<T>(b, ST_LAST, 4);
+int launch_group_stage(sbp_batch* b, int g, int stage, int rk, cudaStream_t s) {
+  BCK(launch_group_stage_cfg<T>(b, g, b->cfg[g], stage, rk, s));
+  b->launches++;
+  return SBP_OK;
+}
+
+// `steps` RK4 steps of group g on stream s.
+template <typename T>
+int enqueue_group(sbp_batch* b, int g, long long steps, cudaStream_t s) {
+  static const int kStages[4][2] = {{ST_FIRST, 1}, {ST_MID, 2}, {ST_MID, 3}, {ST_LAST, 4}};
+  for (long long n = 0; n < steps; n++)
+    for (const auto& st : kStages)
+      if (int rc = launch_group_stage<T>(b, g, st[0], st[1], s)) return rc;
+  return SBP_OK;
+}
+
+// The chunk's launches while b->stream is capturing: each used group's chain on its
+// own stream, forked from and joined back into b->stream.
+template <typename T>
+int enqueue_chunk(sbp_batch* b, long long steps) {
+  BCK(cudaEventRecord(b->fork, b->stream));
+  for (int g = 0; g < 6; g++) {
+    if (!group_used(b, g)) continue;
+    BCK(cudaStreamWaitEvent(b->gstream[g], b->fork, 0));
+    if (int rc = enqueue_group<T>(b, g, steps, b->gstream[g])) return rc;
+    BCK(cudaEventRecord(b->join[g], b->gstream[g]));
+    BCK(cudaStreamWaitEvent(b->stream, b->join[g], 0));
+  }
+  return SBP_OK;
 }
 
 long long kernels_per_step(const sbp_batch* b) {
@@ -306,8 +332,7 @@ int run_chunk(sbp_batch* b, long long steps) {
     cudaGraph_t g = nullptr;
     BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     const long long before = b->launches;
-    int rc = SBP_OK;
-    for (long long s = 0; s < steps && rc == SBP_OK; s++) rc = enqueue_step<T>(b);
+    const int rc = enqueue_chunk<T>(b, steps);
     cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
     b->launches = before;
     if (rc) {
@@ -368,13 +393,18 @@ void write_cache(const char* path, const std::map<std::string, int>& m) {
 void release(sbp_batch* b) {
   for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
   b->graphs.clear();
-  void* bufs[] = {b->un, b->acc, b->wa, b->wb, b->comp, b->d_wave, b->d_maps, b->d_line, b->io, b->err};
+  void* bufs[] = {b->un, b->acc, b->wa, b->wb, b->comp, b->d_wave, b->d_maps, b->d_line, b->d_maps_adv, b->io, b->err};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (int oi = 0; oi < 3; oi++) {
     if (b->d_tiles_wave[oi]) cudaFree(b->d_tiles_wave[oi]);
     if (b->d_tiles_line[oi]) cudaFree(b->d_tiles_line[oi]);
   }
+  for (int g = 0; g < 6; g++) {
+    if (b->gstream[g]) cudaStreamDestroy(b->gstream[g]);
+    if (b->join[g]) cudaEventDestroy(b->join[g]);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
 }
 
@@ -450,6 +480,14 @@ int sbp_batch_create(const sbp_instance* list, int count, int precision, int dev
       return cuda_fail("cudaStreamCreate", e);
     b->own_stream = true;
   }
+  for (int g = 0; g < 6; g++) {
+    if ((e = cudaStreamCreateWithFlags(&b->gstream[g], cudaStreamNonBlocking)) != cudaSuccess)
+      return cuda_fail("cudaStreamCreate(group)", e);
+    if ((e = cudaEventCreateWithFlags(&b->join[g], cudaEventDisableTiming)) != cudaSuccess)
+      return cuda_fail("cudaEventCreate", e);
+  }
+  if ((e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess)
+    return cuda_fail("cudaEventCreate", e);
   void** pools[] = {&b->un, &b->acc, &b->wa, &b->wb};
   for (void** p : pools) {
     if ((e = cudaMalloc(p, b->pool_bytes)) != cudaSuccess) return cuda_fail("cudaMalloc(pool)", e);
@@ -563,56 +601,50 @@ int sbp_batch_autotune(sbp_batch* b, const char* cache_path) {
   BCK(cudaGetDeviceProperties(&prop, b->device));
   std::map<std::string, int> cache = read_cache(cache_path);
   bool dirty = false;
-  const int cand64[2] = {8, 16}, cand32[2] = {16, 32};
-  const int* cand = b->fp32 ? cand32 : cand64;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   int rc = SBP_OK;
-  for (int oi = 0; oi < 3 && rc == SBP_OK; oi++) {
-    const int order = 2 * (oi + 1);
+  for (int g = 0; g < 6 && rc == SBP_OK; g++) {
+    const int order = group_order(g);
+    const bool wave = group_is_wave(g);
     long long pts = 0;
     for (size_t i = 0; i < b->inst.size(); i++)
-      if (b->geo[i].wave && b->geo[i].order == order) pts += b->geo[i].nx * b->geo[i].ny;
+      if (b->geo[i].wave == wave && b->geo[i].order == order) pts += b->geo[i].nx * b->geo[i].ny;
     if (!pts) continue;
-    // key: device, precision, order, group size rounded to 2 significant digits
+    // key: device, precision, kind, order, group size rounded to 2 significant digits
     const double mag = std::pow(10.0, std::floor(std::log10((double)pts)) - 1);
     const long long bucket = (long long)(std::round(pts / mag) * mag);
-    const std::string key = std::string(prop.name) + "|" + (b->fp32 ? "fp32" : "fp64") + "|order" +
-                            std::to_string(order) + "|points" + std::to_string(bucket);
+    const std::string key = std::string(prop.name) + "|" + (b->fp32 ? "fp32" : "fp64") + "|" +
+                            (wave ? "wave" : "advection") + "|order" + std::to_string(order) + "|points" +
+                            std::to_string(bucket) + "|cfg";
     auto hit = cache.find(key);
-    if (hit != cache.end() && (hit->second == cand[0] || hit->second == cand[1])) {
-      if (hit->second != b->ty[oi]) rc = build_wave_group(b, oi, hit->second);
+    if (hit != cache.end() && hit->second >= 0 && hit->second < kBatchCfgs) {
+      if (hit->second != b->cfg[g]) rc = build_group(b, g, hit->second);
       continue;
     }
     float best_ms = 1e30f;
-    int best = cand[0];
-    for (int c = 0; c < 2 && rc == SBP_OK; c++) {
-      if ((rc = build_wave_group(b, oi, cand[c]))) break;
-      // time the middle stage (it writes only the accumulator and a stage buffer)
+    int best = 0;
+    for (int c = 0; c < kBatchCfgs && rc == SBP_OK; c++) {
+      if ((rc = build_group(b, g, c))) break;
+      // time the middle stage (it writes only the accumulator and a stage buffer): one
+      // untimed launch, then three
       float ms = 0;
       for (int rep = 0; rep < 4 && rc == SBP_OK; rep++) {
         if (rep == 1) cudaEventRecord(e0, b->stream);
-        if (b->fp32)
-          rc = launch_wave_batch<float>(order, ST_MID, cand[c], (const BatchWave<float>*)b->d_wave, b->d_maps,
-                                        b->d_tiles_wave[oi], b->n_tiles_wave[oi], 2, b->err, b->stream) == cudaSuccess
-                   ? SBP_OK
-                   : SBP_ERR_CUDA;
-        else
-          rc = launch_wave_batch<double>(order, ST_MID, cand[c], (const BatchWave<double>*)b->d_wave, b->d_maps,
-                                         b->d_tiles_wave[oi], b->n_tiles_wave[oi], 2, b->err, b->stream) == cudaSuccess
-                   ? SBP_OK
-                   : SBP_ERR_CUDA;
+        if ((b->fp32 ? launch_group_stage_cfg<float>(b, g, c, ST_MID, 2, b->stream)
+                     : launch_group_stage_cfg<double>(b, g, c, ST_MID, 2, b->stream)) != cudaSuccess)
+          rc = bfail(b, SBP_ERR_CUDA, "autotune launch failed");
       }
       cudaEventRecord(e1, b->stream);
-      if (cudaEventSynchronize(e1) != cudaSuccess) rc = SBP_ERR_CUDA;
+      if (cudaEventSynchronize(e1) != cudaSuccess) rc = bfail(b, SBP_ERR_CUDA, "autotune launch failed");
       cudaEventElapsedTime(&ms, e0, e1);
       if (rc == SBP_OK && ms < best_ms) {
         best_ms = ms;
-        best = cand[c];
+        best = c;
       }
     }
-    if (rc == SBP_OK && best != b->ty[oi]) rc = build_wave_group(b, oi, best);
+    if (rc == SBP_OK && best != b->cfg[g]) rc = build_group(b, g, best);
     cache[key] = best;
     dirty = true;
   }
@@ -625,7 +657,34 @@ int sbp_batch_autotune(sbp_batch* b, const char* cache_path) {
 
 int sbp_batch_tile_height(const sbp_batch* b, int order) {
   if (!b || (order != 2 && order != 4 && order != 6)) return SBP_ERR_INVALID;
-  return b->ty[order_index(order)];
+  const int g = 2 * order_index(order);
+  return group_used(b, g) ? group_cfg(b, g, b->cfg[g]).ty : 0;
+}
+
+int sbp_batch_select_config(sbp_batch* b, int order, int problem, int index) {
+  if (!b || (order != 2 && order != 4 && order != 6) ||
+      (problem != SBP_WAVE_HOM_2D && problem != SBP_ADVECTION_2D) || index < 0 || index >= kBatchCfgs)
+    return SBP_ERR_INVALID;
+  BCK(cudaSetDevice(b->device));
+  const int g = 2 * order_index(order) + (problem == SBP_ADVECTION_2D ? 1 : 0);
+  return index == b->cfg[g] ? SBP_OK : build_group(b, g, index);
+}
+
+int sbp_batch_kernel_config(const sbp_batch* b, int order, int problem, int* cfg) {
+  if (!b || !cfg || (order != 2 && order != 4 && order != 6) ||
+      (problem != SBP_WAVE_HOM_2D && problem != SBP_ADVECTION_2D))
+    return SBP_ERR_INVALID;
+  const int g = 2 * order_index(order) + (problem == SBP_ADVECTION_2D ? 1 : 0);
+  if (!group_used(b, g)) {
+    cfg[0] = cfg[1] = cfg[2] = cfg[3] = 0;
+    return SBP_OK;
+  }
+  const BatchCfg c = group_cfg(b, g, b->cfg[g]);
+  cfg[0] = c.ty;
+  cfg[1] = c.warps;
+  cfg[2] = c.nst;
+  cfg[3] = c.ctas;
+  return SBP_OK;
 }
 
 int sbp_batch_get_stream(const sbp_batch* b, void** stream) {

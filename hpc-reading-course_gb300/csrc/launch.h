@@ -90,45 +90,40 @@ cudaError_t launch_wave3d(int order, int stage, const Wave3Params<T>& prm, cudaS
 // Shared-memory opt-in of the 3D stage kernels of one order (outside stream capture).
 template <typename T> cudaError_t configure_wave3d(int order);
 
-// Batched stage kernels (wave_batch_inst.cu, one unit per order). `ty` is the
-// tile height: 8 or 16 (FP64), 16 or 32 (FP32).
+// Batched stage kernels (wave_batch_inst.cu, one unit per order): configuration
+// `cfg` of the wave (wave = true) or advection table of wave_batch.cuh.
 #define SBP_DECLARE_BATCH(o)                                                                                    \
-  template <typename T> cudaError_t configure_wave_batch_o##o(int ty);                                          \
+  template <typename T> cudaError_t configure_batch_o##o(bool wave, int cfg);                                   \
   template <typename T>                                                                                         \
-  cudaError_t launch_wave_batch_o##o(int stage, int ty, const BatchWave<T>* insts, const CUtensorMap* maps,     \
-                                     const BatchTile* tiles, int ntiles, int rk, int* err, unsigned grid,          \
-                                     cudaStream_t s);                                                              \
-  template <typename T>                                                                                         \
-  cudaError_t launch_adv_batch_o##o(int stage, const BatchLine<T>* insts, const BatchTile* tiles, int ntiles, int rk, \
-                                    cudaStream_t s);
+  cudaError_t launch_batch_o##o(bool wave, int stage, int cfg, const void* insts, const CUtensorMap* maps,      \
+                                const BatchTile* tiles, int ntiles, int rk, int* err, unsigned grid, cudaStream_t s);
 SBP_DECLARE_BATCH(2)
 SBP_DECLARE_BATCH(4)
 SBP_DECLARE_BATCH(6)
 #undef SBP_DECLARE_BATCH
 
-template <typename T> inline cudaError_t configure_wave_batch(int order, int ty) {
-  return order == 2 ? configure_wave_batch_o2<T>(ty)
-                    : (order == 4 ? configure_wave_batch_o4<T>(ty) : configure_wave_batch_o6<T>(ty));
+// The configuration `cfg` of a group's table (wave or advection kernel).
+template <typename T> inline BatchCfg batch_cfg(bool wave, int cfg) {
+  return wave ? BatchCfgTable<T>::wave[cfg] : BatchCfgTable<T>::adv[cfg];
 }
-template <typename T>
-inline cudaError_t launch_wave_batch(int order, int stage, int ty, const BatchWave<T>* insts, const CUtensorMap* maps,
-                                     const BatchTile* tiles, int ntiles, int rk, int* err, cudaStream_t s) {
-  const int nsm = device_sm_count();
-  const unsigned grid = (unsigned)(ntiles < nsm ? ntiles : nsm);
-  switch (order) {
-    case 2: return launch_wave_batch_o2<T>(stage, ty, insts, maps, tiles, ntiles, rk, err, grid, s);
-    case 4: return launch_wave_batch_o4<T>(stage, ty, insts, maps, tiles, ntiles, rk, err, grid, s);
-    case 6: return launch_wave_batch_o6<T>(stage, ty, insts, maps, tiles, ntiles, rk, err, grid, s);
-    default: return cudaErrorInvalidValue;
-  }
+
+template <typename T> inline cudaError_t configure_batch(int order, bool wave, int cfg) {
+  if (cfg < 0 || cfg >= kBatchCfgs) return cudaErrorInvalidValue;
+  return order == 2 ? configure_batch_o2<T>(wave, cfg)
+                    : (order == 4 ? configure_batch_o4<T>(wave, cfg) : configure_batch_o6<T>(wave, cfg));
 }
+// One stage of one group: a persistent grid of (CTAs per SM) x SMs, or one CTA per
+// tile when the group has fewer tiles.
 template <typename T>
-inline cudaError_t launch_adv_batch(int order, int stage, const BatchLine<T>* insts, const BatchTile* tiles, int ntiles,
-                                    int rk, cudaStream_t s) {
+inline cudaError_t launch_batch(int order, bool wave, int stage, int cfg, const void* insts, const CUtensorMap* maps,
+                                const BatchTile* tiles, int ntiles, int rk, int* err, cudaStream_t s) {
+  if (cfg < 0 || cfg >= kBatchCfgs) return cudaErrorInvalidValue;
+  const int slots = device_sm_count() * batch_cfg<T>(wave, cfg).ctas;
+  const unsigned grid = (unsigned)(ntiles < slots ? ntiles : slots);
   switch (order) {
-    case 2: return launch_adv_batch_o2<T>(stage, insts, tiles, ntiles, rk, s);
-    case 4: return launch_adv_batch_o4<T>(stage, insts, tiles, ntiles, rk, s);
-    case 6: return launch_adv_batch_o6<T>(stage, insts, tiles, ntiles, rk, s);
+    case 2: return launch_batch_o2<T>(wave, stage, cfg, insts, maps, tiles, ntiles, rk, err, grid, s);
+    case 4: return launch_batch_o4<T>(wave, stage, cfg, insts, maps, tiles, ntiles, rk, err, grid, s);
+    case 6: return launch_batch_o6<T>(wave, stage, cfg, insts, maps, tiles, ntiles, rk, err, grid, s);
     default: return cudaErrorInvalidValue;
   }
 }

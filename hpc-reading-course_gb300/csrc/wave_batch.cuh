@@ -63,41 +63,58 @@ struct BatchTile {
   int slot, i0, j0, pad;
 };
 
-// Consumer warps of the batched wave kernel per precision.
-#ifndef SBP_BATCH_WARPS_F32
-#define SBP_BATCH_WARPS_F32 16
-#endif
-#ifndef SBP_BATCH_WARPS_F64
-#define SBP_BATCH_WARPS_F64 8
-#endif
-template <typename T> constexpr int batch_warps() { return sizeof(T) == 4 ? SBP_BATCH_WARPS_F32 : SBP_BATCH_WARPS_F64; }
-template <typename T, int ORD, int STAGE, int TY>
-using BatchWaveTile = WaveTile<T, ORD, STAGE, TY, (int)sizeof(BatchWave<T>), false, 2, batch_warps<T>()>;
+// A batched stage kernel's configuration: tile rows, compute warps, ring depth
+// (tiles in flight) and resident CTAs per SM. Each (operator order, problem kind)
+// group of a batch runs the configuration the autotuner picked from its table
+// by timing the group's middle stage on the batch itself (sbp_batch_autotune);
+// entry 0 is the default. Every entry fits the 227 KB of shared memory a CTA may
+// use, and with 2 CTAs per SM the 228 KB of the SM (static_asserts below). 17 warps
+// per SM leave 96 registers a thread, which the FP32 wave kernel with 16-row
+// tiles and a 3-deep ring exceeds (it spilled): its 3-deep entry has 8 warps.
+struct BatchCfg {
+  int ty, warps, nst, ctas;
+};
+constexpr int kBatchCfgs = 4;
+template <typename T> struct BatchCfgTable;
+template <> struct BatchCfgTable<float> {
+  static constexpr BatchCfg wave[kBatchCfgs] = {{32, 16, 2, 1}, {16, 8, 3, 1}, {16, 8, 2, 2}, {16, 8, 4, 1}};
+  static constexpr BatchCfg adv[kBatchCfgs] = {{32, 8, 4, 1}, {64, 16, 3, 1}, {16, 4, 4, 2}, {32, 8, 2, 2}};
+};
+template <> struct BatchCfgTable<double> {
+  static constexpr BatchCfg wave[kBatchCfgs] = {{16, 8, 2, 1}, {8, 8, 2, 1}, {8, 8, 3, 1}, {8, 4, 2, 2}};
+  static constexpr BatchCfg adv[kBatchCfgs] = {{16, 8, 4, 1}, {32, 8, 3, 1}, {16, 4, 3, 2}, {8, 4, 6, 2}};
+};
+template <typename T, int CFG> constexpr BatchCfg batch_wave_cfg() { return BatchCfgTable<T>::wave[CFG]; }
+template <typename T, int CFG> constexpr BatchCfg batch_adv_cfg() { return BatchCfgTable<T>::adv[CFG]; }
+
+template <typename T, int ORD, int STAGE, int CFG>
+using BatchWaveTile = WaveTile<T, ORD, STAGE, batch_wave_cfg<T, CFG>().ty, (int)sizeof(BatchWave<T>), false,
+                               batch_wave_cfg<T, CFG>().nst, batch_wave_cfg<T, CFG>().warps>;
 
 // A CTA takes every gridDim.x-th tile of the list, so neighbouring tiles of an
 // instance run at the same time on neighbouring CTAs and share their halo rows in
 // L2. Measured at 512 instances: contiguous ranges of the list per CTA ran at
 // 1.39e10 (FP64) / 2.36e10 (FP32) point-stage updates/s against 1.72e10 / 3.22e10,
 // and prefetching the next instance's tensor maps changed nothing.
-template <typename T, int ORD, int STAGE, int TY>
-__global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, TY>::THREADS, 1)
+template <typename T, int ORD, int STAGE, int CFG>
+__global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, CFG>::THREADS, batch_wave_cfg<T, CFG>().ctas)
     wave_batch_stage_kernel(const BatchWave<T>* __restrict__ insts, const CUtensorMap* __restrict__ maps,
                             const BatchTile* __restrict__ tiles, int ntiles, int rk, int* err) {
-  using Tile = BatchWaveTile<T, ORD, STAGE, TY>;
-  constexpr int HX = Tile::HX, HY = Tile::HY;
+  using Tile = BatchWaveTile<T, ORD, STAGE, CFG>;
+  static_assert(batch_wave_cfg<T, CFG>().ctas * (Tile::SMEM + 1024) <= 228 * 1024, "CTAs per SM exceed shared memory");
+  constexpr int HX = Tile::HX, HY = Tile::HY, NST = Tile::NST;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
-  uint64_t* empty = full + 2;
+  uint64_t* empty = full + NST;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   uint64_t* dbar = reinterpret_cast<uint64_t*>(smem + Tile::OFF_DBAR);
   if (threadIdx.x == 0) {
-    mbar_init(&full[0], 1);
-    mbar_init(&full[1], 1);
-    mbar_init(&empty[0], Tile::WARPS);
-    mbar_init(&empty[1], Tile::WARPS);
-    mbar_init(&dbar[0], Tile::WARPS);
-    mbar_init(&dbar[1], Tile::WARPS);
+    for (int s = 0; s < NST; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], Tile::WARPS);
+      mbar_init(&dbar[s], Tile::WARPS);
+    }
     fence_barrier_init();
   }
   __syncthreads();
@@ -111,8 +128,8 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, TY>::THREADS, 1)
       for (int tile = first; tile < end; tile += step, k++) {
         const BatchTile tt = next;
         if (tile + step < end) next = tiles[tile + step];  // the next descriptor, read ahead
-        const int b = k & 1;
-        if (k >= 2 && !mbar_wait_bounded(&empty[b], ((k >> 1) - 1) & 1)) {
+        const int b = k % NST;
+        if (k >= NST && !mbar_wait_bounded(&empty[b], ((k / NST) - 1) & 1)) {
           atomicOr(err, ERR_TMA_TIMEOUT);
           break;
         }
@@ -128,8 +145,8 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, TY>::THREADS, 1)
         if (Tile::LOAD_COMP) tma_load_3d(st + Tile::OFF_C, &m[11], i0, j0, 0, &full[b]);
         bulk_copy_g2s(st + Tile::OFF_PRM, &insts[tt.slot], (uint32_t)sizeof(BatchWave<T>), &full[b]);
       }
-      for (int kk = (k >= 2 ? k - 2 : 0); kk < k; kk++)
-        if (!mbar_wait_bounded(&full[kk & 1], (kk >> 1) & 1)) atomicOr(err, ERR_TMA_TIMEOUT);
+      for (int kk = (k >= NST ? k - NST : 0); kk < k; kk++)
+        if (!mbar_wait_bounded(&full[kk % NST], (kk / NST) & 1)) atomicOr(err, ERR_TMA_TIMEOUT);
     }
     return;
   }
@@ -137,8 +154,8 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, TY>::THREADS, 1)
   uint32_t dphase = 0;  // parity of each stage's next deferred-pass barrier phase
   int k = 0;
   for (int tile = first; tile < end; tile += step, k++) {
-    const int b = k & 1;
-    if (!mbar_wait_bounded(&full[b], (k >> 1) & 1)) {
+    const int b = k % NST;
+    if (!mbar_wait_bounded(&full[b], (k / NST) & 1)) {
       if (lane == 0) atomicOr(err, ERR_TMA_TIMEOUT);
       break;
     }
@@ -157,45 +174,183 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, TY>::THREADS, 1)
   }
 }
 
-// Batched 2D advection: one CTA of 32 x 8 threads per 32 x 32 (instance, tile)
-// pair, 4 rows per thread; the instance block is staged in shared memory once.
-// Staging the tile's stage input with its halo in shared memory as well (a fill
-// and a barrier per CTA) measured slower: batched FP32 6.67e10 against 7.27e10
-// point-stage updates/s; the taps' reuse is served by L1.
+// Per-instance block of a batched advection instance (16-byte multiple, bulk-copied
+// into shared memory beside each tile).
 template <typename T> struct alignas(16) BatchLine {
-  LineParams<T> prm;  // geometry, taps, SAT factors, un/acc/comp pointers
+  LineParams<T> prm;  // geometry, taps (velocities folded in), SAT factors, un/acc/comp pointers
   T* wa;
   T* wb;
   double dt;
   T c_acc[4], c_w[4];  // RK4 stage rk's coefficients at [rk - 1], computed on the host
 };
 
-constexpr int kLineTileX = 32, kLineTileY = 32, kLineThreadsY = 8;
+// Tensor maps of one batched advection instance (one component), in global memory:
+// [s] = stage input s (0: u^n, 1: wa, 2: wb) with the tile box and its halo;
+// [3], [4], [5] = u^n, acc, comp point boxes.
+constexpr int kAdvMaps = 6;
 
-template <typename T, int ORD, int STAGE>
-__global__ void __launch_bounds__(kLineTileX * kLineThreadsY)
-    adv_batch_stage_kernel(const BatchLine<T>* __restrict__ insts, const BatchTile* __restrict__ tiles, int rk) {
-  __shared__ __align__(16) unsigned char blk[sizeof(BatchLine<T>)];
-  const BatchTile tt = tiles[blockIdx.x];
-  {
-    const uint4* src = reinterpret_cast<const uint4*>(&insts[tt.slot]);
-    uint4* dst = reinterpret_cast<uint4*>(blk);
-    for (int k = threadIdx.y * kLineTileX + threadIdx.x; k < (int)(sizeof(BatchLine<T>) / 16);
-         k += kLineTileX * kLineThreadsY)
-      dst[k] = src[k];
+// The shared-memory stage of the batched advection kernel: the stage input's
+// box (tile + R halo lines each side; x halo rounded up to 16 bytes), the u^n,
+// acc and comp point boxes the stage reads, and the instance block.
+template <typename T, int ORD, int STAGE, int CFG>
+struct AdvTile {
+  static constexpr BatchCfg C = batch_adv_cfg<T, CFG>();
+  static constexpr int TY = C.ty, WARPS = C.warps, NST = C.nst, THREADS = 32 * (WARPS + 1);
+  static constexpr int R = (OpShape<ORD>::W - 1) / 2;
+  static constexpr int HXA = 16 / sizeof(T);
+  static constexpr int HX = ((R + HXA - 1) / HXA) * HXA, HY = R;
+  static constexpr int PW = kWaveTX + 2 * HX, PH = TY + 2 * HY;
+  static constexpr bool COMP = sizeof(T) == 4;  // FP32: compensated RK4 update
+  static constexpr bool LOAD_UN = (STAGE == ST_MID) || (STAGE == ST_LAST && COMP);
+  static constexpr bool LOAD_ACC = (STAGE == ST_MID) || (STAGE == ST_LAST);
+  static constexpr bool LOAD_COMP = (STAGE == ST_LAST && COMP);
+  static constexpr int align128(int b) { return (b + 127) / 128 * 128; }
+  static constexpr int BYTES_P = PH * PW * (int)sizeof(T);
+  static constexpr int BYTES_PT = TY * kWaveTX * (int)sizeof(T);
+  static constexpr int OFF_N = align128(BYTES_P);
+  static constexpr int OFF_A = OFF_N + (LOAD_UN ? BYTES_PT : 0);
+  static constexpr int OFF_C = OFF_A + (LOAD_ACC ? BYTES_PT : 0);
+  static constexpr int OFF_PRM = align128(OFF_C + (LOAD_COMP ? BYTES_PT : 0));
+  static constexpr int STAGE_BYTES = OFF_PRM + align128((int)sizeof(BatchLine<T>));
+  static constexpr int OFF_BAR = NST * STAGE_BYTES;  // full[8], empty[8]
+  static constexpr int SMEM = OFF_BAR + 128;
+  static constexpr uint32_t TX_BYTES = BYTES_P + (LOAD_UN ? BYTES_PT : 0) + (LOAD_ACC ? BYTES_PT : 0) +
+                                       (LOAD_COMP ? BYTES_PT : 0) + (int)sizeof(BatchLine<T>);
+  static_assert(TY % WARPS == 0, "tile rows must split evenly over the compute warps");
+  static_assert(NST >= 2 && NST <= 8, "ring depth");
+  static_assert(SMEM <= 227 * 1024, "advection tile pipeline exceeds shared memory");
+  static_assert(C.ctas * (SMEM + 1024) <= 228 * 1024, "CTAs per SM exceed shared memory");
+};
+
+// Batched 2D advection u_t = -(a u_x + b u_y) (code/demo/advection/advection_rhs.h:155-393,
+// 460-528), persistent like the wave kernel: the producer warp loads each (instance,
+// tile) pair's boxes with the instance's tensor maps and bulk-copies its parameter
+// block beside them into a ring of NST stages; each compute warp takes TY / WARPS rows
+// of 64 points (two per lane). Interior taps read the stage input's box, closure rows
+// read global memory (the closure reaches past the tile halo), the SAT is FP64 at
+// boundary points; the taps and their order of accumulation are the single-instance
+// line kernel's, so both give the same bits. A CTA takes every gridDim.x-th tile.
+template <typename T, int ORD, int STAGE, int CFG>
+__global__ void __launch_bounds__(AdvTile<T, ORD, STAGE, CFG>::THREADS, batch_adv_cfg<T, CFG>().ctas)
+    adv_batch_stage_kernel(const BatchLine<T>* __restrict__ insts, const CUtensorMap* __restrict__ maps,
+                           const BatchTile* __restrict__ tiles, int ntiles, int rk, int* err) {
+  using Tile = AdvTile<T, ORD, STAGE, CFG>;
+  constexpr int HX = Tile::HX, HY = Tile::HY, NST = Tile::NST, WARPS = Tile::WARPS, PW = Tile::PW;
+  constexpr int W = OpShape<ORD>::W, CS = OpShape<ORD>::CS, R = Tile::R, ROWS = Tile::TY / WARPS;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
+  uint64_t* empty = full + 8;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NST; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], WARPS);
+    }
+    fence_barrier_init();
   }
   __syncthreads();
-  const BatchLine<T>& I = *reinterpret_cast<const BatchLine<T>*>(blk);
-  const T* in = rk == 1 ? I.prm.un : (rk == 3 ? I.wb : I.wa);
-  T* wout = (rk == 1 || rk == 3) ? I.wa : I.wb;
-  const T c_acc = I.c_acc[rk - 1];
-  const T c_w = I.c_w[rk - 1];
-  const int i = tt.i0 + threadIdx.x;
-  if (i >= I.prm.nx) return;
+  const int sel = rk == 1 ? 0 : (rk == 3 ? 2 : 1);  // which buffer is the stage input
+  const int first = blockIdx.x, step = gridDim.x, end = ntiles;
+
+  if (warp == WARPS) {  // producer
+    if (lane == 0) {
+      int k = 0;
+      BatchTile next = first < end ? tiles[first] : BatchTile{0, 0, 0, 0};
+      for (int tile = first; tile < end; tile += step, k++) {
+        const BatchTile tt = next;
+        if (tile + step < end) next = tiles[tile + step];  // the next descriptor, read ahead
+        const int b = k % NST;
+        if (k >= NST && !mbar_wait_bounded(&empty[b], ((k / NST) - 1) & 1)) {
+          atomicOr(err, ERR_TMA_TIMEOUT);
+          break;
+        }
+        const CUtensorMap* m = maps + (long long)tt.slot * kAdvMaps;
+        unsigned char* st = smem + b * Tile::STAGE_BYTES;
+        mbar_arrive_expect_tx(&full[b], Tile::TX_BYTES);
+        tma_load_3d(st, &m[sel], tt.i0 - HX, tt.j0 - HY, 0, &full[b]);
+        if (Tile::LOAD_UN) tma_load_3d(st + Tile::OFF_N, &m[3], tt.i0, tt.j0, 0, &full[b]);
+        if (Tile::LOAD_ACC) tma_load_3d(st + Tile::OFF_A, &m[4], tt.i0, tt.j0, 0, &full[b]);
+        if (Tile::LOAD_COMP) tma_load_3d(st + Tile::OFF_C, &m[5], tt.i0, tt.j0, 0, &full[b]);
+        bulk_copy_g2s(st + Tile::OFF_PRM, &insts[tt.slot], (uint32_t)sizeof(BatchLine<T>), &full[b]);
+      }
+      for (int kk = (k >= NST ? k - NST : 0); kk < k; kk++)
+        if (!mbar_wait_bounded(&full[kk % NST], (kk / NST) & 1)) atomicOr(err, ERR_TMA_TIMEOUT);
+    }
+    return;
+  }
+
+  int k = 0;
+  for (int tile = first; tile < end; tile += step, k++) {
+    const int b = k % NST;
+    if (!mbar_wait_bounded(&full[b], (k / NST) & 1)) {
+      if (lane == 0) atomicOr(err, ERR_TMA_TIMEOUT);
+      break;
+    }
+    const unsigned char* st = smem + b * Tile::STAGE_BYTES;
+    const BatchLine<T>& I = *reinterpret_cast<const BatchLine<T>*>(st + Tile::OFF_PRM);
+    const LineParams<T>& prm = I.prm;
+    const T* sP = reinterpret_cast<const T*>(st);
+    const T* sN = reinterpret_cast<const T*>(st + Tile::OFF_N);
+    const T* sA = reinterpret_cast<const T*>(st + Tile::OFF_A);
+    const T* sC = reinterpret_cast<const T*>(st + Tile::OFF_C);
+    const BatchTile tt = tiles[tile];
+    const T* in = rk == 1 ? prm.un : (rk == 3 ? I.wb : I.wa);
+    T* wout = (rk == 1 || rk == 3) ? I.wa : I.wb;
+    const T c_acc = I.c_acc[rk - 1], c_w = I.c_w[rk - 1];
+    const int nx = prm.nx, ny = prm.ny;
+    const long long pitch = prm.pitch;
 #pragma unroll
-  for (int r = 0; r < kLineTileY / kLineThreadsY; r++) {
-    const int j = tt.j0 + threadIdx.y + kLineThreadsY * r;
-    if (j < I.prm.ny) line_point<T, ORD, LK_ADV2D, STAGE>(I.prm, in, wout, c_acc, c_w, i, j);
+    for (int rr = 0; rr < ROWS; rr++) {
+      const int y = warp * ROWS + rr, j = tt.j0 + y;
+      if (j >= ny) break;
+#pragma unroll
+      for (int cc = 0; cc < kWaveTX / 32; cc++) {
+        const int x = lane + 32 * cc, i = tt.i0 + x;
+        if (i >= nx) continue;
+        const T* c = sP + (y + HY) * PW + (x + HX);  // the point in the stage input's box
+        T kx, ky;
+        if (i >= CS && i < nx - CS) {
+          kx = prm.dx.taps[0] * c[-R];
+#pragma unroll
+          for (int s = 1; s < W; s++)
+            if (s != R) kx = fma(prm.dx.taps[s], c[s - R], kx);
+        } else {
+          kx = closure_line<T, ORD>(in + (long long)j * pitch, 1, nx, i, prm.dx.cls);
+        }
+        if (j >= CS && j < ny - CS) {
+          ky = prm.dy.taps[0] * c[-R * PW];
+#pragma unroll
+          for (int s = 1; s < W; s++)
+            if (s != R) ky = fma(prm.dy.taps[s], c[(s - R) * PW], ky);
+        } else {
+          ky = closure_line<T, ORD>(in + i, pitch, ny, j, prm.dy.cls);
+        }
+        const T cen = *c;
+        const T kk = adv2d_sat<T>(prm, i, j, kx + ky, cen);
+        const long long o = (long long)j * pitch + i;
+        const int p = y * kWaveTX + x;  // the point in a point box
+        if constexpr (STAGE == ST_FIRST) {
+          prm.acc[o] = Tile::COMP ? c_acc * kk : fma(c_acc, kk, cen);
+          wout[o] = fma(c_w, kk, cen);
+        } else if constexpr (STAGE == ST_MID) {
+          prm.acc[o] = fma(c_acc, kk, sA[p]);
+          wout[o] = fma(c_w, kk, sN[p]);
+        } else {
+          const T d = fma(c_acc, kk, sA[p]);
+          if constexpr (Tile::COMP) {  // Kahan: u^n + d with the carried error
+            const T u0 = sN[p], e = sC[p];
+            const T yv = d - e;
+            const T tv = u0 + yv;
+            prm.comp[o] = (tv - u0) - yv;
+            prm.un[o] = tv;
+          } else {
+            prm.un[o] = d;
+          }
+        }
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[b]);
   }
 }
 

@@ -1,6 +1,7 @@
 // wave_batch_inst.cu -- instantiations and launchers of the batched stage
-// kernels for one SBP order (compiled once per order with -DSBP_ORDER=2/4/6).
-// Tile heights offered to the autotuner: FP64 8 or 16 rows, FP32 16 or 32.
+// kernels for one SBP order (compiled once per order with -DSBP_ORDER=2/4/6):
+// every configuration of the wave and advection tables (wave_batch.cuh) for
+// the three RK4 stage kinds, FP32 and FP64.
 #include "launch.h"
 
 #ifndef SBP_ORDER
@@ -14,97 +15,104 @@ namespace sbp {
 
 namespace {
 
-template <typename T, int STAGE, int TY>
-constexpr int batch_smem() {
-  return BatchWaveTile<T, SBP_ORDER, STAGE, TY>::SMEM;
+template <typename T, int STAGE, int CFG>
+cudaError_t configure_wave_one() {
+  return cudaFuncSetAttribute(wave_batch_stage_kernel<T, SBP_ORDER, STAGE, CFG>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              BatchWaveTile<T, SBP_ORDER, STAGE, CFG>::SMEM);
 }
 
-template <typename T, int TY>
-cudaError_t configure_ty() {
+template <typename T, int STAGE, int CFG>
+cudaError_t configure_adv_one() {
+  return cudaFuncSetAttribute(adv_batch_stage_kernel<T, SBP_ORDER, STAGE, CFG>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, AdvTile<T, SBP_ORDER, STAGE, CFG>::SMEM);
+}
+
+template <typename T, int CFG>
+cudaError_t configure_cfg(bool wave) {
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(wave_batch_stage_kernel<T, SBP_ORDER, ST_FIRST, TY>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, batch_smem<T, ST_FIRST, TY>())) !=
-      cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(wave_batch_stage_kernel<T, SBP_ORDER, ST_MID, TY>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, batch_smem<T, ST_MID, TY>())) !=
-      cudaSuccess)
-    return e;
-  return cudaFuncSetAttribute(wave_batch_stage_kernel<T, SBP_ORDER, ST_LAST, TY>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, batch_smem<T, ST_LAST, TY>());
+  if (wave) {
+    if ((e = configure_wave_one<T, ST_FIRST, CFG>()) != cudaSuccess) return e;
+    if ((e = configure_wave_one<T, ST_MID, CFG>()) != cudaSuccess) return e;
+    return configure_wave_one<T, ST_LAST, CFG>();
+  }
+  if ((e = configure_adv_one<T, ST_FIRST, CFG>()) != cudaSuccess) return e;
+  if ((e = configure_adv_one<T, ST_MID, CFG>()) != cudaSuccess) return e;
+  return configure_adv_one<T, ST_LAST, CFG>();
 }
 
-template <typename T, int TY>
-cudaError_t launch_ty(int stage, const BatchWave<T>* insts, const CUtensorMap* maps, const BatchTile* tiles, int ntiles,
-                      int rk, int* err, unsigned grid, cudaStream_t s) {
-  switch (stage) {
-    case ST_FIRST:
-      wave_batch_stage_kernel<T, SBP_ORDER, ST_FIRST, TY>
-          <<<grid, BatchWaveTile<T, SBP_ORDER, ST_FIRST, TY>::THREADS, batch_smem<T, ST_FIRST, TY>(), s>>>(insts, maps, tiles, ntiles, rk, err);
-      break;
-    case ST_MID:
-      wave_batch_stage_kernel<T, SBP_ORDER, ST_MID, TY>
-          <<<grid, BatchWaveTile<T, SBP_ORDER, ST_MID, TY>::THREADS, batch_smem<T, ST_MID, TY>(), s>>>(insts, maps, tiles, ntiles, rk, err);
-      break;
-    case ST_LAST:
-      wave_batch_stage_kernel<T, SBP_ORDER, ST_LAST, TY>
-          <<<grid, BatchWaveTile<T, SBP_ORDER, ST_LAST, TY>::THREADS, batch_smem<T, ST_LAST, TY>(), s>>>(insts, maps, tiles, ntiles, rk, err);
-      break;
-    default: return cudaErrorInvalidValue;
+template <typename T, int STAGE, int CFG>
+void launch_wave_one(const BatchWave<T>* insts, const CUtensorMap* maps, const BatchTile* tiles, int ntiles, int rk,
+                     int* err, unsigned grid, cudaStream_t s) {
+  using Tile = BatchWaveTile<T, SBP_ORDER, STAGE, CFG>;
+  wave_batch_stage_kernel<T, SBP_ORDER, STAGE, CFG><<<grid, Tile::THREADS, Tile::SMEM, s>>>(insts, maps, tiles, ntiles,
+                                                                                            rk, err);
+}
+
+template <typename T, int STAGE, int CFG>
+void launch_adv_one(const BatchLine<T>* insts, const CUtensorMap* maps, const BatchTile* tiles, int ntiles, int rk,
+                    int* err, unsigned grid, cudaStream_t s) {
+  using Tile = AdvTile<T, SBP_ORDER, STAGE, CFG>;
+  adv_batch_stage_kernel<T, SBP_ORDER, STAGE, CFG><<<grid, Tile::THREADS, Tile::SMEM, s>>>(insts, maps, tiles, ntiles,
+                                                                                           rk, err);
+}
+
+template <typename T, int CFG>
+cudaError_t launch_cfg(bool wave, int stage, const void* insts, const CUtensorMap* maps, const BatchTile* tiles,
+                       int ntiles, int rk, int* err, unsigned grid, cudaStream_t s) {
+  if (wave) {
+    const BatchWave<T>* w = static_cast<const BatchWave<T>*>(insts);
+    switch (stage) {
+      case ST_FIRST: launch_wave_one<T, ST_FIRST, CFG>(w, maps, tiles, ntiles, rk, err, grid, s); break;
+      case ST_MID: launch_wave_one<T, ST_MID, CFG>(w, maps, tiles, ntiles, rk, err, grid, s); break;
+      case ST_LAST: launch_wave_one<T, ST_LAST, CFG>(w, maps, tiles, ntiles, rk, err, grid, s); break;
+      default: return cudaErrorInvalidValue;
+    }
+  } else {
+    const BatchLine<T>* l = static_cast<const BatchLine<T>*>(insts);
+    switch (stage) {
+      case ST_FIRST: launch_adv_one<T, ST_FIRST, CFG>(l, maps, tiles, ntiles, rk, err, grid, s); break;
+      case ST_MID: launch_adv_one<T, ST_MID, CFG>(l, maps, tiles, ntiles, rk, err, grid, s); break;
+      case ST_LAST: launch_adv_one<T, ST_LAST, CFG>(l, maps, tiles, ntiles, rk, err, grid, s); break;
+      default: return cudaErrorInvalidValue;
+    }
   }
   return cudaGetLastError();
 }
 
 }  // namespace
 
-template <>
-cudaError_t CAT(configure_wave_batch_o, SBP_ORDER)<double>(int ty) {
-  return ty == 8 ? configure_ty<double, 8>() : (ty == 16 ? configure_ty<double, 16>() : cudaErrorInvalidValue);
-}
-template <>
-cudaError_t CAT(configure_wave_batch_o, SBP_ORDER)<float>(int ty) {
-  return ty == 16 ? configure_ty<float, 16>() : (ty == 32 ? configure_ty<float, 32>() : cudaErrorInvalidValue);
-}
+static_assert(kBatchCfgs == 4, "the switches below cover four configurations");
 
-template <>
-cudaError_t CAT(launch_wave_batch_o, SBP_ORDER)<double>(int stage, int ty, const BatchWave<double>* insts,
-                                                        const CUtensorMap* maps, const BatchTile* tiles, int ntiles, int rk,
-                                                        int* err, unsigned grid, cudaStream_t s) {
-  if (ty == 8) return launch_ty<double, 8>(stage, insts, maps, tiles, ntiles, rk, err, grid, s);
-  if (ty == 16) return launch_ty<double, 16>(stage, insts, maps, tiles, ntiles, rk, err, grid, s);
-  return cudaErrorInvalidValue;
-}
-template <>
-cudaError_t CAT(launch_wave_batch_o, SBP_ORDER)<float>(int stage, int ty, const BatchWave<float>* insts,
-                                                       const CUtensorMap* maps, const BatchTile* tiles, int ntiles, int rk,
-                                                       int* err, unsigned grid, cudaStream_t s) {
-  if (ty == 16) return launch_ty<float, 16>(stage, insts, maps, tiles, ntiles, rk, err, grid, s);
-  if (ty == 32) return launch_ty<float, 32>(stage, insts, maps, tiles, ntiles, rk, err, grid, s);
-  return cudaErrorInvalidValue;
+template <typename T>
+cudaError_t CAT(configure_batch_o, SBP_ORDER)(bool wave, int cfg) {
+  switch (cfg) {
+    case 0: return configure_cfg<T, 0>(wave);
+    case 1: return configure_cfg<T, 1>(wave);
+    case 2: return configure_cfg<T, 2>(wave);
+    case 3: return configure_cfg<T, 3>(wave);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 template <typename T>
-static cudaError_t adv_launch(int stage, const BatchLine<T>* insts, const BatchTile* tiles, int ntiles, int rk,
-                              cudaStream_t s) {
-  const dim3 block(kLineTileX, kLineThreadsY);
-  switch (stage) {
-    case ST_FIRST: adv_batch_stage_kernel<T, SBP_ORDER, ST_FIRST><<<ntiles, block, 0, s>>>(insts, tiles, rk); break;
-    case ST_MID: adv_batch_stage_kernel<T, SBP_ORDER, ST_MID><<<ntiles, block, 0, s>>>(insts, tiles, rk); break;
-    case ST_LAST: adv_batch_stage_kernel<T, SBP_ORDER, ST_LAST><<<ntiles, block, 0, s>>>(insts, tiles, rk); break;
+cudaError_t CAT(launch_batch_o, SBP_ORDER)(bool wave, int stage, int cfg, const void* insts, const CUtensorMap* maps,
+                                          const BatchTile* tiles, int ntiles, int rk, int* err, unsigned grid,
+                                          cudaStream_t s) {
+  switch (cfg) {
+    case 0: return launch_cfg<T, 0>(wave, stage, insts, maps, tiles, ntiles, rk, err, grid, s);
+    case 1: return launch_cfg<T, 1>(wave, stage, insts, maps, tiles, ntiles, rk, err, grid, s);
+    case 2: return launch_cfg<T, 2>(wave, stage, insts, maps, tiles, ntiles, rk, err, grid, s);
+    case 3: return launch_cfg<T, 3>(wave, stage, insts, maps, tiles, ntiles, rk, err, grid, s);
     default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
-template <>
-cudaError_t CAT(launch_adv_batch_o, SBP_ORDER)<double>(int stage, const BatchLine<double>* insts, const BatchTile* tiles,
-                                                       int ntiles, int rk, cudaStream_t s) {
-  return adv_launch<double>(stage, insts, tiles, ntiles, rk, s);
-}
-template <>
-cudaError_t CAT(launch_adv_batch_o, SBP_ORDER)<float>(int stage, const BatchLine<float>* insts, const BatchTile* tiles,
-                                                      int ntiles, int rk, cudaStream_t s) {
-  return adv_launch<float>(stage, insts, tiles, ntiles, rk, s);
-}
+template cudaError_t CAT(configure_batch_o, SBP_ORDER)<float>(bool, int);
+template cudaError_t CAT(configure_batch_o, SBP_ORDER)<double>(bool, int);
+template cudaError_t CAT(launch_batch_o, SBP_ORDER)<float>(bool, int, int, const void*, const CUtensorMap*,
+                                                          const BatchTile*, int, int, int*, unsigned, cudaStream_t);
+template cudaError_t CAT(launch_batch_o, SBP_ORDER)<double>(bool, int, int, const void*, const CUtensorMap*,
+                                                           const BatchTile*, int, int, int*, unsigned, cudaStream_t);
 
 }  // namespace sbp

@@ -39,7 +39,7 @@ EXPORTS = ("sbp_create", "sbp_destroy", "sbp_last_error", "sbp_dofs", "sbp_rhs",
            "sbp_wave_rhs_noalloc", "sbp_write_petsc_vec", "sbp_read_petsc_vec",
            "sbp_batch_create", "sbp_batch_destroy", "sbp_batch_last_error", "sbp_batch_set_state",
            "sbp_batch_get_state", "sbp_batch_rk4_resident", "sbp_batch_synchronize", "sbp_batch_autotune",
-           "sbp_batch_tile_height", "sbp_batch_get_stream", "sbp_batch_points", "sbp_batch_launch_count",
+           "sbp_batch_tile_height", "sbp_batch_kernel_config", "sbp_batch_select_config", "sbp_batch_get_stream", "sbp_batch_points", "sbp_batch_launch_count",
            "sbp_cnn_create", "sbp_cnn_destroy", "sbp_cnn_last_error", "sbp_cnn_param_count", "sbp_cnn_init",
            "sbp_cnn_get_params", "sbp_cnn_set_params", "sbp_cnn_forward", "sbp_cnn_gradients", "sbp_cnn_train_step",
            "sbp_cnn_features", "sbp_cnn_correct", "sbp_cnn_launch_count",
@@ -139,6 +139,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.sbp_batch_synchronize.argtypes = [P]
     L.sbp_batch_autotune.argtypes = [P, C.c_char_p]
     L.sbp_batch_tile_height.argtypes = [P, C.c_int]
+    L.sbp_batch_kernel_config.argtypes = [P, C.c_int, C.c_int, C.POINTER(C.c_int)]
+    L.sbp_batch_select_config.argtypes = [P, C.c_int, C.c_int, C.c_int]
     L.sbp_batch_get_stream.argtypes = [P, C.POINTER(C.c_void_p)]
     L.sbp_batch_points.argtypes = [P]
     L.sbp_batch_points.restype = C.c_longlong
@@ -532,6 +534,17 @@ class Batch:
 
     def tile_height(self, order: int) -> int:
         return self._L.sbp_batch_tile_height(self._h, order)
+
+    def kernel_config(self, order: int, problem: int) -> dict:
+        """The kernel configuration of one (order, problem) group: tile rows, compute warps,
+        ring depth and CTAs per SM (zeros for an empty group)."""
+        cfg = (C.c_int * 4)()
+        self._check(self._L.sbp_batch_kernel_config(self._h, order, problem, cfg))
+        return dict(zip(("rows", "warps", "ring", "ctas_per_sm"), list(cfg)))
+
+    def select_config(self, order: int, problem: int, index: int):
+        """Runs entry `index` (0..3) of the group's configuration table from now on."""
+        self._check(self._L.sbp_batch_select_config(self._h, order, problem, index))
 
     @property
     def points(self) -> int:

@@ -246,12 +246,21 @@ int sbp_batch_get_state(sbp_batch* batch, int index, double* v, int where);
 /* nsteps RK4 steps of every instance (each with its own dt); enqueues only. */
 int sbp_batch_rk4_resident(sbp_batch* batch, long long nsteps);
 int sbp_batch_synchronize(sbp_batch* batch);
-/* Picks each order group's tile height (FP64: 8 or 16 rows, FP32: 16 or 32)
- * by timing the stage kernel on this batch; results are cached in the flat
- * JSON file cache_path (NULL: no cache). Call between steps: it writes only
- * the stage scratch buffers, never the states. */
+/* Picks the kernel configuration of each (order, problem) group -- tile rows,
+ * compute warps, ring depth, CTAs per SM, from a table of four per kind and
+ * precision -- by timing the group's middle stage on this batch; results are
+ * cached in the flat JSON file cache_path (NULL: no cache). Call between steps:
+ * it writes only the stage scratch buffers, never the states. */
 int sbp_batch_autotune(sbp_batch* batch, const char* cache_path);
+/* Tile rows of the order's wave group (0: no wave instance of that order). */
 int sbp_batch_tile_height(const sbp_batch* batch, int order);
+/* cfg[0..3] = tile rows, compute warps, ring depth, CTAs per SM of the group of
+ * `order` and `problem` (SBP_WAVE_HOM_2D or SBP_ADVECTION_2D); zeros for an
+ * empty group. */
+int sbp_batch_kernel_config(const sbp_batch* batch, int order, int problem, int* cfg);
+/* Makes entry `index` (0..3) of the group's configuration table the one it runs
+ * (what sbp_batch_autotune does with the fastest). Call between steps. */
+int sbp_batch_select_config(sbp_batch* batch, int order, int problem, int index);
 int sbp_batch_get_stream(const sbp_batch* batch, void** stream);
 long long sbp_batch_points(const sbp_batch* batch);       /* grid points over all instances */
 long long sbp_batch_launch_count(const sbp_batch* batch); /* kernels launched so far */

@@ -87,14 +87,47 @@ def test_batch_autotune_keeps_states_and_caches(sbp, tmp_path):
         b.autotune(cache)
         for order in (2, 4, 6):
             assert b.tile_height(order) in (0, 8, 16)
+            for problem in (sbp.WAVE_HOM_2D, sbp.ADVECTION_2D):
+                cfg = b.kernel_config(order, problem)
+                assert cfg == dict(rows=0, warps=0, ring=0, ctas_per_sm=0) or (
+                    cfg["rows"] % cfg["warps"] == 0 and 2 <= cfg["ring"] <= 8 and cfg["ctas_per_sm"] in (1, 2)), cfg
         b.step_resident(20)
         b.synchronize()
         got = [b.get_state(k) for k in range(len(insts))]
     entries = json.load(open(cache))
-    assert entries and all(v in (8, 16) for v in entries.values())
+    assert entries and all(v in range(4) for v in entries.values())
     for k, d in enumerate(insts):
         ref = _single(sbp, d, v0[k], 20, 0)
         assert np.max(np.abs(got[k] - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_every_kernel_configuration_gives_the_same_bits(sbp, precision):
+    """Each of the four table entries of every group (tile rows, warps, ring depth, CTAs per SM)
+    computes each point with the same operations in the same order: the states agree bit for bit
+    after steps that cross a graph chunk."""
+    insts = _instances(sbp, 21 + precision, 12)
+    v0 = [_state(d, k) for k, d in enumerate(insts)]
+    results = []
+    for index in range(4):
+        with sbp.Batch(insts, precision=precision) as b:
+            for k, v in enumerate(v0):
+                b.set_state(k, v)
+            for order in (2, 4, 6):
+                for problem in (sbp.WAVE_HOM_2D, sbp.ADVECTION_2D):
+                    b.select_config(order, problem, index)
+            b.step_resident(105)
+            b.synchronize()
+            results.append([b.get_state(k) for k in range(len(insts))])
+    for index in range(1, 4):
+        for k in range(len(insts)):
+            assert np.array_equal(results[index][k], results[0][k]), (index, k, insts[k])
+
+
+def test_select_config_rejects_bad_arguments(sbp):
+    """Argument checks run before any device work."""
+    assert sbp.load().sbp_batch_select_config(None, 4, sbp.WAVE_HOM_2D, 0) == sbp.ERR_INVALID
 
 
 @pytest.mark.gpu
