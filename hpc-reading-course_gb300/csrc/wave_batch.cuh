@@ -68,9 +68,9 @@ struct BatchTile {
 // group of a batch runs the configuration the autotuner picked from its table
 // by timing the group's middle stage on the batch itself (sbp_batch_autotune);
 // entry 0 is the default. Every entry fits the 227 KB of shared memory a CTA may
-// use, and with 2 CTAs per SM the 228 KB of the SM (static_asserts below). 17 warps
-// per SM leave 96 registers a thread, which the FP32 wave kernel with 16-row
-// tiles and a 3-deep ring exceeds (it spilled): its 3-deep entry has 8 warps.
+// use, and with 2 CTAs per SM the 228 KB of the SM (static_asserts below). More
+// than 16 warps per SM leave 96 registers a thread, which the FP32 wave kernel
+// with 16-row tiles and a 3-deep ring exceeds (it spilled): that entry has 8 warps.
 struct BatchCfg {
   int ty, warps, nst, ctas;
 };
@@ -78,7 +78,7 @@ constexpr int kBatchCfgs = 4;
 template <typename T> struct BatchCfgTable;
 template <> struct BatchCfgTable<float> {
   static constexpr BatchCfg wave[kBatchCfgs] = {{32, 16, 2, 1}, {16, 8, 3, 1}, {16, 8, 2, 2}, {16, 8, 4, 1}};
-  static constexpr BatchCfg adv[kBatchCfgs] = {{32, 8, 4, 1}, {64, 16, 3, 1}, {16, 4, 4, 2}, {32, 8, 2, 2}};
+  static constexpr BatchCfg adv[kBatchCfgs] = {{32, 8, 4, 1}, {64, 8, 3, 1}, {16, 4, 4, 2}, {32, 8, 2, 2}};
 };
 template <> struct BatchCfgTable<double> {
   static constexpr BatchCfg wave[kBatchCfgs] = {{16, 8, 2, 1}, {8, 8, 2, 1}, {8, 8, 3, 1}, {8, 4, 2, 2}};
@@ -109,6 +109,8 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, CFG>::THREADS, ba
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   uint64_t* dbar = reinterpret_cast<uint64_t*>(smem + Tile::OFF_DBAR);
+  int2* origin = reinterpret_cast<int2*>(smem + Tile::OFF_BAR + 192);  // each stage's tile origin
+  static_assert(NST <= 8, "tile origins: 64 bytes");
   if (threadIdx.x == 0) {
     for (int s = 0; s < NST; s++) {
       mbar_init(&full[s], 1);
@@ -136,6 +138,7 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, CFG>::THREADS, ba
         const int i0 = tt.i0, j0 = tt.j0;
         const CUtensorMap* m = maps + (long long)tt.slot * kBatchMaps;
         unsigned char* st = smem + b * Tile::STAGE_BYTES;
+        origin[b] = make_int2(i0, j0);  // published by the arrive below
         mbar_arrive_expect_tx(&full[b], Tile::TX_BYTES);
         tma_load_3d(st, &m[3 * sel + 0], i0 - HX, j0 - HY, 2, &full[b]);
         tma_load_3d(st + Tile::OFF_U, &m[3 * sel + 1], i0 - HX, j0, 0, &full[b]);
@@ -161,8 +164,8 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, CFG>::THREADS, ba
     }
     const unsigned char* st = smem + b * Tile::STAGE_BYTES;
     const BatchWave<T>& I = *reinterpret_cast<const BatchWave<T>*>(st + Tile::OFF_PRM);
-    const BatchTile tt = tiles[tile];
-    const int i0 = tt.i0, j0 = tt.j0;
+    const int2 o0 = origin[b];
+    const int i0 = o0.x, j0 = o0.y;
     const T* in;
     T* wout;
     T c_acc, c_w;
@@ -211,9 +214,12 @@ struct AdvTile {
   static constexpr int OFF_A = OFF_N + (LOAD_UN ? BYTES_PT : 0);
   static constexpr int OFF_C = OFF_A + (LOAD_ACC ? BYTES_PT : 0);
   static constexpr int OFF_PRM = align128(OFF_C + (LOAD_COMP ? BYTES_PT : 0));
-  static constexpr int STAGE_BYTES = OFF_PRM + align128((int)sizeof(BatchLine<T>));
-  static constexpr int OFF_BAR = NST * STAGE_BYTES;  // full[8], empty[8]
-  static constexpr int SMEM = OFF_BAR + 128;
+  // the RHS and centre value of the tile's x-face points, kept for the deferred SAT pass ([side][row][2])
+  static constexpr int OFF_DEF = OFF_PRM + align128((int)sizeof(BatchLine<T>));
+  static constexpr int STAGE_BYTES = OFF_DEF + align128(2 * TY * 2 * (int)sizeof(T));
+  // full[8] (+0), empty[8] (+64), deferred-pass barriers[8] (+128), tile origins int2[8] (+192)
+  static constexpr int OFF_BAR = NST * STAGE_BYTES;
+  static constexpr int SMEM = OFF_BAR + 256;
   static constexpr uint32_t TX_BYTES = BYTES_P + (LOAD_UN ? BYTES_PT : 0) + (LOAD_ACC ? BYTES_PT : 0) +
                                        (LOAD_COMP ? BYTES_PT : 0) + (int)sizeof(BatchLine<T>);
   static_assert(TY % WARPS == 0, "tile rows must split evenly over the compute warps");
@@ -222,29 +228,64 @@ struct AdvTile {
   static_assert(C.ctas * (SMEM + 1024) <= 228 * 1024, "CTAs per SM exceed shared memory");
 };
 
+// Closure row of D1 along a line held in shared memory: closure_line's operations
+// in its order (the same bits), with plain loads.
+template <typename T, int ORD>
+__device__ __forceinline__ T closure_line_smem(const T* line, int st, int n, int i, const T (&cls)[6][9]) {
+  constexpr int CW = OpShape<ORD>::CW;
+  T s;
+  if (i < OpShape<ORD>::CS) {
+    s = cls[i][0] * line[0];
+#pragma unroll
+    for (int k = 1; k < CW; k++) s = fma(cls[i][k], line[k * st], s);
+  } else {
+    const int r = n - 1 - i;
+    const T* base = line + (n - CW) * st;
+    s = -cls[r][CW - 1] * base[0];
+#pragma unroll
+    for (int k = 1; k < CW; k++) s = fma(-cls[r][CW - 1 - k], base[k * st], s);
+  }
+  return s;
+}
+
+// A closure row from global memory for the advection kernel's rare tiles whose
+// closure stencil leaves the box; out of line, so its registers stay out of the
+// kernel's main loop.
+template <typename T, int ORD>
+__device__ __noinline__ T closure_line_global(const T* line, long long st, int n, int i, const T (&cls)[6][9]) {
+  return closure_line<T, ORD>(line, st, n, i, cls);
+}
+
 // Batched 2D advection u_t = -(a u_x + b u_y) (code/demo/advection/advection_rhs.h:155-393,
 // 460-528), persistent like the wave kernel: the producer warp loads each (instance,
-// tile) pair's boxes with the instance's tensor maps and bulk-copies its parameter
-// block beside them into a ring of NST stages; each compute warp takes TY / WARPS rows
-// of 64 points (two per lane). Interior taps read the stage input's box, closure rows
-// read global memory (the closure reaches past the tile halo), the SAT is FP64 at
-// boundary points; the taps and their order of accumulation are the single-instance
-// line kernel's, so both give the same bits. A CTA takes every gridDim.x-th tile.
+// tile) pair's boxes with the instance's tensor maps, bulk-copies its parameter block
+// beside them and writes the tile's origin into the stage's slot, in a ring of NST
+// stages; each compute warp takes TY / WARPS rows of 64 points (two per lane). Taps
+// read the stage input's box -- closure rows too, where their stencil lies inside it
+// (else global memory) -- in the single-instance line kernel's order, so both give
+// the same bits. The SAT is FP64: inline at y-face points (whole warp rows), and for
+// the x-face points, which hold one lane of a row each, in a deferred pass of one warp
+// over the tile's two x faces (one FP64 sequence per 32 face points instead of one
+// per row). A CTA takes every gridDim.x-th tile.
 template <typename T, int ORD, int STAGE, int CFG>
 __global__ void __launch_bounds__(AdvTile<T, ORD, STAGE, CFG>::THREADS, batch_adv_cfg<T, CFG>().ctas)
     adv_batch_stage_kernel(const BatchLine<T>* __restrict__ insts, const CUtensorMap* __restrict__ maps,
                            const BatchTile* __restrict__ tiles, int ntiles, int rk, int* err) {
   using Tile = AdvTile<T, ORD, STAGE, CFG>;
-  constexpr int HX = Tile::HX, HY = Tile::HY, NST = Tile::NST, WARPS = Tile::WARPS, PW = Tile::PW;
-  constexpr int W = OpShape<ORD>::W, CS = OpShape<ORD>::CS, R = Tile::R, ROWS = Tile::TY / WARPS;
+  constexpr int HX = Tile::HX, HY = Tile::HY, NST = Tile::NST, WARPS = Tile::WARPS, PW = Tile::PW, TY = Tile::TY;
+  constexpr int W = OpShape<ORD>::W, CS = OpShape<ORD>::CS, CW = OpShape<ORD>::CW, R = Tile::R;
+  constexpr int ROWS = TY / WARPS;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
   uint64_t* empty = full + 8;
+  uint64_t* dbar = full + 16;
+  int2* origin = reinterpret_cast<int2*>(smem + Tile::OFF_BAR + 192);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int s = 0; s < NST; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], WARPS);
+      mbar_init(&dbar[s], WARPS);
     }
     fence_barrier_init();
   }
@@ -266,6 +307,7 @@ __global__ void __launch_bounds__(AdvTile<T, ORD, STAGE, CFG>::THREADS, batch_ad
         }
         const CUtensorMap* m = maps + (long long)tt.slot * kAdvMaps;
         unsigned char* st = smem + b * Tile::STAGE_BYTES;
+        origin[b] = make_int2(tt.i0, tt.j0);  // published by the arrive below
         mbar_arrive_expect_tx(&full[b], Tile::TX_BYTES);
         tma_load_3d(st, &m[sel], tt.i0 - HX, tt.j0 - HY, 0, &full[b]);
         if (Tile::LOAD_UN) tma_load_3d(st + Tile::OFF_N, &m[3], tt.i0, tt.j0, 0, &full[b]);
@@ -279,6 +321,7 @@ __global__ void __launch_bounds__(AdvTile<T, ORD, STAGE, CFG>::THREADS, batch_ad
     return;
   }
 
+  uint32_t dphase = 0;  // parity of each stage's next deferred-pass barrier phase
   int k = 0;
   for (int tile = first; tile < end; tile += step, k++) {
     const int b = k % NST;
@@ -293,19 +336,51 @@ __global__ void __launch_bounds__(AdvTile<T, ORD, STAGE, CFG>::THREADS, batch_ad
     const T* sN = reinterpret_cast<const T*>(st + Tile::OFF_N);
     const T* sA = reinterpret_cast<const T*>(st + Tile::OFF_A);
     const T* sC = reinterpret_cast<const T*>(st + Tile::OFF_C);
-    const BatchTile tt = tiles[tile];
+    T* sD = reinterpret_cast<T*>(const_cast<unsigned char*>(st) + Tile::OFF_DEF);
+    const int2 o0 = origin[b];
+    const int i0 = o0.x, j0 = o0.y;
     const T* in = rk == 1 ? prm.un : (rk == 3 ? I.wb : I.wa);
     T* wout = (rk == 1 || rk == 3) ? I.wa : I.wb;
     const T c_acc = I.c_acc[rk - 1], c_w = I.c_w[rk - 1];
     const int nx = prm.nx, ny = prm.ny;
     const long long pitch = prm.pitch;
+    // closure stencils inside the box (columns i0 - HX .. i0 + 64 + HX - 1, rows j0 - HY ..
+    // j0 + TY + HY - 1): the first CW points of a line when the tile starts it, the last CW
+    // when they neither start before nor end after the box
+    static_assert(CW <= kWaveTX && CW <= TY + HY, "a tile that starts a line holds its closure stencil");
+    const bool xl_in = i0 == 0, xr_in = nx - CW >= i0 - HX && nx <= i0 + kWaveTX + HX;
+    const bool yl_in = j0 == 0, yr_in = ny - CW >= j0 - HY && ny <= j0 + TY + HY;
+    const bool xfaces = prm.bc && (i0 == 0 || i0 + kWaveTX >= nx);  // the tile holds column 0 or nx - 1
+    // the RK4 stage update of point (i, j), (x, y) in the tile
+    auto store = [&](int i, int j, int x, int y, T kk, T cen) {
+      const long long o = (long long)j * pitch + i;
+      const int p = y * kWaveTX + x;  // the point in a point box
+      if constexpr (STAGE == ST_FIRST) {
+        prm.acc[o] = Tile::COMP ? c_acc * kk : fma(c_acc, kk, cen);
+        wout[o] = fma(c_w, kk, cen);
+      } else if constexpr (STAGE == ST_MID) {
+        prm.acc[o] = fma(c_acc, kk, sA[p]);
+        wout[o] = fma(c_w, kk, sN[p]);
+      } else {
+        const T d = fma(c_acc, kk, sA[p]);
+        if constexpr (Tile::COMP) {  // Kahan: u^n + d with the carried error
+          const T u0 = sN[p], e = sC[p];
+          const T yv = d - e;
+          const T tv = u0 + yv;
+          prm.comp[o] = (tv - u0) - yv;
+          prm.un[o] = tv;
+        } else {
+          prm.un[o] = d;
+        }
+      }
+    };
 #pragma unroll
     for (int rr = 0; rr < ROWS; rr++) {
-      const int y = warp * ROWS + rr, j = tt.j0 + y;
+      const int y = warp * ROWS + rr, j = j0 + y;
       if (j >= ny) break;
 #pragma unroll
       for (int cc = 0; cc < kWaveTX / 32; cc++) {
-        const int x = lane + 32 * cc, i = tt.i0 + x;
+        const int x = lane + 32 * cc, i = i0 + x;
         if (i >= nx) continue;
         const T* c = sP + (y + HY) * PW + (x + HX);  // the point in the stage input's box
         T kx, ky;
@@ -314,37 +389,46 @@ __global__ void __launch_bounds__(AdvTile<T, ORD, STAGE, CFG>::THREADS, batch_ad
 #pragma unroll
           for (int s = 1; s < W; s++)
             if (s != R) kx = fma(prm.dx.taps[s], c[s - R], kx);
+        } else if (i < CS ? xl_in : xr_in) {
+          kx = closure_line_smem<T, ORD>(c - i, 1, nx, i, prm.dx.cls);  // c - i: the line's point 0
         } else {
-          kx = closure_line<T, ORD>(in + (long long)j * pitch, 1, nx, i, prm.dx.cls);
+          kx = closure_line_global<T, ORD>(in + (long long)j * pitch, 1, nx, i, prm.dx.cls);
         }
         if (j >= CS && j < ny - CS) {
           ky = prm.dy.taps[0] * c[-R * PW];
 #pragma unroll
           for (int s = 1; s < W; s++)
             if (s != R) ky = fma(prm.dy.taps[s], c[(s - R) * PW], ky);
+        } else if (j < CS ? yl_in : yr_in) {
+          ky = closure_line_smem<T, ORD>(c - j * PW, PW, ny, j, prm.dy.cls);
         } else {
-          ky = closure_line<T, ORD>(in + i, pitch, ny, j, prm.dy.cls);
+          ky = closure_line_global<T, ORD>(in + i, pitch, ny, j, prm.dy.cls);
         }
         const T cen = *c;
-        const T kk = adv2d_sat<T>(prm, i, j, kx + ky, cen);
-        const long long o = (long long)j * pitch + i;
-        const int p = y * kWaveTX + x;  // the point in a point box
-        if constexpr (STAGE == ST_FIRST) {
-          prm.acc[o] = Tile::COMP ? c_acc * kk : fma(c_acc, kk, cen);
-          wout[o] = fma(c_w, kk, cen);
-        } else if constexpr (STAGE == ST_MID) {
-          prm.acc[o] = fma(c_acc, kk, sA[p]);
-          wout[o] = fma(c_w, kk, sN[p]);
+        if (xfaces && (i == 0 || i == nx - 1)) {  // x-face point: its SAT in the deferred pass
+          T* d = sD + ((i == 0 ? 0 : TY) + y) * 2;
+          d[0] = kx + ky;
+          d[1] = cen;
+          continue;
+        }
+        store(i, j, x, y, adv2d_sat<T>(prm, i, j, kx + ky, cen), cen);
+      }
+    }
+    if (xfaces) {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&dbar[b]);  // this warp's deferred entries are in shared memory
+      const uint32_t par = (dphase >> b) & 1u;
+      dphase ^= 1u << b;
+      if (warp == k % WARPS) {
+        if (!mbar_wait_bounded(&dbar[b], par)) {
+          if (lane == 0) atomicOr(err, ERR_TMA_TIMEOUT);
         } else {
-          const T d = fma(c_acc, kk, sA[p]);
-          if constexpr (Tile::COMP) {  // Kahan: u^n + d with the carried error
-            const T u0 = sN[p], e = sC[p];
-            const T yv = d - e;
-            const T tv = u0 + yv;
-            prm.comp[o] = (tv - u0) - yv;
-            prm.un[o] = tv;
-          } else {
-            prm.un[o] = d;
+          for (int e = lane; e < 2 * TY; e += 32) {
+            const int side = e / TY, y = e - side * TY, j = j0 + y;
+            const int i = side == 0 ? 0 : nx - 1;
+            if (j >= ny || i < i0 || i >= i0 + kWaveTX) continue;
+            const T* d = sD + (side * TY + y) * 2;
+            store(i, j, i - i0, y, adv2d_sat<T>(prm, i, j, d[0], d[1]), d[1]);
           }
         }
       }
