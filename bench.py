@@ -62,7 +62,8 @@ def parse():
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the forms record (other orders and sizes, FP32, the batched form)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--study", default=None, choices=["precision", "batched", "learned", "rk45", "wave3d", "decomp"],
+    ap.add_argument("--study", default=None,
+                    choices=["precision", "batched", "learned", "rk45", "wave3d", "decomp", "cnn"],
                     help="precision: variable rho, K (seeded Fourier fields) to --t-end in FP64 and in "
                          "compensated FP32; prints errors of FP32 against FP64 and both wall times. "
                          "batched: 512 uneven wave/advection instances in one batch, FP64 and FP32. "
@@ -777,8 +778,68 @@ def run_learned_study(args):
     print(json.dumps(out), flush=True)
 
 
+def run_cnn_study(args):
+    """The learned correction's network at the learned study's shape (8 images of 258 x 257, the
+    coarse two-layer grid): one forward pass, and one training step (forward, loss, weight, bias and
+    input gradients, Adam), random inputs, CUDA events on the network's stream after warm-up. FLOPs:
+    2 * 9 * cin * cout per pixel and convolution (padded channels 32, 32, 32, 32 -> 32, 32, 32, 16);
+    a training step adds the input gradients of layers 1-3 and the four weight gradients."""
+    import numpy as np
+    import torch
+
+    import build as gpu_build
+    import sbpgpu
+
+    gpu_build.build()
+    B, H, W = 8, 258, 257
+    rng = np.random.default_rng(11)
+    x = torch.from_numpy(rng.standard_normal((B, H, W, 24)).astype(np.float32)).cuda()
+    t = torch.from_numpy((0.1 * rng.standard_normal((B, H, W, 3))).astype(np.float32)).cuda()
+    out = torch.empty((B, H, W, 3), dtype=torch.float32, device="cuda")
+    P = B * H * W
+    convs = [(32, 32), (32, 32), (32, 32), (32, 16)]
+    fwd_flops = sum(2 * 9 * ci * co for ci, co in convs) * P
+    train_flops = fwd_flops + sum(2 * 9 * ci * co for ci, co in convs[1:]) * P + fwd_flops
+    peak = measured_peaks_tensor()
+    res = {"study": "cnn", "batch": B, "height": H, "width": W}
+    stream = torch.cuda.current_stream()
+    with sbpgpu.Cnn(H, W, B, stream=stream.cuda_stream) as net:  # on torch's stream: the events below see it
+        for _ in range(3):
+            net.forward(x.data_ptr(), B, out.data_ptr())
+            net.train_step(x.data_ptr(), t.data_ptr(), B, 1e-4)
+        torch.cuda.synchronize()
+        reps = max(3, args.steps)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(reps):
+            net.forward(x.data_ptr(), B, out.data_ptr())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        fwd_s = ev0.elapsed_time(ev1) / 1e3 / reps
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            net.train_step(x.data_ptr(), t.data_ptr(), B, 1e-4)
+        train_s = (time.perf_counter() - t0) / reps  # train_step synchronizes
+    res["forward"] = {"ms": fwd_s * 1e3, "tflops": fwd_flops / fwd_s / 1e12, "of_bf16_peak": fwd_flops / fwd_s / 1e12 / peak}
+    res["train_step"] = {"ms": train_s * 1e3, "tflops": train_flops / train_s / 1e12,
+                         "note": "wall time per synchronous step, host launch overhead included"}
+    res["bf16_peak_tflops"] = peak
+    print(json.dumps(res), flush=True)
+
+
+def measured_peaks_tensor():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except (OSError, KeyError, ValueError):
+        return 1900.0
+
+
 def main():
     args = parse()
+    if args.study == "cnn":
+        run_cnn_study(args)
+        return
     if args.study == "learned":
         run_learned_study(args)
         return

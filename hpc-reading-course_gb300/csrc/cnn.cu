@@ -3,12 +3,12 @@
 // the GPU by the kernels in this file. No counterpart in the reference.
 //
 // Tensors are NHWC. Activations and weights are BF16; every product is
-// accumulated in FP32 on the tensor cores (mma.sync m16n8k16, BF16 inputs,
-// FP32 accumulators); master weights, biases and Adam moments are FP32.
-// Channel counts are padded to multiples of 16 (the MMA K step): input 24 -> 32,
-// output 3 -> 16; the padding carries zeros.
+// accumulated in FP32 on the tensor cores; master weights, biases and Adam
+// moments are FP32. Channel counts are padded to multiples of 16 (the MMA K
+// step): input 24 -> 32, output 3 -> 16; the padding carries zeros.
 //
-//   conv3x3_fwd_kernel    implicit GEMM, M = pixels, N = output channels,
+//   conv3x3_tc_kernel     implicit GEMM on tcgen05 (TMA tiles, tensor-memory
+//                         accumulator), M = 128 pixels, N = output channels,
 //                         K = 9 taps x input channels; also computes the input
 //                         gradient (dgrad) with the spatially flipped,
 //                         transposed weights.
@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "../../include/sbpgpu.h"
+#include "sbp_device.cuh"
 
 namespace sbp {
 namespace cnn {
@@ -55,80 +56,196 @@ __device__ __forceinline__ void mma_16816(float (&d)[4], const uint32_t (&a)[4],
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// y[p][n] = act(bias[n] + sum_{tap,c} x[p + off(tap)][c] * w[n][tap][c]), zero padding outside
-// the image. One warp computes 16 pixels x COUT channels; 4 warps per CTA.
+// ---------------------------------------------------------------- tcgen05 convolution
+// The forward and input-gradient 3x3 convolutions on the 5th-generation tensor cores:
+// an implicit GEMM per 128-pixel tile (th x tw pixels of one image), M = 128 pixels,
+// N = COUT, K = 9 taps x CIN. TMA loads each tap's shifted input tile (a 4D box
+// {CIN, tw, th, 1} of the NHWC activations: the image border comes back as zeros)
+// and each tap's weight tile into shared memory, rows of CIN BF16 values swizzled
+// by the TMA (64-byte swizzle for 32 channels, 32-byte for 16) -- the K-major
+// layout the MMA's shared-memory descriptors describe. One thread issues
+// tcgen05.mma (kind::f16, BF16 inputs, FP32 accumulator in tensor memory) tap by
+// tap as the tiles land, K = 16 per instruction; tcgen05.commit signals the
+// epilogue, where each warp reads its 32 accumulator lanes (pixels) with
+// tcgen05.ld, adds the bias, applies ReLU and stores. Every wait is bounded.
+
+// Shared-memory descriptor of a K-major operand tile with rows of `rowb` bytes
+// swizzled in 8-row atoms (stride between atoms: 8 rows), tcgen05 version.
+__device__ __forceinline__ uint64_t umma_smem_desc(uint32_t saddr, uint32_t atom_bytes, uint32_t layout) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);  // start address
+  d |= (uint64_t)1u << 16;                           // leading offset: unused by swizzled K-major tiles
+  d |= (uint64_t)((atom_bytes >> 4) & 0x3FFFu) << 32;  // stride offset: one 8-row atom
+  d |= (uint64_t)1u << 46;                           // descriptor version of tcgen05
+  d |= (uint64_t)layout << 61;                       // swizzle mode
+  return d;
+}
+
+// Instruction descriptor of kind::f16: BF16 A and B (both K-major), FP32 D, M x N.
+constexpr uint32_t umma_idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t"
+      "}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accum)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(slot)), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive accumulator columns of this thread's lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Shared-memory layout of conv3x3_tc_kernel: the nine taps' input tiles (128 pixel
+// rows of CIN BF16), the nine taps' weight tiles (COUT rows of CIN), barriers and
+// the tensor-memory address; tiles 1024-byte aligned (whole swizzle atoms).
+template <int CIN, int COUT>
+struct TcConv {
+  static_assert(CIN == 16 || CIN == 32, "input channels: one or two K steps of 16 per tap");
+  static_assert(COUT == 16 || COUT == 32, "output channels: the MMA's N");
+  static constexpr int ROWB = CIN * 2;  // bytes per row: the swizzle span
+  static constexpr uint32_t LAYOUT = CIN == 32 ? 4u : 6u;  // 64-byte / 32-byte swizzle
+  static constexpr uint32_t ATOM = 8 * ROWB;
+  static constexpr int A_BYTES = 128 * ROWB, B_BYTES = COUT * ROWB;
+  static constexpr int OFF_B = 9 * A_BYTES;
+  static constexpr int OFF_BAR = OFF_B + ((9 * B_BYTES + 1023) / 1024) * 1024;
+  static constexpr int SMEM = OFF_BAR + 128 + 1024;  // + alignment slack of the dynamic base
+  static constexpr uint32_t IDESC = umma_idesc_bf16(128, COUT);
+  static_assert(A_BYTES % 1024 == 0 && B_BYTES % 256 == 0, "tiles start on swizzle atoms");
+};
+
+// y[p][n] = act(bias[n] + sum_{tap,c} x[p + off(tap)][c] * w[n][tap][c]) for the th x tw
+// pixels of tile blockIdx.x; x through xmap ({CIN, W, H, B}), w through wmap ({CIN, 9, COUT}).
 template <int CIN, int COUT, bool RELU, bool OUT_F32>
-__global__ void __launch_bounds__(128) conv3x3_fwd_kernel(const bf16* __restrict__ x, const bf16* __restrict__ w,
-                                                          const float* __restrict__ bias, void* __restrict__ y, int B,
-                                                          int H, int W) {
-  static_assert(CIN % 16 == 0 && COUT % 8 == 0, "channel padding");
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int g = lane >> 2, t = lane & 3;
-  const long long P = (long long)B * H * W;
-  const long long p0 = ((long long)blockIdx.x * 4 + warp) * 16;
-  if (p0 >= P) return;
-  long long pr[2];
-  int pb[2], ph[2], pw[2];
-  bool pv[2];
-#pragma unroll
-  for (int r = 0; r < 2; r++) {
-    pr[r] = p0 + g + 8 * r;
-    pv[r] = pr[r] < P;
-    const long long q = pv[r] ? pr[r] : 0;
-    pw[r] = (int)(q % W);
-    ph[r] = (int)((q / W) % H);
-    pb[r] = (int)(q / ((long long)W * H));
+__global__ void __launch_bounds__(128) conv3x3_tc_kernel(const __grid_constant__ CUtensorMap xmap,
+                                                         const __grid_constant__ CUtensorMap wmap,
+                                                         const float* __restrict__ bias, void* __restrict__ y, int H,
+                                                         int W, int tw, int th, int* err) {
+  using L = TcConv<CIN, COUT>;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = smem_raw + ((1024 - (smem_addr(smem_raw) & 1023)) & 1023);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);  // [9]: tap tiles landed
+  uint64_t* wbar = full + 9;                                          // weight tiles landed
+  uint64_t* done = full + 10;                                         // accumulator complete
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(full + 11);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntw = (W + tw - 1) / tw, nth = (H + th - 1) / th;
+  const int wb = blockIdx.x % ntw, hb = (blockIdx.x / ntw) % nth, b = blockIdx.x / (ntw * nth);
+  const int w0 = wb * tw, h0 = hb * th;
+  if (threadIdx.x == 0) {
+    for (int t = 0; t < 9; t++) mbar_init(&full[t], 1);
+    mbar_init(wbar, 1);
+    mbar_init(done, 1);
+    fence_barrier_init();
   }
-  float acc[COUT / 8][4];
-#pragma unroll
-  for (int nb = 0; nb < COUT / 8; nb++) acc[nb][0] = acc[nb][1] = acc[nb][2] = acc[nb][3] = 0.f;
-#pragma unroll 1
-  for (int tap = 0; tap < 9; tap++) {
-    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-    const bf16* src[2];
-    bool ok[2];
-#pragma unroll
-    for (int r = 0; r < 2; r++) {
-      const int hh = ph[r] + dy, ww = pw[r] + dx;
-      ok[r] = pv[r] && hh >= 0 && hh < H && ww >= 0 && ww < W;
-      src[r] = x + (((long long)pb[r] * H + (ok[r] ? hh : 0)) * W + (ok[r] ? ww : 0)) * CIN;
+  if (warp == 0) tmem_alloc(tslot, 32);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(wbar, 9 * L::B_BYTES);
+    for (int t = 0; t < 9; t++) tma_load_3d(smem + L::OFF_B + t * L::B_BYTES, &wmap, 0, t, 0, wbar);
+    for (int t = 0; t < 9; t++) {
+      mbar_arrive_expect_tx(&full[t], L::A_BYTES);
+      tma_load_4d(smem + t * L::A_BYTES, &xmap, 0, w0 + t % 3 - 1, h0 + t / 3 - 1, b, &full[t]);
     }
+    bool ok = mbar_wait_bounded(wbar, 0);
+    int t = 0;
+    for (; ok && t < 9; t++) {
+      if (!(ok = mbar_wait_bounded(&full[t], 0))) break;
+      tc_fence_after();
+      const uint32_t a0 = smem_addr(smem + t * L::A_BYTES), b0 = smem_addr(smem + L::OFF_B + t * L::B_BYTES);
 #pragma unroll
-    for (int c0 = 0; c0 < CIN; c0 += 16) {
-      uint32_t a[4];
-      a[0] = ok[0] ? ld_pair(src[0] + c0 + 2 * t) : 0u;
-      a[1] = ok[1] ? ld_pair(src[1] + c0 + 2 * t) : 0u;
-      a[2] = ok[0] ? ld_pair(src[0] + c0 + 8 + 2 * t) : 0u;
-      a[3] = ok[1] ? ld_pair(src[1] + c0 + 8 + 2 * t) : 0u;
-#pragma unroll
-      for (int nb = 0; nb < COUT / 8; nb++) {
-        const bf16* wp = w + ((long long)(nb * 8 + g) * 9 + tap) * CIN + c0;
-        const uint32_t b[2] = {ld_pair(wp + 2 * t), ld_pair(wp + 8 + 2 * t)};
-        mma_16816(acc[nb], a, b);
-      }
+      for (int k = 0; k < CIN / 16; k++)
+        umma_bf16(tmem, umma_smem_desc(a0 + 32 * k, L::ATOM, L::LAYOUT), umma_smem_desc(b0 + 32 * k, L::ATOM, L::LAYOUT),
+                  L::IDESC, (t | k) != 0);
+    }
+    umma_commit(done);  // after the MMAs issued so far
+    if (!ok) {          // a copy did not land in time: flag it and let the others finish
+      atomicOr(err, 1);
+      for (int u = t; u < 9; u++) mbar_wait_bounded(&full[u], 0);
     }
   }
+  const bool fin = mbar_wait_bounded(done, 0);
+  tc_fence_after();
+  if (fin) {
+    const int m = 32 * warp + lane;  // this thread's accumulator lane: pixel m of the tile
+    const int hh = h0 + m / tw, ww = w0 + m % tw;
+    const bool mine = hh < H && ww < W;
+    const long long p = ((long long)b * H + hh) * W + ww;
 #pragma unroll
-  for (int nb = 0; nb < COUT / 8; nb++) {
-    const int n = nb * 8 + 2 * t;
-    const float b0 = bias ? bias[n] : 0.f, b1 = bias ? bias[n + 1] : 0.f;
+    for (int c0 = 0; c0 < COUT; c0 += 16) {
+      uint32_t r[16];
+      tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, r);
+      tmem_wait_ld();
+      if (!mine) continue;
+      float v[16];
 #pragma unroll
-    for (int r = 0; r < 2; r++) {
-      if (!pv[r]) continue;
-      float v0 = acc[nb][2 * r] + b0, v1 = acc[nb][2 * r + 1] + b1;
-      if (RELU) {
-        v0 = fmaxf(v0, 0.f);
-        v1 = fmaxf(v1, 0.f);
+      for (int j = 0; j < 16; j++) {
+        v[j] = __uint_as_float(r[j]) + (bias ? bias[c0 + j] : 0.f);
+        if (RELU) v[j] = fmaxf(v[j], 0.f);
       }
       if (OUT_F32) {
-        float* yp = static_cast<float*>(y) + pr[r] * COUT + n;
-        yp[0] = v0;
-        yp[1] = v1;
+        float4* yp = reinterpret_cast<float4*>(static_cast<float*>(y) + p * COUT + c0);
+#pragma unroll
+        for (int j = 0; j < 4; j++) yp[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
       } else {
-        bf16* yp = static_cast<bf16*>(y) + pr[r] * COUT + n;
-        *reinterpret_cast<uint32_t*>(yp) = pack_pair(__float2bfloat16(v0), __float2bfloat16(v1));
+        uint4* yp = reinterpret_cast<uint4*>(static_cast<bf16*>(y) + p * COUT + c0);
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+          yp[j] = make_uint4(pack_pair(__float2bfloat16(v[8 * j]), __float2bfloat16(v[8 * j + 1])),
+                             pack_pair(__float2bfloat16(v[8 * j + 2]), __float2bfloat16(v[8 * j + 3])),
+                             pack_pair(__float2bfloat16(v[8 * j + 4]), __float2bfloat16(v[8 * j + 5])),
+                             pack_pair(__float2bfloat16(v[8 * j + 6]), __float2bfloat16(v[8 * j + 7])));
       }
     }
+  } else if (lane == 0) {
+    atomicOr(err, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 32);
   }
 }
 
@@ -421,6 +538,8 @@ struct sbp_cnn {
   bf16* dact2 = nullptr;
   float* out16 = nullptr;    // last layer output (FP32, 16 channels)
   float* loss = nullptr;
+  int* err = nullptr;        // the tensor-core convolutions' error word (a bounded wait ran out)
+  int tw = 0, th = 0;        // their pixel tile: th rows of tw pixels, th * tw = 128
   long long launches = 0;
   std::string msg;
 };
@@ -451,33 +570,88 @@ void cnn_release(sbp_cnn* c) {
     for (void* p : ps)
       if (p) cudaFree(p);
   }
-  void* ps[] = {c->dact, c->dact2, c->out16, c->loss};
+  void* ps[] = {c->dact, c->dact2, c->out16, c->loss, c->err};
   for (void* p : ps)
     if (p) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
 }
 
-// Launch one conv of layer l (forward) or its input-gradient conv.
-cudaError_t conv_fwd(int l, const bf16* x, void* y, const sbp_cnn* c, int batch, cudaStream_t s) {
-  const long long P = (long long)batch * c->H * c->W;
-  const int grid = (int)((P + 63) / 64);
-  switch (l) {
-    case 0: conv3x3_fwd_kernel<32, 32, true, false><<<grid, 128, 0, s>>>(x, c->wb[0], c->bias[0], y, batch, c->H, c->W); break;
-    case 1: conv3x3_fwd_kernel<32, 32, true, false><<<grid, 128, 0, s>>>(x, c->wb[1], c->bias[1], y, batch, c->H, c->W); break;
-    case 2: conv3x3_fwd_kernel<32, 32, true, false><<<grid, 128, 0, s>>>(x, c->wb[2], c->bias[2], y, batch, c->H, c->W); break;
-    default: conv3x3_fwd_kernel<32, 16, false, true><<<grid, 128, 0, s>>>(x, c->wb[3], c->bias[3], y, batch, c->H, c->W); break;
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
   }
+  return fn;
+}
+
+// The tensor maps of one convolution: the NHWC BF16 input ({ch, W, H, B}, box {ch, tw,
+// th, 1}) and the weights ([cout][9][ch]: {ch, 9, cout}, box {ch, 1, cout}), rows
+// swizzled over their ch * 2 bytes. Out-of-range boxes read zeros (the image border).
+cudaError_t encode_conv_maps(const sbp_cnn* c, const bf16* x, const bf16* w, int ch, int cout, int batch,
+                             CUtensorMap* xm, CUtensorMap* wm) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return cudaErrorNotSupported;
+  const CUtensorMapSwizzle sw = ch == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
+  const cuuint64_t xd[4] = {(cuuint64_t)ch, (cuuint64_t)c->W, (cuuint64_t)c->H, (cuuint64_t)batch};
+  const cuuint64_t xs[3] = {(cuuint64_t)ch * 2, (cuuint64_t)c->W * ch * 2, (cuuint64_t)c->H * c->W * ch * 2};
+  const cuuint32_t xb[4] = {(cuuint32_t)ch, (cuuint32_t)c->tw, (cuuint32_t)c->th, 1};
+  const cuuint32_t e[4] = {1, 1, 1, 1};
+  if (enc(xm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(x), xd, xs, xb, e, CU_TENSOR_MAP_INTERLEAVE_NONE,
+          sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  const cuuint64_t wd[3] = {(cuuint64_t)ch, 9, (cuuint64_t)cout};
+  const cuuint64_t ws[2] = {(cuuint64_t)ch * 2, (cuuint64_t)9 * ch * 2};
+  const cuuint32_t wbx[3] = {(cuuint32_t)ch, 1, (cuuint32_t)cout};
+  if (enc(wm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16*>(w), wd, ws, wbx, e, CU_TENSOR_MAP_INTERLEAVE_NONE,
+          sw, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  return cudaSuccess;
+}
+
+template <int CIN, int COUT, bool RELU, bool OUT_F32>
+cudaError_t configure_tc() {
+  return cudaFuncSetAttribute(conv3x3_tc_kernel<CIN, COUT, RELU, OUT_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              TcConv<CIN, COUT>::SMEM);
+}
+
+template <int CIN, int COUT, bool RELU, bool OUT_F32>
+cudaError_t launch_tc(const bf16* x, const bf16* w, const float* bias, void* y, const sbp_cnn* c, int batch,
+                      cudaStream_t s) {
+  CUtensorMap xm, wm;
+  cudaError_t e = encode_conv_maps(c, x, w, CIN, COUT, batch, &xm, &wm);
+  if (e != cudaSuccess) return e;
+  const long long tiles = (long long)batch * ((c->H + c->th - 1) / c->th) * ((c->W + c->tw - 1) / c->tw);
+  conv3x3_tc_kernel<CIN, COUT, RELU, OUT_F32><<<(unsigned)tiles, 128, TcConv<CIN, COUT>::SMEM, s>>>(
+      xm, wm, bias, y, c->H, c->W, c->tw, c->th, c->err);
   return cudaGetLastError();
 }
 
+// Shared-memory opt-in of the four tensor-core convolutions (outside stream capture).
+cudaError_t configure_convs() {
+  cudaError_t e;
+  if ((e = configure_tc<32, 32, true, false>()) != cudaSuccess) return e;
+  if ((e = configure_tc<32, 16, false, true>()) != cudaSuccess) return e;
+  if ((e = configure_tc<32, 32, false, false>()) != cudaSuccess) return e;
+  return configure_tc<16, 32, false, false>();
+}
+
+// Launch one conv of layer l (forward) or its input-gradient conv.
+cudaError_t conv_fwd(int l, const bf16* x, void* y, const sbp_cnn* c, int batch, cudaStream_t s) {
+  if (l < kLayers - 1) return launch_tc<32, 32, true, false>(x, c->wb[l], c->bias[l], y, c, batch, s);
+  return launch_tc<32, 16, false, true>(x, c->wb[l], c->bias[l], y, c, batch, s);
+}
+
 cudaError_t conv_dgrad(int l, const bf16* dy, bf16* dx, const sbp_cnn* c, int batch, cudaStream_t s) {
-  const long long P = (long long)batch * c->H * c->W;
-  const int grid = (int)((P + 63) / 64);
-  if (l == 3)
-    conv3x3_fwd_kernel<16, 32, false, false><<<grid, 128, 0, s>>>(dy, c->wT[3], nullptr, dx, batch, c->H, c->W);
-  else
-    conv3x3_fwd_kernel<32, 32, false, false><<<grid, 128, 0, s>>>(dy, c->wT[l], nullptr, dx, batch, c->H, c->W);
-  return cudaGetLastError();
+  if (l == kLayers - 1) return launch_tc<16, 32, false, false>(dy, c->wT[l], nullptr, dx, c, batch, s);
+  return launch_tc<32, 32, false, false>(dy, c->wT[l], nullptr, dx, c, batch, s);
 }
 
 cudaError_t conv_wgrad(int l, const bf16* x, const bf16* dy, float* dw, const sbp_cnn* c, int batch, cudaStream_t s) {
@@ -576,8 +750,23 @@ int sbp_cnn_create(int height, int width, int max_batch, int device, void* strea
     cudaMemset(c->vbias[l], 0, nb * 4);
   }
   if (cudaMalloc(&c->dact, (size_t)P * 32 * 2) || cudaMalloc(&c->dact2, (size_t)P * 32 * 2) ||
-      cudaMalloc(&c->out16, (size_t)P * 16 * 4) || cudaMalloc(&c->loss, 4))
+      cudaMalloc(&c->out16, (size_t)P * 16 * 4) || cudaMalloc(&c->loss, 4) || cudaMalloc(&c->err, 4))
     return bad("cudaMalloc(activations)");
+  cudaMemset(c->err, 0, 4);
+  // the tensor-core convolutions' tile: 128 pixels, th rows of tw (a power of two), the
+  // shape whose tiles cover the image with the fewest padding pixels (ties: wider rows)
+  long long best = -1;
+  for (int tw = 128; tw >= 1; tw /= 2) {
+    const int th = 128 / tw;
+    const long long area = (long long)((width + tw - 1) / tw) * tw * ((height + th - 1) / th) * th;
+    if (best < 0 || area < best) {
+      best = area;
+      c->tw = tw;
+      c->th = th;
+    }
+  }
+  if (configure_convs() != cudaSuccess) return bad("cudaFuncSetAttribute(convolutions)");
+  if (!encode_fn()) return bad("cuTensorMapEncodeTiled is not available from the driver");
   *out = c;
   return sbp_cnn_init(c, 1234);
 }
@@ -699,8 +888,14 @@ static int backward(sbp_cnn* c, const float* x, const float* target, int batch, 
     dnext = tmp;
   }
   float h = 0;
+  int e = 0;
   CCK(cudaMemcpyAsync(&h, c->loss, 4, cudaMemcpyDeviceToHost, c->stream));
+  CCK(cudaMemcpyAsync(&e, c->err, 4, cudaMemcpyDeviceToHost, c->stream));
   CCK(cudaStreamSynchronize(c->stream));
+  if (e) {
+    CCK(cudaMemsetAsync(c->err, 0, 4, c->stream));
+    return cfail(c, SBP_ERR_DEVICE, "a tensor-core convolution's wait for its tiles ran out");
+  }
   if (loss) *loss = h / (float)(P * kOutReal);
   return SBP_OK;
 }

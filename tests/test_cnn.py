@@ -1,6 +1,7 @@
 """The learned-correction network: the CPU checker (oracle/cnn_oracle.py)
-against finite differences, and the GPU kernels (BF16 tensor-core convolutions,
-FP32 accumulation) against the checker."""
+against finite differences, and the GPU kernels (BF16 tensor-core convolutions:
+tcgen05 forward and input-gradient, mma.sync weight gradient; FP32 accumulation)
+against the checker."""
 import numpy as np
 import pytest
 
@@ -48,15 +49,20 @@ def _relerr(a, b):
 
 
 @pytest.mark.gpu
-def test_gpu_forward_and_gradients_match_oracle(sbp):
+@pytest.mark.parametrize("shape", [(2, 19, 23), (3, 32, 40), (1, 64, 64), (1, 9, 200)],
+                         ids=["2x19x23", "3x32x40", "1x64x64", "1x9x200"])
+def test_gpu_forward_and_gradients_match_oracle(sbp, shape):
+    """Tolerances from what BF16 storage with FP32 accumulation leaves against the oracle, which
+    rounds the same tensors to BF16 and sums in FP64 (measured: output <= 1.9e-3, loss <= 8e-6,
+    each layer's weight and bias gradients <= 8e-4, max-norm relative), with a margin of 2.5-6x."""
     import torch
 
-    B, H, W = 2, 19, 23
-    rng = np.random.default_rng(3)
+    B, H, W = shape
+    rng = np.random.default_rng(3 + H)
     x = rng.standard_normal((B, H, W, N.IN_REAL)).astype(np.float32)
     t = rng.standard_normal((B, H, W, 3)).astype(np.float32)
     with sbp.Cnn(H, W, B) as net:
-        vec = _small_params(7).astype(np.float32)
+        vec = _small_params(7 + W).astype(np.float32)
         net.set_params(vec)
         dx = torch.from_numpy(x).cuda()
         dt = torch.from_numpy(t).cuda()
@@ -64,14 +70,14 @@ def test_gpu_forward_and_gradients_match_oracle(sbp):
         net.forward(dx.data_ptr(), B, out.data_ptr())
         loss, g = net.gradients(dx.data_ptr(), dt.data_ptr(), B)
     ref_out, _, _ = N.forward(vec.astype(np.float64), x.astype(np.float64), bf16=True)
-    assert _relerr(out.cpu().numpy(), ref_out) < 2e-2
+    assert _relerr(out.cpu().numpy(), ref_out) < 5e-3
     ref_loss, ref_g = N.loss_and_grad(vec.astype(np.float64), x.astype(np.float64), t.astype(np.float64), bf16=True)
-    assert loss == pytest.approx(ref_loss, rel=2e-2)
+    assert loss == pytest.approx(ref_loss, rel=1e-4)
     o = 0
-    for ci, co, _ in N.LAYERS:
+    for layer, (ci, co, _) in enumerate(N.LAYERS):
         nw = co * 9 * ci
-        assert _relerr(g[o:o + nw], ref_g[o:o + nw]) < 5e-2
-        assert _relerr(g[o + nw:o + nw + co], ref_g[o + nw:o + nw + co]) < 5e-2
+        assert _relerr(g[o:o + nw], ref_g[o:o + nw]) < 5e-3, ("weights", layer)
+        assert _relerr(g[o + nw:o + nw + co], ref_g[o + nw:o + nw + co]) < 5e-3, ("bias", layer)
         o += nw + co
 
 
