@@ -12,13 +12,10 @@
 //                         K = 9 taps x input channels; also computes the input
 //                         gradient (dgrad) with the spatially flipped,
 //                         transposed weights.
-//   conv3x3_wgrad_kernel  GEMM per tap, M = output channels, N = input channels,
-//                         K = pixels: a CTA stages a 8 x 16 pixel tile of dy and
-//                         the matching x tile with its one-pixel halo in shared
-//                         memory once for all nine taps, builds the fragments
-//                         with ldmatrix.trans (K runs over pixels, the rows of
-//                         both NHWC arrays), and folds its FP32 sums into dw
-//                         with atomics once at the end.
+//   conv3x3_wgrad_tc_kernel  weight gradient on tcgen05, K = pixels: four taps'
+//                         shifted input tiles stacked along M (MN-major operands),
+//                         accumulated over all of a CTA's pixel tiles in tensor
+//                         memory and added to dw once per CTA.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -42,19 +39,10 @@ constexpr int kCin[kLayers] = {32, 32, 32, 32};   // padded input channels
 constexpr int kCout[kLayers] = {32, 32, 32, 16};  // padded output channels
 constexpr int kInReal = 24, kOutReal = 3;
 
-__device__ __forceinline__ uint32_t ld_pair(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
-
 __device__ __forceinline__ uint32_t pack_pair(bf16 lo, bf16 hi) {
   return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
 
-// D += A * B, A 16x16 (row), B 16x8 (col), BF16 in, FP32 accumulate.
-__device__ __forceinline__ void mma_16816(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
 
 // ---------------------------------------------------------------- tcgen05 convolution
 // The forward and input-gradient 3x3 convolutions on the 5th-generation tensor cores:
@@ -77,6 +65,19 @@ __device__ __forceinline__ uint64_t umma_smem_desc(uint32_t saddr, uint32_t atom
   d |= (uint64_t)((atom_bytes >> 4) & 0x3FFFu) << 32;  // stride offset: one 8-row atom
   d |= (uint64_t)1u << 46;                           // descriptor version of tcgen05
   d |= (uint64_t)layout << 61;                       // swizzle mode
+  return d;
+}
+
+// The same for an MN-major operand: rows along K of one swizzle span of M (or N)
+// values; `lead` = byte stride between swizzle spans along M, `stride` = between
+// 8-row groups along K.
+__device__ __forceinline__ uint64_t umma_smem_desc_mn(uint32_t saddr, uint32_t lead, uint32_t stride,
+                                                      uint32_t layout) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lead >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((stride >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1u << 46;
+  d |= (uint64_t)layout << 61;
   return d;
 }
 
@@ -133,9 +134,9 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// Shared-memory layout of conv3x3_tc_kernel: the nine taps' input tiles (128 pixel
-// rows of CIN BF16), the nine taps' weight tiles (COUT rows of CIN), barriers and
-// the tensor-memory address; tiles 1024-byte aligned (whole swizzle atoms).
+// Shared-memory layout of conv3x3_tc_kernel: a ring of NS tap tiles (128 pixel rows
+// of CIN BF16), the nine taps' weight tiles (COUT rows of CIN), barriers and the
+// tensor-memory address; tiles 1024-byte aligned (whole swizzle atoms).
 template <int CIN, int COUT>
 struct TcConv {
   static_assert(CIN == 16 || CIN == 32, "input channels: one or two K steps of 16 per tap");
@@ -143,200 +144,302 @@ struct TcConv {
   static constexpr int ROWB = CIN * 2;  // bytes per row: the swizzle span
   static constexpr uint32_t LAYOUT = CIN == 32 ? 4u : 6u;  // 64-byte / 32-byte swizzle
   static constexpr uint32_t ATOM = 8 * ROWB;
+  static constexpr int NS = 9;  // tap tiles in flight: one pixel tile per CTA, two CTAs per SM
+  static constexpr int CTAS = 2;  // resident CTAs per SM (measured at 8 x 258 x 257, forward pass:
+                                  // 0.198 ms; one CTA with 18 slots 0.310 ms, one tile per CTA
+                                  // 0.271 ms, the mma.sync form 0.471 ms)
   static constexpr int A_BYTES = 128 * ROWB, B_BYTES = COUT * ROWB;
-  static constexpr int OFF_B = 9 * A_BYTES;
+  static constexpr int OFF_B = NS * A_BYTES;
   static constexpr int OFF_BAR = OFF_B + ((9 * B_BYTES + 1023) / 1024) * 1024;
-  static constexpr int SMEM = OFF_BAR + 128 + 1024;  // + alignment slack of the dynamic base
+  // full[NS], empty[NS], wbar, accfull[2], accempty[2], done; then the tensor-memory address
+  static constexpr int NBAR = 2 * NS + 6;
+  static constexpr int SMEM = OFF_BAR + 8 * NBAR + 16 + 1024;  // + alignment slack of the dynamic base
   static constexpr uint32_t IDESC = umma_idesc_bf16(128, COUT);
+  static constexpr int THREADS = 192;  // producer, MMA issuer, four epilogue warps
   static_assert(A_BYTES % 1024 == 0 && B_BYTES % 256 == 0, "tiles start on swizzle atoms");
+  static_assert(CTAS * (SMEM + 1024) <= 228 * 1024, "shared memory");
 };
 
-// y[p][n] = act(bias[n] + sum_{tap,c} x[p + off(tap)][c] * w[n][tap][c]) for the th x tw
-// pixels of tile blockIdx.x; x through xmap ({CIN, W, H, B}), w through wmap ({CIN, 9, COUT}).
+// y[p][n] = act(bias[n] + sum_{tap,c} x[p + off(tap)][c] * w[n][tap][c]); x through xmap
+// ({CIN, W, H, B}), w through wmap ({CIN, 9, COUT}). Persistent, two CTAs per SM: a CTA
+// takes every gridDim.x-th 128-pixel tile (th rows of tw pixels). Warp roles: warp 0 loads the weights
+// once, then each tile's nine shifted tap tiles into a ring of NS slots; warp 1 (which owns
+// the tensor memory) issues each tap's MMAs as its tile lands, frees the slot with
+// tcgen05.commit, and commits each pixel tile into one of two accumulators (32 columns
+// each); warps 2-5 read an accumulator (warp w: lanes 32 (w % 4) ..), release it, and add
+// bias, apply ReLU and store while the next tile accumulates in the other. Bounded waits.
 template <int CIN, int COUT, bool RELU, bool OUT_F32>
-__global__ void __launch_bounds__(128) conv3x3_tc_kernel(const __grid_constant__ CUtensorMap xmap,
-                                                         const __grid_constant__ CUtensorMap wmap,
-                                                         const float* __restrict__ bias, void* __restrict__ y, int H,
-                                                         int W, int tw, int th, int* err) {
+__global__ void __launch_bounds__(TcConv<CIN, COUT>::THREADS, TcConv<CIN, COUT>::CTAS)
+    conv3x3_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap wmap,
+                      const float* __restrict__ bias, void* __restrict__ y, int B, int H, int W, int tw, int th,
+                      int* err) {
   using L = TcConv<CIN, COUT>;
+  constexpr int NS = L::NS;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* smem = smem_raw + ((1024 - (smem_addr(smem_raw) & 1023)) & 1023);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);  // [9]: tap tiles landed
-  uint64_t* wbar = full + 9;                                          // weight tiles landed
-  uint64_t* done = full + 10;                                         // accumulator complete
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(full + 11);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);
+  uint64_t* empty = full + NS;
+  uint64_t* wbar = empty + NS;
+  uint64_t* accfull = wbar + 1;
+  uint64_t* accempty = accfull + 2;
+  uint64_t* done = accempty + 2;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntw = (W + tw - 1) / tw, nth = (H + th - 1) / th;
-  const int wb = blockIdx.x % ntw, hb = (blockIdx.x / ntw) % nth, b = blockIdx.x / (ntw * nth);
-  const int w0 = wb * tw, h0 = hb * th;
+  const int ntiles = B * nth * ntw;
   if (threadIdx.x == 0) {
-    for (int t = 0; t < 9; t++) mbar_init(&full[t], 1);
+    for (int s = 0; s < NS; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
     mbar_init(wbar, 1);
+    for (int s = 0; s < 2; s++) {
+      mbar_init(&accfull[s], 1);
+      mbar_init(&accempty[s], 4);
+    }
     mbar_init(done, 1);
     fence_barrier_init();
   }
-  if (warp == 0) tmem_alloc(tslot, 32);
+  if (warp == 1) tmem_alloc(tslot, 64);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
 
-  if (threadIdx.x == 0) {
-    mbar_arrive_expect_tx(wbar, 9 * L::B_BYTES);
-    for (int t = 0; t < 9; t++) tma_load_3d(smem + L::OFF_B + t * L::B_BYTES, &wmap, 0, t, 0, wbar);
-    for (int t = 0; t < 9; t++) {
-      mbar_arrive_expect_tx(&full[t], L::A_BYTES);
-      tma_load_4d(smem + t * L::A_BYTES, &xmap, 0, w0 + t % 3 - 1, h0 + t / 3 - 1, b, &full[t]);
+  if (warp == 0) {  // ---- loads
+    if (lane == 0) {
+      mbar_arrive_expect_tx(wbar, 9 * L::B_BYTES);
+      for (int t = 0; t < 9; t++) tma_load_3d(smem + L::OFF_B + t * L::B_BYTES, &wmap, 0, t, 0, wbar);
+      int k = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+        const int w0 = (tile % ntw) * tw, h0 = ((tile / ntw) % nth) * th, b = tile / (ntw * nth);
+        for (int t = 0; t < 9; t++, k++) {
+          const int s = k % NS;
+          if (k >= NS && !mbar_wait_bounded(&empty[s], ((k / NS) - 1) & 1)) {
+            atomicOr(err, 1);
+            ok = false;
+            break;
+          }
+          mbar_arrive_expect_tx(&full[s], L::A_BYTES);
+          tma_load_4d(smem + s * L::A_BYTES, &xmap, 0, w0 + t % 3 - 1, h0 + t / 3 - 1, b, &full[s]);
+        }
+      }
+      // no copy may be in flight when the CTA exits
+      mbar_wait_bounded(wbar, 0);
+      for (int kk = (k >= NS ? k - NS : 0); kk < k; kk++) mbar_wait_bounded(&full[kk % NS], (kk / NS) & 1);
     }
-    bool ok = mbar_wait_bounded(wbar, 0);
-    int t = 0;
-    for (; ok && t < 9; t++) {
-      if (!(ok = mbar_wait_bounded(&full[t], 0))) break;
+  } else if (warp == 1) {  // ---- MMAs
+    if (lane == 0) {
+      bool ok = mbar_wait_bounded(wbar, 0);
+      int k = 0, it = 0;
+      for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x, it++) {
+        const int buf = it & 1;
+        if (it >= 2 && !(ok = mbar_wait_bounded(&accempty[buf], ((it / 2) - 1) & 1))) break;
+        tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(32 * buf);
+        for (int t = 0; t < 9; t++, k++) {
+          const int s = k % NS;
+          if (!(ok = mbar_wait_bounded(&full[s], (k / NS) & 1))) break;
+          tc_fence_after();
+          const uint32_t a0 = smem_addr(smem + s * L::A_BYTES), b0 = smem_addr(smem + L::OFF_B + t * L::B_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < CIN / 16; kk++)
+            umma_bf16(d, umma_smem_desc(a0 + 32 * kk, L::ATOM, L::LAYOUT),
+                      umma_smem_desc(b0 + 32 * kk, L::ATOM, L::LAYOUT), L::IDESC, (t | kk) != 0);
+          umma_commit(&empty[s]);  // the slot is free once these MMAs have read it
+        }
+        if (!ok) break;
+        umma_commit(&accfull[buf]);
+      }
+      if (!ok) atomicOr(err, 1);
+      umma_commit(done);  // every MMA issued has completed once this arrives
+      mbar_wait_bounded(done, 0);
+    }
+  } else {  // ---- epilogue: warps 2-5
+    const int q = warp & 3;  // the lane quarter this warp may read
+    float bv[COUT];
+#pragma unroll
+    for (int j = 0; j < COUT; j++) bv[j] = bias ? bias[j] : 0.f;
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {
+      const int buf = it & 1;
+      if (!mbar_wait_bounded(&accfull[buf], (it / 2) & 1)) {
+        if (lane == 0) atomicOr(err, 1);
+        break;
+      }
       tc_fence_after();
-      const uint32_t a0 = smem_addr(smem + t * L::A_BYTES), b0 = smem_addr(smem + L::OFF_B + t * L::B_BYTES);
-#pragma unroll
-      for (int k = 0; k < CIN / 16; k++)
-        umma_bf16(tmem, umma_smem_desc(a0 + 32 * k, L::ATOM, L::LAYOUT), umma_smem_desc(b0 + 32 * k, L::ATOM, L::LAYOUT),
-                  L::IDESC, (t | k) != 0);
-    }
-    umma_commit(done);  // after the MMAs issued so far
-    if (!ok) {          // a copy did not land in time: flag it and let the others finish
-      atomicOr(err, 1);
-      for (int u = t; u < 9; u++) mbar_wait_bounded(&full[u], 0);
-    }
-  }
-  const bool fin = mbar_wait_bounded(done, 0);
-  tc_fence_after();
-  if (fin) {
-    const int m = 32 * warp + lane;  // this thread's accumulator lane: pixel m of the tile
-    const int hh = h0 + m / tw, ww = w0 + m % tw;
-    const bool mine = hh < H && ww < W;
-    const long long p = ((long long)b * H + hh) * W + ww;
-#pragma unroll
-    for (int c0 = 0; c0 < COUT; c0 += 16) {
-      uint32_t r[16];
-      tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, r);
+      uint32_t r[COUT];
+      const uint32_t src = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * buf);
+      tmem_ld16(src, *reinterpret_cast<uint32_t(*)[16]>(&r[0]));
+      if (COUT == 32) tmem_ld16(src + 16, *reinterpret_cast<uint32_t(*)[16]>(&r[COUT == 32 ? 16 : 0]));
       tmem_wait_ld();
-      if (!mine) continue;
-      float v[16];
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&accempty[buf]);  // the accumulator may take the tile after next
+      const int w0 = (tile % ntw) * tw, h0 = ((tile / ntw) % nth) * th, b = tile / (ntw * nth);
+      const int m = 32 * q + lane;  // this thread's accumulator lane: pixel m of the tile
+      const int hh = h0 + m / tw, ww = w0 + m % tw;
+      if (hh >= H || ww >= W) continue;
+      const long long p = ((long long)b * H + hh) * W + ww;
+      float v[COUT];
 #pragma unroll
-      for (int j = 0; j < 16; j++) {
-        v[j] = __uint_as_float(r[j]) + (bias ? bias[c0 + j] : 0.f);
+      for (int j = 0; j < COUT; j++) {
+        v[j] = __uint_as_float(r[j]) + bv[j];
         if (RELU) v[j] = fmaxf(v[j], 0.f);
       }
       if (OUT_F32) {
-        float4* yp = reinterpret_cast<float4*>(static_cast<float*>(y) + p * COUT + c0);
+        float4* yp = reinterpret_cast<float4*>(static_cast<float*>(y) + p * COUT);
 #pragma unroll
-        for (int j = 0; j < 4; j++) yp[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+        for (int j = 0; j < COUT / 4; j++) yp[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
       } else {
-        uint4* yp = reinterpret_cast<uint4*>(static_cast<bf16*>(y) + p * COUT + c0);
+        uint4* yp = reinterpret_cast<uint4*>(static_cast<bf16*>(y) + p * COUT);
 #pragma unroll
-        for (int j = 0; j < 2; j++)
+        for (int j = 0; j < COUT / 8; j++)
           yp[j] = make_uint4(pack_pair(__float2bfloat16(v[8 * j]), __float2bfloat16(v[8 * j + 1])),
                              pack_pair(__float2bfloat16(v[8 * j + 2]), __float2bfloat16(v[8 * j + 3])),
                              pack_pair(__float2bfloat16(v[8 * j + 4]), __float2bfloat16(v[8 * j + 5])),
                              pack_pair(__float2bfloat16(v[8 * j + 6]), __float2bfloat16(v[8 * j + 7])));
       }
     }
-  } else if (lane == 0) {
-    atomicOr(err, 1);
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (warp == 1) {
     tc_fence_after();
-    tmem_dealloc(tmem, 32);
+    tmem_dealloc(tmem, 64);
   }
 }
 
-// Four 8x8 b16 matrices from shared memory, transposed: lanes 8q..8q+7 give the row
-// addresses of matrix q; a thread receives rows 2(lane%4), 2(lane%4)+1 of column lane/4.
-__device__ __forceinline__ void ldsm_x4_trans(uint32_t (&r)[4], const bf16* p) {
-  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-               : "r"(a));
-}
+// ---------------------------------------------------------------- tcgen05 weight gradient
+// dw[n][tap][c] += sum_p dy[p][n] * x[p + off(tap)][c] as tcgen05 MMAs with K = pixels:
+// per 128-pixel tile, TMA loads the nine shifted x tiles (as in the forward pass) and the
+// dy tile into one stage. Both operands are MN-major there (channels contiguous per
+// pixel row). Four taps' x tiles, 8 KB apart, form one 128-row A operand (rows (tap, c):
+// the spacing is the descriptor's leading offset), so three MMA groups -- taps 0-3, 4-7
+// and 5-8 (whose last quarter, tap 8, is the one kept) -- cover the nine taps with
+// M = 128, N = COUT, eight K steps of 16 pixels each. The accumulators (3 x COUT
+// tensor-memory columns) sum over every tile the CTA takes; at the end the four
+// epilogue warps read them and add them to dw with one FP32 atomic per entry and CTA.
+template <int COUT>
+struct TcWgrad {
+  static_assert(COUT == 16 || COUT == 32, "output channels: the MMA's N");
+  static constexpr int CIN = 32;
+  static constexpr int A_BYTES = 128 * CIN * 2;  // one tap's x tile
+  static constexpr int B_ROWB = COUT * 2;
+  static constexpr int B_BYTES = 128 * B_ROWB;   // the dy tile
+  static constexpr uint32_t A_LAYOUT = 4u, B_LAYOUT = COUT == 32 ? 4u : 6u;  // 64-byte / 32-byte swizzle
+  static constexpr uint32_t A_SBO = 8 * CIN * 2, B_SBO = 8 * B_ROWB;
+  static constexpr int STAGE = 9 * A_BYTES + B_BYTES;
+  static constexpr int NST = 2;  // stages: the next tile loads while this one's MMAs run
+  static constexpr int OFF_BAR = NST * STAGE;
+  static constexpr int SMEM = OFF_BAR + 64 + 1024;
+  static constexpr uint32_t IDESC = umma_idesc_bf16(128, COUT) | (1u << 15) | (1u << 16);  // A, B MN-major
+  static constexpr int THREADS = 192;
+  static_assert(STAGE % 1024 == 0 && SMEM <= 227 * 1024, "shared memory");
+  // one instruction reads two 8-row K groups of four M spans of A (at most 8 KB + 2 KB past
+  // its start, the last group starting at tap 5 plus seven K steps) and of one span of dy:
+  // inside its stage
+  static_assert(5 * A_BYTES + 14 * A_SBO + A_BYTES + 4 * A_SBO <= 9 * A_BYTES, "operand reads stay in the stage");
+};
 
-constexpr int kWgTH = 8, kWgTW = 16;  // pixel tile: 8 rows of 16 = 8 K steps of 16 pixels
-
-// dw[n][tap][c] += sum_p dy[p][n] * x[p + off(tap)][c], zero padding outside the image.
-// 4 warps: warp w owns output channels 16 (w % MT) .. +15 and input channels 16 (role / MT)
-// .. +15 for all nine taps; when there are fewer (m, n) blocks than warps, the warps of a
-// block split the tile's K steps.
-template <int CIN, int COUT>
-__global__ void __launch_bounds__(128) conv3x3_wgrad_kernel(const bf16* __restrict__ x, const bf16* __restrict__ dy,
-                                                            float* __restrict__ dw, int B, int H, int W) {
-  static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channel padding");
-  constexpr int RSX = CIN + 8, RSY = COUT + 8;  // shared row strides (16-byte padding: no bank conflicts)
-  constexpr int HR = kWgTH + 2, HC = kWgTW + 2;  // x tile with its halo
-  constexpr int MT = COUT / 16, NB = CIN / 16, ROLES = MT * NB, KG = 4 / ROLES;
-  static_assert(ROLES >= 1 && ROLES <= 4 && 4 % ROLES == 0, "warp roles");
-  __shared__ __align__(16) bf16 sX[HR * HC * RSX];
-  __shared__ __align__(16) bf16 sY[kWgTH * kWgTW * RSY];
+template <int COUT>
+__global__ void __launch_bounds__(TcWgrad<COUT>::THREADS, 1)
+    conv3x3_wgrad_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap dymap,
+                            float* __restrict__ dw, int B, int H, int W, int tw, int th, int* err) {
+  using L = TcWgrad<COUT>;
+  constexpr int NST = L::NST, CIN = L::CIN;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* smem = smem_raw + ((1024 - (smem_addr(smem_raw) & 1023)) & 1023);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + L::OFF_BAR);
+  uint64_t* empty = full + NST;
+  uint64_t* accfull = empty + NST;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(accfull + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int role = warp % ROLES, kg = warp / ROLES;
-  const int mt = role % MT, nb = role / MT;
-  float acc[9][2][4];
-#pragma unroll
-  for (int tp = 0; tp < 9; tp++)
-#pragma unroll
-    for (int j = 0; j < 2; j++) acc[tp][j][0] = acc[tp][j][1] = acc[tp][j][2] = acc[tp][j][3] = 0.f;
-  const int tilesX = (W + kWgTW - 1) / kWgTW, tilesY = (H + kWgTH - 1) / kWgTH;
-  const long long ntiles = (long long)B * tilesY * tilesX;
-  const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
-  const int q = lane >> 3, r = lane & 7;
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int b = (int)(tile / ((long long)tilesY * tilesX));
-    const int rem = (int)(tile - (long long)b * tilesY * tilesX);
-    const int ty0 = (rem / tilesX) * kWgTH, tx0 = (rem % tilesX) * kWgTW;
-    // dy tile: pixel p = row * 16 + column, COUT channels in 16-byte chunks
-    for (int e = threadIdx.x; e < kWgTH * kWgTW * (COUT / 8); e += 128) {
-      const int p = e / (COUT / 8), ch = e % (COUT / 8);
-      const int yy = ty0 + p / kWgTW, xx = tx0 + p % kWgTW;
-      uint4 v = zero;
-      if (yy < H && xx < W) v = *reinterpret_cast<const uint4*>(dy + (((long long)b * H + yy) * W + xx) * COUT + ch * 8);
-      *reinterpret_cast<uint4*>(sY + p * RSY + ch * 8) = v;
+  const int ntw = (W + tw - 1) / tw, nth = (H + th - 1) / th;
+  const int ntiles = B * nth * ntw;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NST; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
     }
-    // x tile with a one-pixel halo
-    for (int e = threadIdx.x; e < HR * HC * (CIN / 8); e += 128) {
-      const int rr = e / (CIN / 8), ch = e % (CIN / 8);
-      const int yy = ty0 - 1 + rr / HC, xx = tx0 - 1 + rr % HC;
-      uint4 v = zero;
-      if (yy >= 0 && yy < H && xx >= 0 && xx < W)
-        v = *reinterpret_cast<const uint4*>(x + (((long long)b * H + yy) * W + xx) * CIN + ch * 8);
-      *reinterpret_cast<uint4*>(sX + rr * RSX + ch * 8) = v;
-    }
-    __syncthreads();
-    for (int st = kg; st < kWgTH; st += KG) {  // K step: tile row st, 16 pixels
-      // A = dy^T (16 output channels x 16 pixels): matrices (pixels +8(q>>1), channels +8(q&1))
-      uint32_t a[4];
-      ldsm_x4_trans(a, sY + (st * kWgTW + r + 8 * (q >> 1)) * RSY + mt * 16 + 8 * (q & 1));
-#pragma unroll
-      for (int tp = 0; tp < 9; tp++) {
-        // B = x shifted by the tap (16 pixels x 16 input channels): matrices
-        // (pixels +8(q&1), channels +8(q>>1)) -> b0, b1 of channels 0-7 and of 8-15
-        const int hy = st + tp / 3, hx = r + 8 * (q & 1) + tp % 3;
-        uint32_t bq[4];
-        ldsm_x4_trans(bq, sX + (hy * HC + hx) * RSX + nb * 16 + 8 * (q >> 1));
-        const uint32_t b0[2] = {bq[0], bq[1]}, b1[2] = {bq[2], bq[3]};
-        mma_16816(acc[tp][0], a, b0);
-        mma_16816(acc[tp][1], a, b1);
-      }
-    }
-    __syncthreads();
+    mbar_init(accfull, 1);
+    fence_barrier_init();
   }
-  // accumulator (m, n): c0, c1 at (g, 2t), (g, 2t+1); c2, c3 at (g+8, 2t), (g+8, 2t+1)
-  const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-  for (int tp = 0; tp < 9; tp++)
-#pragma unroll
-    for (int j = 0; j < 2; j++)
-#pragma unroll
-      for (int e = 0; e < 4; e++) {
-        const int m = mt * 16 + g + 8 * (e >> 1), n = nb * 16 + j * 8 + 2 * t + (e & 1);
-        atomicAdd(dw + ((long long)m * 9 + tp) * CIN + n, acc[tp][j][e]);
+  if (warp == 1) tmem_alloc(tslot, 128);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  if (warp == 0) {  // ---- loads
+    if (lane == 0) {
+      int it = 0;
+      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {
+        const int s = it % NST;
+        if (it >= NST && !mbar_wait_bounded(&empty[s], ((it / NST) - 1) & 1)) {
+          atomicOr(err, 1);
+          break;
+        }
+        const int w0 = (tile % ntw) * tw, h0 = ((tile / ntw) % nth) * th, b = tile / (ntw * nth);
+        unsigned char* st = smem + s * L::STAGE;
+        mbar_arrive_expect_tx(&full[s], L::STAGE);
+        for (int t = 0; t < 9; t++) tma_load_4d(st + t * L::A_BYTES, &xmap, 0, w0 + t % 3 - 1, h0 + t / 3 - 1, b, &full[s]);
+        tma_load_4d(st + 9 * L::A_BYTES, &dymap, 0, w0, h0, b, &full[s]);
       }
+      for (int kk = (it >= NST ? it - NST : 0); kk < it; kk++) mbar_wait_bounded(&full[kk % NST], (kk / NST) & 1);
+    }
+  } else if (warp == 1) {  // ---- MMAs
+    if (lane == 0) {
+      bool ok = true;
+      int it = 0;
+      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {
+        const int s = it % NST;
+        if (!(ok = mbar_wait_bounded(&full[s], (it / NST) & 1))) break;
+        tc_fence_after();
+        const uint32_t st = smem_addr(smem + s * L::STAGE), dy0 = st + 9 * L::A_BYTES;
+#pragma unroll
+        for (int g = 0; g < 3; g++) {
+          const uint32_t a0 = st + (g == 0 ? 0 : (g == 1 ? 4 : 5)) * L::A_BYTES;
+#pragma unroll
+          for (int k = 0; k < 8; k++)  // 16 pixels = two 8-row groups per K step
+            umma_bf16(tmem + (uint32_t)(g * COUT),
+                      umma_smem_desc_mn(a0 + 2 * k * L::A_SBO, L::A_BYTES, L::A_SBO, L::A_LAYOUT),
+                      umma_smem_desc_mn(dy0 + 2 * k * L::B_SBO, L::B_SBO, L::B_SBO, L::B_LAYOUT), L::IDESC,
+                      (it | k) != 0);
+        }
+        umma_commit(&empty[s]);
+      }
+      if (!ok) atomicOr(err, 1);
+      umma_commit(accfull);  // every MMA issued has completed once this arrives
+    }
+  } else {  // ---- epilogue: warps 2-5, once per CTA
+    const int q = warp & 3;  // lane quarter: row (tap offset q within a group, c = lane)
+    if (mbar_wait_bounded(accfull, 0)) {
+      tc_fence_after();
+#pragma unroll
+      for (int g = 0; g < 3; g++) {
+        if (g == 2 && q != 3) continue;  // taps 5-7 again: kept from the second group
+        const int tap = (g == 0 ? 0 : (g == 1 ? 4 : 5)) + q;
+#pragma unroll
+        for (int n0 = 0; n0 < COUT; n0 += 16) {
+          uint32_t r[16];
+          tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(g * COUT + n0), r);
+          tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 16; j++) atomicAdd(&dw[((long long)(n0 + j) * 9 + tap) * CIN + lane], __uint_as_float(r[j]));
+        }
+      }
+    } else if (lane == 0) {
+      atomicOr(err, 1);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 128);
+  }
 }
 
 template <int COUT>
@@ -540,6 +643,7 @@ struct sbp_cnn {
   float* loss = nullptr;
   int* err = nullptr;        // the tensor-core convolutions' error word (a bounded wait ran out)
   int tw = 0, th = 0;        // their pixel tile: th rows of tw pixels, th * tw = 128
+  int nsm = 1;               // SMs: the persistent convolutions' grid
   long long launches = 0;
   std::string msg;
 };
@@ -629,18 +733,28 @@ cudaError_t launch_tc(const bf16* x, const bf16* w, const float* bias, void* y, 
   cudaError_t e = encode_conv_maps(c, x, w, CIN, COUT, batch, &xm, &wm);
   if (e != cudaSuccess) return e;
   const long long tiles = (long long)batch * ((c->H + c->th - 1) / c->th) * ((c->W + c->tw - 1) / c->tw);
-  conv3x3_tc_kernel<CIN, COUT, RELU, OUT_F32><<<(unsigned)tiles, 128, TcConv<CIN, COUT>::SMEM, s>>>(
-      xm, wm, bias, y, c->H, c->W, c->tw, c->th, c->err);
+  const long long slots = (long long)TcConv<CIN, COUT>::CTAS * c->nsm;  // persistent: every CTA resident
+  const unsigned grid = (unsigned)(tiles < slots ? tiles : slots);
+  conv3x3_tc_kernel<CIN, COUT, RELU, OUT_F32><<<grid, TcConv<CIN, COUT>::THREADS, TcConv<CIN, COUT>::SMEM, s>>>(
+      xm, wm, bias, y, batch, c->H, c->W, c->tw, c->th, c->err);
   return cudaGetLastError();
 }
 
-// Shared-memory opt-in of the four tensor-core convolutions (outside stream capture).
+template <int COUT>
+cudaError_t configure_wgrad_tc() {
+  return cudaFuncSetAttribute(conv3x3_wgrad_tc_kernel<COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              TcWgrad<COUT>::SMEM);
+}
+
+// Shared-memory opt-in of the tensor-core convolutions (outside stream capture).
 cudaError_t configure_convs() {
   cudaError_t e;
   if ((e = configure_tc<32, 32, true, false>()) != cudaSuccess) return e;
   if ((e = configure_tc<32, 16, false, true>()) != cudaSuccess) return e;
   if ((e = configure_tc<32, 32, false, false>()) != cudaSuccess) return e;
-  return configure_tc<16, 32, false, false>();
+  if ((e = configure_tc<16, 32, false, false>()) != cudaSuccess) return e;
+  if ((e = configure_wgrad_tc<32>()) != cudaSuccess) return e;
+  return configure_wgrad_tc<16>();
 }
 
 // Launch one conv of layer l (forward) or its input-gradient conv.
@@ -654,18 +768,23 @@ cudaError_t conv_dgrad(int l, const bf16* dy, bf16* dx, const sbp_cnn* c, int ba
   return launch_tc<32, 32, false, false>(dy, c->wT[l], nullptr, dx, c, batch, s);
 }
 
+// dw += the weight gradient of layer l (x: its input, 32 channels; dy: its output gradient).
 cudaError_t conv_wgrad(int l, const bf16* x, const bf16* dy, float* dw, const sbp_cnn* c, int batch, cudaStream_t s) {
-  // at most one CTA per SM: each CTA adds its sums to dw once, so this bounds the atomics per entry
-  const long long ntiles = (long long)batch * ((c->H + kWgTH - 1) / kWgTH) * ((c->W + kWgTW - 1) / kWgTW);
-  int nsm = 0;
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
-  const unsigned grid = (unsigned)(ntiles < nsm ? ntiles : (nsm > 0 ? nsm : 1));
-  switch (l) {
-    case 0:
-    case 1:
-    case 2: conv3x3_wgrad_kernel<32, 32><<<grid, 128, 0, s>>>(x, dy, dw, batch, c->H, c->W); break;
-    default: conv3x3_wgrad_kernel<32, 16><<<grid, 128, 0, s>>>(x, dy, dw, batch, c->H, c->W); break;
-  }
+  CUtensorMap xm, dym, unused;
+  const int cout = kCout[l];
+  // x: 32-channel tap tiles; dy: one unshifted tile of cout channels (its map from the same
+  // encoder, with dy as the "input" and the weights map unused)
+  cudaError_t e = encode_conv_maps(c, x, c->wb[l], 32, cout, batch, &xm, &unused);
+  if (e == cudaSuccess) e = encode_conv_maps(c, dy, c->wb[l], cout, cout, batch, &dym, &unused);
+  if (e != cudaSuccess) return e;
+  const long long tiles = (long long)batch * ((c->H + c->th - 1) / c->th) * ((c->W + c->tw - 1) / c->tw);
+  const unsigned grid = (unsigned)(tiles < c->nsm ? tiles : c->nsm);
+  if (cout == 32)
+    conv3x3_wgrad_tc_kernel<32><<<grid, TcWgrad<32>::THREADS, TcWgrad<32>::SMEM, s>>>(xm, dym, dw, batch, c->H, c->W,
+                                                                                     c->tw, c->th, c->err);
+  else
+    conv3x3_wgrad_tc_kernel<16><<<grid, TcWgrad<16>::THREADS, TcWgrad<16>::SMEM, s>>>(xm, dym, dw, batch, c->H, c->W,
+                                                                                     c->tw, c->th, c->err);
   return cudaGetLastError();
 }
 
@@ -766,6 +885,8 @@ int sbp_cnn_create(int height, int width, int max_batch, int device, void* strea
     }
   }
   if (configure_convs() != cudaSuccess) return bad("cudaFuncSetAttribute(convolutions)");
+  if (cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || c->nsm < 1)
+    return bad("cudaDeviceGetAttribute(SMs)");
   if (!encode_fn()) return bad("cuTensorMapEncodeTiled is not available from the driver");
   *out = c;
   return sbp_cnn_init(c, 1234);

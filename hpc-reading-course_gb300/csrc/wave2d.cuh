@@ -338,10 +338,6 @@ __device__ __noinline__ Rhs3<T> apply_sat(const WaveParams<T>& prm, const T* in,
   return Rhs3<T>{(T)ku64, (T)kv64, (T)kp64};
 }
 
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
-
 // RK4 stage update of component c of one point (o: its offset in the state,
 // sp: its place in a tile's 3-component point boxes).
 template <typename T, int STAGE, typename Tile>

@@ -1,7 +1,7 @@
 """The learned-correction network: the CPU checker (oracle/cnn_oracle.py)
-against finite differences, and the GPU kernels (BF16 tensor-core convolutions:
-tcgen05 forward and input-gradient, mma.sync weight gradient; FP32 accumulation)
-against the checker."""
+against finite differences, and the GPU kernels (BF16 tcgen05 convolutions --
+forward, input gradient, weight gradient -- with FP32 accumulation in tensor
+memory) against the checker."""
 import numpy as np
 import pytest
 
