@@ -279,6 +279,33 @@ __device__ __forceinline__ T closure_line(const T* __restrict__ line, long long 
   return s;
 }
 
+// Closure row of D1 along a line held in shared memory: closure_line's operations
+// in its order (the same bits), with plain loads.
+template <typename T, int ORD>
+__device__ __forceinline__ T closure_line_smem(const T* line, int st, int n, int i, const T (&cls)[6][9]) {
+  constexpr int CW = OpShape<ORD>::CW;
+  T s;
+  if (i < OpShape<ORD>::CS) {
+    s = cls[i][0] * line[0];
+#pragma unroll
+    for (int k = 1; k < CW; k++) s = fma(cls[i][k], line[k * st], s);
+  } else {
+    const int r = n - 1 - i;
+    const T* base = line + (n - CW) * st;
+    s = -cls[r][CW - 1] * base[0];
+#pragma unroll
+    for (int k = 1; k < CW; k++) s = fma(-cls[r][CW - 1 - k], base[k * st], s);
+  }
+  return s;
+}
+
+// A closure row from global memory, for the rare points whose closure stencil leaves
+// their tile's boxes; out of line, so its registers stay out of the kernels' main loops.
+template <typename T, int ORD>
+__device__ __noinline__ T closure_line_global(const T* line, long long st, int n, int i, const T (&cls)[6][9]) {
+  return closure_line<T, ORD>(line, st, n, i, cls);
+}
+
 __device__ __forceinline__ double mms_x(double xl, int i, double hi) { return xl + (double)i / hi; }
 
 template <typename T> struct Rhs3 { T u, v, p; };
@@ -444,6 +471,12 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
   (void)sA;
   (void)sC;
   (void)sK;
+  // Closure lines come from the boxes where their stencil lies inside them (box columns
+  // i0 - HX .. i0 + 63 + HX, rows j0 - HY .. j0 + TY - 1 + HY), else from global memory:
+  // the first CW points of a line when the tile starts it, the last CW when they start no
+  // earlier and end no later than the box. The same values either way.
+  constexpr int CW = OpShape<ORD>::CW;
+  const bool xl_in = i0 == 0, xr_in = nx - CW >= i0 - HX && nx <= i0 + kWaveTX + HX;
 #pragma unroll ROW_UNROLL
   for (int rr = 0; rr < ROWS; rr++) {
     const int y = warp * ROWS + rr;
@@ -454,6 +487,8 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
     const int nyb = (prm.ysplit > 0) ? (j >= prm.ysplit ? ny - prm.ysplit : prm.ysplit) : ny;
     const int jl = j - jb0;
     const bool yint = (jl >= CS) && (jl < nyb - CS);
+    const int yb = jl < CS ? jb0 : jb0 + nyb - CW;  // the first row of this point's y closure stencil
+    const bool y_in = yb >= j0 - HY && yb + CW <= j0 + TY + HY;
 #pragma unroll
     for (int cc = 0; cc < kWaveTX / 32; cc++) {
       const int x = lane + 32 * cc;
@@ -483,31 +518,39 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
 #pragma unroll
         for (int s = 1; s < W; s++)
           if (s != R) dxp = fma(prm.dx.taps[s], rowP[s], dxp);
+      } else if (i < CS ? xl_in : xr_in) {
+        dxp = closure_line_smem<T, ORD>(sP + (y + HY) * PW + (HX - i0), 1, nx, i, prm.dx.cls);
       } else {
-        dxp = closure_line<T, ORD>(in + 2 * plane + (long long)j * pitch, 1, nx, i, prm.dx.cls);
+        dxp = closure_line_global<T, ORD>(in + 2 * plane + (long long)j * pitch, 1, nx, i, prm.dx.cls);
       }
       if (yint) {
         dyp = prm.dy.taps[0] * colP[0];
 #pragma unroll
         for (int s = 1; s < W; s++)
           if (s != R) dyp = fma(prm.dy.taps[s], colP[s * PW], dyp);
+      } else if (y_in) {
+        dyp = closure_line_smem<T, ORD>(sP + (jb0 - j0 + HY) * PW + (x + HX), PW, nyb, jl, prm.dy.cls);
       } else {
-        dyp = closure_line<T, ORD>(in + 2 * plane + (long long)jb0 * pitch + i, pitch, nyb, jl, prm.dy.cls);
+        dyp = closure_line_global<T, ORD>(in + 2 * plane + (long long)jb0 * pitch + i, pitch, nyb, jl, prm.dy.cls);
       }
       if (xint) {
         kp = prm.dx.taps[0] * rowU[0];
 #pragma unroll
         for (int s = 1; s < W; s++)
           if (s != R) kp = fma(prm.dx.taps[s], rowU[s], kp);
+      } else if (i < CS ? xl_in : xr_in) {
+        kp = closure_line_smem<T, ORD>(sU + y * PW + (HX - i0), 1, nx, i, prm.dx.cls);
       } else {
-        kp = closure_line<T, ORD>(in + (long long)j * pitch, 1, nx, i, prm.dx.cls);
+        kp = closure_line_global<T, ORD>(in + (long long)j * pitch, 1, nx, i, prm.dx.cls);
       }
       if (yint) {
 #pragma unroll
         for (int s = 0; s < W; s++)
           if (s != R) kp = fma(prm.dy.taps[s], colV[s * kWaveTX], kp);
+      } else if (y_in) {
+        kp += closure_line_smem<T, ORD>(sV + (jb0 - j0 + HY) * kWaveTX + x, kWaveTX, nyb, jl, prm.dy.cls);
       } else {
-        kp += closure_line<T, ORD>(in + plane + (long long)jb0 * pitch + i, pitch, nyb, jl, prm.dy.cls);
+        kp += closure_line_global<T, ORD>(in + plane + (long long)jb0 * pitch + i, pitch, nyb, jl, prm.dy.cls);
       }
 
       const long long q = (long long)j * pitch + i;

@@ -228,33 +228,7 @@ struct AdvTile {
   static_assert(C.ctas * (SMEM + 1024) <= 228 * 1024, "CTAs per SM exceed shared memory");
 };
 
-// Closure row of D1 along a line held in shared memory: closure_line's operations
-// in its order (the same bits), with plain loads.
-template <typename T, int ORD>
-__device__ __forceinline__ T closure_line_smem(const T* line, int st, int n, int i, const T (&cls)[6][9]) {
-  constexpr int CW = OpShape<ORD>::CW;
-  T s;
-  if (i < OpShape<ORD>::CS) {
-    s = cls[i][0] * line[0];
-#pragma unroll
-    for (int k = 1; k < CW; k++) s = fma(cls[i][k], line[k * st], s);
-  } else {
-    const int r = n - 1 - i;
-    const T* base = line + (n - CW) * st;
-    s = -cls[r][CW - 1] * base[0];
-#pragma unroll
-    for (int k = 1; k < CW; k++) s = fma(-cls[r][CW - 1 - k], base[k * st], s);
-  }
-  return s;
-}
 
-// A closure row from global memory for the advection kernel's rare tiles whose
-// closure stencil leaves the box; out of line, so its registers stay out of the
-// kernel's main loop.
-template <typename T, int ORD>
-__device__ __noinline__ T closure_line_global(const T* line, long long st, int n, int i, const T (&cls)[6][9]) {
-  return closure_line<T, ORD>(line, st, n, i, cls);
-}
 
 // Batched 2D advection u_t = -(a u_x + b u_y) (code/demo/advection/advection_rhs.h:155-393,
 // 460-528), persistent like the wave kernel: the producer warp loads each (instance,
