@@ -167,8 +167,19 @@ template <typename T, int KIND> constexpr int wave_ty() {
 #ifndef SBP_FP64_CONV
 #define SBP_FP64_CONV 6
 #endif
-template <typename T, int KIND> constexpr int wave_ring() {
-  return (sizeof(T) == 4 && KIND != WK_VAR) ? SBP_FP32_RING : (sizeof(T) == 8 && KIND == WK_HOM ? SBP_FP64_RING : 2);
+// The first and last stages of the constant-coefficient FP64 kernel load one point box
+// less than the middle stages, which leaves room for a fourth ring stage (4096^2, order 4:
+// 5.73e10 against 5.64e10 point-stage updates/s with three; 8 converter warps instead of
+// 6 measured slower with either depth, 1024^2 unchanged).
+#ifndef SBP_FP64_RING_FL
+#define SBP_FP64_RING_FL 4
+#endif
+template <typename T, int KIND, int STAGE = ST_MID> constexpr int wave_ring() {
+  return (sizeof(T) == 4 && KIND != WK_VAR)
+             ? SBP_FP32_RING
+             : (sizeof(T) == 8 && KIND == WK_HOM ? ((STAGE == ST_FIRST || STAGE == ST_LAST) ? SBP_FP64_RING_FL
+                                                                                            : SBP_FP64_RING)
+                                                 : 2);
 }
 // Consumer warps of the single-instance kernel. The variable-coefficient and
 // manufactured-solution FP64 kernels need up to 166 registers a thread, which
@@ -664,7 +675,7 @@ __device__ __forceinline__ void wave_tile_compute(const WaveParams<T>& prm, cons
 // The Tile type of the single-instance kernel for (T, order, kind, stage).
 template <typename T, int ORD, int KIND, int STAGE>
 using WaveStageTile = WaveTile<T, ORD, STAGE, wave_ty<T, KIND>(), 0, KIND == WK_VAR && SBP_VAR_COEF != 0,
-                               wave_ring<T, KIND>(), wave_warps<T, KIND>(), wave_fixed<T, KIND, STAGE>(),
+                               wave_ring<T, KIND, STAGE>(), wave_warps<T, KIND>(), wave_fixed<T, KIND, STAGE>(),
                                wave_fixed<T, KIND, STAGE>() ? SBP_FP64_CONV : 0>;
 
 // The producer (one lane): takes the CTA's tiles, from the dynamic queue or with a
