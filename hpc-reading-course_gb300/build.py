@@ -118,6 +118,47 @@ def build_driver(force: bool = False) -> str:
     return DRIVER
 
 
+PETSC_LIB = os.path.join(LIB_DIR, "libsbpgpu_petsc.so")
+
+
+def petsc_include_dirs() -> list[str] | None:
+    """PETSc's include directories from $PETSC_DIR (and $PETSC_ARCH), or None when its headers
+    are not there."""
+    base = os.environ.get("PETSC_DIR")
+    if not base:
+        return None
+    dirs = [os.path.join(base, "include")]
+    arch = os.environ.get("PETSC_ARCH")
+    if arch:
+        dirs.append(os.path.join(base, arch, "include"))
+    return dirs if os.path.exists(os.path.join(dirs[0], "petscts.h")) else None
+
+
+def build_petsc_adapter(force: bool = False) -> str | None:
+    """libsbpgpu_petsc.so (petsc/sbp_petsc.cpp, include/sbp_petsc.h): the TSSetRHSFunction
+    callback and ts_rk4 / ts_rk45 drop-ins over libsbpgpu, built where PETSc's headers are
+    found ($PETSC_DIR[/$PETSC_ARCH]). Returns its path, or None without PETSc."""
+    inc = petsc_include_dirs()
+    if inc is None:
+        return None
+    lib = build()
+    src = os.path.join(PKG, "petsc", "sbp_petsc.cpp")
+    if not force and os.path.exists(PETSC_LIB) and os.path.getmtime(PETSC_LIB) >= max(os.path.getmtime(src),
+                                                                                       os.path.getmtime(lib)):
+        return PETSC_LIB
+    base, arch = os.environ["PETSC_DIR"], os.environ.get("PETSC_ARCH", "")
+    cmd = (["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include")] +
+           [a for d in inc for a in ("-I", d)] +
+           [src, "-o", PETSC_LIB + ".tmp", "-L", LIB_DIR, "-lsbpgpu", "-Wl,-rpath,$ORIGIN",
+            "-L", os.path.join(base, arch, "lib"), "-lpetsc"])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stdout + r.stderr)
+        raise RuntimeError("build of libsbpgpu_petsc failed")
+    os.replace(PETSC_LIB + ".tmp", PETSC_LIB)
+    return PETSC_LIB
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--force", action="store_true")

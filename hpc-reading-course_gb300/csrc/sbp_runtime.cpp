@@ -824,6 +824,8 @@ const char* sbp_last_error(const sbp_ctx* ctx) { return ctx ? ctx->msg.c_str() :
 
 int sbp_dofs(const sbp_ctx* ctx) { return ctx ? ctx->dofs : SBP_ERR_INVALID; }
 
+long long sbp_size(const sbp_ctx* ctx) { return ctx ? ctx->nscalar : SBP_ERR_INVALID; }
+
 int sbp_rhs(sbp_ctx* ctx, double t, const double* src, double* dst, int where) {
   return rhs_impl(ctx, t, src, dst, where, 1);
 }

@@ -32,7 +32,7 @@ DOFS = {WAVE_HOM_2D: 3, WAVE_MMS_2D: 3, WAVE_VAR_2D: 3, ADVECTION_1D: 1, ADVECTI
         WAVE_2BLOCK_2D: 3, WAVE_3D: 4}
 
 # Every exported entry point of include/sbpgpu.h.
-EXPORTS = ("sbp_create", "sbp_destroy", "sbp_last_error", "sbp_dofs", "sbp_rhs", "sbp_apply", "sbp_rk4_nsteps",
+EXPORTS = ("sbp_create", "sbp_destroy", "sbp_last_error", "sbp_dofs", "sbp_size", "sbp_rhs", "sbp_apply", "sbp_rk4_nsteps",
            "sbp_ts_rk4", "sbp_rk4", "sbp_set_state", "sbp_get_state", "sbp_rk4_resident", "sbp_synchronize",
            "sbp_error_norms", "sbp_hnorm", "sbp_get_stream", "sbp_launch_count", "sbp_probe_dfma_rate",
            "sbp_set_wait_limit", "sbp_test_drop_tile",
@@ -105,6 +105,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.sbp_last_error.argtypes = [P]
     L.sbp_last_error.restype = C.c_char_p
     L.sbp_dofs.argtypes = [P]
+    L.sbp_size.argtypes = [P]
+    L.sbp_size.restype = C.c_longlong
     for n in ("sbp_rhs", "sbp_apply"):
         getattr(L, n).argtypes = [P, C.c_double, C.c_void_p, C.c_void_p, C.c_int]
     L.sbp_rk4_nsteps.argtypes = [C.c_double, _dp]

@@ -104,6 +104,8 @@ int sbp_destroy(sbp_ctx* ctx);
 const char* sbp_last_error(const sbp_ctx* ctx);
 /* Scalars per grid point of the context's problem (4, 3, 2 or 1). */
 int sbp_dofs(const sbp_ctx* ctx);
+/* Doubles in one state in the AoS format: dofs * nx * ny (* nz). */
+long long sbp_size(const sbp_ctx* ctx);
 
 /* RHS callback body: dst = F(t, src) = matrix-free apply + boundary terms.
  * Replaces PetscErrorCode rhs_serial(TS, PetscReal t, Vec src, Vec dst, void*)
