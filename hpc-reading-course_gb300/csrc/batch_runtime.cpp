@@ -14,8 +14,10 @@
 //
 // Autotuner: each group's kernel configuration (tile rows, compute warps, ring
 // depth, CTAs per SM: the tables of wave_batch.cuh) is chosen by timing the
-// group's middle stage on the batch itself; choices are cached in a flat JSON
-// file keyed by device, precision, problem kind, order and the group's size.
+// group's middle stage on the batch itself; then the whole step is timed with
+// those choices and with every group on each table entry, and the fastest kept.
+// Choices are cached in a flat JSON file keyed by device, precision, problem
+// kind, order and the group's size.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -351,6 +353,65 @@ int run_chunk(sbp_batch* b, long long steps) {
   return SBP_OK;
 }
 
+// Among the per-group choices and the four uniform assignments (every group on entry e),
+// keeps the one whose whole step -- all groups, their chains side by side -- is fastest:
+// a group timed alone does not see how the groups share the device. The states (u^n, and
+// comp in FP32) are saved before the trial steps and restored after them.
+template <typename T>
+int whole_step_choice(sbp_batch* b) {
+  constexpr long long kSteps = 5;
+  constexpr int NC = kBatchCfgs + 1;
+  int cand[NC][6];
+  for (int g = 0; g < 6; g++) {
+    cand[0][g] = b->cfg[g];
+    for (int e = 0; e < kBatchCfgs; e++) cand[e + 1][g] = e;
+  }
+  struct Scratch {
+    void* un = nullptr;
+    void* comp = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ~Scratch() {
+      if (un) cudaFree(un);
+      if (comp) cudaFree(comp);
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+    }
+  } sc;
+  BCK(cudaEventCreate(&sc.e0));
+  BCK(cudaEventCreate(&sc.e1));
+  BCK(cudaMalloc(&sc.un, b->pool_bytes));
+  BCK(cudaMemcpyAsync(sc.un, b->un, b->pool_bytes, cudaMemcpyDeviceToDevice, b->stream));
+  if (b->comp) {
+    BCK(cudaMalloc(&sc.comp, b->pool_bytes));
+    BCK(cudaMemcpyAsync(sc.comp, b->comp, b->pool_bytes, cudaMemcpyDeviceToDevice, b->stream));
+  }
+  const long long launches = b->launches;
+  float best_ms = 1e30f;
+  int best = 0, rc = SBP_OK;
+  for (int c = 0; c < NC && rc == SBP_OK; c++) {
+    for (int g = 0; g < 6 && rc == SBP_OK; g++)
+      if (group_used(b, g) && b->cfg[g] != cand[c][g]) rc = build_group(b, g, cand[c][g]);
+    if (rc || (rc = run_chunk<T>(b, kSteps))) break;  // captures this assignment's graph
+    BCK(cudaEventRecord(sc.e0, b->stream));
+    if ((rc = run_chunk<T>(b, kSteps))) break;
+    BCK(cudaEventRecord(sc.e1, b->stream));
+    BCK(cudaEventSynchronize(sc.e1));
+    float ms = 0;
+    BCK(cudaEventElapsedTime(&ms, sc.e0, sc.e1));
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  }
+  for (int g = 0; g < 6 && rc == SBP_OK; g++)
+    if (group_used(b, g) && b->cfg[g] != cand[best][g]) rc = build_group(b, g, cand[best][g]);
+  BCK(cudaMemcpyAsync(b->un, sc.un, b->pool_bytes, cudaMemcpyDeviceToDevice, b->stream));
+  if (b->comp) BCK(cudaMemcpyAsync(b->comp, sc.comp, b->pool_bytes, cudaMemcpyDeviceToDevice, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  b->launches = launches;
+  return rc;
+}
+
 // ---- tiny flat JSON cache {"key": int, ...}
 std::map<std::string, int> read_cache(const char* path) {
   std::map<std::string, int> m;
@@ -605,6 +666,8 @@ int sbp_batch_autotune(sbp_batch* b, const char* cache_path) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   int rc = SBP_OK;
+  std::vector<std::pair<int, std::string>> keys;  // (group, cache key) of the groups in the batch
+  bool timed = false;                              // a group missed the cache: choices to confirm
   for (int g = 0; g < 6 && rc == SBP_OK; g++) {
     const int order = group_order(g);
     const bool wave = group_is_wave(g);
@@ -618,11 +681,13 @@ int sbp_batch_autotune(sbp_batch* b, const char* cache_path) {
     const std::string key = std::string(prop.name) + "|" + (b->fp32 ? "fp32" : "fp64") + "|" +
                             (wave ? "wave" : "advection") + "|order" + std::to_string(order) + "|points" +
                             std::to_string(bucket) + "|cfg";
+    keys.emplace_back(g, key);
     auto hit = cache.find(key);
     if (hit != cache.end() && hit->second >= 0 && hit->second < kBatchCfgs) {
       if (hit->second != b->cfg[g]) rc = build_group(b, g, hit->second);
       continue;
     }
+    timed = true;
     float best_ms = 1e30f;
     int best = 0;
     for (int c = 0; c < kBatchCfgs && rc == SBP_OK; c++) {
@@ -645,12 +710,15 @@ int sbp_batch_autotune(sbp_batch* b, const char* cache_path) {
       }
     }
     if (rc == SBP_OK && best != b->cfg[g]) rc = build_group(b, g, best);
-    cache[key] = best;
-    dirty = true;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (rc == SBP_OK && timed) rc = b->fp32 ? whole_step_choice<float>(b) : whole_step_choice<double>(b);
   if (rc) return bfail(b, rc, b->msg.empty() ? "autotune failed" : b->msg);
+  if (timed) {
+    for (const auto& k : keys) cache[k.second] = b->cfg[k.first];
+    dirty = true;
+  }
   if (dirty) write_cache(cache_path, cache);
   return sbp_batch_synchronize(b);
 }

@@ -77,8 +77,8 @@ struct BatchCfg {
 constexpr int kBatchCfgs = 4;
 template <typename T> struct BatchCfgTable;
 template <> struct BatchCfgTable<float> {
-  static constexpr BatchCfg wave[kBatchCfgs] = {{32, 16, 2, 1}, {16, 8, 3, 1}, {16, 8, 2, 2}, {16, 8, 4, 1}};
-  static constexpr BatchCfg adv[kBatchCfgs] = {{32, 8, 4, 1}, {64, 8, 3, 1}, {16, 4, 4, 2}, {32, 8, 2, 2}};
+  static constexpr BatchCfg wave[kBatchCfgs] = {{32, 16, 2, 1}, {8, 8, 3, 2}, {16, 8, 2, 2}, {16, 8, 4, 1}};
+  static constexpr BatchCfg adv[kBatchCfgs] = {{32, 8, 4, 1}, {16, 8, 4, 2}, {16, 4, 4, 2}, {32, 8, 2, 2}};
 };
 template <> struct BatchCfgTable<double> {
   static constexpr BatchCfg wave[kBatchCfgs] = {{16, 8, 2, 1}, {8, 8, 2, 1}, {8, 8, 3, 1}, {8, 4, 2, 2}};

@@ -250,9 +250,11 @@ int sbp_batch_rk4_resident(sbp_batch* batch, long long nsteps);
 int sbp_batch_synchronize(sbp_batch* batch);
 /* Picks the kernel configuration of each (order, problem) group -- tile rows,
  * compute warps, ring depth, CTAs per SM, from a table of four per kind and
- * precision -- by timing the group's middle stage on this batch; results are
- * cached in the flat JSON file cache_path (NULL: no cache). Call between steps:
- * it writes only the stage scratch buffers, never the states. */
+ * precision -- by timing each group's middle stage on this batch, then a few
+ * whole steps with those choices and with every group on each table entry,
+ * keeping the fastest; results are cached in the flat JSON file cache_path
+ * (NULL: no cache). Call between steps: the states are saved before the trial
+ * steps and restored after them (one extra state buffer, freed on return). */
 int sbp_batch_autotune(sbp_batch* batch, const char* cache_path);
 /* Tile rows of the order's wave group (0: no wave instance of that order). */
 int sbp_batch_tile_height(const sbp_batch* batch, int order);
