@@ -83,3 +83,26 @@ def test_decomp_rk4_matches_oracle_and_single_grid(sbp, port, case, char):
     with sbp.Context(sbp.WAVE_HOM_2D, order, nx, ny, bc=bc) as c:
         single = c.rk4(v0, 0.0, dt, 9)
     assert relerr(got, single) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [(4, 1024, 1024, 8, 8), (6, 1000, 1030, 3, 5), (2, 1024, 1024, 2, 1)],
+                         ids=["o4_1024_8x8", "o6_1000x1030_3x5", "o2_1024_2x1"])
+def test_decomp_production_size_matches_single_grid_and_oracle(sbp, port, case):
+    """At 1024^2 every CTA walks many tiles of several subdomains: the tile-geometry slots, the
+    exchange queue's slot reuse and barrier phases, and the dynamic tile queue are all exercised.
+    One RHS against the oracle, and 57 RK4 steps (across a 50-step graph chunk) against the single
+    grid, characteristic SAT, 1e-12 norm-wise relative."""
+    order, nx, ny, px, py = case
+    bc = sbp.BC_CHARACTERISTIC
+    rng = np.random.default_rng(order * 100 + px)
+    src = rng.standard_normal(3 * nx * ny)
+    v0 = port.init_wave_pulse(nx, ny, 0.1, -0.2, 0.3, 1.0) + 0.01 * rng.standard_normal(3 * nx * ny)
+    dt = 0.2 * 2.0 / (max(nx, ny) - 1)
+    with sbp.Decomp(order, nx, ny, px, py, bc=bc) as dec:
+        got_rhs = dec.rhs(src)
+        got = dec.rk4(v0, dt, 57)
+    assert relerr(got_rhs, port.rhs(_oracle_problem(order, nx, ny, True), src)) < 1e-12
+    with sbp.Context(sbp.WAVE_HOM_2D, order, nx, ny, bc=bc) as c:
+        single = c.rk4(v0, 0.0, dt, 57)
+    assert relerr(got, single) < 1e-12
