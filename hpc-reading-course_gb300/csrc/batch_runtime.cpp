@@ -380,24 +380,27 @@ int whole_step_choice(sbp_batch* b) {
   BCK(cudaEventCreate(&sc.e0));
   BCK(cudaEventCreate(&sc.e1));
   BCK(cudaMalloc(&sc.un, b->pool_bytes));
+  if (b->comp) BCK(cudaMalloc(&sc.comp, b->pool_bytes));
   BCK(cudaMemcpyAsync(sc.un, b->un, b->pool_bytes, cudaMemcpyDeviceToDevice, b->stream));
-  if (b->comp) {
-    BCK(cudaMalloc(&sc.comp, b->pool_bytes));
-    BCK(cudaMemcpyAsync(sc.comp, b->comp, b->pool_bytes, cudaMemcpyDeviceToDevice, b->stream));
-  }
+  if (b->comp) BCK(cudaMemcpyAsync(sc.comp, b->comp, b->pool_bytes, cudaMemcpyDeviceToDevice, b->stream));
+  // from here on every path restores the states
   const long long launches = b->launches;
   float best_ms = 1e30f;
   int best = 0, rc = SBP_OK;
+  auto cuda = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && rc == SBP_OK) rc = bfail(b, SBP_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return rc == SBP_OK;
+  };
   for (int c = 0; c < NC && rc == SBP_OK; c++) {
     for (int g = 0; g < 6 && rc == SBP_OK; g++)
       if (group_used(b, g) && b->cfg[g] != cand[c][g]) rc = build_group(b, g, cand[c][g]);
     if (rc || (rc = run_chunk<T>(b, kSteps))) break;  // captures this assignment's graph
-    BCK(cudaEventRecord(sc.e0, b->stream));
+    if (!cuda(cudaEventRecord(sc.e0, b->stream), "cudaEventRecord")) break;
     if ((rc = run_chunk<T>(b, kSteps))) break;
-    BCK(cudaEventRecord(sc.e1, b->stream));
-    BCK(cudaEventSynchronize(sc.e1));
     float ms = 0;
-    BCK(cudaEventElapsedTime(&ms, sc.e0, sc.e1));
+    if (!cuda(cudaEventRecord(sc.e1, b->stream), "cudaEventRecord") ||
+        !cuda(cudaEventSynchronize(sc.e1), "trial steps") || !cuda(cudaEventElapsedTime(&ms, sc.e0, sc.e1), "timing"))
+      break;
     if (ms < best_ms) {
       best_ms = ms;
       best = c;
@@ -405,9 +408,10 @@ int whole_step_choice(sbp_batch* b) {
   }
   for (int g = 0; g < 6 && rc == SBP_OK; g++)
     if (group_used(b, g) && b->cfg[g] != cand[best][g]) rc = build_group(b, g, cand[best][g]);
-  BCK(cudaMemcpyAsync(b->un, sc.un, b->pool_bytes, cudaMemcpyDeviceToDevice, b->stream));
-  if (b->comp) BCK(cudaMemcpyAsync(b->comp, sc.comp, b->pool_bytes, cudaMemcpyDeviceToDevice, b->stream));
-  BCK(cudaStreamSynchronize(b->stream));
+  cuda(cudaMemcpyAsync(b->un, sc.un, b->pool_bytes, cudaMemcpyDeviceToDevice, b->stream), "state restore");
+  if (b->comp)
+    cuda(cudaMemcpyAsync(b->comp, sc.comp, b->pool_bytes, cudaMemcpyDeviceToDevice, b->stream), "state restore");
+  cuda(cudaStreamSynchronize(b->stream), "state restore");
   b->launches = launches;
   return rc;
 }
