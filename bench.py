@@ -433,7 +433,8 @@ def batch_kernel_configs(b, sbpgpu):
         for order in (2, 4, 6):
             cfg = b.kernel_config(order, problem)
             if cfg["rows"]:
-                out[f"{name}_o{order}"] = [cfg["rows"], cfg["warps"], cfg["ring"], cfg["ctas_per_sm"]]
+                out[f"{name}_o{order}"] = [cfg["rows"], cfg["warps"], cfg["ring"], cfg["ctas_per_sm"]] + (
+                    ["fixed-point"] if cfg["converters"] else [])
     return out
 
 

@@ -238,6 +238,22 @@ int fill_params(sbp_batch* b) {
       w.wa = (T*)at(b->wa, g.off);
       w.wb = (T*)at(b->wb, g.off);
       batch_rk4_coefficients<T>(d.dt, w.c_acc, w.c_w);
+      // the fixed-point entries' scales: sigma = -hi/den per direction, the p equation's
+      // times K; each stage's coefficients times each component's scale
+      const double den = d.order == 2 ? 2.0 : (d.order == 4 ? 12.0 : 60.0);
+      p.fx_sig[0] = -hix / den;
+      p.fx_sig[1] = -hiy / den;
+      p.fx_isig[0] = -den / hix;
+      p.fx_isig[1] = -den / hiy;
+      p.fx_rho = hiy / hix;
+      p.fx_square = hix == hiy ? 1 : 0;
+      p.fx_sigp = p.fx_sig[0] * (double)p.kconst;
+      const double sg[3] = {p.fx_sig[0], p.fx_sig[1], p.fx_sigp};
+      for (int rk = 0; rk < 4; rk++)
+        for (int c = 0; c < 3; c++) {
+          w.fxa[rk][c] = (double)w.c_acc[rk] * sg[c];
+          w.fxw[rk][c] = (double)w.c_w[rk] * sg[c];
+        }
       waves.push_back(w);
     } else {
       BatchLine<T> l;
@@ -748,7 +764,7 @@ int sbp_batch_kernel_config(const sbp_batch* b, int order, int problem, int* cfg
     return SBP_ERR_INVALID;
   const int g = 2 * order_index(order) + (problem == SBP_ADVECTION_2D ? 1 : 0);
   if (!group_used(b, g)) {
-    cfg[0] = cfg[1] = cfg[2] = cfg[3] = 0;
+    cfg[0] = cfg[1] = cfg[2] = cfg[3] = cfg[4] = 0;
     return SBP_OK;
   }
   const BatchCfg c = group_cfg(b, g, b->cfg[g]);
@@ -756,6 +772,7 @@ int sbp_batch_kernel_config(const sbp_batch* b, int order, int problem, int* cfg
   cfg[1] = c.warps;
   cfg[2] = c.nst;
   cfg[3] = c.ctas;
+  cfg[4] = c.conv;
   return SBP_OK;
 }
 

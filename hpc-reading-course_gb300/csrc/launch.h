@@ -37,7 +37,8 @@ inline void set_fixed_scales(WaveParams<double>& p, int order, double hix, doubl
   p.fx_isig[1] = -den / hiy;
   p.fx_rho = hiy / hix;
   p.fx_square = hix == hiy ? 1 : 0;
-  const double sg[3] = {p.fx_sig[0], p.fx_sig[1], p.fx_sig[0]};
+  p.fx_sigp = p.fx_sig[0];
+  const double sg[3] = {p.fx_sig[0], p.fx_sig[1], p.fx_sigp};
   for (int c = 0; c < 3; c++) {
     p.fx_ca[c] = p.c_acc * sg[c];
     p.fx_cw[c] = p.c_w * sg[c];

@@ -95,8 +95,10 @@ template <typename T> struct WaveParams {
   // Fixed-point FP64 stages (wave_fixed): the RHS is formed in units of
   // sigma = -hi/den per direction (den: the interior stencil's common denominator),
   // fx_isig = 1/sigma, fx_rho = sigma_y/sigma_x, fx_square = (sigma_x == sigma_y),
-  // and fx_ca/fx_cw are c_acc/c_w times sigma of each component (u: x, v: y, p: x).
-  double fx_sig[2], fx_isig[2], fx_rho;
+  // fx_sigp = the p equation's scale (sigma_x, times K for a constant K != 1),
+  // and fx_ca/fx_cw are c_acc/c_w times the scale of each component (u: sigma_x,
+  // v: sigma_y, p: fx_sigp).
+  double fx_sig[2], fx_isig[2], fx_rho, fx_sigp;
   double fx_ca[3], fx_cw[3];
   int fx_square;
   // Dynamic tile queue: sched[0] hands out tile indices, sched[1] counts the CTAs
@@ -811,8 +813,9 @@ __global__ void __launch_bounds__(32 * (wave_warps<T, KIND>() + 1), 1)
         break;
       }
       const FxGeom g{prm.nx, prm.ny, 0, 0, 0, 0, prm.pitch, prm.plane, 0};
-      wave_tile_fixed<ORD, STAGE, Tile>(prm, g, prm.wout, smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane, emax[0],
-                                        emax[1], bad, &dbar[b], &dphase, b, k);
+      wave_tile_fixed<ORD, STAGE, Tile>(prm, g, prm.in, prm.wout, prm.c_acc, prm.c_w, prm.fx_ca, prm.fx_cw,
+                                        smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane, emax[0], emax[1], bad,
+                                        &dbar[b], &dphase, b, k);
       // the converted boxes were written through the generic proxy; order those writes
       // before the TMA (async proxy) refills the stage
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

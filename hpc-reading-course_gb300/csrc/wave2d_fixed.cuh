@@ -430,19 +430,26 @@ __device__ __forceinline__ void decomp_produce(const WaveParams<double>& prm, un
 // (converted by the converter warps); u^n, acc are FP64 point boxes. Closure rows
 // and SAT faces follow the global indices I = xoff + i, J = yoff + j (prm.nx,
 // prm.ny: the global grid); interior stencils read across subdomain edges from
-// the ghost lines the boxes include.
-template <int ORD, int STAGE, typename Tile>
-__device__ __forceinline__ void wave_tile_fixed(const WaveParams<double>& prm, const FxGeom& g, double* wout,
-                                                const unsigned char* st, const int i0, const int j0, const int warp,
-                                                const int lane, const int ep, const int euv, const bool bad,
-                                                uint64_t* dbar, uint32_t* dphase, const int b, const int k) {
+// the ghost lines the boxes include. `in`, `wout` and the stage's RK4 coefficients
+// (c_acc, c_w in true units, fx_ca / fx_cw scaled per component) come from the
+// caller: the single grid passes prm's, a batch its instance's for the stage.
+// KIND: WK_HOM (rho = K = 1) or WK_CONST (rho = 1, constant K, folded into fx_sigp
+// and the p coefficients; the SAT takes K).
+template <int ORD, int STAGE, typename Tile, int KIND = WK_HOM>
+__device__ __forceinline__ void wave_tile_fixed(const WaveParams<double>& prm, const FxGeom& g, const double* in0,
+                                                double* wout, const double c_acc, const double c_w,
+                                                const double* fx_ca, const double* fx_cw, const unsigned char* st,
+                                                const int i0, const int j0, const int warp, const int lane,
+                                                const int ep, const int euv, const bool bad, uint64_t* dbar,
+                                                uint32_t* dphase, const int b, const int k) {
+  static_assert(KIND == WK_HOM || KIND == WK_CONST, "fixed-point stencils: constant coefficients");
   constexpr int TY = Tile::TY, CS = OpShape<ORD>::CS;
   constexpr int HX = Tile::HX, HY = Tile::HY, PW = Tile::PW;
   constexpr int ROWS = TY / Tile::WARPS;
   constexpr int TPT = TY * kWaveTX;
   const int NX = prm.nx, NY = prm.ny;
   const long long pitch = g.pitch, plane = g.plane;
-  const double* in = prm.in + g.base;
+  const double* in = in0 + g.base;
   const long long* iP = reinterpret_cast<const long long*>(st);
   const long long* iU = reinterpret_cast<const long long*>(st + Tile::OFF_U);
   const long long* iV = reinterpret_cast<const long long*>(st + Tile::OFF_V);
@@ -453,7 +460,7 @@ __device__ __forceinline__ void wave_tile_fixed(const WaveParams<double>& prm, c
   const int iw = -g.xoff, ie = NX - 1 - g.xoff;  // local indices of global columns 0 and NX - 1
   const bool xfaces = dbar != nullptr && prm.bc != BC_NONE &&
                       ((iw >= i0 && iw < i0 + kWaveTX) || (ie >= i0 && ie < i0 + kWaveTX && ie < g.nx));
-  const double sg[3] = {prm.fx_sig[0], prm.fx_sig[1], prm.fx_sig[0]};
+  const double sg[3] = {prm.fx_sig[0], prm.fx_sig[1], prm.fx_sigp};
   const int ebp = ep + 11, ebuv = euv + 11;  // fx_to's exponent bases
   (void)sN;
   (void)sA;
@@ -516,12 +523,12 @@ __device__ __forceinline__ void wave_tile_fixed(const WaveParams<double>& prm, c
         // SAT and the stage update in true units
         const double pc = in[2 * plane + q], uc = in[q], vc = in[plane + q];
         const Rhs3<double> r =
-            apply_sat<double, WK_HOM>(prm, in, I, J, pc, uc, vc, Rhs3<double>{sg[0] * ku, sg[1] * kv, sg[2] * kp});
+            apply_sat<double, KIND>(prm, in, I, J, pc, uc, vc, Rhs3<double>{sg[0] * ku, sg[1] * kv, sg[2] * kp});
         const double kt[3] = {r.u, r.v, r.p};
 #pragma unroll
         for (int c = 0; c < 3; c++) {
           const double cen = (STAGE == ST_FIRST) ? sN[c * TPT + sp] : 0.0;
-          wave_point_store<double, STAGE, Tile>(prm, wout, prm.c_acc, prm.c_w, sA, sN, nullptr, sp, c,
+          wave_point_store<double, STAGE, Tile>(prm, wout, c_acc, c_w, sA, sN, nullptr, sp, c,
                                                 g.base + c * plane + q, kt[c], cen);
         }
         continue;
@@ -534,7 +541,7 @@ __device__ __forceinline__ void wave_tile_fixed(const WaveParams<double>& prm, c
           prm.kout[o] = sg[c] * kf[c];
         } else {
           const double cen = (STAGE == ST_FIRST) ? sN[c * TPT + sp] : 0.0;
-          wave_point_store<double, STAGE, Tile>(prm, wout, prm.fx_ca[c], prm.fx_cw[c], sA, sN, nullptr, sp, c, o,
+          wave_point_store<double, STAGE, Tile>(prm, wout, fx_ca[c], fx_cw[c], sA, sN, nullptr, sp, c, o,
                                                 kf[c], cen);
         }
       }
@@ -559,13 +566,13 @@ __device__ __forceinline__ void wave_tile_fixed(const WaveParams<double>& prm, c
       const double pc = in[2 * plane + q], uc = in[q], vc = in[plane + q];
       const double* d = sD + (side * TY + y) * 3;
       const Rhs3<double> r =
-          apply_sat<double, WK_HOM>(prm, in, I, J, pc, uc, vc, Rhs3<double>{sg[0] * d[0], sg[1] * d[1], sg[2] * d[2]});
+          apply_sat<double, KIND>(prm, in, I, J, pc, uc, vc, Rhs3<double>{sg[0] * d[0], sg[1] * d[1], sg[2] * d[2]});
       const double kt[3] = {r.u, r.v, r.p};
       const int sp = y * kWaveTX + x;
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         const double cen = (STAGE == ST_FIRST) ? sN[c * TPT + sp] : 0.0;
-        wave_point_store<double, STAGE, Tile>(prm, wout, prm.c_acc, prm.c_w, sA, sN, nullptr, sp, c,
+        wave_point_store<double, STAGE, Tile>(prm, wout, c_acc, c_w, sA, sN, nullptr, sp, c,
                                               g.base + c * plane + q, kt[c], cen);
       }
     }
@@ -763,8 +770,9 @@ __global__ void __launch_bounds__(fx_kernel_threads<WaveStageTile<double, ORD, W
     int ep, euv;
     bool bad;
     fx_tile_emax<CONV>(wmax + 16 * b, ep, euv, bad);
-    wave_tile_fixed<ORD, STAGE, Tile>(prm, g, prm.wout, smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane, ep, euv, bad,
-                                      &dbar[b], &dphase, b, k);
+    wave_tile_fixed<ORD, STAGE, Tile>(prm, g, prm.in, prm.wout, prm.c_acc, prm.c_w, prm.fx_ca, prm.fx_cw,
+                                      smem + b * Tile::STAGE_BYTES, i0, j0, warp, lane, ep, euv, bad, &dbar[b], &dphase,
+                                      b, k);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[b]);
   }

@@ -26,6 +26,9 @@ template <typename T> struct alignas(16) BatchWave {
   T* wa;              // stage-input ping-pong buffers
   T* wb;
   T c_acc[4], c_w[4];  // RK4 stage rk's coefficients at [rk - 1], computed on the host
+  // FP64 fixed-point stages: stage rk's coefficients times each component's scale
+  // (prm.fx_sig, and fx_sigp with K folded in), at [rk - 1]
+  double fxa[4][3], fxw[4][3];
 };
 
 // Tensor maps of one batched wave instance, in global memory (64-byte aligned):
@@ -73,6 +76,7 @@ struct BatchTile {
 // with 16-row tiles and a 3-deep ring exceeds (it spilled): that entry has 8 warps.
 struct BatchCfg {
   int ty, warps, nst, ctas;
+  int conv = 0;  // FP64 waves: converter warps of the fixed-point kernel (0: FP64 taps)
 };
 constexpr int kBatchCfgs = 4;
 template <typename T> struct BatchCfgTable;
@@ -81,7 +85,7 @@ template <> struct BatchCfgTable<float> {
   static constexpr BatchCfg adv[kBatchCfgs] = {{32, 8, 4, 1}, {16, 8, 4, 2}, {16, 4, 4, 2}, {32, 8, 2, 2}};
 };
 template <> struct BatchCfgTable<double> {
-  static constexpr BatchCfg wave[kBatchCfgs] = {{16, 8, 2, 1}, {8, 8, 2, 1}, {8, 8, 3, 1}, {8, 4, 2, 2}};
+  static constexpr BatchCfg wave[kBatchCfgs] = {{16, 8, 2, 1}, {14, 14, 3, 1, 6}, {8, 8, 3, 1}, {8, 4, 2, 2}};
   static constexpr BatchCfg adv[kBatchCfgs] = {{16, 8, 4, 1}, {32, 8, 3, 1}, {16, 4, 3, 2}, {8, 4, 6, 2}};
 };
 template <typename T, int CFG> constexpr BatchCfg batch_wave_cfg() { return BatchCfgTable<T>::wave[CFG]; }
@@ -89,7 +93,8 @@ template <typename T, int CFG> constexpr BatchCfg batch_adv_cfg() { return Batch
 
 template <typename T, int ORD, int STAGE, int CFG>
 using BatchWaveTile = WaveTile<T, ORD, STAGE, batch_wave_cfg<T, CFG>().ty, (int)sizeof(BatchWave<T>), false,
-                               batch_wave_cfg<T, CFG>().nst, batch_wave_cfg<T, CFG>().warps>;
+                               batch_wave_cfg<T, CFG>().nst, batch_wave_cfg<T, CFG>().warps,
+                               (batch_wave_cfg<T, CFG>().conv > 0), batch_wave_cfg<T, CFG>().conv>;
 
 // A CTA takes every gridDim.x-th tile of the list, so neighbouring tiles of an
 // instance run at the same time on neighbouring CTAs and share their halo rows in
@@ -172,6 +177,133 @@ __global__ void __launch_bounds__(BatchWaveTile<T, ORD, STAGE, CFG>::THREADS, ba
     batch_stage_buffers(I, rk, in, wout, c_acc, c_w);
     wave_tile_compute<T, ORD, WK_CONST, STAGE, Tile>(I.prm, in, wout, c_acc, c_w, st, i0, j0, warp, lane, nullptr,
                                                      &dbar[b], &dphase, b, k);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[b]);
+  }
+}
+
+// The FP64 wave groups' fixed-point kernel (table entries with converter warps): the
+// single grid's converter-warp stage (wave_fixed_kernel) over the batch's tile list. The
+// producer loads each tile's boxes with its instance's tensor maps and bulk-copies the
+// instance block into the stage, where the compute warps take the instance's parameters,
+// its stage buffers and its scaled RK4 coefficients (fxa, fxw: K folded into p's).
+template <typename Tile>
+__device__ __forceinline__ void batch_fixed_produce(const BatchWave<double>* __restrict__ insts,
+                                                    const CUtensorMap* __restrict__ maps,
+                                                    const BatchTile* __restrict__ tiles, int ntiles, int rk,
+                                                    unsigned char* smem, uint64_t* full, uint64_t* empty, int* tslot,
+                                                    int2* origin, int* err) {
+  constexpr int HX = Tile::HX, HY = Tile::HY, NST = Tile::NST;
+  const int sel = rk == 1 ? 0 : (rk == 3 ? 2 : 1);  // which buffer is the stage input
+  int k = 0;
+  int tile = blockIdx.x;
+  BatchTile next = tile < ntiles ? tiles[tile] : BatchTile{0, 0, 0, 0};
+  for (;; k++) {
+    const int b = k % NST;
+    if (k >= NST && !mbar_wait_bounded(&empty[b], ((k / NST) - 1) & 1)) {
+      atomicOr(err, ERR_TMA_TIMEOUT);
+      break;
+    }
+    if (tile >= ntiles) {  // the end marker: a phase completed without bytes
+      tslot[b] = -1;
+      mbar_arrive(&full[b]);
+      k++;
+      break;
+    }
+    const BatchTile tt = next;
+    tslot[b] = tile;
+    origin[b] = make_int2(tt.i0, tt.j0);
+    tile += gridDim.x;
+    if (tile < ntiles) next = tiles[tile];  // the next descriptor, read ahead
+    const CUtensorMap* m = maps + (long long)tt.slot * kBatchMaps;
+    unsigned char* st = smem + b * Tile::STAGE_BYTES;
+    mbar_arrive_expect_tx(&full[b], Tile::TX_BYTES);
+    tma_load_3d(st, &m[3 * sel + 0], tt.i0 - HX, tt.j0 - HY, 2, &full[b]);
+    tma_load_3d(st + Tile::OFF_U, &m[3 * sel + 1], tt.i0 - HX, tt.j0, 0, &full[b]);
+    tma_load_3d(st + Tile::OFF_V, &m[3 * sel + 2], tt.i0, tt.j0 - HY, 1, &full[b]);
+    if (Tile::LOAD_UN) tma_load_3d(st + Tile::OFF_N, &m[9], tt.i0, tt.j0, 0, &full[b]);
+    if (Tile::LOAD_ACC) tma_load_3d(st + Tile::OFF_A, &m[10], tt.i0, tt.j0, 0, &full[b]);
+    bulk_copy_g2s(st + Tile::OFF_PRM, &insts[tt.slot], (uint32_t)sizeof(BatchWave<double>), &full[b]);
+  }
+  // the CTA must not exit with copies in flight
+  for (int kk = (k >= NST ? k - NST : 0); kk < k; kk++)
+    if (!mbar_wait_bounded(&full[kk % NST], (kk / NST) & 1)) atomicOr(err, ERR_TMA_TIMEOUT);
+}
+
+template <int ORD, int STAGE, int CFG>
+__global__ void __launch_bounds__(BatchWaveTile<double, ORD, STAGE, CFG>::THREADS, 1)
+    wave_batch_fixed_kernel(const BatchWave<double>* __restrict__ insts, const CUtensorMap* __restrict__ maps,
+                            const BatchTile* __restrict__ tiles, int ntiles, int rk, int* err) {
+  using Tile = BatchWaveTile<double, ORD, STAGE, CFG>;
+  constexpr int NST = Tile::NST, WARPS = Tile::WARPS, CONV = Tile::CONV;
+  static_assert(Tile::FIX && CONV >= 1 && NST <= 4, "the converter-warp kernel; four tile origins");
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + Tile::OFF_BAR);
+  uint64_t* empty = full + NST;
+  uint64_t* dbar = reinterpret_cast<uint64_t*>(smem + Tile::OFF_DBAR);
+  int* tslot = reinterpret_cast<int*>(smem + Tile::OFF_BAR + 192);
+  int2* origin = reinterpret_cast<int2*>(smem + Tile::OFF_BAR + 224);
+  uint64_t* fxa = reinterpret_cast<uint64_t*>(smem + Tile::OFF_FX);  // [8]: exponent maxima known
+  uint64_t* conv = fxa + 8;                                          // [8]: stage converted
+  int* wmax = reinterpret_cast<int*>(smem + Tile::OFF_FX + 128);     // [8][8][2]
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NST; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], WARPS);
+      mbar_init(&dbar[s], WARPS);
+      mbar_init(&fxa[s], CONV);
+      mbar_init(&conv[s], CONV);
+    }
+    fence_barrier_init();
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == WARPS + CONV) {
+    if (lane == 0) batch_fixed_produce<Tile>(insts, maps, tiles, ntiles, rk, smem, full, empty, tslot, origin, err);
+    return;
+  }
+  if (warp >= WARPS) {  // ---- converters
+    const int t = threadIdx.x - 32 * WARPS;
+    for (int k = 0;; k++) {
+      const int b = k % NST;
+      if (!mbar_wait_bounded(&full[b], (k / NST) & 1)) {
+        if (lane == 0) atomicOr(err, ERR_TMA_TIMEOUT);
+        break;
+      }
+      const int tile = tslot[b];
+      if (tile >= 0 &&
+          !fx_convert_stage<Tile>(smem + b * Tile::STAGE_BYTES, &fxa[b], wmax + 16 * b, (k / NST) & 1, 0, t)) {
+        if (lane == 0) atomicOr(err, ERR_TMA_TIMEOUT);
+        break;
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&conv[b]);  // converted, or the end marker passed on
+      if (tile < 0) break;
+    }
+    return;
+  }
+  // ---- compute warps
+  uint32_t dphase = 0;  // parity of each stage's next deferred-pass barrier phase
+  for (int k = 0;; k++) {
+    const int b = k % NST;
+    if (!mbar_wait_bounded(&conv[b], (k / NST) & 1)) {
+      if (lane == 0) atomicOr(err, ERR_TMA_TIMEOUT);
+      break;
+    }
+    if (tslot[b] < 0) break;
+    const unsigned char* st = smem + b * Tile::STAGE_BYTES;
+    const BatchWave<double>& I = *reinterpret_cast<const BatchWave<double>*>(st + Tile::OFF_PRM);
+    const int2 o0 = origin[b];
+    const double* in;
+    double* wout;
+    double c_acc, c_w;
+    batch_stage_buffers(I, rk, in, wout, c_acc, c_w);
+    int ep, euv;
+    bool bad;
+    fx_tile_emax<CONV>(wmax + 16 * b, ep, euv, bad);
+    const FxGeom g{I.prm.nx, I.prm.ny, 0, 0, 0, 0, I.prm.pitch, I.prm.plane, 0};
+    wave_tile_fixed<ORD, STAGE, Tile, WK_CONST>(I.prm, g, in, wout, c_acc, c_w, I.fxa[rk - 1], I.fxw[rk - 1], st, o0.x,
+                                                o0.y, warp, lane, ep, euv, bad, &dbar[b], &dphase, b, k);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[b]);
   }

@@ -17,9 +17,16 @@ namespace {
 
 template <typename T, int STAGE, int CFG>
 cudaError_t configure_wave_one() {
-  return cudaFuncSetAttribute(wave_batch_stage_kernel<T, SBP_ORDER, STAGE, CFG>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              BatchWaveTile<T, SBP_ORDER, STAGE, CFG>::SMEM);
+  if constexpr (batch_wave_cfg<T, CFG>().conv > 0) {
+    static_assert(sizeof(T) == 8, "the fixed-point stencils are an FP64 form");
+    return cudaFuncSetAttribute(wave_batch_fixed_kernel<SBP_ORDER, STAGE, CFG>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                BatchWaveTile<T, SBP_ORDER, STAGE, CFG>::SMEM);
+  } else {
+    return cudaFuncSetAttribute(wave_batch_stage_kernel<T, SBP_ORDER, STAGE, CFG>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                BatchWaveTile<T, SBP_ORDER, STAGE, CFG>::SMEM);
+  }
 }
 
 template <typename T, int STAGE, int CFG>
@@ -45,8 +52,12 @@ template <typename T, int STAGE, int CFG>
 void launch_wave_one(const BatchWave<T>* insts, const CUtensorMap* maps, const BatchTile* tiles, int ntiles, int rk,
                      int* err, unsigned grid, cudaStream_t s) {
   using Tile = BatchWaveTile<T, SBP_ORDER, STAGE, CFG>;
-  wave_batch_stage_kernel<T, SBP_ORDER, STAGE, CFG><<<grid, Tile::THREADS, Tile::SMEM, s>>>(insts, maps, tiles, ntiles,
-                                                                                            rk, err);
+  if constexpr (batch_wave_cfg<T, CFG>().conv > 0)
+    wave_batch_fixed_kernel<SBP_ORDER, STAGE, CFG><<<grid, Tile::THREADS, Tile::SMEM, s>>>(insts, maps, tiles, ntiles,
+                                                                                         rk, err);
+  else
+    wave_batch_stage_kernel<T, SBP_ORDER, STAGE, CFG><<<grid, Tile::THREADS, Tile::SMEM, s>>>(insts, maps, tiles,
+                                                                                              ntiles, rk, err);
 }
 
 template <typename T, int STAGE, int CFG>

@@ -539,10 +539,11 @@ class Batch:
 
     def kernel_config(self, order: int, problem: int) -> dict:
         """The kernel configuration of one (order, problem) group: tile rows, compute warps,
-        ring depth and CTAs per SM (zeros for an empty group)."""
-        cfg = (C.c_int * 4)()
+        ring depth, CTAs per SM and converter warps (the FP64 fixed-point wave kernel; zeros
+        for an empty group)."""
+        cfg = (C.c_int * 5)()
         self._check(self._L.sbp_batch_kernel_config(self._h, order, problem, cfg))
-        return dict(zip(("rows", "warps", "ring", "ctas_per_sm"), list(cfg)))
+        return dict(zip(("rows", "warps", "ring", "ctas_per_sm", "converters"), list(cfg)))
 
     def select_config(self, order: int, problem: int, index: int):
         """Runs entry `index` (0..3) of the group's configuration table from now on."""

@@ -249,7 +249,8 @@ int sbp_batch_get_state(sbp_batch* batch, int index, double* v, int where);
 int sbp_batch_rk4_resident(sbp_batch* batch, long long nsteps);
 int sbp_batch_synchronize(sbp_batch* batch);
 /* Picks the kernel configuration of each (order, problem) group -- tile rows,
- * compute warps, ring depth, CTAs per SM, from a table of four per kind and
+ * compute warps, ring depth, CTAs per SM (and, for FP64 waves, the fixed-point
+ * stencil kernel or FP64 taps), from a table of four per kind and
  * precision -- by timing each group's middle stage on this batch, then a few
  * whole steps with those choices and with every group on each table entry,
  * keeping the fastest; results are cached in the flat JSON file cache_path
@@ -258,8 +259,9 @@ int sbp_batch_synchronize(sbp_batch* batch);
 int sbp_batch_autotune(sbp_batch* batch, const char* cache_path);
 /* Tile rows of the order's wave group (0: no wave instance of that order). */
 int sbp_batch_tile_height(const sbp_batch* batch, int order);
-/* cfg[0..3] = tile rows, compute warps, ring depth, CTAs per SM of the group of
- * `order` and `problem` (SBP_WAVE_HOM_2D or SBP_ADVECTION_2D); zeros for an
+/* cfg[0..4] = tile rows, compute warps, ring depth, CTAs per SM and converter
+ * warps (FP64 waves: the fixed-point stencil kernel; 0: FP64 taps) of the group
+ * of `order` and `problem` (SBP_WAVE_HOM_2D or SBP_ADVECTION_2D); zeros for an
  * empty group. */
 int sbp_batch_kernel_config(const sbp_batch* batch, int order, int problem, int* cfg);
 /* Makes entry `index` (0..3) of the group's configuration table the one it runs
