@@ -86,7 +86,7 @@ def test_batch_autotune_keeps_states_and_caches(sbp, tmp_path):
             b.set_state(k, v)
         b.autotune(cache)
         for order in (2, 4, 6):
-            assert b.tile_height(order) in (0, 8, 16)
+            assert b.tile_height(order) in (0, 8, 14, 16)  # the FP64 wave table's rows
             for problem in (sbp.WAVE_HOM_2D, sbp.ADVECTION_2D):
                 cfg = b.kernel_config(order, problem)
                 assert cfg == dict(rows=0, warps=0, ring=0, ctas_per_sm=0, converters=0) or (
