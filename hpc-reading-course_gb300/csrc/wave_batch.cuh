@@ -1,17 +1,19 @@
 // wave_batch.cuh -- many independent wave / advection instances of uneven
 // size, order and coefficients advanced together.
 //
-// Wave instances (rho = 1, K = c^2, one constant per instance) run through a
-// persistent stage kernel per operator order: its grid walks a tile list of
-// (instance, tile) pairs. The producer warp loads each tile's state tiles
-// with TMA from the instance's own tensor maps (kept in global memory) and
-// bulk-copies the instance's parameter block (taps, SAT weights, pointers,
-// time step) into the same shared-memory stage, so consumers read every
-// per-instance constant from shared memory. The per-tile arithmetic is the
-// single-instance kernel's (wave_tile_compute).
+// Each (operator order, problem kind) group runs a persistent stage kernel whose
+// grid walks a tile list of (instance, tile) pairs. The producer warp loads
+// each tile's boxes with TMA from the instance's own tensor maps (kept in
+// global memory) and bulk-copies the instance's parameter block (taps, SAT
+// weights, pointers, time step) into the same shared-memory stage, so the
+// compute warps read every per-instance constant from shared memory.
 //
-// Advection instances (one component) use one CTA per (instance, tile) pair;
-// their per-point arithmetic is the single-instance line kernel's.
+// Wave instances (rho = 1, K = c^2, one constant per instance): the tile
+// arithmetic of the single-instance kernel (wave_tile_compute), or in FP64 its
+// fixed-point stencils with converter warps (wave_tile_fixed). Advection
+// instances (one component): taps from the stage input's box, the single-
+// instance line kernel's operations and order. Each group's kernel shape comes
+// from a small configuration table (below) that the autotuner chooses from.
 #pragma once
 
 #include "line_kernels.cuh"
