@@ -1,9 +1,8 @@
 // decomp.cu -- the 2D wave system (rho = K = 1, FP64) on a P x Q decomposition of
 // one grid, on one GPU: each subdomain holds its own SoA state with R ghost lines
-// on each side, and every RK4 stage first copies the neighbours' edge lines into
-// the ghosts (a halo-exchange kernel), then evaluates the RHS and the stage update
-// of all subdomains in one launch. It is the reference's non-overlapped decomposed
-// path -- rhs_local / rhs_all over a DMDA block grid
+// on each side, and one launch per RK4 stage evaluates the RHS and the stage
+// update of all subdomains while refreshing the ghosts the next stage reads. It is
+// the reference's decomposed path -- rhs_local / rhs_all over a DMDA block grid
 // (code/include/partitioned_rhs/rhs.h:97-181, 183-360) with the VecScatter ghost
 // update of code/src/scatter/scatter_ctx.cpp:149-211 -- with the halo exchange on
 // the device, the step towards one subdomain per GPU.
@@ -17,12 +16,12 @@
 // matches the single grid to rounding. A subdomain's arrays keep ghost_x(order)
 // ghost columns (R rounded up to an even count: TMA x coordinates must be 16-byte
 // aligned) and R ghost rows. In the RK4 loop the exchange is fused into the
-// stages: a point within R of an internal edge also stores the value it gives the
-// next stage input into the neighbour's ghost line, so the exchange overlaps the
-// stage's computation and costs no launch (the reference overlaps its VecScatter
-// with rhs_local, code/demo/wave_hom/wave_eq_hom_sim.cpp:258-261). The halo
-// kernel remains for states set from outside (before an RHS, at the start of a
-// run of steps).
+// stages: the kernel's exchange warp copies each finished tile's points within R
+// of an internal edge into the neighbour's mirroring ghost line, so the exchange
+// overlaps the stage's computation and costs no launch (the reference overlaps
+// its VecScatter with rhs_local, code/demo/wave_hom/wave_eq_hom_sim.cpp:258-261).
+// The halo kernel remains for states set from outside (before an RHS, at the
+// start of a run of steps).
 #include <cuda_runtime.h>
 
 #include <algorithm>
