@@ -976,7 +976,13 @@ int sbp_cnn_forward(sbp_cnn* c, const float* x, int batch, float* out) {
   const long long P = (long long)batch * c->H * c->W;
   unpack_output_kernel<<<blocks_for(P * 3, 256), 256, 0, c->stream>>>(c->out16, out, P);
   c->launches++;
+  int e = 0;
+  CCK(cudaMemcpyAsync(&e, c->err, 4, cudaMemcpyDeviceToHost, c->stream));
   CCK(cudaStreamSynchronize(c->stream));
+  if (e) {
+    CCK(cudaMemsetAsync(c->err, 0, 4, c->stream));
+    return cfail(c, SBP_ERR_DEVICE, "a tensor-core convolution's wait for its tiles ran out");
+  }
   return SBP_OK;
 }
 

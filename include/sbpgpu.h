@@ -301,10 +301,13 @@ int sbp_decomp_rk4_resident(sbp_decomp* dec, double dt, long long nsteps);
  * ReLU) that corrects a coarse solve; no counterpart in the reference.
  * Inputs and outputs are device arrays, NHWC FP32 (features: sbp_cnn_features;
  * outputs: corrections of Z u, Z v, p in units of a scale, sbp_cnn_correct).
- * Inside: BF16 activations and weights, FP32 accumulation on the tensor
- * cores, FP32 master weights, Adam. Parameters as one FP32 vector: per layer
- * the weights [cout][9][cin] (channels padded: layer 1 cin 32 of which 24
- * real, layer 4 cout 16 of which 3 real) then the bias [cout]. */
+ * Inside: BF16 activations and weights, FP32 accumulation in tensor memory
+ * (tcgen05 convolutions), FP32 master weights, Adam. Parameters as one FP32
+ * vector: per layer the weights [cout][9][cin] (channels padded: layer 1 cin 32
+ * of which 24 real, layer 4 cout 16 of which 3 real) then the bias [cout].
+ * forward / gradients / train_step are synchronous; a convolution whose bounded
+ * wait for its tiles ran out makes them return SBP_ERR_DEVICE (the word is
+ * cleared: the network stays usable). */
 typedef struct sbp_cnn sbp_cnn;
 int sbp_cnn_create(int height, int width, int max_batch, int device, void* stream, sbp_cnn** cnn);
 int sbp_cnn_destroy(sbp_cnn* cnn);
