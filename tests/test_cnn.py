@@ -49,12 +49,15 @@ def _relerr(a, b):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("shape", [(2, 19, 23), (3, 32, 40), (1, 64, 64), (1, 9, 200)],
-                         ids=["2x19x23", "3x32x40", "1x64x64", "1x9x200"])
+@pytest.mark.parametrize("shape", [(2, 19, 23), (3, 32, 40), (1, 64, 64), (1, 9, 200), (2, 160, 160)],
+                         ids=["2x19x23", "3x32x40", "1x64x64", "1x9x200", "2x160x160"])
 def test_gpu_forward_and_gradients_match_oracle(sbp, shape):
     """Tolerances from what BF16 storage with FP32 accumulation leaves against the oracle, which
     rounds the same tensors to BF16 and sums in FP64 (measured: output <= 1.9e-3, loss <= 8e-6,
-    each layer's weight and bias gradients <= 8e-4, max-norm relative), with a margin of 2.5-6x."""
+    each layer's weight and bias gradients <= 8e-4, max-norm relative), with a margin of 2.5-6x.
+    2 x 160 x 160 has more 128-pixel tiles (400) than the persistent convolutions have CTAs, so
+    CTAs take several tiles: ring-slot reuse, both tensor-memory accumulators, and the weight
+    gradient's accumulation over tiles are exercised."""
     import torch
 
     B, H, W = shape
