@@ -320,7 +320,8 @@ __global__ void __launch_bounds__(TcConv<CIN, COUT>::THREADS, TcConv<CIN, COUT>:
 // and 5-8 (whose last quarter, tap 8, is the one kept) -- cover the nine taps with
 // M = 128, N = COUT, eight K steps of 16 pixels each. The accumulators (3 x COUT
 // tensor-memory columns) sum over every tile the CTA takes; at the end the four
-// epilogue warps read them and add them to dw with one FP32 atomic per entry and CTA.
+// epilogue warps write them to the CTA's slice of dw_part, which wgrad_reduce_kernel
+// then adds to dw in CTA order (the same bits on every run).
 template <int COUT>
 struct TcWgrad {
   static_assert(COUT == 16 || COUT == 32, "output channels: the MMA's N");
@@ -346,7 +347,7 @@ struct TcWgrad {
 template <int COUT>
 __global__ void __launch_bounds__(TcWgrad<COUT>::THREADS, 1)
     conv3x3_wgrad_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap dymap,
-                            float* __restrict__ dw, int B, int H, int W, int tw, int th, int* err) {
+                            float* __restrict__ dw_part, int B, int H, int W, int tw, int th, int* err) {
   using L = TcWgrad<COUT>;
   constexpr int NST = L::NST, CIN = L::CIN;
   extern __shared__ unsigned char smem_raw[];
@@ -358,6 +359,7 @@ __global__ void __launch_bounds__(TcWgrad<COUT>::THREADS, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntw = (W + tw - 1) / tw, nth = (H + th - 1) / th;
   const int ntiles = B * nth * ntw;
+  float* part = dw_part + (long long)blockIdx.x * COUT * 9 * CIN;  // this CTA's sums, every entry written
   if (threadIdx.x == 0) {
     for (int s = 0; s < NST; s++) {
       mbar_init(&full[s], 1);
@@ -427,7 +429,7 @@ __global__ void __launch_bounds__(TcWgrad<COUT>::THREADS, 1)
           tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(g * COUT + n0), r);
           tmem_wait_ld();
 #pragma unroll
-          for (int j = 0; j < 16; j++) atomicAdd(&dw[((long long)(n0 + j) * 9 + tap) * CIN + lane], __uint_as_float(r[j]));
+          for (int j = 0; j < 16; j++) part[((long long)(n0 + j) * 9 + tap) * CIN + lane] = __uint_as_float(r[j]);
         }
       }
     } else if (lane == 0) {
@@ -439,6 +441,15 @@ __global__ void __launch_bounds__(TcWgrad<COUT>::THREADS, 1)
   if (warp == 1) {
     tc_fence_after();
     tmem_dealloc(tmem, 128);
+  }
+}
+
+// dw[e] += sum over the weight-gradient CTAs of their partial sums, in CTA order.
+__global__ void wgrad_reduce_kernel(const float* __restrict__ part, float* __restrict__ dw, int n, int ctas) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int c = 0; c < ctas; c++) s += part[(long long)c * n + e];
+    dw[e] += s;
   }
 }
 
@@ -644,6 +655,7 @@ struct sbp_cnn {
   int* err = nullptr;        // the tensor-core convolutions' error word (a bounded wait ran out)
   int tw = 0, th = 0;        // their pixel tile: th rows of tw pixels, th * tw = 128
   int nsm = 1;               // SMs: the persistent convolutions' grid
+  float* dw_part = nullptr;  // the weight gradient's per-CTA sums ([nsm][32 * 9 * 32])
   long long launches = 0;
   std::string msg;
 };
@@ -674,7 +686,7 @@ void cnn_release(sbp_cnn* c) {
     for (void* p : ps)
       if (p) cudaFree(p);
   }
-  void* ps[] = {c->dact, c->dact2, c->out16, c->loss, c->err};
+  void* ps[] = {c->dact, c->dact2, c->out16, c->loss, c->err, c->dw_part};
   for (void* p : ps)
     if (p) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -780,11 +792,13 @@ cudaError_t conv_wgrad(int l, const bf16* x, const bf16* dy, float* dw, const sb
   const long long tiles = (long long)batch * ((c->H + c->th - 1) / c->th) * ((c->W + c->tw - 1) / c->tw);
   const unsigned grid = (unsigned)(tiles < c->nsm ? tiles : c->nsm);
   if (cout == 32)
-    conv3x3_wgrad_tc_kernel<32><<<grid, TcWgrad<32>::THREADS, TcWgrad<32>::SMEM, s>>>(xm, dym, dw, batch, c->H, c->W,
-                                                                                     c->tw, c->th, c->err);
+    conv3x3_wgrad_tc_kernel<32><<<grid, TcWgrad<32>::THREADS, TcWgrad<32>::SMEM, s>>>(
+        xm, dym, c->dw_part, batch, c->H, c->W, c->tw, c->th, c->err);
   else
-    conv3x3_wgrad_tc_kernel<16><<<grid, TcWgrad<16>::THREADS, TcWgrad<16>::SMEM, s>>>(xm, dym, dw, batch, c->H, c->W,
-                                                                                     c->tw, c->th, c->err);
+    conv3x3_wgrad_tc_kernel<16><<<grid, TcWgrad<16>::THREADS, TcWgrad<16>::SMEM, s>>>(
+        xm, dym, c->dw_part, batch, c->H, c->W, c->tw, c->th, c->err);
+  const int n = (int)wcount(l);
+  wgrad_reduce_kernel<<<(n + 255) / 256, 256, 0, s>>>(c->dw_part, dw, n, (int)grid);
   return cudaGetLastError();
 }
 
@@ -887,6 +901,8 @@ int sbp_cnn_create(int height, int width, int max_batch, int device, void* strea
   if (configure_convs() != cudaSuccess) return bad("cudaFuncSetAttribute(convolutions)");
   if (cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || c->nsm < 1)
     return bad("cudaDeviceGetAttribute(SMs)");
+  if (cudaMalloc(&c->dw_part, (size_t)c->nsm * 32 * 9 * 32 * sizeof(float)) != cudaSuccess)
+    return bad("cudaMalloc(weight-gradient partial sums)");
   if (!encode_fn()) return bad("cuTensorMapEncodeTiled is not available from the driver");
   *out = c;
   return sbp_cnn_init(c, 1234);
@@ -1005,7 +1021,7 @@ static int backward(sbp_cnn* c, const float* x, const float* target, int batch, 
   for (int l = kLayers - 1; l >= 0; l--) {
     CCK(conv_wgrad(l, c->act[l], dcur, c->gw[l], c, batch, c->stream));
     CCK(bias_grad(l, dcur, c->gb[l], batch, c, c->stream));
-    c->launches += 2;
+    c->launches += 3;  // weight gradient, its reduction, bias gradient
     if (l == 0) break;
     CCK(conv_dgrad(l, dcur, dnext, c, batch, c->stream));
     relu_back_kernel<<<blocks_for(P * kCin[l], 256), 256, 0, c->stream>>>(dnext, c->act[l], P * kCin[l]);
