@@ -15,7 +15,8 @@
 //   conv3x3_wgrad_tc_kernel  weight gradient on tcgen05, K = pixels: four taps'
 //                         shifted input tiles stacked along M (MN-major operands),
 //                         accumulated over all of a CTA's pixel tiles in tensor
-//                         memory and added to dw once per CTA.
+//                         memory; wgrad_reduce_kernel adds the CTAs' sums to dw in
+//                         CTA order (repeatable bits).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
