@@ -43,3 +43,18 @@ def test_adapter_matches_the_library_on_a_device(sbp, tmp_path):
     r = subprocess.run([exe, "gpu"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "FAIL" not in r.stdout and "rhs: the same bits" in r.stdout and "ts_rk4: the same bits" in r.stdout
+
+
+def test_adapter_build_looks_for_petsc_headers(tmp_path, monkeypatch):
+    """build_petsc_adapter() builds only where $PETSC_DIR[/$PETSC_ARCH] holds petscts.h."""
+    import build as gpu_build
+
+    monkeypatch.delenv("PETSC_DIR", raising=False)
+    assert gpu_build.petsc_include_dirs() is None
+    assert gpu_build.build_petsc_adapter() is None
+    monkeypatch.setenv("PETSC_DIR", str(tmp_path))
+    monkeypatch.setenv("PETSC_ARCH", "arch-test")
+    assert gpu_build.petsc_include_dirs() is None  # no headers there
+    (tmp_path / "include").mkdir()
+    (tmp_path / "include" / "petscts.h").write_text("/* stand-in */\n")
+    assert gpu_build.petsc_include_dirs() == [str(tmp_path / "include"), str(tmp_path / "arch-test" / "include")]
