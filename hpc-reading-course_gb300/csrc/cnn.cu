@@ -1006,7 +1006,8 @@ int sbp_cnn_forward(sbp_cnn* c, const float* x, int batch, float* out) {
 // Gradients of the mean squared error of network(x) against target (both device, NHWC FP32,
 // 4 and 3 channels), without updating the parameters; written as one FP32 vector in the
 // layout of sbp_cnn_get_params (host `grad`, may be NULL). Returns the loss in *loss.
-static int backward(sbp_cnn* c, const float* x, const float* target, int batch, float* loss) {
+// bias_grads: also the biases' gradients (the training step leaves biases untrained and skips them).
+static int backward(sbp_cnn* c, const float* x, const float* target, int batch, float* loss, bool bias_grads) {
   const long long P = (long long)batch * c->H * c->W;
   int rc = run_forward(c, x, batch);
   if (rc) return rc;
@@ -1021,8 +1022,11 @@ static int backward(sbp_cnn* c, const float* x, const float* target, int batch, 
   bf16* dnext = c->dact2;
   for (int l = kLayers - 1; l >= 0; l--) {
     CCK(conv_wgrad(l, c->act[l], dcur, c->gw[l], c, batch, c->stream));
-    CCK(bias_grad(l, dcur, c->gb[l], batch, c, c->stream));
-    c->launches += 3;  // weight gradient, its reduction, bias gradient
+    c->launches += 2;  // weight gradient and its reduction
+    if (bias_grads) {
+      CCK(bias_grad(l, dcur, c->gb[l], batch, c, c->stream));
+      c->launches++;
+    }
     if (l == 0) break;
     CCK(conv_dgrad(l, dcur, dnext, c, batch, c->stream));
     relu_back_kernel<<<blocks_for(P * kCin[l], 256), 256, 0, c->stream>>>(dnext, c->act[l], P * kCin[l]);
@@ -1049,7 +1053,7 @@ int sbp_cnn_gradients(sbp_cnn* c, const float* x, const float* target, int batch
   if (!c || !x || !target || batch < 1 || batch > c->maxB) return SBP_ERR_INVALID;
   if (grad && n != sbp_cnn_param_count()) return SBP_ERR_INVALID;
   CCK(cudaSetDevice(c->device));
-  int rc = backward(c, x, target, batch, loss);
+  int rc = backward(c, x, target, batch, loss, true);
   if (rc || !grad) return rc;
   long long o = 0;
   for (int l = 0; l < kLayers; l++) {
@@ -1068,7 +1072,7 @@ int sbp_cnn_gradients(sbp_cnn* c, const float* x, const float* target, int batch
 int sbp_cnn_train_step(sbp_cnn* c, const float* x, const float* target, int batch, float lr, float* loss) {
   if (!c || !x || !target || batch < 1 || batch > c->maxB || !(lr > 0)) return SBP_ERR_INVALID;
   CCK(cudaSetDevice(c->device));
-  int rc = backward(c, x, target, batch, loss);
+  int rc = backward(c, x, target, batch, loss, false);
   if (rc) return rc;
   c->step++;
   const float b1 = 0.9f, b2 = 0.999f;
