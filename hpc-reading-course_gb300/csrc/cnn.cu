@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <new>
 #include <random>
 #include <string>
 #include <vector>
@@ -852,7 +853,8 @@ extern "C" {
 int sbp_cnn_create(int height, int width, int max_batch, int device, void* stream, sbp_cnn** out) {
   if (!out || height < 1 || width < 1 || max_batch < 1) return cfail(nullptr, SBP_ERR_INVALID, "bad network size");
   *out = nullptr;
-  sbp_cnn* c = new sbp_cnn();
+  sbp_cnn* c = new (std::nothrow) sbp_cnn();
+  if (!c) return cfail(nullptr, SBP_ERR_INVALID, "out of host memory");
   c->H = height;
   c->W = width;
   c->maxB = max_batch;
@@ -905,8 +907,16 @@ int sbp_cnn_create(int height, int width, int max_batch, int device, void* strea
   if (cudaMalloc(&c->dw_part, (size_t)c->nsm * 32 * 9 * 32 * sizeof(float)) != cudaSuccess)
     return bad("cudaMalloc(weight-gradient partial sums)");
   if (!encode_fn()) return bad("cuTensorMapEncodeTiled is not available from the driver");
+  // a network that failed its initialisation is released, not handed out
+  const int rc = sbp_cnn_init(c, 1234);
+  if (rc) {
+    g_cnn_error = c->msg;
+    cnn_release(c);
+    delete c;
+    return rc;
+  }
   *out = c;
-  return sbp_cnn_init(c, 1234);
+  return SBP_OK;
 }
 
 int sbp_cnn_destroy(sbp_cnn* c) {

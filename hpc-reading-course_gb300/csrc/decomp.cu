@@ -490,6 +490,8 @@ const char* sbp_decomp_last_error(const sbp_decomp* c) { return c ? c->msg.c_str
 
 int sbp_decomp_set_state(sbp_decomp* c, const double* aos, int where) {
   if (!c || !aos) return SBP_ERR_INVALID;
+  if (where != SBP_HOST && where != SBP_DEVICE)
+    return dfail(c, SBP_ERR_INVALID, "where must be SBP_HOST or SBP_DEVICE");
   cudaSetDevice(c->d.device);
   const size_t bytes = (size_t)c->d.nx * c->d.ny * 3 * sizeof(double);
   const double* src = aos;
@@ -504,6 +506,8 @@ int sbp_decomp_set_state(sbp_decomp* c, const double* aos, int where) {
 
 int sbp_decomp_get_state(sbp_decomp* c, double* aos, int where) {
   if (!c || !aos) return SBP_ERR_INVALID;
+  if (where != SBP_HOST && where != SBP_DEVICE)
+    return dfail(c, SBP_ERR_INVALID, "where must be SBP_HOST or SBP_DEVICE");
   cudaSetDevice(c->d.device);
   const size_t bytes = (size_t)c->d.nx * c->d.ny * 3 * sizeof(double);
   double* dst = where == SBP_HOST ? c->io : aos;
@@ -515,6 +519,8 @@ int sbp_decomp_get_state(sbp_decomp* c, double* aos, int where) {
 
 int sbp_decomp_rhs(sbp_decomp* c, const double* src, double* dst, int where) {
   if (!c || !src || !dst) return SBP_ERR_INVALID;
+  if (where != SBP_HOST && where != SBP_DEVICE)
+    return dfail(c, SBP_ERR_INVALID, "where must be SBP_HOST or SBP_DEVICE");
   cudaSetDevice(c->d.device);
   const size_t bytes = (size_t)c->d.nx * c->d.ny * 3 * sizeof(double);
   if (where == SBP_HOST) {

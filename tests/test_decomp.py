@@ -44,6 +44,19 @@ def test_decomp_rejects_unsupported_descriptions(sbp, case):
     assert L.sbp_decomp_last_error(None)  # says why
 
 
+@pytest.mark.gpu
+def test_decomp_rejects_unknown_where(sbp):
+    """A `where` that is neither SBP_HOST nor SBP_DEVICE is refused before any copy."""
+    L = sbp.load()
+    v = np.zeros(3 * 20 * 20)
+    with sbp.Decomp(4, 20, 20, 2, 2) as dec:
+        assert L.sbp_decomp_set_state(dec._h, v.ctypes.data, 7) == -1  # SBP_ERR_INVALID
+        assert L.sbp_decomp_get_state(dec._h, v.ctypes.data, 7) == -1  # SBP_ERR_INVALID
+        assert L.sbp_decomp_rhs(dec._h, v.ctypes.data, v.ctypes.data, 7) == -1  # SBP_ERR_INVALID
+        assert b"where" in L.sbp_decomp_last_error(dec._h)
+        dec.set_state(v)  # still usable
+
+
 CASES = [(2, 37, 29, 2, 3), (4, 40, 40, 4, 4), (4, 65, 33, 3, 2), (6, 27, 60, 1, 5), (6, 50, 41, 2, 2), (4, 33, 33, 1, 1)]
 IDS = ["o2_37x29_2x3", "o4_40x40_4x4", "o4_65x33_3x2", "o6_27x60_1x5", "o6_50x41_2x2", "o4_33x33_1x1"]
 
