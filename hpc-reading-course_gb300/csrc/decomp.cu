@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <new>
 #include <string>
 #include <vector>
@@ -160,15 +161,14 @@ struct sbp_decomp {
   double *un = nullptr, *acc = nullptr, *wa = nullptr, *wb = nullptr, *io = nullptr;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  cudaGraphExec_t graph = nullptr;  // a chunk of RK4 steps
-  long long graph_steps = 0;
-  double graph_dt = 0.0;
+  std::map<long long, cudaGraphExec_t> graphs;  // per chunk length, the chunk's RK4 steps
+  double graph_dt = 0.0;                         // the time step the graphs were captured with
   std::string msg;
 };
 
 namespace {
 
-std::string g_decomp_create_error;  // the message of the last failed sbp_decomp_create
+thread_local std::string g_decomp_create_error;  // the message of this thread's last failed sbp_decomp_create
 
 int dfail(sbp_decomp* c, int code, const std::string& m) {
   if (c) c->msg = m;
@@ -176,7 +176,8 @@ int dfail(sbp_decomp* c, int code, const std::string& m) {
 }
 
 void release(sbp_decomp* c) {
-  if (c->graph) cudaGraphExecDestroy(c->graph);
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+  c->graphs.clear();
   cudaFree(c->d_subs);
   cudaFree(c->d_tiles);
   cudaFree(c->d_tinfo);
@@ -546,14 +547,19 @@ int sbp_decomp_rk4_resident(sbp_decomp* c, double dt, long long nsteps) {
   // u^n's ghost lines from its neighbours once (after sbp_decomp_set_state they are
   // stale); from there each stage keeps the next stage input's ghosts current
   DCK(halo(c, c->un));
-  // chunks of up to 50 steps captured once as a CUDA graph (4 launches a step)
+  // chunks of up to 50 steps, each length captured once as a CUDA graph (4 launches a
+  // step); a new time step drops the graphs
   const long long chunk = 50;
+  if (c->graph_dt != dt) {
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    c->graphs.clear();
+    c->graph_dt = dt;
+  }
   long long left = nsteps;
   while (left > 0) {
     const long long n = left < chunk ? left : chunk;
-    if (!c->graph || c->graph_steps != n || c->graph_dt != dt) {
-      if (c->graph) cudaGraphExecDestroy(c->graph);
-      c->graph = nullptr;
+    auto it = c->graphs.find(n);
+    if (it == c->graphs.end()) {
       cudaGraph_t g = nullptr;
       DCK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
       cudaError_t e = cudaSuccess;
@@ -563,13 +569,13 @@ int sbp_decomp_rk4_resident(sbp_decomp* c, double dt, long long nsteps) {
         if (g) cudaGraphDestroy(g);
         return dfail(c, SBP_ERR_CUDA, cudaGetErrorString(e != cudaSuccess ? e : ce));
       }
-      const cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
+      cudaGraphExec_t ex = nullptr;
+      const cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
       cudaGraphDestroy(g);
       DCK(ie);
-      c->graph_steps = n;
-      c->graph_dt = dt;
+      it = c->graphs.emplace(n, ex).first;
     }
-    DCK(cudaGraphLaunch(c->graph, c->stream));
+    DCK(cudaGraphLaunch(it->second, c->stream));
     left -= n;
   }
   return finish(c);

@@ -99,6 +99,25 @@ def test_decomp_rk4_matches_oracle_and_single_grid(sbp, port, case, char):
 
 
 @pytest.mark.gpu
+def test_decomp_graphs_reused_across_chunk_lengths_and_time_steps(sbp):
+    """One context runs 57 steps (a 50-step and a 7-step graph), then 7 steps at another dt
+    (the graphs are dropped and recaptured), then 57 steps again: every run matches the single
+    grid bit for bit in the repeated case and to 1e-12 throughout."""
+    order, nx, ny, px, py = 4, 40, 40, 2, 2
+    bc = sbp.BC_CHARACTERISTIC
+    v0 = np.random.default_rng(11).standard_normal(3 * nx * ny)
+    dt = 0.2 * 2.0 / (nx - 1)
+    with sbp.Decomp(order, nx, ny, px, py, bc=bc) as dec:
+        a = dec.rk4(v0, dt, 57)
+        b = dec.rk4(v0, 0.5 * dt, 7)
+        c = dec.rk4(v0, dt, 57)
+    assert np.array_equal(a, c)
+    with sbp.Context(sbp.WAVE_HOM_2D, order, nx, ny, bc=bc) as s:
+        assert relerr(a, s.rk4(v0, 0.0, dt, 57)) < 1e-12
+        assert relerr(b, s.rk4(v0, 0.0, 0.5 * dt, 7)) < 1e-12
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("case", [(4, 1024, 1024, 8, 8), (6, 1000, 1030, 3, 5), (2, 1024, 1024, 2, 1)],
                          ids=["o4_1024_8x8", "o6_1000x1030_3x5", "o2_1024_2x1"])
 def test_decomp_production_size_matches_single_grid_and_oracle(sbp, port, case):
