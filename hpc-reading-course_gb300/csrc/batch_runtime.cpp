@@ -631,6 +631,7 @@ int sbp_batch_set_state(sbp_batch* b, int index, const double* v, int where) {
 
 int sbp_batch_get_state(sbp_batch* b, int index, double* v, int where) {
   if (!b || !v || index < 0 || index >= (int)b->inst.size()) return SBP_ERR_INVALID;
+  if (where != SBP_HOST && where != SBP_DEVICE) return bfail(b, SBP_ERR_INVALID, "where must be SBP_HOST or SBP_DEVICE");
   BCK(cudaSetDevice(b->device));
   const Geo& g = b->geo[index];
   const size_t n = (size_t)g.dofs * g.nx * g.ny;

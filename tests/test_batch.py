@@ -143,6 +143,17 @@ def test_select_config_rejects_bad_arguments(sbp):
 
 
 @pytest.mark.gpu
+def test_batch_state_copies_reject_unknown_where(sbp):
+    """A `where` that is neither SBP_HOST nor SBP_DEVICE is refused before any copy."""
+    L = sbp.load()
+    v = np.zeros(3 * 40 * 40)
+    with sbp.Batch([dict(problem=sbp.WAVE_HOM_2D, order=4, nx=40, ny=40, c=1.0, dt=0.01)]) as b:
+        assert L.sbp_batch_set_state(b._h, 0, v.ctypes.data, 7) == sbp.ERR_INVALID
+        assert L.sbp_batch_get_state(b._h, 0, v.ctypes.data, 7) == sbp.ERR_INVALID
+        assert b"where" in L.sbp_batch_last_error(b._h)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["fp64", "fp64_fixed", "fp32"])
 def test_batched_configuration_sample_against_oracle(sbp, port, precision):
     """The benchmark's batched configuration -- 512 uneven wave and advection instances

@@ -50,9 +50,9 @@ def test_decomp_rejects_unknown_where(sbp):
     L = sbp.load()
     v = np.zeros(3 * 20 * 20)
     with sbp.Decomp(4, 20, 20, 2, 2) as dec:
-        assert L.sbp_decomp_set_state(dec._h, v.ctypes.data, 7) == -1  # SBP_ERR_INVALID
-        assert L.sbp_decomp_get_state(dec._h, v.ctypes.data, 7) == -1  # SBP_ERR_INVALID
-        assert L.sbp_decomp_rhs(dec._h, v.ctypes.data, v.ctypes.data, 7) == -1  # SBP_ERR_INVALID
+        assert L.sbp_decomp_set_state(dec._h, v.ctypes.data, 7) == sbp.ERR_INVALID
+        assert L.sbp_decomp_get_state(dec._h, v.ctypes.data, 7) == sbp.ERR_INVALID
+        assert L.sbp_decomp_rhs(dec._h, v.ctypes.data, v.ctypes.data, 7) == sbp.ERR_INVALID
         assert b"where" in L.sbp_decomp_last_error(dec._h)
         dec.set_state(v)  # still usable
 
@@ -101,8 +101,8 @@ def test_decomp_rk4_matches_oracle_and_single_grid(sbp, port, case, char):
 @pytest.mark.gpu
 def test_decomp_graphs_reused_across_chunk_lengths_and_time_steps(sbp):
     """One context runs 57 steps (a 50-step and a 7-step graph), then 7 steps at another dt
-    (the graphs are dropped and recaptured), then 57 steps again: every run matches the single
-    grid bit for bit in the repeated case and to 1e-12 throughout."""
+    (the graphs are dropped and recaptured), then 57 steps again: the repeated run reproduces
+    the first bit for bit, and each run matches the single grid to 1e-12."""
     order, nx, ny, px, py = 4, 40, 40, 2, 2
     bc = sbp.BC_CHARACTERISTIC
     v0 = np.random.default_rng(11).standard_normal(3 * nx * ny)
