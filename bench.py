@@ -208,6 +208,18 @@ def cpu_baseline(n: int, order: int, precision: str, bc: str, budget_s: float, r
     return rates, kind, threads, sample
 
 
+def max_over_ranks(value: float, dist, device: str) -> float:
+    """The largest of every rank's `value` (an all_reduce MAX on `device`, which the
+    process group's backend must reach); `value` itself without a process group."""
+    if not dist:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args, rank: int):
     if rank != 0:
         return
@@ -925,10 +937,7 @@ def main():
     ctx.synchronize()
     elapsed_ms = ev0.elapsed_time(ev1)
     launches = ctx.launches - launches0
-    if dist:
-        t = torch.tensor([elapsed_ms], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, dist, f"cuda:{local}")
     sync_all()
     clock_info = clocks.stop()
 
@@ -980,10 +989,7 @@ def main():
             if k >= args.warmup:
                 times.append(el)
         el = statistics.median(times)
-        if dist:
-            t = torch.tensor([el], dtype=torch.float64, device=f"cuda:{local}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            el = float(t.item())
+        el = max_over_ranks(el, dist, f"cuda:{local}")
         e2e = {"value": world * units_per_step / el, "unit": UNIT, "h2d_bytes_per_step": host.nbytes,
                "d2h_bytes_per_step": host.nbytes, "ms_per_step": el * 1e3,
                "call": "sbp_rk4(ctx, 0, dt, steps, host_aos, SBP_HOST)"}

@@ -36,14 +36,17 @@ def test_reference_arm_two_ranks_prints_one_line():
 
 
 def test_max_over_ranks_reduction_gloo(tmp_path):
-    """The timing reduction bench.py uses (all_reduce MAX of elapsed times)."""
+    """bench.py's timing reduction (max_over_ranks: an all_reduce MAX of the ranks' elapsed
+    times) across two gloo ranks, and its one-rank form without a process group."""
     code = r'''
-import os, torch, torch.distributed as dist
+import sys, torch.distributed as dist
+sys.path.insert(0, sys.argv[1])
+import bench
+assert bench.max_over_ranks(7.5, None, "cpu") == 7.5
 dist.init_process_group("gloo")
 r = dist.get_rank()
-t = torch.tensor([10.0 + 5.0 * r], dtype=torch.float64)
-dist.all_reduce(t, op=dist.ReduceOp.MAX)
-assert t.item() == 15.0
+assert bench.max_over_ranks(10.0 + 5.0 * r, dist, "cpu") == 15.0
+assert bench.max_over_ranks(3.0 - r, dist, "cpu") == 3.0
 if r == 0:
     print("OK")
 dist.destroy_process_group()
@@ -51,7 +54,7 @@ dist.destroy_process_group()
     path = tmp_path / "maxreduce_child.py"
     path.write_text(code)
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
-           "--master-addr=127.0.0.1", f"--master-port={_free_port()}", str(path)]
+           "--master-addr=127.0.0.1", f"--master-port={_free_port()}", str(path), ROOT]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr[-2000:]
     assert "OK" in r.stdout
