@@ -281,7 +281,8 @@ long long sbp_batch_launch_count(const sbp_batch* batch); /* kernels launched so
  * neighbours' ghost lines as well (a halo kernel runs once per call, for the
  * state it starts from). Subdomain widths are
  * floor(N*(b+1)/p) - floor(N*b/p) >= the closure width (2 / 6 / 9 points for
- * orders 2 / 4 / 6), else SBP_ERR_INVALID; other problems or FP32:
+ * orders 2 / 4 / 6) and the whole grid at least sbp_create's minimum size,
+ * else SBP_ERR_INVALID; other problems or FP32:
  * SBP_ERR_UNSUPPORTED. Results equal sbp_create's single grid to rounding.
  * States are the full grid's AoS arrays (as sbp_set_state). Synchronous. */
 typedef struct sbp_decomp sbp_decomp;
@@ -293,7 +294,8 @@ int sbp_decomp_get_state(sbp_decomp* dec, double* state, int where);
 /* dst = F(src) (the system is autonomous): halo exchange, then the RHS of every subdomain. */
 int sbp_decomp_rhs(sbp_decomp* dec, const double* src, double* dst, int where);
 /* nsteps classical RK4 steps of the resident state; every stage also fills the ghost lines its
- * successor reads. */
+ * successor reads. The steps run as CUDA graphs of up to 50 steps, one per chunk length,
+ * kept across calls until dt changes. */
 int sbp_decomp_rk4_resident(sbp_decomp* dec, double dt, long long nsteps);
 
 /* ---------------------------------------------------------------- learned correction
