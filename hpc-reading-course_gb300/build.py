@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import argparse
 import os
+import re
 import shutil
 import subprocess
 import sys
@@ -23,8 +24,10 @@ LIB_DIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIB_DIR, "libsbpgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# -Xptxas -v: ptxas reports each kernel's registers, stack and spills; build() keeps
+# the report of every unit beside its object (resource_report() reads them)
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I", os.path.join(ROOT, "include"),
-              "--expt-relaxed-constexpr"] + ARCH
+              "--expt-relaxed-constexpr", "-Xptxas", "-v"] + ARCH
 
 
 def nvcc() -> str:
@@ -76,6 +79,9 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode == 0:
+            with open(os.path.join(BUILD, obj + ".ptxas.txt"), "w") as f:
+                f.write(r.stderr)
         return obj, r
 
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
@@ -95,6 +101,33 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
         raise RuntimeError("link of libsbpgpu.so failed")
     os.replace(tmp, LIB)
     return LIB
+
+
+def resource_report() -> dict[str, dict[str, int]]:
+    """Per kernel (mangled name) its registers, stack frame and spill bytes, from the ptxas
+    reports the last build kept for every translation unit."""
+    out: dict[str, dict[str, int]] = {}
+    for obj, _, _ in units():
+        path = os.path.join(BUILD, obj + ".ptxas.txt")
+        if not os.path.exists(path):
+            raise FileNotFoundError(f"{path}: no ptxas report (rebuild with build(force=True))")
+        cur = None
+        with open(path) as f:
+            for line in f:
+                m = re.search(r"Compiling entry function '(\S+)'", line)
+                if m:
+                    cur = out.setdefault(m.group(1), {"registers": 0, "stack": 0, "spill_stores": 0, "spill_loads": 0})
+                    continue
+                if cur is None:
+                    continue
+                m = re.search(r"(\d+) bytes stack frame, (\d+) bytes spill stores, (\d+) bytes spill loads", line)
+                if m:
+                    cur["stack"], cur["spill_stores"], cur["spill_loads"] = map(int, m.groups())
+                m = re.search(r"Used (\d+) registers", line)
+                if m:
+                    cur["registers"] = int(m.group(1))
+                    cur = None
+    return out
 
 
 DRIVER = os.path.join(LIB_DIR, "sbp_demo")
